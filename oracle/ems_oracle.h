@@ -1,0 +1,75 @@
+/* ems_oracle.h — FP64 CPU restatement of the EMSolvers time loops.
+ *
+ * ORACLE / TEST INFRASTRUCTURE ONLY.  Nothing in the product library links or
+ * calls this code; only the tests, the smoke check and the CPU-baseline leg of
+ * bench.py load it, as the checker.  Each function states the reference
+ * file:line it restates (paths relative to the EMSolvers `src/` tree).
+ *
+ * Parity pinning: the FDTD and fem_v2-family functions are checked against
+ * binaries built from the unmodified reference sources (oracle/build_ref.sh)
+ * and against the golden fixtures in tests/golden/.  Extensions that the
+ * reference does not have (per-cell materials, CPML, tetrahedral elements,
+ * adjoints) reduce exactly to the reference where they overlap and are
+ * otherwise pinned by physical invariants (reflection, cavity modes, energy,
+ * finite differences) in the tests.
+ */
+#ifndef EMS_ORACLE_H
+#define EMS_ORACLE_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- FDTD --- */
+typedef struct {
+    int nx, ny, nz;
+    double h, dt, eps, mu;        /* uniform background (absolute eps, mu) */
+    int time_frequency;
+    /* optional per-cell material: mat_id[nx*ny*nz] indexes mat_eps/mat_sigma */
+    const uint16_t *mat_id;
+    const double *mat_eps;        /* absolute permittivity per material */
+    const double *mat_sigma;      /* conductivity per material [S/m] */
+    int nmat;
+    /* optional CPML on all six faces, `pml` cells thick (0 = none) */
+    int pml;
+    double pml_m, pml_kmax, pml_amax, pml_R0;
+    /* point sources: component 0/1/2 = Ex/Ey/Ez, stored (i,j,k) index */
+    int nsrc;
+    const int *src_comp;
+    const int *src_ijk;
+    const int *src_kind;          /* 0 = reference Gaussian derivative, 1 = Ricker */
+    const double *src_f0;
+    const double *src_amp;
+    /* receivers: obs_n[3*o+c] samples of component c for receiver o */
+    int nobs;
+    const int *obs_n;
+    const int *obs_ijk;           /* concatenated (i,j,k) triples */
+} orc_fdtd_case;
+
+/* Runs nsteps; E[3], H[3] hold the fields in the reference padded layout
+ * (in/out).  traces: nobs*(nsteps/tf+1)*3 doubles. */
+int orc_fdtd_run(const orc_fdtd_case *c, int nsteps, double *E[3], double *H[3], double *traces);
+double orc_fdtd_source(int kind, double f0, double t, double h);
+
+/* ------------------------------------------------------ hexahedral FEM --- */
+enum { ORC_LEAPFROG = 0, ORC_SYMP2 = 1, ORC_SYMP4 = 2 };
+typedef struct {
+    int order, gx, gy, gz;
+    double h, dt, eps, mu;
+    int time_frequency;
+    int integrator;               /* ORC_LEAPFROG / ORC_SYMP2 / ORC_SYMP4 */
+    const double *kmat;           /* unscaled element matrix, TOTAL x TOTAL */
+    int nsrc; const int *src_comp; const int *src_ijk;
+    int nobs; const int *obs_ijk;
+} orc_hexfem_case;
+
+/* ef[c] holds all three levels of component c (reference layout). traces:
+ * nobs * ((nsteps-1)/tf+1) * 4 doubles (t, Ex, Ey, Ez). */
+int orc_hexfem_run(const orc_hexfem_case *c, int nsteps, double *ef[3], double *traces);
+size_t orc_hexfem_ncomp(int gx, int gy, int gz, int comp);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,176 @@
+"""ctypes front end of the FP64 C oracle (oracle/*.c).
+
+ORACLE / TEST INFRASTRUCTURE ONLY — see the package docstring.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = C.CDLL(path)
+        _lib.orc_fdtd_run.restype = C.c_int
+        _lib.orc_fdtd_source.restype = C.c_double
+        _lib.orc_fdtd_source.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double]
+        _lib.orc_hexfem_run.restype = C.c_int
+        if hasattr(_lib, "orc_tet_run"):
+            _lib.orc_tet_run.restype = C.c_int
+    return _lib
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def _ptr(a, t=_dp):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+class _FdtdCase(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("h", C.c_double), ("dt", C.c_double), ("eps", C.c_double), ("mu", C.c_double),
+                ("time_frequency", C.c_int),
+                ("mat_id", C.POINTER(C.c_uint16)), ("mat_eps", _dp), ("mat_sigma", _dp), ("nmat", C.c_int),
+                ("pml", C.c_int), ("pml_m", C.c_double), ("pml_kmax", C.c_double), ("pml_amax", C.c_double),
+                ("pml_R0", C.c_double),
+                ("nsrc", C.c_int), ("src_comp", _ip), ("src_ijk", _ip), ("src_kind", _ip),
+                ("src_f0", _dp), ("src_amp", _dp),
+                ("nobs", C.c_int), ("obs_n", _ip), ("obs_ijk", _ip)]
+
+
+def fdtd_shapes(nx, ny, nz):
+    """Reference padded layout (fdtd/fdtd_simulation.cpp:57-68), x fastest."""
+    return {"Ex": (nz + 2, ny + 2, nx + 1), "Ey": (nz + 2, ny + 1, nx + 2), "Ez": (nz + 1, ny + 2, nx + 2),
+            "Hx": (nz + 1, ny + 1, nx), "Hy": (nz + 1, ny, nx + 1), "Hz": (nz, ny + 1, nx + 1)}
+
+
+def fdtd_source(kind, f0, t, h):
+    return lib().orc_fdtd_source(kind, f0, t, h)
+
+
+def fdtd_run(nx, ny, nz, h, dt, eps, mu, tf, nsteps, sources=(), observations=(),
+             material=None, pml=None, fields=None):
+    """Runs the FP64 oracle FDTD.
+
+    sources: [(comp, (i,j,k), kind, f0, amp)]; observations: [(xs, ys, zs)]
+    lists of (i,j,k) per component; material: (mat_id[nz,ny,nx] uint16,
+    eps_table, sigma_table); pml: dict(cells, m, kmax, amax, R0).
+    Returns (traces[nobs, nsteps//tf+1, 3], fields dict)."""
+    sh = fdtd_shapes(nx, ny, nz)
+    if fields is None:
+        fields = {k: np.zeros(v) for k, v in sh.items()}
+    else:
+        fields = {k: np.ascontiguousarray(fields[k], dtype=np.float64).copy() for k in sh}
+    c = _FdtdCase()
+    c.nx, c.ny, c.nz, c.h, c.dt, c.eps, c.mu, c.time_frequency = nx, ny, nz, h, dt, eps, mu, tf
+    keep = []
+    if material is not None:
+        mid = np.ascontiguousarray(material[0], dtype=np.uint16)
+        me = np.ascontiguousarray(material[1], dtype=np.float64)
+        ms = np.ascontiguousarray(material[2], dtype=np.float64)
+        keep += [mid, me, ms]
+        c.mat_id = mid.ctypes.data_as(C.POINTER(C.c_uint16))
+        c.mat_eps, c.mat_sigma, c.nmat = _ptr(me), _ptr(ms), len(me)
+    if pml:
+        c.pml = pml["cells"]
+        c.pml_m, c.pml_kmax, c.pml_amax, c.pml_R0 = pml.get("m", 3.0), pml.get("kmax", 1.0), pml.get("amax", 0.0), pml.get("R0", 1e-6)
+    c.nsrc = len(sources)
+    if sources:
+        comp = np.array([s[0] for s in sources], np.int32)
+        ijk = np.array([s[1] for s in sources], np.int32).reshape(-1)
+        kind = np.array([s[2] if len(s) > 2 else 0 for s in sources], np.int32)
+        f0 = np.array([s[3] if len(s) > 3 else 1e9 for s in sources], np.float64)
+        amp = np.array([s[4] if len(s) > 4 else 1.0 for s in sources], np.float64)
+        keep += [comp, ijk, kind, f0, amp]
+        c.src_comp, c.src_ijk, c.src_kind = _ptr(comp, _ip), _ptr(ijk, _ip), _ptr(kind, _ip)
+        c.src_f0, c.src_amp = _ptr(f0), _ptr(amp)
+    c.nobs = len(observations)
+    if observations:
+        on = np.array([len(l) for o in observations for l in o], np.int32)
+        oi = np.array([p for o in observations for l in o for p in l], np.int32).reshape(-1)
+        keep += [on, oi]
+        c.obs_n, c.obs_ijk = _ptr(on, _ip), _ptr(oi, _ip)
+    nsamp = nsteps // tf + 1
+    traces = np.zeros((max(len(observations), 1), nsamp, 3))
+    E = (_dp * 3)(*[_ptr(fields[k]) for k in ("Ex", "Ey", "Ez")])
+    H = (_dp * 3)(*[_ptr(fields[k]) for k in ("Hx", "Hy", "Hz")])
+    rc = lib().orc_fdtd_run(C.byref(c), C.c_int(nsteps), E, H, _ptr(traces))
+    if rc != 0:
+        raise RuntimeError(f"orc_fdtd_run failed: {rc}")
+    return traces[:len(observations)], fields
+
+
+# ------------------------------------------------------------ hexahedral FEM
+LEAPFROG, SYMP2, SYMP4 = 0, 1, 2
+
+
+class _HexCase(C.Structure):
+    _fields_ = [("order", C.c_int), ("gx", C.c_int), ("gy", C.c_int), ("gz", C.c_int),
+                ("h", C.c_double), ("dt", C.c_double), ("eps", C.c_double), ("mu", C.c_double),
+                ("time_frequency", C.c_int), ("integrator", C.c_int), ("kmat", _dp),
+                ("nsrc", C.c_int), ("src_comp", _ip), ("src_ijk", _ip),
+                ("nobs", C.c_int), ("obs_ijk", _ip)]
+
+
+def hexfem_sizes(gx, gy, gz):
+    return (gx * (gy + 1) * (gz + 1), (gx + 1) * gy * (gz + 1), (gx + 1) * (gy + 1) * gz)
+
+
+def parse_value(s):
+    """Restates fem_v2/fem_simulation.cpp:1477-1493 (trim quotes/space, a/b)."""
+    t = s.strip(" \t\r\n\"")
+    if not t:
+        return 0.0
+    if "/" in t:
+        a, b = t.split("/", 1)
+        return float(a) / float(b)
+    return float(t)
+
+
+def load_kmat(path):
+    """Restates fem_v2/fem_simulation.cpp:1495-1524 (rows of comma cells)."""
+    rows = []
+    with open(path) as f:
+        for line in f:
+            line = line.rstrip("\n")
+            if not line:
+                continue
+            rows.append([parse_value(c) for c in line.split(",")])
+    return np.array(rows, dtype=np.float64)
+
+
+def hexfem_run(order, grid, h, dt, eps, mu, tf, integrator, kmat, nsteps, sources=(), observations=(), ef=None):
+    """FP64 oracle for the fem_v2 family.  sources: [(comp, (i,j,k))];
+    observations: [(i,j,k)].  ef: optional [3] arrays of 3 levels each.
+    Returns (traces[nobs, (nsteps-1)//tf+1, 4], ef)."""
+    gx, gy, gz = grid
+    sz = hexfem_sizes(gx, gy, gz)
+    if ef is None:
+        ef = [np.zeros(3 * n) for n in sz]
+    else:
+        ef = [np.ascontiguousarray(a, dtype=np.float64).copy() for a in ef]
+    km = np.ascontiguousarray(kmat, dtype=np.float64)
+    c = _HexCase()
+    c.order, c.gx, c.gy, c.gz = order, gx, gy, gz
+    c.h, c.dt, c.eps, c.mu, c.time_frequency, c.integrator = h, dt, eps, mu, tf, integrator
+    c.kmat = _ptr(km)
+    comp = np.array([s[0] for s in sources] or [0], np.int32)
+    sijk = np.array([s[1] for s in sources] or [(0, 0, 0)], np.int32).reshape(-1)
+    oijk = np.array(list(observations) or [(0, 0, 0)], np.int32).reshape(-1)
+    c.nsrc, c.src_comp, c.src_ijk = len(sources), _ptr(comp, _ip), _ptr(sijk, _ip)
+    c.nobs, c.obs_ijk = len(observations), _ptr(oijk, _ip)
+    nsamp = (nsteps - 1) // tf + 1
+    traces = np.zeros((max(len(observations), 1), nsamp, 4))
+    arr = (_dp * 3)(*[_ptr(a) for a in ef])
+    rc = lib().orc_hexfem_run(C.byref(c), C.c_int(nsteps), arr, _ptr(traces))
+    if rc != 0:
+        raise RuntimeError(f"orc_hexfem_run failed: {rc}")
+    return traces[:len(observations)], ef

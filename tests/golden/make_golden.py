@@ -1,0 +1,92 @@
+"""Generates the golden fixtures in this folder from the reference solvers.
+
+Run in a checkout that has the EMSolvers sources (default /root/reference/src,
+or $EMS_REFERENCE_DIR):
+
+    python oracle/build.py            # builds oracle/_ref from the sources
+    python tests/golden/make_golden.py
+
+Outputs (committed, small):
+  kmat/{1,2,3,lamped1}.csv   the reference's element-matrix data files
+                              (fem_v2/kmat), copied byte for byte: they are
+                              solver input data that the engine reads at run
+                              time in the reference's CSV format.
+  fdtd_cases.npz             reference FDTD traces and final fields
+  femv2_cases.npz            reference fem_v2 / symplectic_2 / symplectic_4
+                              traces and final fields, orders 1-3
+Each case records its inputs beside the outputs so the tests can replay it.
+"""
+import json
+import os
+import shutil
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+import refrun  # noqa: E402
+
+EPS0_FDTD, MU0 = 8.854187817e-12, 1.25663706212e-6
+EPS0_FEM = 8.8541878128e-12
+C0 = 1.0 / np.sqrt(EPS0_FEM * MU0)
+
+FDTD_CASES = [
+    # name, grid, h, dt, tf, nsteps, sources, observations
+    ("cube8_jx", (8, 8, 8), 1e-3, 1.6e-12, 1, 30, [(0, (3, 4, 4))],
+     [([(4, 4, 4)], [(3, 3, 4), (3, 4, 4), (4, 3, 4), (4, 4, 4)], [(3, 4, 3), (3, 4, 4), (4, 4, 3), (4, 4, 4)])]),
+    ("box10x10x7_multi", (10, 10, 7), 1e-3, 0.5e-3 / (2.998e8 * np.sqrt(3)), 2, 60,
+     [(0, (3, 4, 4)), (2, (5, 5, 3)), (1, (6, 2, 5))],
+     [([(4, 4, 4)], [(3, 3, 4), (3, 4, 4), (4, 3, 4), (4, 4, 4)], [(3, 4, 3), (3, 4, 4), (4, 4, 3), (4, 4, 4)]),
+      ([(5, 5, 5)], [(5, 5, 5)], [(5, 5, 5), (6, 6, 5)])]),
+]
+
+FEM_CASES = []
+for variant in ("fem_v2", "symplectic_2", "symplectic_4"):
+    for order, ofem in ((1, 1), (1, 0), (2, 1), (3, 1)):
+        g = (6 * order, 5 * order, 4 * order) if order < 3 else (9, 9, 9)
+        FEM_CASES.append((variant, order, ofem, g))
+
+
+def main():
+    if not refrun.available():
+        raise SystemExit("reference binaries missing: run python oracle/build.py first")
+    kdir = os.path.join(HERE, "kmat")
+    os.makedirs(kdir, exist_ok=True)
+    for f in ("1.csv", "2.csv", "3.csv", "lamped1.csv"):
+        shutil.copyfile(os.path.join(refrun.REF_SRC, "fem_v2", "kmat", f), os.path.join(kdir, f))
+
+    out = {}
+    meta = []
+    for name, (nx, ny, nz), h, dt, tf, ns, src, obs in FDTD_CASES:
+        tr, f = refrun.fdtd(nx, ny, nz, h, dt, EPS0_FDTD, MU0, tf, ns, src, obs)
+        out[f"{name}/traces"] = tr
+        for k, v in f.items():
+            out[f"{name}/{k}"] = v
+        meta.append(dict(name=name, grid=[nx, ny, nz], h=h, dt=float(dt), eps=EPS0_FDTD, mu=MU0, tf=tf,
+                         nsteps=ns, sources=[[c, list(p)] for c, p in src],
+                         observations=[[list(map(list, l)) for l in o] for o in obs]))
+    out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "fdtd_cases.npz"), **out)
+
+    out = {}
+    meta = []
+    for variant, order, ofem, g in FEM_CASES:
+        h = 0.1
+        dt = h / (C0 * np.sqrt(3.0)) / 2.0
+        src = (2, (g[0] // 2, g[1] // 2, g[2] // 2))
+        obs = (g[0] // 2 + 1, g[1] // 2, g[2] // 2)
+        tr, ef = refrun.femv2(variant, order, ofem, g, h, dt, EPS0_FEM, MU0, 2, 40, src, obs)
+        name = f"{variant}_o{order}_{'ofem' if ofem else 'lumped'}"
+        out[f"{name}/traces"] = tr
+        for q in range(3):
+            out[f"{name}/ef{q}"] = ef[q]
+        meta.append(dict(name=name, variant=variant, order=order, use_ofem=ofem, grid=list(g), h=h, dt=float(dt),
+                         eps=EPS0_FEM, mu=MU0, tf=2, nsteps=40, source=[src[0], list(src[1])], observation=list(obs)))
+    out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "femv2_cases.npz"), **out)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,73 @@
+"""Pins the FP64 CPU oracle against the reference: bit-identical traces and
+fields on the golden fixtures produced by the unmodified reference solvers,
+and (where the reference tree is present) on live reference runs."""
+import numpy as np
+import pytest
+
+import golden_io
+import oracle
+import refrun
+
+INTEG = {"fem_v2": oracle.LEAPFROG, "symplectic_2": oracle.SYMP2, "symplectic_4": oracle.SYMP4}
+
+
+@pytest.mark.parametrize("case", list(golden_io.fdtd_cases()), ids=lambda c: c[0]["name"])
+def test_fdtd_oracle_matches_reference_bitwise(case):
+    m, tr, fields = case
+    nx, ny, nz = m["grid"]
+    srcs = [(c, tuple(p), 0, 1e9, 1.0) for c, p in m["sources"]]
+    obs = [tuple([tuple(q) for q in l] for l in o) for o in m["observations"]]
+    tr_o, f_o = oracle.fdtd_run(nx, ny, nz, m["h"], m["dt"], m["eps"], m["mu"], m["tf"], m["nsteps"], srcs, obs)
+    assert np.array_equal(tr_o, tr)
+    for k in fields:
+        assert np.array_equal(f_o[k], fields[k]), k
+
+
+@pytest.mark.parametrize("case", list(golden_io.femv2_cases()), ids=lambda c: c[0]["name"])
+def test_hexfem_oracle_matches_reference_bitwise(case):
+    m, tr, ef = case
+    km = oracle.load_kmat(golden_io.kmat_path(m["order"], m["use_ofem"]))
+    src = (m["source"][0], tuple(m["source"][1]))
+    tr_o, ef_o = oracle.hexfem_run(m["order"], tuple(m["grid"]), m["h"], m["dt"], m["eps"], m["mu"], m["tf"],
+                                   INTEG[m["variant"]], km, m["nsteps"], [src], [tuple(m["observation"])])
+    assert np.array_equal(tr_o[0], tr)
+    for q in range(3):
+        assert np.array_equal(ef_o[q], ef[q])
+
+
+def test_kmat_parser_reads_rationals(golden_dir):
+    k = oracle.load_kmat(golden_io.kmat_path(1, 1))
+    assert k.shape == (12, 12)
+    assert k[0, 0] == 7.0 / 4.0 and k[0, 4] == -7.0 / 8.0
+    assert np.allclose(k, k.T)
+    for o, n in ((2, 54), (3, 144)):
+        assert oracle.load_kmat(golden_io.kmat_path(o, 1)).shape == (n, n)
+
+
+@pytest.mark.skipif(not refrun.available(), reason="reference sources not present")
+def test_fdtd_oracle_matches_live_reference_cubic_grid():
+    n = 9
+    h = 1e-3
+    dt = 0.9 * h / (2.998e8 * np.sqrt(3))
+    src = [(2, (4, 4, 4)), (1, (2, 6, 3))]
+    obs = [([(4, 4, 5)], [(4, 4, 5)], [(4, 4, 5)])]
+    tr_r, f_r = refrun.fdtd(n, n, n, h, dt, 8.854187817e-12, 1.25663706212e-6, 3, 45, src, obs)
+    tr_o, f_o = oracle.fdtd_run(n, n, n, h, dt, 8.854187817e-12, 1.25663706212e-6, 3, 45,
+                                [(c, p, 0, 1e9, 1.0) for c, p in src], obs)
+    assert np.array_equal(tr_r, tr_o)
+    for k in f_r:
+        assert np.array_equal(f_r[k], f_o[k])
+
+
+def test_fdtd_material_table_reduces_to_reference_update():
+    """Uniform eps through the material table, sigma = 0: identical bits."""
+    n = 7
+    h, dt, eps, mu = 1e-3, 1.5e-12, 8.854187817e-12, 1.25663706212e-6
+    src = [(0, (3, 3, 3), 0, 1e9, 1.0)]
+    obs = [([(3, 3, 3)], [(3, 3, 3)], [(3, 3, 3)])]
+    tr_a, f_a = oracle.fdtd_run(n, n, n, h, dt, eps, mu, 1, 20, src, obs)
+    mat = (np.zeros((n, n, n), np.uint16), np.array([eps]), np.array([0.0]))
+    tr_b, f_b = oracle.fdtd_run(n, n, n, h, dt, eps, mu, 1, 20, src, obs, material=mat)
+    assert np.array_equal(tr_a, tr_b)
+    for k in f_a:
+        assert np.array_equal(f_a[k], f_b[k])
