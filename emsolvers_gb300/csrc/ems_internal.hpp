@@ -1,0 +1,101 @@
+// Internal declarations shared by the libems translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <array>
+#include <cstdio>
+#include <type_traits>
+#include <string>
+#include <vector>
+
+#include "../../include/ems.h"
+
+namespace ems {
+
+// Status carrier used inside the library; converted to int at the C ABI.
+struct Error {
+    int code;
+    std::string msg;
+};
+
+#define EMS_CUDA(call)                                                                              \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) {                                                                    \
+            if (e_ == cudaErrorMemoryAllocation)                                                    \
+                throw ::ems::Error{EMS_ERR_OUT_OF_MEMORY, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+            throw ::ems::Error{EMS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)};   \
+        }                                                                                           \
+    } while (0)
+
+#define EMS_CHECK_ARG(cond, text)                                          \
+    do {                                                                   \
+        if (!(cond)) throw ::ems::Error{EMS_ERR_INVALID_ARGUMENT, (text)}; \
+    } while (0)
+
+// Device buffer owned by a simulation handle.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void alloc(size_t b);
+    void zero(cudaStream_t s);
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+enum class Kind { FDTD, HEXFEM, TETFEM };
+
+// Base of every simulation handle (the opaque ems_sim of the C ABI).
+struct Sim {
+    Kind kind;
+    std::string last_error;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    double last_ms = 0.0;
+    long long last_launches = 0;
+    int nobs = 0, nsamp = 0, ncols = 0;
+    std::vector<double> traces;   // host copy of the last run's receiver table
+    explicit Sim(Kind k) : kind(k) {}
+    virtual ~Sim();
+    void init_stream();
+    virtual void run(int nsteps) = 0;
+    virtual size_t field_size(int which) const = 0;
+    virtual void get_field(int which, double *out) const = 0;
+    virtual void set_field(int which, const double *in) = 0;
+    virtual void save(const char *path) const = 0;
+    virtual void time_dominant(int launches, double *ms, double *bytes, std::string *name) = 0;
+};
+
+// CSV element matrices in the reference format (fem_v2/fem_simulation.cpp:1477-1524).
+double parse_value(const std::string &s);
+std::vector<std::vector<double>> load_matrix_csv(const std::string &path);
+// Reference file-name helper (fem_v2/fem_simulation.cpp:1446-1475).
+std::string compress_number(double v);
+
+Sim *make_fdtd(const ems_fdtd_params *p);
+Sim *make_hexfem(const ems_hexfem_params *p);
+Sim *make_tetfem(const ems_tetfem_params *p);
+
+// per-kind setters (throw Error on misuse)
+void fdtd_set_source(Sim *s, int comp, const int ijk[3], int waveform, double f0, double amp);
+void fdtd_add_observation(Sim *s, const int *x, int nx, const int *y, int ny, const int *z, int nz);
+void fdtd_set_material(Sim *s, const double *eps, const double *sigma);
+void hexfem_set_source(Sim *s, int comp, const int ijk[3]);
+void hexfem_add_observation(Sim *s, const int ijk[3]);
+void tetfem_set_material(Sim *s, const double *eps_r, const double *sigma);
+void tetfem_add_dipole(Sim *s, const double pos[3], const double dir[3], int waveform, double f0, double amp);
+void tetfem_add_receiver(Sim *s, const double pos[3]);
+void tetfem_time_step(const Sim *s, double *dt, double *lim);
+
+// Source waveforms evaluated on the host in FP64.
+double fdtd_source_value(int kind, double f0, double t, double h);
+
+}  // namespace ems
+
+struct ems_sim {
+    ems::Sim *impl;
+};

@@ -1,0 +1,604 @@
+// Yee FDTD on one GPU: the reference time loop of fdtd/fdtd_simulation.cpp
+// (H from curl E 119-169, E from curl H 170-220, sources 222-239, receivers
+// 261-303) on the reference's padded field layout (55-88), extended with
+// per-cell materials and a convolutional PML.
+//
+// Arithmetic is written with explicitly rounded operations (no contraction
+// into fused multiply-adds) in the reference's operand order, so the FP64
+// path reproduces the reference bit for bit; the FP32 path runs the same
+// operations in single precision.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <iomanip>
+
+#include "ems_internal.hpp"
+
+namespace ems {
+
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+
+// CPML coefficient profile along one axis, sampled at the derivative positions.
+template <class T> struct Prof {
+    const T *b, *a, *kinv;
+    const unsigned char *on;
+};
+
+template <class T> struct FdtdArgs {
+    T *Ex, *Ey, *Ez, *Hx, *Hy, *Hz;
+    int nx, ny, nz;
+    T ch, ce;                      // uniform update coefficients dt/mu/h, dt/eps/h
+    const uint16_t *mat;           // per-cell material id (MAT)
+    const T *ca, *cb;              // per-material E coefficients (MAT)
+    Prof<T> pe[3], ph[3];          // CPML profiles for E- and H-type derivatives (PML)
+    T *psiE[3][2], *psiH[3][2];    // CPML auxiliary fields, full field size (PML)
+};
+
+#define IEX(i, j, k) ((size_t)(i) + (size_t)(j) * (a.nx + 1) + (size_t)(k) * (a.nx + 1) * (a.ny + 2))
+#define IEY(i, j, k) ((size_t)(i) + (size_t)(j) * (a.nx + 2) + (size_t)(k) * (a.nx + 2) * (a.ny + 1))
+#define IEZ(i, j, k) ((size_t)(i) + (size_t)(j) * (a.nx + 2) + (size_t)(k) * (a.nx + 2) * (a.ny + 2))
+#define IHX(i, j, k) ((size_t)(i) + (size_t)(j) * a.nx + (size_t)(k) * a.nx * (a.ny + 1))
+#define IHY(i, j, k) ((size_t)(i) + (size_t)(j) * (a.nx + 1) + (size_t)(k) * (a.nx + 1) * a.ny)
+#define IHZ(i, j, k) ((size_t)(i) + (size_t)(j) * (a.nx + 1) + (size_t)(k) * (a.nx + 1) * (a.ny + 1))
+
+// d = ((p - q) - r) + s, the reference's evaluation order of a curl difference.
+template <class T> __device__ __forceinline__ T curl4(T p, T q, T r, T s) { return radd(rsub(rsub(p, q), r), s); }
+
+// One CPML-stretched update value: kinv1*d1 - kinv2*d2 + psi1 - psi2 with the
+// auxiliary recursions psi = b psi + a d (oracle/orc_fdtd.c order).
+template <class T>
+__device__ __forceinline__ T pml_curl(T d1, T d2, const Prof<T> &p1, int s1, const Prof<T> &p2, int s2, T *psi1, T *psi2)
+{
+    T q1 = radd(rmul(p1.b[s1], *psi1), rmul(p1.a[s1], d1));
+    T q2 = radd(rmul(p2.b[s2], *psi2), rmul(p2.a[s2], d2));
+    *psi1 = q1;
+    *psi2 = q2;
+    return rsub(radd(rsub(rmul(p1.kinv[s1], d1), rmul(p2.kinv[s2], d2)), q1), q2);
+}
+
+// H from curl E at cell (i,j,k): fdtd_simulation.cpp:119-169.
+template <class T, bool PML>
+__global__ void __launch_bounds__(256) fdtd_h_kernel(FdtdArgs<T> a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > a.nx || j > a.ny || k > a.nz) return;
+    if (i < a.nx) {
+        size_t p = IHX(i, j, k);
+        T e1 = a.Ez[IEZ(i + 1, j + 1, k)], e2 = a.Ez[IEZ(i + 1, j, k)];
+        T e3 = a.Ey[IEY(i + 1, j, k + 1)], e4 = a.Ey[IEY(i + 1, j, k)];
+        if (PML && (a.ph[1].on[j] | a.ph[2].on[k])) {
+            T c = pml_curl(rsub(e1, e2), rsub(e3, e4), a.ph[1], j, a.ph[2], k, &a.psiH[0][0][p], &a.psiH[0][1][p]);
+            a.Hx[p] = rsub(a.Hx[p], rmul(a.ch, c));
+        } else {
+            a.Hx[p] = rsub(a.Hx[p], rmul(a.ch, curl4(e1, e2, e3, e4)));
+        }
+    }
+    if (j < a.ny) {
+        size_t p = IHY(i, j, k);
+        T e1 = a.Ex[IEX(i, j + 1, k + 1)], e2 = a.Ex[IEX(i, j + 1, k)];
+        T e3 = a.Ez[IEZ(i + 1, j + 1, k)], e4 = a.Ez[IEZ(i, j + 1, k)];
+        if (PML && (a.ph[2].on[k] | a.ph[0].on[i])) {
+            T c = pml_curl(rsub(e1, e2), rsub(e3, e4), a.ph[2], k, a.ph[0], i, &a.psiH[1][0][p], &a.psiH[1][1][p]);
+            a.Hy[p] = rsub(a.Hy[p], rmul(a.ch, c));
+        } else {
+            a.Hy[p] = rsub(a.Hy[p], rmul(a.ch, curl4(e1, e2, e3, e4)));
+        }
+    }
+    if (k < a.nz) {
+        size_t p = IHZ(i, j, k);
+        T e1 = a.Ey[IEY(i + 1, j, k + 1)], e2 = a.Ey[IEY(i, j, k + 1)];
+        T e3 = a.Ex[IEX(i, j + 1, k + 1)], e4 = a.Ex[IEX(i, j, k + 1)];
+        if (PML && (a.ph[0].on[i] | a.ph[1].on[j])) {
+            T c = pml_curl(rsub(e1, e2), rsub(e3, e4), a.ph[0], i, a.ph[1], j, &a.psiH[2][0][p], &a.psiH[2][1][p]);
+            a.Hz[p] = rsub(a.Hz[p], rmul(a.ch, c));
+        } else {
+            a.Hz[p] = rsub(a.Hz[p], rmul(a.ch, curl4(e1, e2, e3, e4)));
+        }
+    }
+}
+
+// E from curl H at (i,j,k): fdtd_simulation.cpp:170-220, E = ca E + cb curl.
+template <class T, bool MAT, bool PML>
+__global__ void __launch_bounds__(256) fdtd_e_kernel(FdtdArgs<T> a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    if (i > a.nx || j > a.ny || k > a.nz) return;
+    const int nx = a.nx, ny = a.ny, nz = a.nz;
+    auto cell = [&](int ci, int cj, int ck) { return a.mat[(size_t)ci + (size_t)cj * nx + (size_t)ck * nx * ny]; };
+    auto upd = [&](T *f, size_t p, T ca, T cb, T c) {
+        if (MAT) f[p] = radd(rmul(ca, f[p]), rmul(cb, c));
+        else f[p] = radd(f[p], rmul(a.ce, c));
+    };
+    if (j >= 1 && k >= 1) {  // Ex, i in [0,nx]
+        size_t p = IEX(i, j, k);
+        T ca = 1, cb = 0;
+        if (MAT) { int m = cell(i < nx ? i : nx - 1, j - 1, k - 1); ca = a.ca[m]; cb = a.cb[m]; }
+        T h1 = a.Hz[IHZ(i, j, k - 1)], h2 = a.Hz[IHZ(i, j - 1, k - 1)];
+        T h3 = a.Hy[IHY(i, j - 1, k)], h4 = a.Hy[IHY(i, j - 1, k - 1)];
+        if (PML && (a.pe[1].on[j] | a.pe[2].on[k])) {
+            T c = pml_curl(rsub(h1, h2), rsub(h3, h4), a.pe[1], j, a.pe[2], k, &a.psiE[0][0][p], &a.psiE[0][1][p]);
+            T cbb = MAT ? cb : a.ce;
+            T caa = MAT ? ca : T(1);
+            a.Ex[p] = radd(rmul(caa, a.Ex[p]), rmul(cbb, c));
+        } else {
+            upd(a.Ex, p, ca, cb, curl4(h1, h2, h3, h4));
+        }
+    }
+    if (i >= 1 && k >= 1) {  // Ey, j in [0,ny]
+        size_t p = IEY(i, j, k);
+        T ca = 1, cb = 0;
+        if (MAT) { int m = cell(i - 1, j < ny ? j : ny - 1, k - 1); ca = a.ca[m]; cb = a.cb[m]; }
+        T h1 = a.Hx[IHX(i - 1, j, k)], h2 = a.Hx[IHX(i - 1, j, k - 1)];
+        T h3 = a.Hz[IHZ(i, j, k - 1)], h4 = a.Hz[IHZ(i - 1, j, k - 1)];
+        if (PML && (a.pe[2].on[k] | a.pe[0].on[i])) {
+            T c = pml_curl(rsub(h1, h2), rsub(h3, h4), a.pe[2], k, a.pe[0], i, &a.psiE[1][0][p], &a.psiE[1][1][p]);
+            T cbb = MAT ? cb : a.ce;
+            T caa = MAT ? ca : T(1);
+            a.Ey[p] = radd(rmul(caa, a.Ey[p]), rmul(cbb, c));
+        } else {
+            upd(a.Ey, p, ca, cb, curl4(h1, h2, h3, h4));
+        }
+    }
+    if (i >= 1 && j >= 1) {  // Ez, k in [0,nz]
+        size_t p = IEZ(i, j, k);
+        T ca = 1, cb = 0;
+        if (MAT) { int m = cell(i - 1, j - 1, k < nz ? k : nz - 1); ca = a.ca[m]; cb = a.cb[m]; }
+        T h1 = a.Hy[IHY(i, j - 1, k)], h2 = a.Hy[IHY(i - 1, j - 1, k)];
+        T h3 = a.Hx[IHX(i - 1, j, k)], h4 = a.Hx[IHX(i - 1, j - 1, k)];
+        if (PML && (a.pe[0].on[i] | a.pe[1].on[j])) {
+            T c = pml_curl(rsub(h1, h2), rsub(h3, h4), a.pe[0], i, a.pe[1], j, &a.psiE[2][0][p], &a.psiE[2][1][p]);
+            T cbb = MAT ? cb : a.ce;
+            T caa = MAT ? ca : T(1);
+            a.Ez[p] = radd(rmul(caa, a.Ez[p]), rmul(cbb, c));
+        } else {
+            upd(a.Ez, p, ca, cb, curl4(h1, h2, h3, h4));
+        }
+    }
+}
+
+// Point sources in insertion order: E[src] -= v (fdtd_simulation.cpp:222-239).
+template <class T>
+__global__ void fdtd_source_kernel(T *Ex, T *Ey, T *Ez, const int *comp, const size_t *off, const double *vals, int nsrc)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int s = 0; s < nsrc; ++s) {
+        T *f = comp[s] == 0 ? Ex : comp[s] == 1 ? Ey : Ez;
+        f[off[s]] = rsub(f[off[s]], (T)vals[s]);
+    }
+}
+
+// Receiver averages (fdtd_simulation.cpp:261-303): one thread per receiver,
+// summing its listed samples in order, then dividing by the count.
+template <class T>
+__global__ void fdtd_receiver_kernel(const T *Ex, const T *Ey, const T *Ez, int nobs, const int *cnt,
+                                     const int *start, const size_t *off, double *trace_row, int nsamp)
+{
+    int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nobs) return;
+    double *out = trace_row + (size_t)o * nsamp * 3;
+    int q = start[o];
+    for (int c = 0; c < 3; ++c) {
+        const T *f = c == 0 ? Ex : c == 1 ? Ey : Ez;
+        int n = cnt[3 * o + c];
+        double acc = out[c];
+        for (int r = 0; r < n; ++r, ++q) acc = __dadd_rn(acc, (double)f[off[q]]);
+        out[c] = acc / (double)n;
+    }
+}
+
+double fdtd_source_value(int kind, double f0, double t, double h)
+{
+    if (kind == EMS_WAVE_REFERENCE)
+        return -4.0 * M_PI * M_PI * f0 * f0 * (t - 1.0 / f0) *
+               std::exp(-2.0 * M_PI * M_PI * f0 * f0 * (t - 1.0 / f0) * (t - 1.0 / f0)) / h / h / h * 0.001;
+    double tau = t - std::sqrt(2.0) / f0;
+    return (1.0 - 2.0 * M_PI * M_PI * f0 * f0 * tau * tau) * std::exp(-M_PI * M_PI * f0 * f0 * tau * tau) / h / h / h * 0.001;
+}
+
+struct FdtdSource {
+    int comp;
+    int ijk[3];
+    int kind;
+    double f0, amp;
+    size_t off;
+};
+
+struct FdtdSim : Sim {
+    ems_fdtd_params P;
+    int nx, ny, nz;
+    bool fp64;
+    size_t n[6];
+    DevBuf F[6];
+    // materials
+    std::vector<uint16_t> mat_host;
+    std::vector<double> mat_eps, mat_sigma;
+    DevBuf d_mat, d_ca, d_cb;
+    // CPML
+    DevBuf d_prof[2][3][4];   // [E/H][axis][b,a,kinv,on]
+    DevBuf d_psiE[3][2], d_psiH[3][2];
+    // sources, receivers
+    std::vector<FdtdSource> srcs;
+    std::vector<std::vector<std::array<int, 3>>> obs_lists;   // 3 per receiver
+    std::vector<int> obs_n;
+    DevBuf d_src_comp, d_src_off, d_src_vals, d_obs_cnt, d_obs_start, d_obs_off, d_traces;
+    bool dirty = true;
+
+    explicit FdtdSim(const ems_fdtd_params *p) : Sim(Kind::FDTD), P(*p)
+    {
+        nx = P.grid[0]; ny = P.grid[1]; nz = P.grid[2];
+        EMS_CHECK_ARG(nx > 0 && ny > 0 && nz > 0, "grid sizes must be positive");
+        EMS_CHECK_ARG(P.h > 0 && P.dt > 0 && P.permittivity > 0 && P.permeability > 0, "h, dt, eps, mu must be positive");
+        EMS_CHECK_ARG(P.time_frequency > 0, "time_frequency must be positive");
+        EMS_CHECK_ARG(P.precision == EMS_FP64 || P.precision == EMS_FP32, "precision must be EMS_FP64 or EMS_FP32");
+        // the reference's check_params condition (fdtd_simulation.cpp:358): c*dt < h
+        double c = 1.0 / std::sqrt(P.permittivity * P.permeability);
+        EMS_CHECK_ARG(c * P.dt < P.h, "time step violates c*dt < h (reference check_params)");
+        EMS_CHECK_ARG(P.pml_cells >= 0 && 2 * P.pml_cells < std::min(nx, std::min(ny, nz)), "pml_cells too large for the grid");
+        if (P.pml_order == 0) P.pml_order = 3.0;
+        if (P.pml_kappa_max == 0) P.pml_kappa_max = 1.0;
+        if (P.pml_reflection == 0) P.pml_reflection = 1e-6;
+        fp64 = P.precision == EMS_FP64;
+        n[0] = (size_t)(nx + 1) * (ny + 2) * (nz + 2);
+        n[1] = (size_t)(nx + 2) * (ny + 1) * (nz + 2);
+        n[2] = (size_t)(nx + 2) * (ny + 2) * (nz + 1);
+        n[3] = (size_t)nx * (ny + 1) * (nz + 1);
+        n[4] = (size_t)(nx + 1) * ny * (nz + 1);
+        n[5] = (size_t)(nx + 1) * (ny + 1) * nz;
+        init_stream();
+        size_t w = fp64 ? 8 : 4;
+        for (int q = 0; q < 6; ++q) { F[q].alloc(n[q] * w); F[q].zero(stream); }
+        if (P.pml_cells > 0) setup_pml();
+        EMS_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    void setup_pml()
+    {
+        const int nn[3] = {nx, ny, nz};
+        const int L = P.pml_cells;
+        double eta = std::sqrt(P.permeability / P.permittivity);
+        double smax = -(P.pml_order + 1.0) * std::log(P.pml_reflection) / (2.0 * eta * L * P.h);
+        for (int eh = 0; eh < 2; ++eh)
+            for (int d = 0; d < 3; ++d) {
+                int cnt = nn[d] + 2;
+                std::vector<double> b(cnt, 0.0), av(cnt, 0.0), kinv(cnt, 1.0);
+                std::vector<unsigned char> on(cnt, 0);
+                double shift = eh == 0 ? -0.5 : 0.0;
+                for (int s = 0; s < cnt; ++s) {
+                    double x = s + shift, lo = L - x, hi = x - (nn[d] - L);
+                    double dd = lo > hi ? lo : hi;
+                    dd = dd < 0.0 ? 0.0 : (dd > L ? 1.0 : dd / L);
+                    if (dd <= 0.0) continue;
+                    double g = std::pow(dd, P.pml_order);
+                    double sig = smax * g, kap = 1.0 + (P.pml_kappa_max - 1.0) * g, alp = P.pml_alpha_max * (1.0 - dd);
+                    double bb = std::exp(-(sig / kap + alp) * P.dt / P.permittivity);
+                    b[s] = bb;
+                    av[s] = sig > 0.0 ? sig / (sig * kap + kap * kap * alp) * (bb - 1.0) : 0.0;
+                    kinv[s] = 1.0 / kap;
+                    on[s] = 1;
+                }
+                upload_real(d_prof[eh][d][0], b);
+                upload_real(d_prof[eh][d][1], av);
+                upload_real(d_prof[eh][d][2], kinv);
+                d_prof[eh][d][3].alloc(cnt);
+                EMS_CUDA(cudaMemcpyAsync(d_prof[eh][d][3].p, on.data(), cnt, cudaMemcpyHostToDevice, stream));
+            }
+        size_t w = fp64 ? 8 : 4;
+        for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < 2; ++r) {
+                d_psiE[c][r].alloc(n[c] * w); d_psiE[c][r].zero(stream);
+                d_psiH[c][r].alloc(n[3 + c] * w); d_psiH[c][r].zero(stream);
+            }
+        EMS_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    void upload_real(DevBuf &d, const std::vector<double> &v)
+    {
+        if (fp64) {
+            d.alloc(v.size() * 8);
+            EMS_CUDA(cudaMemcpyAsync(d.p, v.data(), v.size() * 8, cudaMemcpyHostToDevice, stream));
+        } else {
+            std::vector<float> f(v.begin(), v.end());
+            d.alloc(f.size() * 4);
+            EMS_CUDA(cudaMemcpyAsync(d.p, f.data(), f.size() * 4, cudaMemcpyHostToDevice, stream));
+        }
+        EMS_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    size_t ex_index(int c, const int *q) const
+    {
+        if (c == 0) return (size_t)q[0] + (size_t)q[1] * (nx + 1) + (size_t)q[2] * (nx + 1) * (ny + 2);
+        if (c == 1) return (size_t)q[0] + (size_t)q[1] * (nx + 2) + (size_t)q[2] * (nx + 2) * (ny + 1);
+        return (size_t)q[0] + (size_t)q[1] * (nx + 2) + (size_t)q[2] * (nx + 2) * (ny + 2);
+    }
+    bool in_e(int c, const int *q) const
+    {
+        int lim[3][3] = {{nx, ny + 1, nz + 1}, {nx + 1, ny, nz + 1}, {nx + 1, ny + 1, nz}};
+        for (int d = 0; d < 3; ++d)
+            if (q[d] < 0 || q[d] > lim[c][d]) return false;
+        return true;
+    }
+
+    void set_material(const double *eps, const double *sigma)
+    {
+        EMS_CHECK_ARG(eps != nullptr, "eps array required");
+        size_t nc = (size_t)nx * ny * nz;
+        std::map<std::pair<double, double>, int> ids;
+        mat_host.assign(nc, 0);
+        mat_eps.clear(); mat_sigma.clear();
+        for (size_t q = 0; q < nc; ++q) {
+            double e = eps[q], s = sigma ? sigma[q] : 0.0;
+            EMS_CHECK_ARG(std::isfinite(e) && e > 0 && std::isfinite(s) && s >= 0, "eps must be > 0 and sigma >= 0");
+            auto key = std::make_pair(e, s);
+            auto it = ids.find(key);
+            int id;
+            if (it == ids.end()) {
+                EMS_CHECK_ARG(ids.size() < 65535, "more than 65535 distinct (eps, sigma) pairs");
+                id = (int)ids.size();
+                ids.emplace(key, id);
+                mat_eps.push_back(e); mat_sigma.push_back(s);
+            } else {
+                id = it->second;
+            }
+            mat_host[q] = (uint16_t)id;
+        }
+        std::vector<double> ca(mat_eps.size()), cb(mat_eps.size());
+        for (size_t m = 0; m < mat_eps.size(); ++m) {
+            double s = mat_sigma[m] * P.dt / (2.0 * mat_eps[m]);
+            ca[m] = (1.0 - s) / (1.0 + s);
+            cb[m] = P.dt / mat_eps[m] / P.h / (1.0 + s);
+        }
+        d_mat.alloc(nc * 2);
+        EMS_CUDA(cudaMemcpyAsync(d_mat.p, mat_host.data(), nc * 2, cudaMemcpyHostToDevice, stream));
+        upload_real(d_ca, ca);
+        upload_real(d_cb, cb);
+    }
+
+    template <class T> FdtdArgs<T> args() const
+    {
+        FdtdArgs<T> a{};
+        a.Ex = F[0].as<T>(); a.Ey = F[1].as<T>(); a.Ez = F[2].as<T>();
+        a.Hx = F[3].as<T>(); a.Hy = F[4].as<T>(); a.Hz = F[5].as<T>();
+        a.nx = nx; a.ny = ny; a.nz = nz;
+        a.ch = (T)(P.dt / P.permeability / P.h);
+        a.ce = (T)(P.dt / P.permittivity / P.h);
+        a.mat = d_mat.as<uint16_t>();
+        a.ca = d_ca.as<T>(); a.cb = d_cb.as<T>();
+        if (P.pml_cells > 0)
+            for (int d = 0; d < 3; ++d) {
+                a.pe[d] = Prof<T>{d_prof[0][d][0].as<T>(), d_prof[0][d][1].as<T>(), d_prof[0][d][2].as<T>(), d_prof[0][d][3].as<unsigned char>()};
+                a.ph[d] = Prof<T>{d_prof[1][d][0].as<T>(), d_prof[1][d][1].as<T>(), d_prof[1][d][2].as<T>(), d_prof[1][d][3].as<unsigned char>()};
+                for (int r = 0; r < 2; ++r) { a.psiE[d][r] = d_psiE[d][r].as<T>(); a.psiH[d][r] = d_psiH[d][r].as<T>(); }
+            }
+        return a;
+    }
+
+    dim3 block() const { return dim3(32, 8, 1); }
+    dim3 grid() const { return dim3((nx + 1 + 31) / 32, (ny + 1 + 7) / 8, nz + 1); }
+
+    template <class T> void launch_h(const FdtdArgs<T> &a)
+    {
+        if (P.pml_cells > 0) fdtd_h_kernel<T, true><<<grid(), block(), 0, stream>>>(a);
+        else fdtd_h_kernel<T, false><<<grid(), block(), 0, stream>>>(a);
+    }
+    template <class T> void launch_e(const FdtdArgs<T> &a)
+    {
+        bool mat = !mat_host.empty(), pml = P.pml_cells > 0;
+        if (mat && pml) fdtd_e_kernel<T, true, true><<<grid(), block(), 0, stream>>>(a);
+        else if (mat) fdtd_e_kernel<T, true, false><<<grid(), block(), 0, stream>>>(a);
+        else if (pml) fdtd_e_kernel<T, false, true><<<grid(), block(), 0, stream>>>(a);
+        else fdtd_e_kernel<T, false, false><<<grid(), block(), 0, stream>>>(a);
+    }
+
+    template <class T> void run_t(int nsteps)
+    {
+        const int tf = P.time_frequency;
+        nsamp = nsteps / tf + 1;
+        nobs = (int)obs_n.size() / 3;
+        ncols = 3;
+        // source values per step, computed on the host in FP64 exactly as the
+        // reference does (time accumulated by repeated addition of dt)
+        int ns = (int)srcs.size();
+        std::vector<double> vals((size_t)std::max(ns, 1) * nsteps, 0.0);
+        double t = 0.0;
+        for (int st = 0; st < nsteps; ++st) {
+            for (int s = 0; s < ns; ++s) {
+                const FdtdSource &q = srcs[s];
+                double eps = P.permittivity, div = 1.0;
+                if (!mat_host.empty()) {
+                    int ci = q.ijk[0], cj = q.ijk[1], ck = q.ijk[2];
+                    if (q.comp == 0) { ci = ci < nx ? ci : nx - 1; cj -= 1; ck -= 1; }
+                    else if (q.comp == 1) { ci -= 1; cj = cj < ny ? cj : ny - 1; ck -= 1; }
+                    else { ci -= 1; cj -= 1; ck = ck < nz ? ck : nz - 1; }
+                    int m = mat_host[(size_t)ci + (size_t)cj * nx + (size_t)ck * nx * ny];
+                    eps = mat_eps[m];
+                    div = 1.0 + mat_sigma[m] * P.dt / (2.0 * mat_eps[m]);
+                }
+                double v = fdtd_source_value(q.kind, q.f0, t, P.h) * q.amp * P.dt / eps;
+                if (div != 1.0) v /= div;
+                vals[(size_t)st * ns + s] = v;
+            }
+            t += P.dt;
+        }
+        std::vector<int> comp(std::max(ns, 1));
+        std::vector<size_t> off(std::max(ns, 1));
+        for (int s = 0; s < ns; ++s) { comp[s] = srcs[s].comp; off[s] = srcs[s].off; }
+        d_src_comp.alloc(comp.size() * 4); d_src_off.alloc(off.size() * 8); d_src_vals.alloc(vals.size() * 8);
+        EMS_CUDA(cudaMemcpyAsync(d_src_comp.p, comp.data(), comp.size() * 4, cudaMemcpyHostToDevice, stream));
+        EMS_CUDA(cudaMemcpyAsync(d_src_off.p, off.data(), off.size() * 8, cudaMemcpyHostToDevice, stream));
+        EMS_CUDA(cudaMemcpyAsync(d_src_vals.p, vals.data(), vals.size() * 8, cudaMemcpyHostToDevice, stream));
+        // receivers
+        std::vector<int> start(std::max(nobs, 1), 0);
+        std::vector<size_t> roff;
+        for (int o = 0; o < nobs; ++o) {
+            start[o] = (int)roff.size();
+            for (int c = 0; c < 3; ++c)
+                for (auto &q : obs_lists[3 * o + c]) roff.push_back(ex_index(c, q.data()));
+        }
+        if (roff.empty()) roff.push_back(0);
+        d_obs_cnt.alloc(std::max<size_t>(obs_n.size(), 1) * 4);
+        d_obs_start.alloc(start.size() * 4);
+        d_obs_off.alloc(roff.size() * 8);
+        if (!obs_n.empty()) EMS_CUDA(cudaMemcpyAsync(d_obs_cnt.p, obs_n.data(), obs_n.size() * 4, cudaMemcpyHostToDevice, stream));
+        EMS_CUDA(cudaMemcpyAsync(d_obs_start.p, start.data(), start.size() * 4, cudaMemcpyHostToDevice, stream));
+        EMS_CUDA(cudaMemcpyAsync(d_obs_off.p, roff.data(), roff.size() * 8, cudaMemcpyHostToDevice, stream));
+        size_t ntr = (size_t)std::max(nobs, 1) * nsamp * 3;
+        d_traces.alloc(ntr * 8);
+        d_traces.zero(stream);
+
+        FdtdArgs<T> a = args<T>();
+        long long launches = 0;
+        EMS_CUDA(cudaEventRecord(ev0, stream));
+        for (int step = 1; step < nsteps + 1; ++step) {
+            launch_h<T>(a);
+            launch_e<T>(a);
+            launches += 2;
+            if (ns > 0) {
+                fdtd_source_kernel<T><<<1, 32, 0, stream>>>(a.Ex, a.Ey, a.Ez, d_src_comp.as<int>(), d_src_off.as<size_t>(),
+                                                           d_src_vals.as<double>() + (size_t)(step - 1) * ns, ns);
+                ++launches;
+            }
+            if (nobs > 0 && step % tf == 0) {
+                fdtd_receiver_kernel<T><<<(nobs + 127) / 128, 128, 0, stream>>>(
+                    a.Ex, a.Ey, a.Ez, nobs, d_obs_cnt.as<int>(), d_obs_start.as<int>(), d_obs_off.as<size_t>(),
+                    d_traces.as<double>() + (size_t)(step / tf) * 3, nsamp);
+                ++launches;
+            }
+        }
+        EMS_CUDA(cudaGetLastError());
+        EMS_CUDA(cudaEventRecord(ev1, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        float ms = 0;
+        EMS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        last_ms = ms;
+        last_launches = launches;
+        traces.assign(ntr, 0.0);
+        EMS_CUDA(cudaMemcpy(traces.data(), d_traces.p, ntr * 8, cudaMemcpyDeviceToHost));
+        traces.resize((size_t)nobs * nsamp * 3);
+    }
+
+    void run(int nsteps) override
+    {
+        EMS_CHECK_ARG(nsteps >= 0, "num_steps must be >= 0");
+        if (fp64) run_t<double>(nsteps); else run_t<float>(nsteps);
+    }
+
+    size_t field_size(int which) const override
+    {
+        if (which < 0 || which > 5) throw Error{EMS_ERR_INVALID_ARGUMENT, "field index must be 0..5 (Ex,Ey,Ez,Hx,Hy,Hz)"};
+        return n[which];
+    }
+    void get_field(int which, double *out) const override
+    {
+        size_t cnt = field_size(which);
+        if (fp64) {
+            EMS_CUDA(cudaMemcpy(out, F[which].p, cnt * 8, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> tmp(cnt);
+            EMS_CUDA(cudaMemcpy(tmp.data(), F[which].p, cnt * 4, cudaMemcpyDeviceToHost));
+            for (size_t q = 0; q < cnt; ++q) out[q] = tmp[q];
+        }
+    }
+    void set_field(int which, const double *in) override
+    {
+        size_t cnt = field_size(which);
+        if (fp64) {
+            EMS_CUDA(cudaMemcpy(F[which].p, in, cnt * 8, cudaMemcpyHostToDevice));
+        } else {
+            std::vector<float> tmp(in, in + cnt);
+            EMS_CUDA(cudaMemcpy(F[which].p, tmp.data(), cnt * 4, cudaMemcpyHostToDevice));
+        }
+    }
+
+    // fdtd_simulation.cpp:308-331: results_<i>_<dt>_<h>_<N>.csv in `path`
+    // (a directory; "." if empty), default stream precision, columns
+    // time,Ex,Ey,Ez with time = j*tf*dt.
+    void save(const char *path) const override
+    {
+        std::string dir = (path && *path) ? path : ".";
+        int nsteps_run = (nsamp - 1) * P.time_frequency;
+        for (int o = 0; o < nobs; ++o) {
+            std::string fn = dir + "/results_" + std::to_string(o) + "_" + std::to_string(P.dt) + "_" +
+                             std::to_string(P.h) + "_" + std::to_string(nsteps_run) + ".csv";
+            std::ofstream f(fn);
+            if (!f.is_open()) throw Error{EMS_ERR_IO, "cannot open " + fn};
+            f << "time,Ex,Ey,Ez" << std::endl;
+            for (int j = 0; j < nsamp; ++j) {
+                const double *r = &traces[((size_t)o * nsamp + j) * 3];
+                f << j * P.time_frequency * P.dt << "," << r[0] << "," << r[1] << "," << r[2] << std::endl;
+            }
+        }
+    }
+
+    void time_dominant(int launches, double *ms, double *bytes, std::string *name) override
+    {
+        // E update: reads H (3), reads and writes E (3), plus the material id
+        size_t w = fp64 ? 8 : 4;
+        size_t cells = (size_t)nx * ny * nz;
+        double b = (double)cells * 9.0 * w + (mat_host.empty() ? 0.0 : 2.0 * cells);
+        std::vector<DevBuf> save(3);
+        for (int q = 0; q < 3; ++q) {
+            save[q].alloc(F[q].bytes);
+            EMS_CUDA(cudaMemcpyAsync(save[q].p, F[q].p, F[q].bytes, cudaMemcpyDeviceToDevice, stream));
+        }
+        float t = 0;
+        if (fp64) { auto a = args<double>(); launch_e<double>(a); EMS_CUDA(cudaEventRecord(ev0, stream)); for (int r = 0; r < launches; ++r) launch_e<double>(a); }
+        else { auto a = args<float>(); launch_e<float>(a); EMS_CUDA(cudaEventRecord(ev0, stream)); for (int r = 0; r < launches; ++r) launch_e<float>(a); }
+        EMS_CUDA(cudaEventRecord(ev1, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        EMS_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
+        for (int q = 0; q < 3; ++q)
+            EMS_CUDA(cudaMemcpyAsync(F[q].p, save[q].p, F[q].bytes, cudaMemcpyDeviceToDevice, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        *ms = t / launches;
+        *bytes = b;
+        *name = fp64 ? "fdtd_e_kernel<double>" : "fdtd_e_kernel<float>";
+    }
+};
+
+Sim *make_fdtd(const ems_fdtd_params *p) { return new FdtdSim(p); }
+
+void fdtd_set_source(Sim *s, int comp, const int ijk[3], int waveform, double f0, double amp)
+{
+    auto *f = static_cast<FdtdSim *>(s);
+    EMS_CHECK_ARG(comp >= 0 && comp < 3, "component must be 0, 1 or 2");
+    EMS_CHECK_ARG(ijk != nullptr && f->in_e(comp, ijk), "source index outside the field array");
+    EMS_CHECK_ARG(waveform == EMS_WAVE_REFERENCE || waveform == EMS_WAVE_RICKER, "unknown waveform");
+    EMS_CHECK_ARG(f0 > 0 && std::isfinite(amp), "f0 must be positive");
+    FdtdSource q{comp, {ijk[0], ijk[1], ijk[2]}, waveform, f0, amp, f->ex_index(comp, ijk)};
+    f->srcs.push_back(q);
+}
+
+void fdtd_add_observation(Sim *s, const int *x, int nx_, const int *y, int ny_, const int *z, int nz_)
+{
+    auto *f = static_cast<FdtdSim *>(s);
+    const int *lists[3] = {x, y, z};
+    int cnt[3] = {nx_, ny_, nz_};
+    for (int c = 0; c < 3; ++c) {
+        EMS_CHECK_ARG(cnt[c] >= 0 && (cnt[c] == 0 || lists[c] != nullptr), "observation list missing");
+        std::vector<std::array<int, 3>> v;
+        for (int r = 0; r < cnt[c]; ++r) {
+            EMS_CHECK_ARG(f->in_e(c, lists[c] + 3 * r), "observation index outside the field array");
+            v.push_back({lists[c][3 * r], lists[c][3 * r + 1], lists[c][3 * r + 2]});
+        }
+        f->obs_lists.push_back(v);
+        f->obs_n.push_back(cnt[c]);
+    }
+}
+
+void fdtd_set_material(Sim *s, const double *eps, const double *sigma) { static_cast<FdtdSim *>(s)->set_material(eps, sigma); }
+
+}  // namespace ems

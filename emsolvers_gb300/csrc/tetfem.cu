@@ -1,0 +1,967 @@
+// Tetrahedral edge-element (Whitney / lowest-order Nedelec) FEM on one GPU.
+//
+// The reference has hexahedral elements only; this solver carries its
+// symplectic and leapfrog time loops (symplectic_2/fem_simulation.cpp:557-672,
+// symplectic_4/fem_simulation.cpp:1347-1350, fem_v2/fem_simulation.cpp:
+// 627-654) to a mesh of cubes split into six Kuhn tetrahedra:
+//
+//   DOF layout   edge slot 7*node + d, d over the 7 edge directions leaving a
+//                node; node-major, so the 7 edges of a node are contiguous.
+//   K apply      tet_curl_kernel: per tetrahedron, B_T = |T|/mu_T curl(E|_T)
+//                (3 values); tet_kick_kernel: per edge slot, the curl-
+//                transpose gathered over the slot's edge->element incidence
+//                list (deterministic, no atomics).
+//   mass inverse per-node 7x7 blocks, built and inverted in FP64 on the GPU
+//                (tet_minv_setup_kernel), stored packed symmetric in the run
+//                precision; applied inside the kick kernel by eight lanes per
+//                node exchanging values with warp shuffles.
+// Units are normalised (cube edge 1, c0 = 1); the API converts.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+
+#include "ems_internal.hpp"
+
+namespace ems {
+
+namespace {
+
+const int kPerm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+const int kLoc[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+const int kDir[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+
+struct Shape {
+    double grad[4][3];
+    int vert[4][3];
+    double curl[6][3], wint[6][3], wsq[6];
+};
+
+Shape make_shape(int p)
+{
+    Shape s{};
+    int a = kPerm[p][0], b = kPerm[p][1], c = kPerm[p][2];
+    s.grad[0][a] = -1.0;
+    s.grad[1][a] = 1.0; s.grad[1][b] = -1.0;
+    s.grad[2][b] = 1.0; s.grad[2][c] = -1.0;
+    s.grad[3][c] = 1.0;
+    s.vert[1][a] = 1;
+    s.vert[2][a] = 1; s.vert[2][b] = 1;
+    s.vert[3][0] = s.vert[3][1] = s.vert[3][2] = 1;
+    const double vol = 1.0 / 6.0;
+    for (int l = 0; l < 6; ++l) {
+        const double *gm = s.grad[kLoc[l][0]], *gn = s.grad[kLoc[l][1]];
+        s.curl[l][0] = 2.0 * (gm[1] * gn[2] - gm[2] * gn[1]);
+        s.curl[l][1] = 2.0 * (gm[2] * gn[0] - gm[0] * gn[2]);
+        s.curl[l][2] = 2.0 * (gm[0] * gn[1] - gm[1] * gn[0]);
+        for (int q = 0; q < 3; ++q) s.wint[l][q] = vol / 4.0 * (gn[q] - gm[q]);
+        double nn = gn[0] * gn[0] + gn[1] * gn[1] + gn[2] * gn[2];
+        double mm = gm[0] * gm[0] + gm[1] * gm[1] + gm[2] * gm[2];
+        double mn = gm[0] * gn[0] + gm[1] * gn[1] + gm[2] * gn[2];
+        s.wsq[l] = vol / 10.0 * (nn - mn + mm);
+    }
+    return s;
+}
+
+int dir_index(int dx, int dy, int dz)
+{
+    for (int d = 0; d < 7; ++d)
+        if (kDir[d][0] == dx && kDir[d][1] == dy && kDir[d][2] == dz) return d;
+    return -1;
+}
+
+}  // namespace
+
+// Shape tables in constant memory: curl of the six Whitney functions of each
+// of the six Kuhn tetrahedron types (scaled by nothing: unit cube).
+__constant__ float c_curl_f[6][6][3];
+__constant__ double c_curl_d[6][6][3];
+__constant__ double c_wint[6][6][3];
+__constant__ double c_wsq[6][6];
+__constant__ int c_dir[7][3];
+__constant__ unsigned char c_pack[7][7];   // packed symmetric index of (r,c)
+
+template <class T> __device__ __forceinline__ T curl_tab(int p, int l, int q);
+template <> __device__ __forceinline__ float curl_tab<float>(int p, int l, int q) { return c_curl_f[p][l][q]; }
+template <> __device__ __forceinline__ double curl_tab<double>(int p, int l, int q) { return c_curl_d[p][l][q]; }
+
+// ---------------------------------------------------------------- setup
+__device__ void sym3_eig(double A[3][3], double w[3], double V[3][3])
+{
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) V[i][j] = i == j ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 50; ++sweep) {
+        double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
+        if (off == 0.0) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                if (A[p][q] == 0.0) continue;
+                double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 3; ++k) {
+                    double akp = A[k][p], akq = A[k][q];
+                    A[k][p] = c * akp - s * akq;
+                    A[k][q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    double apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = c * apk - s * aqk;
+                    A[q][k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - s * vkq;
+                    V[k][q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    for (int i = 0; i < 3; ++i) w[i] = A[i][i];
+}
+
+__device__ void sym3_pinv(const double Ain[3][3], double P[3][3])
+{
+    double A[3][3], w[3], V[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) A[i][j] = Ain[i][j];
+    sym3_eig(A, w, V);
+    double mx = fmax(fabs(w[0]), fmax(fabs(w[1]), fabs(w[2])));
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double s = 0.0;
+            for (int k = 0; k < 3; ++k)
+                if (w[k] > 1e-10 * mx) s += V[i][k] * V[j][k] / w[k];
+            P[i][j] = s;
+        }
+}
+
+// Per-node inverse mass block in FP64: M_v = W S^+ W^T + alpha (I - D G^+ D^T)
+// over the node's active slots (W_i = sum_T eps_T int_T w_i, D_i the edge
+// vector, S = sym(D^T W), G = D^T D, alpha = mean consistent diagonal), then
+// inverted by Cholesky.  Writes 49 doubles per node; status[v] = 1 if the
+// block is not positive definite.
+__global__ void tet_minv_setup_kernel(size_t nnode, const unsigned char *__restrict__ pec, const int *__restrict__ inc_ptr,
+                                      const int *__restrict__ inc, const double *__restrict__ eps, double *__restrict__ minv,
+                                      int *__restrict__ status)
+{
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nnode) return;
+    double *B = minv + 49 * v;
+    for (int q = 0; q < 49; ++q) B[q] = 0.0;
+    int slot[7], k = 0;
+    for (int d = 0; d < 7; ++d)
+        if (!pec[7 * v + d]) slot[k++] = d;
+    if (k == 0) return;
+    double W[7][3], D[7][3], diag[7];
+    for (int r = 0; r < k; ++r) {
+        size_t e = 7 * v + slot[r];
+        W[r][0] = W[r][1] = W[r][2] = 0.0;
+        diag[r] = 0.0;
+        for (int q = 0; q < 3; ++q) D[r][q] = c_dir[slot[r]][q];
+        for (int s = inc_ptr[e]; s < inc_ptr[e + 1]; ++s) {
+            int t = inc[s] >> 3, l = inc[s] & 7, p = t % 6;
+            double ep = eps[t];
+            for (int q = 0; q < 3; ++q) W[r][q] += ep * c_wint[p][l][q];
+            diag[r] += ep * c_wsq[p][l];
+        }
+    }
+    double S[3][3], G[3][3], Sp[3][3], Gp[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            double s1 = 0.0, s2 = 0.0, g = 0.0;
+            for (int r = 0; r < k; ++r) { s1 += D[r][a] * W[r][b]; s2 += W[r][a] * D[r][b]; g += D[r][a] * D[r][b]; }
+            S[a][b] = 0.5 * (s1 + s2);
+            G[a][b] = g;
+        }
+    sym3_pinv(S, Sp);
+    sym3_pinv(G, Gp);
+    double alpha = 0.0;
+    for (int r = 0; r < k; ++r) alpha += diag[r];
+    alpha /= k;
+    double M[7][7], L[7][7], Li[7][7];
+    for (int r = 0; r < k; ++r)
+        for (int c = 0; c < k; ++c) {
+            double ws = 0.0, dq = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    ws += W[r][a] * Sp[a][b] * W[c][b];
+                    dq += D[r][a] * Gp[a][b] * D[c][b];
+                }
+            M[r][c] = ws + alpha * ((r == c ? 1.0 : 0.0) - dq);
+        }
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) { L[i][j] = 0.0; Li[i][j] = 0.0; }
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j <= i; ++j) {
+            double s = M[i][j];
+            for (int q = 0; q < j; ++q) s -= L[i][q] * L[j][q];
+            if (i == j) {
+                if (!(s > 0.0)) { status[v] = 1; return; }
+                L[i][i] = sqrt(s);
+            } else {
+                L[i][j] = s / L[j][j];
+            }
+        }
+    for (int i = 0; i < k; ++i) {
+        Li[i][i] = 1.0 / L[i][i];
+        for (int j = 0; j < i; ++j) {
+            double s = 0.0;
+            for (int q = j; q < i; ++q) s += L[i][q] * Li[q][j];
+            Li[i][j] = -s / L[i][i];
+        }
+    }
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) {
+            double s = 0.0;
+            for (int q = (i > j ? i : j); q < k; ++q) s += Li[q][i] * Li[q][j];
+            B[slot[i] * 7 + slot[j]] = s;
+        }
+}
+
+template <class T>
+__global__ void tet_pack_minv_kernel(size_t nnode, const double *__restrict__ full, T *__restrict__ packed)
+{
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nnode) return;
+    for (int r = 0; r < 7; ++r)
+        for (int c = r; c < 7; ++c) packed[28 * v + c_pack[r][c]] = (T)full[49 * v + 7 * r + c];
+}
+
+// ---------------------------------------------------------------- time step
+// B_T = |T|/mu_T * sum_l U_l curl(w_l)   (|T| = 1/6 on the unit cube)
+template <class T>
+__global__ void __launch_bounds__(256) tet_curl_kernel(size_t ntet, const int *__restrict__ tet_edge, const T *__restrict__ U,
+                                                       const T *__restrict__ mu_inv, T *__restrict__ Bx, T *__restrict__ By,
+                                                       T *__restrict__ Bz)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntet) return;
+    const int p = (int)(t % 6);
+    const int *e = tet_edge + 6 * t;
+    T c0 = 0, c1 = 0, c2 = 0;
+#pragma unroll
+    for (int l = 0; l < 6; ++l) {
+        T u = U[e[l]];
+        c0 = fma(u, curl_tab<T>(p, l, 0), c0);
+        c1 = fma(u, curl_tab<T>(p, l, 1), c1);
+        c2 = fma(u, curl_tab<T>(p, l, 2), c2);
+    }
+    T s = T(1.0 / 6.0);
+    if (mu_inv) s *= mu_inv[t];
+    Bx[t] = s * c0;
+    By[t] = s * c1;
+    Bz[t] = s * c2;
+}
+
+// Curl-transpose gathered for slot e: F_e = sum over (t,l) in inc(e) of B_t . curl(w_l).
+template <class T>
+__device__ __forceinline__ T gather_force(size_t e, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                                          const T *__restrict__ Bx, const T *__restrict__ By, const T *__restrict__ Bz)
+{
+    T f = 0;
+    const int s1 = inc_ptr[e + 1];
+    for (int s = inc_ptr[e]; s < s1; ++s) {
+        int code = inc[s];
+        int t = code >> 3, l = code & 7, p = t % 6;
+        f = fma(Bx[t], curl_tab<T>(p, l, 0), f);
+        f = fma(By[t], curl_tab<T>(p, l, 1), f);
+        f = fma(Bz[t], curl_tab<T>(p, l, 2), f);
+    }
+    return f;
+}
+
+// (Minv_v x)_d with x_j held by lane j of the node's 8-lane group.
+template <class T>
+__device__ __forceinline__ T block_apply(const T *__restrict__ mv, int d, T x, unsigned mask)
+{
+    T y = 0;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) {
+        T xj = __shfl_sync(mask, x, j, 8);
+        if (d < 7) y = fma(mv[c_pack[d < j ? d : j][d < j ? j : d]], xj, y);
+    }
+    return y;
+}
+
+// Kick + drift, eight lanes per node (lane 7 idle):
+//   P_e -= a * F_e (F = K U gathered, zero on PEC slots),
+//   U_e += c * (Minv_v P)_e.
+template <class T>
+__global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                                                       const unsigned char *__restrict__ pec, const T *__restrict__ Bx,
+                                                       const T *__restrict__ By, const T *__restrict__ Bz,
+                                                       const T *__restrict__ minv, T *__restrict__ P, T *__restrict__ U, T a, T c)
+{
+    size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t v = g >> 3;
+    int d = (int)(g & 7);
+    const unsigned mask = 0xffffffffu;
+    bool live = v < nnode && d < 7;
+    size_t e = 7 * v + d;
+    T p = 0;
+    if (live) {
+        p = P[e];
+        if (!pec[e]) p = fma(-a, gather_force<T>(e, inc_ptr, inc, Bx, By, Bz), p);
+        P[e] = p;
+    }
+    if (minv == nullptr) return;     // force-only use (uniform across the grid)
+    if (v >= nnode) v = nnode - 1;   // keep the whole warp in the shuffles
+    T y = block_apply<T>(minv + 28 * v, d, p, mask);
+    if (live && c != T(0)) U[e] = fma(c, y, U[e]);
+}
+
+// U += c * Minv P (drift alone).
+template <class T>
+__global__ void __launch_bounds__(256) tet_drift_kernel(size_t nnode, const T *__restrict__ minv, const T *__restrict__ P,
+                                                        T *__restrict__ U, T c)
+{
+    size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t v = g >> 3;
+    int d = (int)(g & 7);
+    bool live = v < nnode && d < 7;
+    size_t e = 7 * v + d;
+    T p = live ? P[e] : T(0);
+    if (v >= nnode) v = nnode - 1;
+    T y = block_apply<T>(minv + 28 * v, d, p, 0xffffffffu);
+    if (live) U[e] = fma(c, y, U[e]);
+}
+
+// Leapfrog: Unew = 2U - Uold - dt^2 Minv (K U); PEC slots stay zero.
+template <class T>
+__global__ void __launch_bounds__(256) tet_leapfrog_kernel(size_t nnode, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                                                           const unsigned char *__restrict__ pec, const T *__restrict__ Bx,
+                                                           const T *__restrict__ By, const T *__restrict__ Bz,
+                                                           const T *__restrict__ minv, const T *__restrict__ U,
+                                                           const T *__restrict__ Uold, T *__restrict__ Unew, T dt2)
+{
+    size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t v = g >> 3;
+    int d = (int)(g & 7);
+    bool live = v < nnode && d < 7;
+    size_t e = 7 * v + d;
+    T f = 0;
+    if (live && !pec[e]) f = gather_force<T>(e, inc_ptr, inc, Bx, By, Bz);
+    if (v >= nnode) v = nnode - 1;
+    T y = block_apply<T>(minv + 28 * v, d, f, 0xffffffffu);
+    if (live) Unew[e] = pec[e] ? T(0) : fma(-dt2, y, T(2) * U[e] - Uold[e]);
+}
+
+// Point-dipole load, added by one thread in a fixed order:
+//   symplectic: P_e += a * f_e ;  leapfrog: Unew += dt^2 Minv f.
+template <class T>
+__global__ void tet_source_kernel(int n, const int *__restrict__ slot, const double *__restrict__ coef, const double *__restrict__ g,
+                                  int ndip, T *__restrict__ P, T a, const T *__restrict__ minv, T *__restrict__ Unew, T dt2)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int k = 0; k < n; ++k) {
+        double f = coef[k] * g[k / 6];
+        if (P) P[slot[k]] += a * (T)f;
+        if (Unew) {
+            int v = slot[k] / 7, dd = slot[k] % 7;
+            for (int j = 0; j < 7; ++j) {
+                T m = minv[28 * (size_t)v + c_pack[dd < j ? dd : j][dd < j ? j : dd]];
+                if (m != T(0)) Unew[7 * (size_t)v + j] += dt2 * m * (T)f;
+            }
+        }
+    }
+}
+
+// Receivers: E(x) = sum_l U[e_l] w_l(x), written as (Ex, Ey, Ez) at sample s.
+template <class T>
+__global__ void tet_receiver_kernel(int nrec, const int *__restrict__ edges, const double *__restrict__ w, const T *__restrict__ U,
+                                    double *__restrict__ tr, int nsamp, int s)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    double e[3] = {0, 0, 0};
+    for (int l = 0; l < 6; ++l) {
+        double u = (double)U[edges[6 * r + l]];
+        for (int q = 0; q < 3; ++q) e[q] += u * w[18 * r + 3 * l + q];
+    }
+    double *o = tr + ((size_t)r * nsamp + s) * 4;
+    o[1] = e[0]; o[2] = e[1]; o[3] = e[2];
+}
+
+// Block partial sums of x.y (deterministic two-pass reduction, FP64).
+__global__ void dot_partial_kernel(size_t n, const double *__restrict__ x, const double *__restrict__ y, double *__restrict__ part)
+{
+    __shared__ double sh[256];
+    double s = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) s += x[i] * y[i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+__global__ void scale_kernel(size_t n, double *x, double *y, double s)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) { x[i] *= s; y[i] *= s; }
+}
+
+// -------------------------------------------------------------- host side
+double tet_wave(int kind, double f0, double t)
+{
+    if (kind == EMS_WAVE_RICKER) {
+        double tau = t - std::sqrt(2.0) / f0;
+        return (1.0 - 2.0 * M_PI * M_PI * f0 * f0 * tau * tau) * std::exp(-M_PI * M_PI * f0 * f0 * tau * tau);
+    }
+    double delay = t - 1.0 / f0, zeta = 2.0 * M_PI * M_PI * f0 * f0;
+    return 2.0 * zeta * (2.0 * zeta * delay * delay - 1.0) * std::exp(0.0 - zeta * delay * delay) / (2.0 * zeta);
+}
+
+double stability_constant(int integrator)
+{
+    if (integrator != EMS_SYMP4) return 2.0;
+    double x1 = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0)), x2 = 1.0 - 2.0 * x1;
+    double sub[3] = {x1, x2, x1}, lo = 0.0, hi = 4.0;
+    for (int it = 0; it < 200; ++it) {
+        double mid = 0.5 * (lo + hi);
+        bool stable = true;
+        for (int s = 1; s <= 64 && stable; ++s) {
+            double w = mid * s / 64.0, A[2][2] = {{1, 0}, {0, 1}};
+            for (int q = 0; q < 3; ++q) {
+                double a = sub[q] * w;
+                double D[2][2] = {{1, a / 2}, {0, 1}}, K[2][2] = {{1, 0}, {-a, 1}}, T1[2][2], T2[2][2], R[2][2];
+                for (int i = 0; i < 2; ++i)
+                    for (int j = 0; j < 2; ++j) T1[i][j] = K[i][0] * D[0][j] + K[i][1] * D[1][j];
+                for (int i = 0; i < 2; ++i)
+                    for (int j = 0; j < 2; ++j) T2[i][j] = D[i][0] * T1[0][j] + D[i][1] * T1[1][j];
+                for (int i = 0; i < 2; ++i)
+                    for (int j = 0; j < 2; ++j) R[i][j] = T2[i][0] * A[0][j] + T2[i][1] * A[1][j];
+                std::memcpy(A, R, sizeof(A));
+            }
+            if (std::fabs(A[0][0] + A[1][1]) > 2.0) stable = false;
+        }
+        if (stable) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+struct Dipole {
+    int slot[6];
+    double coef[6];
+    int kind;
+    double f0n;   // normalised frequency
+};
+
+struct TetFemSim : Sim {
+    ems_tetfem_params P;
+    int nx, ny, nz;
+    size_t nnode, nslot, ntet;
+    bool fp64;
+    double c0 = 299792458.0;
+    double tscale;                  // seconds per normalised time unit (h / c0)
+    double dtn = 0.0, dt_lim_n = 0.0, lambda_max = 0.0;
+    std::vector<int> tet_edge_h, inc_ptr_h, inc_h;
+    std::vector<unsigned char> pec_h;
+    std::vector<double> eps_h;
+    DevBuf d_tet_edge, d_inc_ptr, d_inc, d_pec, d_eps, d_minv64, d_minv, d_B, d_U, d_P, d_Uold, d_status;
+    std::vector<Dipole> dips;
+    std::vector<std::array<int, 6>> rec_edges;
+    std::vector<std::array<double, 18>> rec_w;
+    DevBuf d_src_slot, d_src_coef, d_src_g, d_rec_e, d_rec_w, d_tr;
+    bool ready = false;
+    double cur_time = 0.0;          // normalised
+
+    explicit TetFemSim(const ems_tetfem_params *p) : Sim(Kind::TETFEM), P(*p)
+    {
+        nx = P.cells[0]; ny = P.cells[1]; nz = P.cells[2];
+        EMS_CHECK_ARG(nx > 0 && ny > 0 && nz > 0, "cell counts must be positive");
+        EMS_CHECK_ARG(P.h > 0, "h must be positive");
+        EMS_CHECK_ARG(P.order == 1, "only lowest-order (order 1) Nedelec tetrahedra are implemented");
+        EMS_CHECK_ARG(P.integrator == EMS_LEAPFROG || P.integrator == EMS_SYMP2 || P.integrator == EMS_SYMP4,
+                      "tetrahedral integrator must be EMS_LEAPFROG, EMS_SYMP2 or EMS_SYMP4");
+        EMS_CHECK_ARG(P.precision == EMS_FP64 || P.precision == EMS_FP32, "precision must be EMS_FP64 or EMS_FP32");
+        EMS_CHECK_ARG(P.dt >= 0 && P.time_frequency > 0, "dt must be >= 0 and time_frequency > 0");
+        if (P.cfl_fraction <= 0) P.cfl_fraction = 0.9;
+        EMS_CHECK_ARG(P.cfl_fraction < 1.0, "cfl_fraction must be below 1");
+        fp64 = P.precision == EMS_FP64;
+        tscale = P.h / c0;
+        nnode = (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+        nslot = 7 * nnode;
+        ntet = 6 * (size_t)nx * ny * nz;
+        EMS_CHECK_ARG(ntet < (size_t)1 << 28, "mesh too large for 28-bit element indices");
+        build_mesh();
+        eps_h.assign(ntet, 1.0);
+        init_stream();
+        upload_tables();
+        upload_mesh();
+    }
+
+    size_t node(int i, int j, int k) const { return (size_t)i + (size_t)(nx + 1) * ((size_t)j + (size_t)(ny + 1) * k); }
+
+    void build_mesh()
+    {
+        Shape sh[6];
+        for (int p = 0; p < 6; ++p) sh[p] = make_shape(p);
+        tet_edge_h.resize(6 * ntet);
+        for (int k = 0; k < nz; ++k)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i)
+                    for (int p = 0; p < 6; ++p) {
+                        size_t t = 6 * ((size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)) + p;
+                        for (int l = 0; l < 6; ++l) {
+                            const int *vm = sh[p].vert[kLoc[l][0]], *vn = sh[p].vert[kLoc[l][1]];
+                            int d = dir_index(vn[0] - vm[0], vn[1] - vm[1], vn[2] - vm[2]);
+                            tet_edge_h[6 * t + l] = (int)(7 * node(i + vm[0], j + vm[1], k + vm[2]) + d);
+                        }
+                    }
+        pec_h.assign(nslot, 0);
+        const int lim[3] = {nx, ny, nz};
+        for (int k = 0; k <= nz; ++k)
+            for (int j = 0; j <= ny; ++j)
+                for (int i = 0; i <= nx; ++i)
+                    for (int d = 0; d < 7; ++d) {
+                        int a[3] = {i, j, k}, b[3] = {i + kDir[d][0], j + kDir[d][1], k + kDir[d][2]};
+                        bool bad = b[0] > nx || b[1] > ny || b[2] > nz;
+                        for (int q = 0; q < 3 && !bad; ++q)
+                            if (a[q] == b[q] && (a[q] == 0 || a[q] == lim[q])) bad = true;
+                        pec_h[7 * node(i, j, k) + d] = bad ? 1 : 0;
+                    }
+        inc_ptr_h.assign(nslot + 1, 0);
+        for (size_t t = 0; t < ntet; ++t)
+            for (int l = 0; l < 6; ++l) inc_ptr_h[tet_edge_h[6 * t + l] + 1]++;
+        for (size_t s = 0; s < nslot; ++s) inc_ptr_h[s + 1] += inc_ptr_h[s];
+        inc_h.resize(6 * ntet);
+        std::vector<int> fill(nslot, 0);
+        for (size_t t = 0; t < ntet; ++t)
+            for (int l = 0; l < 6; ++l) {
+                int e = tet_edge_h[6 * t + l];
+                inc_h[inc_ptr_h[e] + fill[e]++] = (int)(t * 8 + l);
+            }
+    }
+
+    void upload_tables()
+    {
+        float cf[6][6][3];
+        double cd[6][6][3], wi[6][6][3], ws[6][6];
+        for (int p = 0; p < 6; ++p) {
+            Shape s = make_shape(p);
+            for (int l = 0; l < 6; ++l) {
+                for (int q = 0; q < 3; ++q) { cd[p][l][q] = s.curl[l][q]; cf[p][l][q] = (float)s.curl[l][q]; wi[p][l][q] = s.wint[l][q]; }
+                ws[p][l] = s.wsq[l];
+            }
+        }
+        unsigned char pk[7][7];
+        int q = 0;
+        for (int r = 0; r < 7; ++r)
+            for (int c = r; c < 7; ++c) pk[r][c] = pk[c][r] = (unsigned char)q++;
+        EMS_CUDA(cudaMemcpyToSymbol(c_curl_f, cf, sizeof(cf)));
+        EMS_CUDA(cudaMemcpyToSymbol(c_curl_d, cd, sizeof(cd)));
+        EMS_CUDA(cudaMemcpyToSymbol(c_wint, wi, sizeof(wi)));
+        EMS_CUDA(cudaMemcpyToSymbol(c_wsq, ws, sizeof(ws)));
+        EMS_CUDA(cudaMemcpyToSymbol(c_dir, kDir, sizeof(kDir)));
+        EMS_CUDA(cudaMemcpyToSymbol(c_pack, pk, sizeof(pk)));
+    }
+
+    template <class V> void up(DevBuf &d, const std::vector<V> &v)
+    {
+        d.alloc(v.size() * sizeof(V));
+        EMS_CUDA(cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, stream));
+    }
+
+    void upload_mesh()
+    {
+        up(d_tet_edge, tet_edge_h);
+        up(d_inc_ptr, inc_ptr_h);
+        up(d_inc, inc_h);
+        up(d_pec, pec_h);
+        size_t w = fp64 ? 8 : 4;
+        d_U.alloc(nslot * w); d_U.zero(stream);
+        d_P.alloc(nslot * w); d_P.zero(stream);
+        d_Uold.alloc(nslot * w); d_Uold.zero(stream);
+        d_B.alloc(3 * ntet * w);
+        d_minv.alloc(28 * nnode * w);
+        EMS_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    void set_material(const double *eps_r, const double *sigma)
+    {
+        EMS_CHECK_ARG(eps_r != nullptr, "eps_r required");
+        for (size_t t = 0; t < ntet; ++t) EMS_CHECK_ARG(std::isfinite(eps_r[t]) && eps_r[t] > 0, "eps_r must be positive");
+        if (sigma)
+            for (size_t t = 0; t < ntet; ++t)
+                if (sigma[t] != 0.0) throw Error{EMS_ERR_UNSUPPORTED, "conductivity in the tetrahedral solver is not supported"};
+        eps_h.assign(eps_r, eps_r + ntet);
+        ready = false;
+    }
+
+    // FP64 mass-inverse setup on the GPU, then the stability limit by power
+    // iteration (Rayleigh quotient x.Kx / x.Mx) and the time step.
+    void setup()
+    {
+        up(d_eps, eps_h);
+        d_minv64.alloc(49 * nnode * 8);
+        d_status.alloc(nnode * 4);
+        d_status.zero(stream);
+        unsigned nb = (unsigned)((nnode + 127) / 128);
+        tet_minv_setup_kernel<<<nb, 128, 0, stream>>>(nnode, d_pec.as<unsigned char>(), d_inc_ptr.as<int>(), d_inc.as<int>(),
+                                                      d_eps.as<double>(), d_minv64.as<double>(), d_status.as<int>());
+        EMS_CUDA(cudaGetLastError());
+        std::vector<int> st(nnode);
+        EMS_CUDA(cudaMemcpyAsync(st.data(), d_status.p, nnode * 4, cudaMemcpyDeviceToHost, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        for (int s : st)
+            if (s) throw Error{EMS_ERR_NOT_FINITE, "mass block is not positive definite"};
+        DevBuf minv_d;   // FP64 packed copy for the setup iterations
+        minv_d.alloc(28 * nnode * 8);
+        tet_pack_minv_kernel<double><<<nb, 128, 0, stream>>>(nnode, d_minv64.as<double>(), minv_d.as<double>());
+        if (fp64)
+            EMS_CUDA(cudaMemcpyAsync(d_minv.p, minv_d.p, 28 * nnode * 8, cudaMemcpyDeviceToDevice, stream));
+        else
+            tet_pack_minv_kernel<float><<<nb, 128, 0, stream>>>(nnode, d_minv64.as<double>(), d_minv.as<float>());
+        EMS_CUDA(cudaGetLastError());
+        if (P.dt > 0) {
+            dtn = P.dt / tscale;
+            lambda_max = power_iteration(minv_d, 300);
+            dt_lim_n = stability_constant(P.integrator) / std::sqrt(lambda_max);
+        } else {
+            lambda_max = power_iteration(minv_d, 300);
+            dt_lim_n = stability_constant(P.integrator) / std::sqrt(lambda_max);
+            dtn = P.cfl_fraction * dt_lim_n;
+        }
+        if (dtn >= dt_lim_n) throw Error{EMS_ERR_INVALID_ARGUMENT, "time step exceeds the stability limit of the integrator"};
+        d_minv64.release();
+        ready = true;
+    }
+
+    double dot(const DevBuf &x, const DevBuf &y, DevBuf &part)
+    {
+        const int nb = 512;
+        dot_partial_kernel<<<nb, 256, 0, stream>>>(nslot, x.as<double>(), y.as<double>(), part.as<double>());
+        std::vector<double> h(nb);
+        EMS_CUDA(cudaMemcpyAsync(h.data(), part.p, nb * 8, cudaMemcpyDeviceToHost, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        double s = 0.0;
+        for (double v : h) s += v;
+        return s;
+    }
+
+    // y = K x in FP64 through the curl kernel and a gather (kick with a = -1 on zero P)
+    void applyK64(const DevBuf &x, DevBuf &z, DevBuf &B)
+    {
+        unsigned nbt = (unsigned)((ntet + 255) / 256);
+        tet_curl_kernel<double><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), x.as<double>(), nullptr, B.as<double>(),
+                                                         B.as<double>() + ntet, B.as<double>() + 2 * ntet);
+        z.zero(stream);
+        unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
+        // P = 0, a = -1: P becomes +F; c = 0 leaves U untouched
+        tet_kick_kernel<double><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+                                                         B.as<double>(), B.as<double>() + ntet, B.as<double>() + 2 * ntet,
+                                                         nullptr, z.as<double>(), nullptr, -1.0, 0.0);
+    }
+
+    double power_iteration(const DevBuf &minv_d, int iters)
+    {
+        DevBuf x, z, p, B, part;
+        x.alloc(nslot * 8); z.alloc(nslot * 8); p.alloc(nslot * 8); B.alloc(3 * ntet * 8); part.alloc(512 * 8);
+        std::vector<double> x0(nslot);
+        unsigned long long st = 0x9E3779B97F4A7C15ull;
+        for (size_t e = 0; e < nslot; ++e) {
+            st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+            x0[e] = pec_h[e] ? 0.0 : ((double)(st >> 11) / 9007199254740992.0 - 0.5);
+        }
+        EMS_CUDA(cudaMemcpyAsync(x.p, x0.data(), nslot * 8, cudaMemcpyHostToDevice, stream));
+        unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
+        applyK64(x, p, B);                   // p = K x0
+        x.zero(stream);
+        tet_drift_kernel<double><<<nbn, 256, 0, stream>>>(nnode, minv_d.as<double>(), p.as<double>(), x.as<double>(), 1.0);
+        double lam = 0.0;
+        for (int it = 0; it < iters; ++it) {
+            applyK64(x, z, B);
+            double num = dot(x, z, part), den = dot(x, p, part);
+            lam = num / den;
+            EMS_CUDA(cudaMemcpyAsync(p.p, z.p, nslot * 8, cudaMemcpyDeviceToDevice, stream));
+            x.zero(stream);
+            tet_drift_kernel<double><<<nbn, 256, 0, stream>>>(nnode, minv_d.as<double>(), p.as<double>(), x.as<double>(), 1.0);
+            double nrm = dot(x, x, part);
+            scale_kernel<<<(unsigned)((nslot + 255) / 256), 256, 0, stream>>>(nslot, x.as<double>(), p.as<double>(), 1.0 / std::sqrt(nrm));
+        }
+        EMS_CUDA(cudaGetLastError());
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        return lam;
+    }
+
+    void locate(const double xn[3], double w[6][3], int edges[6]) const
+    {
+        int cell[3], lim[3] = {nx, ny, nz};
+        double s[3];
+        for (int q = 0; q < 3; ++q) {
+            int c = (int)std::floor(xn[q]);
+            c = std::max(0, std::min(c, lim[q] - 1));
+            cell[q] = c;
+            s[q] = xn[q] - c;
+        }
+        int ax[3] = {0, 1, 2};
+        for (int a = 1; a < 3; ++a)
+            for (int b = a; b > 0 && s[ax[b - 1]] < s[ax[b]]; --b) std::swap(ax[b], ax[b - 1]);
+        int p = 0;
+        for (; p < 6; ++p)
+            if (kPerm[p][0] == ax[0] && kPerm[p][1] == ax[1] && kPerm[p][2] == ax[2]) break;
+        double lam[4] = {1.0 - s[ax[0]], s[ax[0]] - s[ax[1]], s[ax[1]] - s[ax[2]], s[ax[2]]};
+        Shape sh = make_shape(p);
+        for (int l = 0; l < 6; ++l) {
+            int a = kLoc[l][0], b = kLoc[l][1];
+            for (int q = 0; q < 3; ++q) w[l][q] = lam[a] * sh.grad[b][q] - lam[b] * sh.grad[a][q];
+            const int *vm = sh.vert[a], *vn = sh.vert[b];
+            int d = dir_index(vn[0] - vm[0], vn[1] - vm[1], vn[2] - vm[2]);
+            edges[l] = (int)(7 * node(cell[0] + vm[0], cell[1] + vm[1], cell[2] + vm[2]) + d);
+        }
+    }
+
+    template <class T> void run_t(int nsteps)
+    {
+        if (!ready) setup();
+        const int tf = P.time_frequency;
+        nobs = (int)rec_edges.size();
+        nsamp = nsteps > 0 ? (nsteps - 1) / tf + 1 : 0;
+        ncols = 4;
+        // receivers
+        std::vector<int> re;
+        std::vector<double> rw;
+        for (int r = 0; r < nobs; ++r) {
+            re.insert(re.end(), rec_edges[r].begin(), rec_edges[r].end());
+            rw.insert(rw.end(), rec_w[r].begin(), rec_w[r].end());
+        }
+        if (re.empty()) { re.assign(6, 0); rw.assign(18, 0.0); }
+        up(d_rec_e, re);
+        up(d_rec_w, rw);
+        size_t ntr = (size_t)std::max(nobs, 1) * std::max(nsamp, 1) * 4;
+        d_tr.alloc(ntr * 8);
+        d_tr.zero(stream);
+        // sources: (slot, coef) pairs and per-substep waveform values
+        std::vector<int> sslot;
+        std::vector<double> scoef;
+        for (auto &d : dips)
+            for (int l = 0; l < 6; ++l) { sslot.push_back(d.slot[l]); scoef.push_back(d.coef[l]); }
+        int nsrc = (int)sslot.size();
+        if (sslot.empty()) { sslot.push_back(0); scoef.push_back(0.0); }
+        up(d_src_slot, sslot);
+        up(d_src_coef, scoef);
+        const double x1 = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0)), x2 = 1.0 - 2.0 * x1;
+        int nsub = P.integrator == EMS_SYMP4 ? 3 : 1;
+        double sub[3] = {dtn, 0, 0}, off[3] = {0, 0, 0};
+        if (nsub == 3) { sub[0] = x1 * dtn; sub[1] = x2 * dtn; sub[2] = x1 * dtn; off[1] = x1 * dtn; off[2] = (x1 + x2) * dtn; }
+        size_t nd = std::max<size_t>(dips.size(), 1);
+        std::vector<double> gv((size_t)std::max(nsteps, 1) * nsub * nd, 0.0);
+        std::vector<double> times(std::max(nsamp, 1), 0.0);
+        double t = cur_time;
+        for (int st = 0; st < nsteps; ++st) {
+            for (int q = 0; q < nsub; ++q)
+                for (size_t k = 0; k < dips.size(); ++k) {
+                    double tt = P.integrator == EMS_LEAPFROG ? t : t + off[q] + 0.5 * sub[q];
+                    gv[((size_t)st * nsub + q) * nd + k] = tet_wave(dips[k].kind, dips[k].f0n, tt);
+                }
+            if (st % tf == 0) times[st / tf] = t;
+            t += dtn;
+        }
+        up(d_src_g, gv);
+
+        const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
+        T *Bx = d_B.as<T>(), *By = Bx + ntet, *Bz = By + ntet;
+        long long launches = 0;
+        EMS_CUDA(cudaEventRecord(ev0, stream));
+        for (int st = 0; st < nsteps; ++st) {
+            if (nobs > 0 && st % tf == 0) {
+                tet_receiver_kernel<T><<<(nobs + 63) / 64, 64, 0, stream>>>(nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), d_U.as<T>(),
+                                                                           d_tr.as<double>(), nsamp, st / tf);
+                ++launches;
+            }
+            if (P.integrator == EMS_LEAPFROG) {
+                tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), d_U.as<T>(), nullptr, Bx, By, Bz);
+                tet_leapfrog_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+                                                                Bx, By, Bz, d_minv.as<T>(), d_U.as<T>(), d_P.as<T>(), d_Uold.as<T>(),
+                                                                (T)(dtn * dtn));
+                launches += 2;
+                if (nsrc) {
+                    tet_source_kernel<T><<<1, 32, 0, stream>>>(nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(),
+                                                               d_src_g.as<double>() + (size_t)st * nd, (int)dips.size(), nullptr, T(0),
+                                                               d_minv.as<T>(), d_Uold.as<T>(), (T)(dtn * dtn));
+                    ++launches;
+                }
+                // ring: P holds E^{n-1}; new level written into Uold
+                std::swap(d_P.p, d_U.p);      // P <- E^n
+                std::swap(d_U.p, d_Uold.p);   // U <- E^{n+1}, Uold <- E^{n-1} storage (overwritten next step)
+            } else {
+                for (int q = 0; q < nsub; ++q) {
+                    double a = sub[q];
+                    if (q == 0) {
+                        tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(), (T)(0.5 * a));
+                        ++launches;
+                    }
+                    tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), d_U.as<T>(), nullptr, Bx, By, Bz);
+                    ++launches;
+                    if (nsrc) {
+                        tet_source_kernel<T><<<1, 32, 0, stream>>>(nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(),
+                                                                   d_src_g.as<double>() + ((size_t)st * nsub + q) * nd,
+                                                                   (int)dips.size(), d_P.as<T>(), (T)a, nullptr, nullptr, T(0));
+                        ++launches;
+                    }
+                    double c = q + 1 < nsub ? 0.5 * a + 0.5 * sub[q + 1] : 0.5 * a;
+                    tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+                                                                Bx, By, Bz, d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(), (T)a, (T)c);
+                    ++launches;
+                }
+            }
+        }
+        EMS_CUDA(cudaGetLastError());
+        EMS_CUDA(cudaEventRecord(ev1, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        float ms = 0;
+        EMS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        last_ms = ms;
+        last_launches = launches;
+        cur_time = t;
+        traces.assign(ntr, 0.0);
+        EMS_CUDA(cudaMemcpy(traces.data(), d_tr.p, ntr * 8, cudaMemcpyDeviceToHost));
+        traces.resize((size_t)nobs * nsamp * 4);
+        for (int r = 0; r < nobs; ++r)
+            for (int s = 0; s < nsamp; ++s) traces[((size_t)r * nsamp + s) * 4] = times[s] * tscale;
+    }
+
+    void run(int nsteps) override
+    {
+        EMS_CHECK_ARG(nsteps >= 0, "num_steps must be >= 0");
+        if (fp64) run_t<double>(nsteps); else run_t<float>(nsteps);
+    }
+
+    size_t field_size(int which) const override
+    {
+        if (which < 0 || which > 1) throw Error{EMS_ERR_INVALID_ARGUMENT, "field index must be 0 (U) or 1 (P)"};
+        return nslot;
+    }
+    void get_field(int which, double *out) const override
+    {
+        const DevBuf &b = which == 0 ? d_U : d_P;
+        if (fp64) {
+            EMS_CUDA(cudaMemcpy(out, b.p, nslot * 8, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> tmp(nslot);
+            EMS_CUDA(cudaMemcpy(tmp.data(), b.p, nslot * 4, cudaMemcpyDeviceToHost));
+            for (size_t q = 0; q < nslot; ++q) out[q] = tmp[q];
+        }
+    }
+    void set_field(int which, const double *in) override
+    {
+        DevBuf &b = which == 0 ? d_U : d_P;
+        if (fp64) {
+            EMS_CUDA(cudaMemcpy(b.p, in, nslot * 8, cudaMemcpyHostToDevice));
+        } else {
+            std::vector<float> tmp(in, in + nslot);
+            EMS_CUDA(cudaMemcpy(b.p, tmp.data(), nslot * 4, cudaMemcpyHostToDevice));
+        }
+    }
+    void save(const char *path) const override
+    {
+        EMS_CHECK_ARG(path && *path, "file name required");
+        for (int o = 0; o < nobs; ++o) {
+            std::string fn = path;
+            if (o > 0) {
+                size_t dot = fn.rfind('.');
+                std::string suf = "_" + std::to_string(o);
+                if (dot == std::string::npos) fn += suf; else fn.insert(dot, suf);
+            }
+            std::ofstream f(fn);
+            if (!f.is_open()) throw Error{EMS_ERR_IO, "cannot open " + fn};
+            f << std::setprecision(15) << std::scientific << "time,Ex,Ey,Ez" << std::endl;
+            for (int s = 0; s < nsamp; ++s) {
+                const double *r = &traces[((size_t)o * nsamp + s) * 4];
+                f << r[0] << "," << r[1] << "," << r[2] << "," << r[3] << std::endl;
+            }
+        }
+    }
+
+    void time_dominant(int launches, double *ms, double *bytes, std::string *name) override
+    {
+        if (!ready) setup();
+        size_t w = fp64 ? 8 : 4;
+        DevBuf saveU, saveP;
+        saveU.alloc(d_U.bytes); saveP.alloc(d_P.bytes);
+        EMS_CUDA(cudaMemcpyAsync(saveU.p, d_U.p, d_U.bytes, cudaMemcpyDeviceToDevice, stream));
+        EMS_CUDA(cudaMemcpyAsync(saveP.p, d_P.p, d_P.bytes, cudaMemcpyDeviceToDevice, stream));
+        const unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
+        auto body = [&](auto tag) {
+            using T = decltype(tag);
+            T *Bx = d_B.as<T>(), *By = Bx + ntet, *Bz = By + ntet;
+            for (int r = 0; r <= launches; ++r) {
+                if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
+                tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+                                                            Bx, By, Bz, d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(), T(0), T(0));
+            }
+        };
+        if (fp64) body(double()); else body(float());
+        EMS_CUDA(cudaEventRecord(ev1, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        float t = 0;
+        EMS_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
+        EMS_CUDA(cudaMemcpyAsync(d_U.p, saveU.p, d_U.bytes, cudaMemcpyDeviceToDevice, stream));
+        EMS_CUDA(cudaMemcpyAsync(d_P.p, saveP.p, d_P.bytes, cudaMemcpyDeviceToDevice, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        *ms = t / launches;
+        // unique bytes of one kick: incidence list + row pointers + B (3 per
+        // tet) + P read/write + U read/write + packed mass blocks + PEC flags
+        *bytes = (double)(6 * ntet) * 4 + (double)(nslot + 1) * 4 + (double)(3 * ntet) * w + (double)nslot * 4 * w +
+                 (double)(28 * nnode) * w + (double)nslot;
+        *name = fp64 ? "tet_kick_kernel<double>" : "tet_kick_kernel<float>";
+    }
+};
+
+Sim *make_tetfem(const ems_tetfem_params *p) { return new TetFemSim(p); }
+
+void tetfem_set_material(Sim *s, const double *eps_r, const double *sigma) { static_cast<TetFemSim *>(s)->set_material(eps_r, sigma); }
+
+void tetfem_add_dipole(Sim *s, const double pos[3], const double dir[3], int waveform, double f0, double amp)
+{
+    auto *f = static_cast<TetFemSim *>(s);
+    EMS_CHECK_ARG(pos && dir, "position and direction required");
+    EMS_CHECK_ARG(waveform == EMS_WAVE_REFERENCE || waveform == EMS_WAVE_RICKER, "unknown waveform");
+    EMS_CHECK_ARG(f0 > 0 && std::isfinite(amp), "f0 must be positive");
+    double xn[3] = {pos[0] / f->P.h, pos[1] / f->P.h, pos[2] / f->P.h};
+    const int lim[3] = {f->nx, f->ny, f->nz};
+    for (int q = 0; q < 3; ++q) EMS_CHECK_ARG(xn[q] >= 0 && xn[q] <= lim[q], "dipole outside the domain");
+    EMS_CHECK_ARG(f->dips.size() < 64, "at most 64 dipoles");
+    double w[6][3];
+    Dipole d{};
+    f->locate(xn, w, d.slot);
+    // loads on PEC slots vanish (the force is zero there)
+    for (int l = 0; l < 6; ++l)
+        d.coef[l] = f->pec_h[d.slot[l]] ? 0.0 : (w[l][0] * dir[0] + w[l][1] * dir[1] + w[l][2] * dir[2]) * amp;
+    d.kind = waveform;
+    d.f0n = f0 * f->tscale;
+    f->dips.push_back(d);
+}
+
+void tetfem_add_receiver(Sim *s, const double pos[3])
+{
+    auto *f = static_cast<TetFemSim *>(s);
+    EMS_CHECK_ARG(pos != nullptr, "position required");
+    double xn[3] = {pos[0] / f->P.h, pos[1] / f->P.h, pos[2] / f->P.h};
+    const int lim[3] = {f->nx, f->ny, f->nz};
+    for (int q = 0; q < 3; ++q) EMS_CHECK_ARG(xn[q] >= 0 && xn[q] <= lim[q], "receiver outside the domain");
+    double w[6][3];
+    std::array<int, 6> e;
+    f->locate(xn, w, e.data());
+    std::array<double, 18> ww;
+    for (int l = 0; l < 6; ++l)
+        for (int q = 0; q < 3; ++q) ww[3 * l + q] = w[l][q];
+    f->rec_edges.push_back(e);
+    f->rec_w.push_back(ww);
+}
+
+void tetfem_time_step(const Sim *s, double *dt, double *lim)
+{
+    auto *f = const_cast<TetFemSim *>(static_cast<const TetFemSim *>(s));
+    if (!f->ready) f->setup();
+    if (dt) *dt = f->dtn * f->tscale;
+    if (lim) *lim = f->dt_lim_n * f->tscale;
+}
+
+}  // namespace ems

@@ -1,0 +1,172 @@
+/* ems.h — C ABI of libems, the GB300 (sm_103a) time-domain Maxwell engine.
+ *
+ * Drop-in for the time loops of EMSolvers (paths relative to its src/ tree):
+ *   fdtd/          Yee FDTD                 -> ems_fdtd_*
+ *   fem_v2/, symplectic_2/, symplectic_4/   -> ems_hexfem_* (leapfrog, symp2, symp4)
+ *   fem_abm/       Adams-Bashforth-Moulton  -> ems_hexfem_* with EMS_ABM
+ *   (new)          tetrahedral Nedelec FEM  -> ems_tetfem_*
+ * The reference exposes C++ classes named FemSimulation; each entry point
+ * below names the member it replaces.  Conventions:
+ *   - every function returns an int status: EMS_OK (0) or a negative code;
+ *     ems_last_error() gives a message for the handle;
+ *   - handles are independent (the reference keeps file-scope globals, so
+ *     only one instance per process works there); each handle owns its
+ *     device memory and one CUDA stream;
+ *   - the caller owns every host buffer passed in; plain pointers and sizes,
+ *     no library types cross the boundary;
+ *   - all sizes count elements, not bytes.
+ */
+#ifndef EMS_H
+#define EMS_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EMS_ABI_VERSION 1
+
+typedef struct ems_sim ems_sim;
+
+enum ems_status {
+    EMS_OK = 0,
+    EMS_ERR_INVALID_ARGUMENT = -1,  /* bad parameter, index out of domain, CFL violated */
+    EMS_ERR_CUDA = -2,              /* a CUDA runtime call failed */
+    EMS_ERR_OUT_OF_MEMORY = -3,     /* device or host allocation failed */
+    EMS_ERR_IO = -4,                /* file missing / unreadable / malformed */
+    EMS_ERR_STATE = -5,             /* call not valid in the handle's state */
+    EMS_ERR_DEVICE_TIMEOUT = -6,    /* a bounded device-side wait gave up */
+    EMS_ERR_NOT_FINITE = -7,        /* NaN/Inf detected in the fields */
+    EMS_ERR_UNSUPPORTED = -8        /* combination not implemented */
+};
+
+enum ems_precision { EMS_FP64 = 0, EMS_FP32 = 1 };
+enum ems_integrator { EMS_LEAPFROG = 0, EMS_SYMP2 = 1, EMS_SYMP4 = 2, EMS_ABM = 3 };
+enum ems_waveform {
+    EMS_WAVE_REFERENCE = 0,  /* the reference solver's own source function */
+    EMS_WAVE_RICKER = 1      /* Ricker wavelet, centre frequency f0, delay sqrt(2)/f0 */
+};
+
+int ems_abi_version(void);
+const char *ems_status_string(int status);
+const char *ems_last_error(const ems_sim *sim);
+/* Number of CUDA devices visible (0 when none); never fails. */
+int ems_device_count(void);
+
+/* ------------------------------------------------------------------ FDTD */
+typedef struct {
+    int grid[3];                /* cells nx, ny, nz */
+    double h;                   /* cell size [m] (reference: domain_size) */
+    double dt;                  /* time step [s] */
+    double permittivity;        /* background eps [F/m] */
+    double permeability;        /* mu [H/m] */
+    int time_frequency;         /* sample receivers every this many steps */
+    int precision;              /* EMS_FP64 (bit-identical to the reference) or EMS_FP32 */
+    int pml_cells;              /* CPML thickness on every face (0 = PEC only, as the reference) */
+    double pml_order;           /* polynomial grading m (default 3 if 0) */
+    double pml_kappa_max;       /* kappa_max (default 1 if 0) */
+    double pml_alpha_max;       /* alpha_max [S/m] */
+    double pml_reflection;      /* target normal reflection R0 (default 1e-6 if 0) */
+} ems_fdtd_params;
+
+/* Replaces FemSimulation::FemSimulation (fdtd/fdtd_simulation.cpp:38-53,
+ * layout 55-88).  Fields use the reference's padded layout: Ex (nx+1)(ny+2)(nz+2),
+ * Ey (nx+2)(ny+1)(nz+2), Ez (nx+2)(ny+2)(nz+1), Hx nx(ny+1)(nz+1),
+ * Hy (nx+1)ny(nz+1), Hz (nx+1)(ny+1)nz, x fastest. */
+int ems_fdtd_create(const ems_fdtd_params *params, ems_sim **out);
+/* Replaces setSource_x/_y/_z (fdtd/fdtd_simulation.cpp:90-106; injection
+ * 222-239).  component 0/1/2 = Ex/Ey/Ez; ijk is the padded-array index. */
+int ems_fdtd_set_source(ems_sim *sim, int component, const int ijk[3], int waveform, double f0, double amplitude);
+/* Replaces setObservationPoint (fdtd/fdtd_simulation.cpp:108-113): one
+ * receiver averaging n_x Ex samples, n_y Ey samples and n_z Ez samples
+ * (triples of padded indices).  As in the reference, an empty list gives NaN. */
+int ems_fdtd_add_observation(ems_sim *sim, const int *x_ijk, int n_x, const int *y_ijk, int n_y,
+                             const int *z_ijk, int n_z);
+/* New: per-cell absolute permittivity [F/m] and conductivity [S/m], arrays of
+ * nx*ny*nz (x fastest).  Each E sample takes the material of one owning cell
+ * (Ex(i,j,k) -> cell (min(i,nx-1), j-1, k-1), Ey -> (i-1, min(j,ny-1), k-1),
+ * Ez -> (i-1, j-1, min(k,nz-1))).  At most 65535 distinct (eps, sigma) pairs. */
+int ems_fdtd_set_material(ems_sim *sim, const double *eps, const double *sigma);
+
+/* --------------------------------------------------------- hexahedral FEM */
+typedef struct {
+    int order;                  /* element order 1..3 */
+    int grid[3];                /* fine grid (edges) per direction; elements = grid/order */
+    double h;                   /* fine cell size [m] (reference: domain_size) */
+    double dt;                  /* time step [s] */
+    double permittivity, permeability;
+    int time_frequency;
+    int use_ofem;               /* 1: kmat/{o}.csv, 0: kmat/lamped{o}.csv */
+    int integrator;             /* EMS_LEAPFROG (fem_v2), EMS_SYMP2, EMS_SYMP4, EMS_ABM */
+    int precision;              /* EMS_FP64 or EMS_FP32 */
+    const char *kmat_dir;       /* directory holding the element-matrix CSVs ("kmat" if NULL) */
+} ems_hexfem_params;
+
+/* Replaces FemSimulation::FemSimulation + calculateElementStiffnessMatrix of
+ * fem_v2/fem_simulation.cpp:89-160,458-490 (symplectic_2 scaling at 473).
+ * Field levels keep the reference layout: per component 3 levels of
+ * gx(gy+1)(gz+1) / (gx+1)gy(gz+1) / (gx+1)(gy+1)gz values.
+ * Leapfrog: levels rotate (E^{n-1}, E^n, E^{n+1}); symplectic: U, P, F. */
+int ems_hexfem_create(const ems_hexfem_params *params, ems_sim **out);
+/* Replaces setSource_x/_y/_z (fem_v2/fem_simulation.cpp:492-545): a point
+ * source on the fine-grid edge (i,j,k) of the given component. */
+int ems_hexfem_set_source(ems_sim *sim, int component, const int ijk[3]);
+/* Replaces setObservationPoint (fem_v2/fem_simulation.cpp:547-563). */
+int ems_hexfem_add_observation(ems_sim *sim, const int ijk[3]);
+
+/* -------------------------------------------------------- tetrahedral FEM */
+typedef struct {
+    int cells[3];               /* structured cube of cells, each split into 6 tetrahedra */
+    double h;                   /* cube edge [m] */
+    int order;                  /* Nedelec order (1) */
+    int integrator;             /* EMS_LEAPFROG, EMS_SYMP2, EMS_SYMP4 */
+    int precision;              /* EMS_FP64 or EMS_FP32 */
+    double dt;                  /* time step [s]; 0 = cfl_fraction x stability limit */
+    double cfl_fraction;        /* used when dt == 0 (default 0.9) */
+    int time_frequency;
+} ems_tetfem_params;
+
+int ems_tetfem_create(const ems_tetfem_params *params, ems_sim **out);
+/* Relative permittivity and conductivity [S/m] per tetrahedron (6 per cell,
+ * cells x fastest, tetrahedron index = 6*cell + permutation). sigma may be NULL. */
+int ems_tetfem_set_material(ems_sim *sim, const double *eps_r, const double *sigma);
+/* Point dipole at pos [m] with direction dir, Ricker (or reference) wavelet. */
+int ems_tetfem_add_dipole(ems_sim *sim, const double pos[3], const double dir[3], int waveform, double f0,
+                          double amplitude);
+/* Receiver recording E (x,y,z) at pos [m] by Whitney interpolation. */
+int ems_tetfem_add_receiver(ems_sim *sim, const double pos[3]);
+/* Time step in use (after automatic selection) and the stability limit. */
+int ems_tetfem_time_step(const ems_sim *sim, double *dt, double *dt_limit);
+
+/* ------------------------------------------------------ common operations */
+/* Replaces FemSimulation::run (fdtd :242-306, fem_v2 :1249-1320,
+ * symplectic_2/4 :1278-1351): advance num_steps steps, recording receivers.
+ * Blocks until the device work has finished. */
+int ems_run(ems_sim *sim, int num_steps);
+/* Trace table written by the last ems_run: nobs receivers x nsamp samples x
+ * ncols columns (FDTD: Ex,Ey,Ez; FEM: t,Ex,Ey,Ez). */
+int ems_trace_shape(const ems_sim *sim, int *nobs, int *nsamp, int *ncols);
+int ems_get_traces(const ems_sim *sim, double *out, size_t n);
+/* Replaces saveResults (fdtd :308-331 names results_<i>_<dt>_<h>_<N>.csv;
+ * fem_v2 :1322-1344 writes the given file name, one file per receiver with
+ * suffix _<i> when there is more than one). */
+int ems_save_results(const ems_sim *sim, const char *path);
+/* Field access in the reference layout, converted to/from double.
+ * FDTD: which 0..5 = Ex,Ey,Ez,Hx,Hy,Hz.  Hex FEM: which 0..2 = component
+ * x,y,z (all levels).  Tet FEM: 0 = U (edge values), 1 = P. */
+int ems_field_size(const ems_sim *sim, int which, size_t *n);
+int ems_get_field(const ems_sim *sim, int which, double *out, size_t n);
+int ems_set_field(ems_sim *sim, int which, const double *in, size_t n);
+/* Device time of the last ems_run [ms] and the number of kernel launches it
+ * made; the average device time of one launch of the dominant kernel, timed
+ * by CUDA events on the handle's stream over `launches` repeated launches on
+ * the current state (fields are restored afterwards). */
+int ems_last_run_stats(const ems_sim *sim, double *device_ms, long long *launches);
+int ems_time_dominant_kernel(ems_sim *sim, int launches, double *ms_per_launch, double *bytes_per_launch,
+                             char *name, size_t name_cap);
+int ems_destroy(ems_sim *sim);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -69,6 +69,34 @@ typedef struct {
 int orc_hexfem_run(const orc_hexfem_case *c, int nsteps, double *ef[3], double *traces);
 size_t orc_hexfem_ncomp(int gx, int gy, int gz, int comp);
 
+/* ----------------------------------------------------- tetrahedral FEM --- */
+typedef struct {
+    int nx, ny, nz;               /* cubes; 6 Kuhn tetrahedra each */
+    const double *eps_r;          /* per tetrahedron */
+    const double *mu_r;           /* per tetrahedron or NULL (= 1) */
+    int integrator;               /* ORC_LEAPFROG / ORC_SYMP2 / ORC_SYMP4 */
+    double dt;                    /* normalised time step */
+    int time_frequency;
+    int ndip;
+    const double *dip_pos, *dip_dir, *dip_f0, *dip_amp;   /* normalised units */
+    const int *dip_kind;          /* 1 = Ricker, 0 = Gaussian second derivative */
+    int nrec;
+    const double *rec_pos;
+} orc_tet_case;
+
+int orc_tet_run(const orc_tet_case *c, int nsteps, double *U, double *P, double *traces);
+int orc_tet_minv(int nx, int ny, int nz, const double *eps_r, double *minv);
+double orc_tet_lambda_max(int nx, int ny, int nz, const double *eps_r, const double *mu_inv, int iters);
+double orc_stability_constant(int integrator);
+double orc_tet_energy(int nx, int ny, int nz, const double *eps_r, const double *U, const double *P);
+double orc_tet_wave(int kind, double f0, double t);
+long orc_tet_locate(int nx, int ny, int nz, const double x[3], double w[6][3], int edges[6]);
+void orc_tet_shape(int p, double grad[4][3], int vert[4][3], double curl[6][3], double wint[6][3], double wsq[6]);
+int orc_tet_dir_index(int dx, int dy, int dz);
+void orc_sym3_eig(const double A[3][3], double w[3], double V[3][3]);
+void orc_sym3_pinv(const double A[3][3], double P[3][3]);
+int orc_spd_inverse7(double *A, int k);
+
 #ifdef __cplusplus
 }
 #endif

@@ -174,3 +174,88 @@ def hexfem_run(order, grid, h, dt, eps, mu, tf, integrator, kmat, nsteps, source
     if rc != 0:
         raise RuntimeError(f"orc_hexfem_run failed: {rc}")
     return traces[:len(observations)], ef
+
+
+# ------------------------------------------------------------ tetrahedral FEM
+class _TetCase(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("eps_r", _dp), ("mu_r", _dp),
+                ("integrator", C.c_int), ("dt", C.c_double), ("time_frequency", C.c_int),
+                ("ndip", C.c_int), ("dip_pos", _dp), ("dip_dir", _dp), ("dip_f0", _dp), ("dip_amp", _dp),
+                ("dip_kind", _ip), ("nrec", C.c_int), ("rec_pos", _dp)]
+
+
+def tet_sizes(n):
+    nx, ny, nz = n
+    nnode = (nx + 1) * (ny + 1) * (nz + 1)
+    return nnode, 7 * nnode, 6 * nx * ny * nz
+
+
+def _tlib():
+    L = lib()
+    L.orc_tet_lambda_max.restype = C.c_double
+    L.orc_stability_constant.restype = C.c_double
+    L.orc_tet_energy.restype = C.c_double
+    L.orc_tet_wave.restype = C.c_double
+    L.orc_tet_wave.argtypes = [C.c_int, C.c_double, C.c_double]
+    L.orc_tet_locate.restype = C.c_long
+    return L
+
+
+def tet_run(n, eps_r, integrator, dt, nsteps, tf=1, dipoles=(), receivers=(), mu_r=None, U=None, P=None):
+    """FP64 oracle of the tetrahedral solver in normalised units (cube edge 1,
+    c0 = 1).  dipoles: [(pos, dir, kind, f0, amp)]; receivers: [pos].
+    Returns (traces[nrec, nsamp, 4], U, P)."""
+    nnode, nslot, ntet = tet_sizes(n)
+    eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
+    assert eps.size == ntet
+    mu = None if mu_r is None else np.ascontiguousarray(mu_r, dtype=np.float64).reshape(-1)
+    U = np.zeros(nslot) if U is None else np.ascontiguousarray(U, dtype=np.float64).copy()
+    P = np.zeros(nslot) if P is None else np.ascontiguousarray(P, dtype=np.float64).copy()
+    c = _TetCase()
+    c.nx, c.ny, c.nz = n
+    c.eps_r, c.mu_r = _ptr(eps), _ptr(mu) if mu is not None else None
+    c.integrator, c.dt, c.time_frequency = integrator, dt, tf
+    dp = np.array([d[0] for d in dipoles] or [(0, 0, 0)], np.float64).reshape(-1)
+    dd = np.array([d[1] for d in dipoles] or [(0, 0, 1)], np.float64).reshape(-1)
+    dk = np.array([d[2] for d in dipoles] or [1], np.int32)
+    df = np.array([d[3] for d in dipoles] or [1.0], np.float64)
+    da = np.array([d[4] for d in dipoles] or [1.0], np.float64)
+    rp = np.array(list(receivers) or [(0, 0, 0)], np.float64).reshape(-1)
+    c.ndip, c.dip_pos, c.dip_dir, c.dip_kind, c.dip_f0, c.dip_amp = len(dipoles), _ptr(dp), _ptr(dd), _ptr(dk, _ip), _ptr(df), _ptr(da)
+    c.nrec, c.rec_pos = len(receivers), _ptr(rp)
+    nsamp = (nsteps - 1) // tf + 1 if nsteps > 0 else 0
+    tr = np.zeros((max(len(receivers), 1), max(nsamp, 1), 4))
+    rc = _tlib().orc_tet_run(C.byref(c), C.c_int(nsteps), _ptr(U), _ptr(P), _ptr(tr))
+    if rc != 0:
+        raise RuntimeError(f"orc_tet_run failed: {rc}")
+    return tr[:len(receivers), :nsamp], U, P
+
+
+def tet_minv(n, eps_r):
+    nnode, _, _ = tet_sizes(n)
+    out = np.zeros((nnode, 7, 7))
+    eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
+    if _tlib().orc_tet_minv(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(eps), _ptr(out)) != 0:
+        raise RuntimeError("mass block not positive definite")
+    return out
+
+
+def tet_lambda_max(n, eps_r, iters=300, mu_r=None):
+    eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
+    mui = None if mu_r is None else np.ascontiguousarray(1.0 / np.asarray(mu_r, np.float64).reshape(-1))
+    return _tlib().orc_tet_lambda_max(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(eps),
+                                      _ptr(mui) if mui is not None else None, C.c_int(iters))
+
+
+def stability_constant(integrator):
+    return _tlib().orc_stability_constant(C.c_int(integrator))
+
+
+def tet_energy(n, eps_r, U, P):
+    eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
+    return _tlib().orc_tet_energy(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(eps),
+                                  _ptr(np.ascontiguousarray(U, np.float64)), _ptr(np.ascontiguousarray(P, np.float64)))
+
+
+def tet_wave(kind, f0, t):
+    return _tlib().orc_tet_wave(kind, f0, t)

@@ -1,0 +1,137 @@
+"""FDTD on the GPU through the C ABI against the reference (golden fixtures
+produced by the unmodified reference) and the FP64 oracle.
+
+FP64 results must be bit-identical.  FP32 results are compared to the FP64
+oracle by relative L2 error with tolerance 2e-5 on fields and traces (single
+precision rounding over a few hundred steps)."""
+import numpy as np
+import pytest
+
+import golden_io
+import oracle
+from gpu_util import rel_l2
+import emsolvers_gb300 as ems
+
+pytestmark = pytest.mark.gpu
+EPS0, MU0 = 8.854187817e-12, 1.25663706212e-6
+FP32_TOL = 2e-5
+
+
+def field_errors(f, ref):
+    """Relative L2 error of each component, normalised by the norm of all
+    components of the same field (E or H): a component that is zero up to
+    round-off in FP64 (e.g. Hx of an x-directed dipole) is judged against the
+    field it belongs to."""
+    out = {}
+    for group in (("Ex", "Ey", "Ez"), ("Hx", "Hy", "Hz")):
+        norm = np.sqrt(sum(np.sum(np.asarray(ref[k], np.float64) ** 2) for k in group))
+        for k in group:
+            out[k] = np.linalg.norm((np.asarray(f[k], np.float64) - ref[k]).ravel()) / norm
+    return out
+
+
+def _run(m, precision):
+    nx, ny, nz = m["grid"]
+    s = ems.FdtdSimulation((nx, ny, nz), m["h"], m["dt"], m["eps"], m["mu"], m["tf"], precision=precision)
+    for c, p in m["sources"]:
+        [s.setSource_x, s.setSource_y, s.setSource_z][c](p)
+    for o in m["observations"]:
+        s.setObservationPoint(o)
+    s.run(m["nsteps"])
+    return s.traces(), s.fields()
+
+
+@pytest.mark.parametrize("case", list(golden_io.fdtd_cases()), ids=lambda c: c[0]["name"])
+def test_fp64_bitwise_equal_to_reference(case):
+    m, tr, fields = case
+    t, f = _run(m, ems.FP64)
+    assert np.array_equal(t, tr)
+    for k in fields:
+        assert np.array_equal(f[k], fields[k]), k
+
+
+@pytest.mark.parametrize("case", list(golden_io.fdtd_cases()), ids=lambda c: c[0]["name"])
+def test_fp32_within_tolerance_of_reference(case):
+    m, tr, fields = case
+    t, f = _run(m, ems.FP32)
+    assert rel_l2(t, tr) < FP32_TOL
+    for k, err in field_errors(f, fields).items():
+        assert err < FP32_TOL, k
+
+
+def _sphere_case(n=20, pml=0, sigma=0.0):
+    h = 1e-3
+    dt = 0.99 * h / (2.998e8 * np.sqrt(3))
+    zz, yy, xx = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    r = np.sqrt((xx + 0.5 - n / 2) ** 2 + (yy + 0.5 - n / 2) ** 2 + (zz + 0.5 - n / 2) ** 2)
+    eps = np.where(r < n / 4, 4.0, 1.0) * EPS0
+    sig = np.where(r < n / 4, sigma, 0.0)
+    return h, dt, eps, sig
+
+
+@pytest.mark.parametrize("pml,sigma", [(0, 0.0), (0, 0.02), (4, 0.0), (4, 0.01)])
+def test_fp64_materials_and_cpml_bitwise_equal_to_oracle(pml, sigma):
+    n = 20
+    h, dt, eps, sig = _sphere_case(n, pml, sigma)
+    c = n // 2
+    src = [(2, (c, c, c), ems.WAVE_RICKER, 10e9, 1.0)]
+    obs = [([(c + 3, c, c)], [(c, c + 3, c)], [(c + 4, c, c)]), ([], [], [(c, c + 5, c)])]
+    pmld = dict(cells=pml, m=3.0, kmax=2.0, amax=0.02, R0=1e-6) if pml else None
+    # oracle material table in the library's first-occurrence order
+    keys = {}
+    ids = np.zeros(eps.size, np.uint16)
+    for q, (e, s) in enumerate(zip(eps.ravel(), sig.ravel())):
+        ids[q] = keys.setdefault((e, s), len(keys))
+    table = sorted(keys.items(), key=lambda kv: kv[1])
+    mat = (ids.reshape(eps.shape), np.array([k[0] for k, _ in table]), np.array([k[1] for k, _ in table]))
+    tr_o, f_o = oracle.fdtd_run(n, n, n, h, dt, EPS0, MU0, 1, 60, src, obs, material=mat, pml=pmld)
+    s = ems.FdtdSimulation((n, n, n), h, dt, EPS0, MU0, 1, precision=ems.FP64, pml_cells=pml, pml_order=3.0,
+                           pml_kappa_max=2.0, pml_alpha_max=0.02, pml_reflection=1e-6)
+    s.set_material(eps, sig)
+    s.setSource_z((c, c, c), waveform=ems.WAVE_RICKER, f0=10e9)
+    for o in obs:
+        s.setObservationPoint(o)
+    s.run(60)
+    t = s.traces()
+    np.testing.assert_array_equal(t[0], tr_o[0])
+    assert np.isnan(t[1, 1:, 0]).all() and np.isnan(tr_o[1, 1:, 0]).all()  # empty list: 0/0 as the reference
+    np.testing.assert_array_equal(t[1, :, 2], tr_o[1, :, 2])
+    f = s.fields()
+    for k in f:
+        np.testing.assert_array_equal(f[k], f_o[k], err_msg=k)
+    # FP32 of the same case
+    s32 = ems.FdtdSimulation((n, n, n), h, dt, EPS0, MU0, 1, precision=ems.FP32, pml_cells=pml, pml_order=3.0,
+                             pml_kappa_max=2.0, pml_alpha_max=0.02, pml_reflection=1e-6)
+    s32.set_material(eps, sig)
+    s32.setSource_z((c, c, c), waveform=ems.WAVE_RICKER, f0=10e9)
+    for o in obs:
+        s32.setObservationPoint(o)
+    s32.run(60)
+    assert rel_l2(s32.traces()[0], tr_o[0]) < FP32_TOL
+    for k, err in field_errors(s32.fields(), f_o).items():
+        assert err < FP32_TOL, k
+
+
+def test_save_results_matches_reference_format(tmp_path):
+    m, tr, _ = next(iter(golden_io.fdtd_cases()))
+    nx, ny, nz = m["grid"]
+    s = ems.FdtdSimulation((nx, ny, nz), m["h"], m["dt"], m["eps"], m["mu"], m["tf"])
+    s.setSource_x(m["sources"][0][1])
+    s.setObservationPoint(m["observations"][0])
+    s.run(m["nsteps"])
+    s.saveResults(directory=str(tmp_path))
+    files = list(tmp_path.glob("results_0_*.csv"))
+    assert len(files) == 1
+    lines = files[0].read_text().splitlines()
+    assert lines[0] == "time,Ex,Ey,Ez"
+    assert len(lines) == m["nsteps"] // m["tf"] + 2
+    assert lines[1].startswith("0,0,0,0")
+
+
+def test_runs_are_deterministic():
+    m, _, _ = next(iter(golden_io.fdtd_cases()))
+    a, fa = _run(m, ems.FP32)
+    b, fb = _run(m, ems.FP32)
+    assert np.array_equal(a, b)
+    for k in fa:
+        assert np.array_equal(fa[k], fb[k])
