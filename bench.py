@@ -1,0 +1,292 @@
+"""Benchmark of the GB300 Maxwell engine on its headline workload.
+
+Workload (one bench step = one complete forward solve): lowest-order Nedelec
+FEM on a 32^3 cube of unit cells, each split into 6 tetrahedra (196,608 tets,
+238,688 edges), eps_r i.i.d. U[1,4] per tet (seeded), mu_r = 1, sigma = 0, PEC
+walls, 4th-order symplectic integrator, dt = 0.9 x the stability limit, 2000
+time steps, one Ricker dipole with f0 set for 10 cells per wavelength, 8
+receivers, FP32 fields.  Metric: DOF-updates/s (edges x time steps / time).
+
+`value`   device time of the solve (CUDA events on the solver's stream),
+          inputs resident, L2 flushed between solves.
+`e2e`     the same solve through the C ABI from host buffers: material upload,
+          FP64 mass-block setup and stability limit, time loop, trace download.
+`roofline` the dominant kernel (tet_kick_kernel) timed alone on the same state.
+`cpu_baseline` the FP64 oracle on the host cores over a bounded sample.
+A secondary object `fdtd_512` times the 512^3 FP32 Yee update with a 10-cell
+CPML (HBM-bound) for a bounded number of steps.
+
+`--impl reference` times the FP64 CPU oracle (the reference has no
+tetrahedral solver; this is the restated algorithm) with all host threads.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+C0 = 299792458.0
+N = 32
+STEPS_PER_SOLVE = 2000
+H = 1e-3
+SEED = 2024
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def workload():
+    ntet = 6 * N ** 3
+    rng = np.random.default_rng(SEED)
+    eps = rng.uniform(1.0, 4.0, ntet)
+    f0 = C0 / (10 * H * np.sqrt(eps.mean()))         # 10 cells per wavelength at the mean speed
+    src = (np.array([0.5, 0.5, 0.5]) * N + np.array([0.13, 0.27, 0.41])) * H
+    ang = np.arange(8) * np.pi / 4
+    recs = [np.array([N / 2 + 10 * np.cos(a), N / 2 + 10 * np.sin(a), N / 2 + 0.3]) * H for a in ang]
+    return eps, f0, src, recs
+
+
+def n_edges(n):
+    return 3 * n * (n + 1) ** 2 + 3 * n ** 2 * (n + 1) + n ** 3
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    def __init__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", delete=False, suffix=".csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = [l.split(",") for l in open(self.f.name).read().splitlines() if l.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) >= 9 for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def flush_l2(buf):
+    buf.zero_()
+
+
+def cpu_oracle_rate(steps, threads):
+    """FP64 oracle on `steps` time steps of the same case: DOF-updates/s."""
+    import oracle
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    eps, f0, src, recs = workload()
+    ts = H / C0
+    lam = None
+    dtn = 0.9 * oracle.stability_constant(oracle.SYMP4) / np.sqrt(oracle.tet_lambda_max((N, N, N), eps, 100)) if lam is None else lam
+    dip = (tuple(src / H), (0.0, 0.0, 1.0), 1, f0 * ts, 1.0)
+    t0 = time.perf_counter()
+    oracle.tet_run((N, N, N), eps, oracle.SYMP4, dtn, steps, 1, [dip], [tuple(r / H) for r in recs])
+    dt = time.perf_counter() - t0
+    return n_edges(N) * steps / dt, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    steps = 40
+    for _ in range(args.warmup):
+        cpu_oracle_rate(5, threads)
+    rates, secs = [], []
+    for _ in range(args.steps):
+        r, s = cpu_oracle_rate(steps, threads)
+        rates.append(r)
+        secs.append(s)
+    value = float(np.mean(rates))
+    sample = f"{steps} of {STEPS_PER_SOLVE} time steps per bench step (FP64 oracle, OpenMP)"
+    print(json.dumps({
+        "impl": "reference", "metric": "DOF-updates/s (32^3x6 tet Nedelec FEM, symp4, 2000 steps)", "value": value,
+        "unit": "DOF-updates/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * float(np.mean(secs)) * STEPS_PER_SOLVE / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "tet32_symp4_2000", "cells": N, "tets": 6 * N ** 3, "edges": n_edges(N),
+                   "integrator": "symp4", "steps_per_solve": STEPS_PER_SOLVE, "parallelism": "replicas"},
+        "cpu_baseline": {"value": value, "unit": "DOF-updates/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "DOF-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def fdtd_512(steps=60):
+    """512^3 FP32 Yee step with a 10-cell CPML: device rate and roofline of the E kernel."""
+    import emsolvers_gb300 as ems
+    n, h = 512, 1e-3
+    eps0, mu0 = 8.854187817e-12, 1.25663706212e-6
+    dt = 0.99 * h / (C0 * np.sqrt(3))
+    rng = np.random.default_rng(SEED)
+    nb = n // 16
+    blk_eps = 10 ** rng.uniform(0, 1, nb ** 3) * eps0
+    blk_sig = rng.uniform(0, 0.05, nb ** 3)
+    idx = (np.arange(n) // 16)
+    cell_blk = (idx[None, None, :] + nb * (idx[None, :, None] + nb * idx[:, None, None])).reshape(-1)
+    s = ems.FdtdSimulation((n, n, n), h, dt, eps0, mu0, 1, precision=ems.FP32, pml_cells=10, pml_order=3.0,
+                           pml_kappa_max=1.0, pml_alpha_max=0.0, pml_reflection=1e-6)
+    s.set_material(blk_eps[cell_blk], blk_sig[cell_blk])
+    del cell_blk
+    for q in range(4):
+        c = rng.integers(20, n - 20, 3)
+        s.setSource_z(tuple(int(v) for v in c), waveform=ems.WAVE_RICKER, f0=float(rng.uniform(5e9, 15e9)))
+    s.run(2)
+    s.run(steps)
+    ms, launches = s.run_stats()
+    kms, kbytes, kname = s.time_dominant_kernel(10)
+    cells = n ** 3
+    s.close()
+    return {"workload": "fdtd512_fp32_cpml10", "steps": steps, "ms_per_step": ms / steps,
+            "cell_updates_per_s": cells * steps / (ms * 1e-3),
+            "dof_updates_per_s": 6 * cells * steps / (ms * 1e-3),
+            "kernel": kname, "kernel_ms": kms, "kernel_bytes": kbytes, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
+
+
+def run_gpu(args):
+    import torch
+    import emsolvers_gb300 as ems
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    eps, f0, src, recs = workload()
+    ts = H / C0
+    sim = ems.TetFemSimulation((N, N, N), H, 1, ems.SYMP4, ems.FP32, dt=0.0, cfl_fraction=0.9, time_frequency=1)
+    sim.set_material(eps)
+    sim.add_dipole(src, (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0, 1.0)
+    for r in recs:
+        sim.add_receiver(r)
+    dt, lim = sim.time_step()
+    l2 = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(max(args.warmup, 3)):
+        sim.reset()
+        sim.run(STEPS_PER_SOLVE)
+    # ---- device-resident timing: K solves, L2 flushed between them
+    clocks = Clocks()
+    dev_ms, launches = [], 0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.reset()
+        flush_l2(l2)
+        torch.cuda.synchronize()
+        sim.run(STEPS_PER_SOLVE)
+        ms, nl = sim.run_stats()
+        dev_ms.append(ms)
+        launches += nl
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    total_ms = float(np.sum(dev_ms))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    dofs = n_edges(N)
+    value = world * dofs * STEPS_PER_SOLVE * args.steps / (total_ms * 1e-3)
+    traces = sim.traces()
+    # ---- end to end through the C ABI from host buffers
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush_l2(l2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sim.set_material(eps)          # host -> device, FP64 mass setup + stability limit
+        sim.reset()
+        sim.run(STEPS_PER_SOLVE)
+        tr = sim.traces()              # device -> host
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e = world * dofs * STEPS_PER_SOLVE * args.steps / (np.sum(e2e_ms) * 1e-3)
+    # ---- dominant kernel roofline
+    kms, kbytes, kname = sim.time_dominant_kernel(200)
+    peak, peak_kind = peaks()
+    achieved = kbytes / (kms * 1e-3) / 1e9
+    out = {
+        "metric": "DOF-updates/s (32^3x6 tet Nedelec FEM, symp4, 2000 steps)", "value": value, "unit": "DOF-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded eps_r U[1,4] per tet)",
+        "config": {"workload": "tet32_symp4_2000", "cells": N, "tets": 6 * N ** 3, "edges": dofs, "integrator": "symp4",
+                   "steps_per_solve": STEPS_PER_SOLVE, "dt_s": dt, "dt_limit_s": lim, "receivers": len(recs),
+                   "l2": "flushed between solves (512 MB write)", "parallelism": "replicas" if world > 1 else "single"},
+        "e2e": {"value": float(e2e), "unit": "DOF-updates/s", "h2d_bytes_per_step": int(eps.nbytes),
+                "d2h_bytes_per_step": int(tr.nbytes)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": kname, "kernel_us": kms * 1e3, "bytes_per_launch": kbytes,
+                     "peak_source": peak_kind},
+        "clocks": clk,
+        "wall_s": wall,
+    }
+    if rank == 0:
+        if not args.no_cpu:
+            r, s = cpu_oracle_rate(20, os.cpu_count() or 1)
+            out["cpu_baseline"] = {"value": r, "unit": "DOF-updates/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                   "sample": f"20 of {STEPS_PER_SOLVE} time steps, FP64 oracle, {s:.1f} s"}
+        if not args.no_fdtd:
+            try:
+                out["fdtd_512"] = fdtd_512()
+                out["fdtd_512"]["hbm_frac"] = out["fdtd_512"]["kernel_gbs"] / peak
+            except Exception as e:  # secondary measurement only
+                out["fdtd_512"] = {"error": str(e)}
+        print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fdtd", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

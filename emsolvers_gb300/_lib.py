@@ -90,6 +90,7 @@ def lib():
         "ems_set_field": (C.c_int, [vp, C.c_int, dp, C.c_size_t]),
         "ems_last_run_stats": (C.c_int, [vp, dp, C.POINTER(C.c_longlong)]),
         "ems_time_dominant_kernel": (C.c_int, [vp, C.c_int, dp, dp, C.c_char_p, C.c_size_t]),
+        "ems_reset": (C.c_int, [vp]),
         "ems_destroy": (C.c_int, [vp]),
     }
     for name, (res, args) in sig.items():

@@ -214,6 +214,11 @@ int ems_time_dominant_kernel(ems_sim *s, int launches, double *ms, double *bytes
         }
     });
 }
+int ems_reset(ems_sim *s)
+{
+    if (!s) return EMS_ERR_INVALID_ARGUMENT;
+    return guard(s, [&] { s->impl->reset(); });
+}
 int ems_destroy(ems_sim *s)
 {
     if (!s) return EMS_OK;

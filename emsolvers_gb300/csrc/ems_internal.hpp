@@ -68,6 +68,7 @@ struct Sim {
     virtual void set_field(int which, const double *in) = 0;
     virtual void save(const char *path) const = 0;
     virtual void time_dominant(int launches, double *ms, double *bytes, std::string *name) = 0;
+    virtual void reset() = 0;
 };
 
 // CSV element matrices in the reference format (fem_v2/fem_simulation.cpp:1477-1524).

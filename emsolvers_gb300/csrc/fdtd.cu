@@ -339,8 +339,14 @@ struct FdtdSim : Sim {
         std::map<std::pair<double, double>, int> ids;
         mat_host.assign(nc, 0);
         mat_eps.clear(); mat_sigma.clear();
+        double last_e = -1.0, last_s = -1.0;
+        int last_id = -1;
         for (size_t q = 0; q < nc; ++q) {
             double e = eps[q], s = sigma ? sigma[q] : 0.0;
+            if (e == last_e && s == last_s) {   // runs of equal material along x
+                mat_host[q] = (uint16_t)last_id;
+                continue;
+            }
             EMS_CHECK_ARG(std::isfinite(e) && e > 0 && std::isfinite(s) && s >= 0, "eps must be > 0 and sigma >= 0");
             auto key = std::make_pair(e, s);
             auto it = ids.find(key);
@@ -354,6 +360,7 @@ struct FdtdSim : Sim {
                 id = it->second;
             }
             mat_host[q] = (uint16_t)id;
+            last_e = e; last_s = s; last_id = id;
         }
         std::vector<double> ca(mat_eps.size()), cb(mat_eps.size());
         for (size_t m = 0; m < mat_eps.size(); ++m) {
@@ -541,6 +548,15 @@ struct FdtdSim : Sim {
                 f << j * P.time_frequency * P.dt << "," << r[0] << "," << r[1] << "," << r[2] << std::endl;
             }
         }
+    }
+
+    void reset() override
+    {
+        for (int q = 0; q < 6; ++q) F[q].zero(stream);
+        if (P.pml_cells > 0)
+            for (int c = 0; c < 3; ++c)
+                for (int r = 0; r < 2; ++r) { d_psiE[c][r].zero(stream); d_psiH[c][r].zero(stream); }
+        EMS_CUDA(cudaStreamSynchronize(stream));
     }
 
     void time_dominant(int launches, double *ms, double *bytes, std::string *name) override

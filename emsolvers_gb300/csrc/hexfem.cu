@@ -496,6 +496,14 @@ struct HexFemSim : Sim {
         }
     }
 
+    void reset() override
+    {
+        for (int q = 0; q < 3; ++q) lev[q].zero(stream);
+        l0 = 0; l1 = 1; l2 = 2;
+        cur_time = 0.0;
+        EMS_CUDA(cudaStreamSynchronize(stream));
+    }
+
     void time_dominant(int launches, double *ms, double *bytes, std::string *name) override
     {
         size_t w = fp64 ? 8 : 4;

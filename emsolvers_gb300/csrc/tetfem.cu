@@ -879,6 +879,13 @@ struct TetFemSim : Sim {
         }
     }
 
+    void reset() override
+    {
+        d_U.zero(stream); d_P.zero(stream); d_Uold.zero(stream);
+        cur_time = 0.0;
+        EMS_CUDA(cudaStreamSynchronize(stream));
+    }
+
     void time_dominant(int launches, double *ms, double *bytes, std::string *name) override
     {
         if (!ready) setup();

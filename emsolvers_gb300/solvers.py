@@ -66,6 +66,10 @@ class _Sim:
         self._check(lib().ems_time_dominant_kernel(self._h, launches, C.byref(ms), C.byref(b), name, 128))
         return ms.value, b.value, name.value.decode()
 
+    def reset(self):
+        """Zero all fields and rewind time (a freshly constructed solver)."""
+        self._check(lib().ems_reset(self._h))
+
     def close(self):
         if self._h:
             lib().ems_destroy(self._h)

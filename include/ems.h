@@ -164,6 +164,10 @@ int ems_set_field(ems_sim *sim, int which, const double *in, size_t n);
 int ems_last_run_stats(const ems_sim *sim, double *device_ms, long long *launches);
 int ems_time_dominant_kernel(ems_sim *sim, int launches, double *ms_per_launch, double *bytes_per_launch,
                              char *name, size_t name_cap);
+/* Zero every field level and rewind the simulation clock to t = 0, keeping
+ * mesh, materials, sources and receivers: the state a freshly constructed
+ * reference FemSimulation starts from. */
+int ems_reset(ems_sim *sim);
 int ems_destroy(ems_sim *sim);
 
 #ifdef __cplusplus

@@ -96,6 +96,8 @@ int orc_tet_dir_index(int dx, int dy, int dz);
 void orc_sym3_eig(const double A[3][3], double w[3], double V[3][3]);
 void orc_sym3_pinv(const double A[3][3], double P[3][3]);
 int orc_spd_inverse7(double *A, int k);
+int orc_tet_apply_op(int nx, int ny, int nz, const double *eps_r, const double *x, double *y);
+void orc_tet_pec_mask(int nx, int ny, int nz, unsigned char *mask);
 
 #ifdef __cplusplus
 }

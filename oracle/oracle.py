@@ -259,3 +259,24 @@ def tet_energy(n, eps_r, U, P):
 
 def tet_wave(kind, f0, t):
     return _tlib().orc_tet_wave(kind, f0, t)
+
+
+def tet_apply_op(n, eps_r, x):
+    """y = M^-1 K x of the tetrahedral scheme."""
+    _, nslot, _ = tet_sizes(n)
+    eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.zeros(nslot)
+    if _tlib().orc_tet_apply_op(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(eps), _ptr(x), _ptr(y)) != 0:
+        raise RuntimeError("mass block not positive definite")
+    return y
+
+
+def tet_pec_mask(n):
+    _, nslot, _ = tet_sizes(n)
+    m = np.zeros(nslot, np.uint8)
+    _tlib().orc_tet_pec_mask(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), m.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return m.astype(bool)
+
+
+TET_DIRS = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0], [1, 0, 1], [0, 1, 1], [1, 1, 1]], np.float64)

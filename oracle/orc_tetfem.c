@@ -543,3 +543,27 @@ double orc_tet_energy(int nx, int ny, int nz, const double *eps_r, const double 
     free_tetmesh(&m);
     return e;
 }
+
+/* y = M^-1 K x (x, y: nslot values); the spatial operator of the scheme. */
+int orc_tet_apply_op(int nx, int ny, int nz, const double *eps_r, const double *x, double *y)
+{
+    tetmesh m;
+    build_tetmesh(&m, nx, ny, nz);
+    double *minv = malloc(sizeof(double) * 49 * m.nnode);
+    if (build_minv(&m, eps_r, minv) != 0) { free(minv); free_tetmesh(&m); return -1; }
+    double *F = malloc(sizeof(double) * m.nslot), *cb = malloc(sizeof(double) * 3 * m.ntet);
+    apply_K_tet(&m, NULL, x, F, cb);
+    apply_minv(&m, minv, F, y);
+    free(F); free(cb); free(minv);
+    free_tetmesh(&m);
+    return 0;
+}
+
+/* Marks unused/PEC slots (1) for tests. */
+void orc_tet_pec_mask(int nx, int ny, int nz, unsigned char *mask)
+{
+    tetmesh m;
+    build_tetmesh(&m, nx, ny, nz);
+    memcpy(mask, m.pec, m.nslot);
+    free_tetmesh(&m);
+}

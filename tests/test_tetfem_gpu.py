@@ -1,0 +1,128 @@
+"""Tetrahedral FEM on the GPU through the C ABI against the FP64 oracle.
+
+Tolerances (relative L2): FP64 GPU vs FP64 oracle 1e-10 (the GPU merges the
+drifts inside a 4th-order step and sums gathers in a different order);
+FP32 GPU vs FP64 oracle 1e-4 on receiver traces, the bound the FP32 path
+must meet."""
+import numpy as np
+import pytest
+
+import oracle
+from gpu_util import rel_l2
+import emsolvers_gb300 as ems
+
+pytestmark = pytest.mark.gpu
+C0 = 299792458.0
+H = 1e-3
+TS = H / C0          # seconds per normalised time unit
+FP64_TOL = 1e-10
+FP32_TOL = 1e-4
+INTEG = {oracle.SYMP2: ems.SYMP2, oracle.SYMP4: ems.SYMP4, oracle.LEAPFROG: ems.LEAPFROG}
+
+
+def _case(n, seed):
+    _, nslot, ntet = oracle.tet_sizes(n)
+    rng = np.random.default_rng(seed)
+    eps = rng.uniform(1.0, 4.0, ntet)
+    dip = ((n[0] * 0.41, n[1] * 0.52, n[2] * 0.47), (0.2, 0.3, 1.0), 1, 0.08, 1.0)
+    recs = [(n[0] * 0.7, n[1] * 0.5, n[2] * 0.5), (n[0] * 0.25, n[1] * 0.3, n[2] * 0.6)]
+    return eps, dip, recs
+
+
+def _gpu(n, eps, dip, recs, integ, dtn, nsteps, precision, tf=1):
+    s = ems.TetFemSimulation(n, H, 1, INTEG[integ], precision, dt=dtn * TS, time_frequency=tf)
+    s.set_material(eps)
+    s.add_dipole(np.array(dip[0]) * H, dip[1], ems.WAVE_RICKER, dip[3] / TS, dip[4])
+    for r in recs:
+        s.add_receiver(np.array(r) * H)
+    s.run(nsteps)
+    return s
+
+
+@pytest.mark.parametrize("integ", [oracle.SYMP2, oracle.SYMP4, oracle.LEAPFROG])
+def test_fp64_matches_oracle(integ):
+    n = (6, 5, 4)
+    eps, dip, recs = _case(n, 7)
+    dtn = 0.8 * oracle.stability_constant(integ) / np.sqrt(oracle.tet_lambda_max(n, eps, 300))
+    tr_o, U_o, P_o = oracle.tet_run(n, eps, integ, dtn, 150, 2, [dip], recs)
+    s = _gpu(n, eps, dip, recs, integ, dtn, 150, ems.FP64, tf=2)
+    t = s.traces()
+    np.testing.assert_allclose(t[:, :, 0], tr_o[:, :, 0] * TS, rtol=1e-12)
+    assert rel_l2(t[:, :, 1:], tr_o[:, :, 1:]) < FP64_TOL
+    assert rel_l2(s.get_field(0), U_o) < FP64_TOL
+    assert rel_l2(s.get_field(1), P_o) < FP64_TOL
+
+
+@pytest.mark.parametrize("integ", [oracle.SYMP2, oracle.SYMP4])
+def test_fp32_traces_within_1e4_of_fp64_oracle(integ):
+    n = (12, 12, 12)
+    eps, dip, recs = _case(n, 11)
+    dtn = 0.9 * oracle.stability_constant(integ) / np.sqrt(oracle.tet_lambda_max(n, eps, 300))
+    tr_o, U_o, _ = oracle.tet_run(n, eps, integ, dtn, 400, 1, [dip], recs)
+    s = _gpu(n, eps, dip, recs, integ, dtn, 400, ems.FP32)
+    assert rel_l2(s.traces()[:, :, 1:], tr_o[:, :, 1:]) < FP32_TOL
+    assert rel_l2(s.get_field(0), U_o) < FP32_TOL
+
+
+@pytest.mark.parametrize("integ", [oracle.SYMP2, oracle.SYMP4, oracle.LEAPFROG])
+def test_automatic_time_step_matches_oracle_stability_limit(integ):
+    n = (8, 7, 6)
+    eps, _, _ = _case(n, 3)
+    s = ems.TetFemSimulation(n, H, 1, INTEG[integ], ems.FP32, dt=0.0, cfl_fraction=0.9)
+    s.set_material(eps)
+    dt, lim = s.time_step()
+    lim_o = oracle.stability_constant(integ) / np.sqrt(oracle.tet_lambda_max(n, eps, 600)) * TS
+    assert abs(lim - lim_o) / lim_o < 1e-5
+    assert abs(dt - 0.9 * lim) / dt < 1e-12
+
+
+def test_fp32_runs_are_bitwise_deterministic():
+    n = (10, 9, 8)
+    eps, dip, recs = _case(n, 5)
+    dtn = 0.8 * oracle.stability_constant(oracle.SYMP4) / np.sqrt(oracle.tet_lambda_max(n, eps, 200))
+    a = _gpu(n, eps, dip, recs, oracle.SYMP4, dtn, 100, ems.FP32)
+    b = _gpu(n, eps, dip, recs, oracle.SYMP4, dtn, 100, ems.FP32)
+    assert np.array_equal(a.traces(), b.traces())
+    assert np.array_equal(a.get_field(0), b.get_field(0))
+
+
+def test_gpu_symplectic_state_conserves_discrete_energy():
+    n = (6, 6, 6)
+    _, nslot, ntet = oracle.tet_sizes(n)
+    rng = np.random.default_rng(9)
+    eps = rng.uniform(1, 4, ntet)
+    pec = oracle.tet_pec_mask(n)
+    U0 = np.where(pec, 0.0, rng.standard_normal(nslot))
+    dtn = 0.4 * oracle.stability_constant(oracle.SYMP4) / np.sqrt(oracle.tet_lambda_max(n, eps, 300))
+    s = ems.TetFemSimulation(n, H, 1, ems.SYMP4, ems.FP64, dt=dtn * TS)
+    s.set_material(eps)
+    s.set_field(0, U0)
+    e0 = oracle.tet_energy(n, eps, U0, np.zeros(nslot))
+    errs = []
+    for _ in range(10):
+        s.run(30)
+        errs.append(abs(oracle.tet_energy(n, eps, s.get_field(0), s.get_field(1)) - e0) / e0)
+    assert max(errs) < 5e-3
+    assert max(errs[5:]) < 1.3 * max(errs[:5]) + 1e-12
+
+
+def test_conductivity_is_rejected_as_unsupported():
+    n = (4, 4, 4)
+    _, _, ntet = oracle.tet_sizes(n)
+    s = ems.TetFemSimulation(n, H, 1, ems.SYMP2, ems.FP32, dt=1e-13)
+    with pytest.raises(ems.EmsError) as e:
+        s.set_material(np.ones(ntet), np.full(ntet, 0.01))
+    assert e.value.status == -8
+
+
+def test_save_results_writes_reference_trace_format(tmp_path):
+    n = (6, 5, 4)
+    eps, dip, recs = _case(n, 7)
+    dtn = 0.5 * 2.0 / np.sqrt(oracle.tet_lambda_max(n, eps, 200))
+    s = _gpu(n, eps, dip, recs, oracle.SYMP2, dtn, 20, ems.FP32)
+    fn = tmp_path / "tet.csv"
+    s.saveResults = None
+    assert ems.lib().ems_save_results(s._h, str(fn).encode()) == 0
+    lines = fn.read_text().splitlines()
+    assert lines[0] == "time,Ex,Ey,Ez" and len(lines) == 21
+    assert (tmp_path / "tet_1.csv").exists()
