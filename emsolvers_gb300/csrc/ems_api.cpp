@@ -147,6 +147,12 @@ int ems_tetfem_time_step(const ems_sim *s, double *dt, double *lim)
     return guard(const_cast<ems_sim *>(s), [&] { ems::tetfem_time_step(s->impl, dt, lim); });
 }
 
+int ems_tetfem_apply_stiffness(ems_sim *s, const double *u, double *f, size_t n)
+{
+    NEED(s, ems::Kind::TETFEM);
+    return guard(s, [&] { ems::tetfem_apply_stiffness(s->impl, u, f, n); });
+}
+
 int ems_run(ems_sim *s, int n)
 {
     if (!s) return EMS_ERR_INVALID_ARGUMENT;

@@ -91,6 +91,7 @@ void tetfem_set_material(Sim *s, const double *eps_r, const double *sigma);
 void tetfem_add_dipole(Sim *s, const double pos[3], const double dir[3], int waveform, double f0, double amp);
 void tetfem_add_receiver(Sim *s, const double pos[3]);
 void tetfem_time_step(const Sim *s, double *dt, double *lim);
+void tetfem_apply_stiffness(Sim *s, const double *u, double *f, size_t n);
 
 // Source waveforms evaluated on the host in FP64.
 double fdtd_source_value(int kind, double f0, double t, double h);

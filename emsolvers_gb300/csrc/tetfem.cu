@@ -879,6 +879,32 @@ struct TetFemSim : Sim {
         }
     }
 
+    // f = K u through the curl kernel (per-tet scratch B) and the gather of
+    // the kick kernel (with P = 0 and a = -1 the kick leaves P = F).
+    void apply_stiffness(const double *u, double *f)
+    {
+        size_t w = fp64 ? 8 : 4;
+        DevBuf in, out;
+        in.alloc(nslot * w);
+        out.alloc(nslot * w);
+        out.zero(stream);
+        const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
+        auto body = [&](auto tag) {
+            using T = decltype(tag);
+            std::vector<T> h(u, u + nslot);
+            EMS_CUDA(cudaMemcpyAsync(in.p, h.data(), nslot * w, cudaMemcpyHostToDevice, stream));
+            T *Bx = d_B.as<T>(), *By = Bx + ntet, *Bz = By + ntet;
+            tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), in.as<T>(), nullptr, Bx, By, Bz);
+            tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+                                                        Bx, By, Bz, nullptr, out.as<T>(), nullptr, T(-1), T(0));
+            EMS_CUDA(cudaGetLastError());
+            EMS_CUDA(cudaMemcpyAsync(h.data(), out.p, nslot * w, cudaMemcpyDeviceToHost, stream));
+            EMS_CUDA(cudaStreamSynchronize(stream));
+            for (size_t q = 0; q < nslot; ++q) f[q] = (double)h[q];
+        };
+        if (fp64) body(double()); else body(float());
+    }
+
     void reset() override
     {
         d_U.zero(stream); d_P.zero(stream); d_Uold.zero(stream);
@@ -961,6 +987,14 @@ void tetfem_add_receiver(Sim *s, const double pos[3])
         for (int q = 0; q < 3; ++q) ww[3 * l + q] = w[l][q];
     f->rec_edges.push_back(e);
     f->rec_w.push_back(ww);
+}
+
+void tetfem_apply_stiffness(Sim *s, const double *u, double *f, size_t n)
+{
+    auto *t = static_cast<TetFemSim *>(s);
+    EMS_CHECK_ARG(u && f, "input and output required");
+    EMS_CHECK_ARG(n == t->nslot, "vector length must be 7*(nx+1)*(ny+1)*(nz+1)");
+    t->apply_stiffness(u, f);
 }
 
 void tetfem_time_step(const Sim *s, double *dt, double *lim)

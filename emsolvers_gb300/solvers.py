@@ -212,6 +212,13 @@ class TetFemSimulation(_Sim):
         a = np.ascontiguousarray(pos, dtype=np.float64)
         self._check(lib().ems_tetfem_add_receiver(self._h, _dptr(a)))
 
+    def apply_stiffness(self, u):
+        """f = K u on edge-slot vectors (normalised units)."""
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        f = np.zeros_like(u)
+        self._check(lib().ems_tetfem_apply_stiffness(self._h, _dptr(u), _dptr(f), u.size))
+        return f
+
     def time_step(self):
         dt, lim = C.c_double(), C.c_double()
         self._check(lib().ems_tetfem_time_step(self._h, C.byref(dt), C.byref(lim)))

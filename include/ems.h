@@ -137,6 +137,13 @@ int ems_tetfem_add_dipole(ems_sim *sim, const double pos[3], const double dir[3]
 int ems_tetfem_add_receiver(ems_sim *sim, const double pos[3]);
 /* Time step in use (after automatic selection) and the stability limit. */
 int ems_tetfem_time_step(const ems_sim *sim, double *dt, double *dt_limit);
+/* One application of the stiffness operator, f = K u, on edge-slot vectors of
+ * 7*(nx+1)(ny+1)(nz+1) values (slot 7*node + d), in normalised units (cube
+ * edge 1, K = C^T diag(|T|/mu) C): the element-by-element curl followed by
+ * the curl-transpose gather of the time step (symplectic_2/fem_simulation.cpp
+ * :603-639 applies the hexahedral counterpart).  Computed in the handle's
+ * precision; PEC and unused slots of f are zero.  Does not touch the state. */
+int ems_tetfem_apply_stiffness(ems_sim *sim, const double *u, double *f, size_t n);
 
 /* ------------------------------------------------------ common operations */
 /* Replaces FemSimulation::run (fdtd :242-306, fem_v2 :1249-1320,

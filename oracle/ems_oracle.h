@@ -98,6 +98,22 @@ void orc_sym3_pinv(const double A[3][3], double P[3][3]);
 int orc_spd_inverse7(double *A, int k);
 int orc_tet_apply_op(int nx, int ny, int nz, const double *eps_r, const double *x, double *y);
 void orc_tet_pec_mask(int nx, int ny, int nz, unsigned char *mask);
+int orc_tet_apply_K(int nx, int ny, int nz, const double *x, double *f);
+
+/* ----------------------------------------- Adams-Bashforth-Moulton (hex) --- */
+typedef struct {
+    int gx, gy, gz;
+    double h, dt, eps, mu;
+    int time_frequency;
+    const double *lamped1;        /* kmat/lamped1.csv, 12 x 12 */
+    int nsrc; const int *src_comp; const int *src_ijk;
+    int ndip; const int *dip_ijk;   /* x-directed Hertz dipoles */
+    int nobs; const int *obs_n; const int *obs_ijk;
+} orc_abm_case;
+
+/* E[c], H[c]: 4 levels each (ring of 3 + scratch).  traces: nobs*(nsteps/tf+1)*3. */
+int orc_abm_run(const orc_abm_case *c, int nsteps, double *E[3], double *H[3], double *traces);
+void orc_abm_kmat(const double *lamped1, double *K);
 
 #ifdef __cplusplus
 }

@@ -280,3 +280,57 @@ def tet_pec_mask(n):
 
 
 TET_DIRS = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0], [1, 0, 1], [0, 1, 1], [1, 1, 1]], np.float64)
+
+
+def tet_apply_K(n, x):
+    """f = K x of the tetrahedral scheme (normalised units, mu_r = 1)."""
+    _, nslot, _ = tet_sizes(n)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    f = np.zeros(nslot)
+    _tlib().orc_tet_apply_K(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(x), _ptr(f))
+    return f
+
+
+# ------------------------------------------------- Adams-Bashforth-Moulton (hex)
+class _AbmCase(C.Structure):
+    _fields_ = [("gx", C.c_int), ("gy", C.c_int), ("gz", C.c_int),
+                ("h", C.c_double), ("dt", C.c_double), ("eps", C.c_double), ("mu", C.c_double),
+                ("time_frequency", C.c_int), ("lamped1", _dp),
+                ("nsrc", C.c_int), ("src_comp", _ip), ("src_ijk", _ip),
+                ("ndip", C.c_int), ("dip_ijk", _ip),
+                ("nobs", C.c_int), ("obs_n", _ip), ("obs_ijk", _ip)]
+
+
+def abm_run(grid, h, dt, eps, mu, tf, nsteps, lamped1, sources=(), dipoles=(), observations=(), E=None, H=None):
+    """FP64 oracle of fem_abm.  sources: [(comp, (i,j,k))]; dipoles: [(i,j,k)]
+    (x-directed); observations: [(xs, ys, zs)].  Returns (traces, E, H) with
+    E, H lists of 4-level arrays per component."""
+    gx, gy, gz = grid
+    sz = hexfem_sizes(gx, gy, gz)
+    E = [np.zeros(4 * n) for n in sz] if E is None else [np.ascontiguousarray(a, np.float64).copy() for a in E]
+    H = [np.zeros(4 * n) for n in sz] if H is None else [np.ascontiguousarray(a, np.float64).copy() for a in H]
+    km = np.ascontiguousarray(lamped1, np.float64)
+    c = _AbmCase()
+    c.gx, c.gy, c.gz, c.h, c.dt, c.eps, c.mu, c.time_frequency = gx, gy, gz, h, dt, eps, mu, tf
+    c.lamped1 = _ptr(km)
+    comp = np.array([s[0] for s in sources] or [0], np.int32)
+    sijk = np.array([s[1] for s in sources] or [(0, 0, 0)], np.int32).reshape(-1)
+    dijk = np.array(list(dipoles) or [(0, 0, 0)], np.int32).reshape(-1)
+    on = np.array([len(l) for o in observations for l in o] or [0], np.int32)
+    oi = np.array([p for o in observations for l in o for p in l] or [(0, 0, 0)], np.int32).reshape(-1)
+    c.nsrc, c.src_comp, c.src_ijk = len(sources), _ptr(comp, _ip), _ptr(sijk, _ip)
+    c.ndip, c.dip_ijk = len(dipoles), _ptr(dijk, _ip)
+    c.nobs, c.obs_n, c.obs_ijk = len(observations), _ptr(on, _ip), _ptr(oi, _ip)
+    nsamp = nsteps // tf + 1
+    tr = np.zeros((max(len(observations), 1), nsamp, 3))
+    Ea = (_dp * 3)(*[_ptr(a) for a in E])
+    Ha = (_dp * 3)(*[_ptr(a) for a in H])
+    if lib().orc_abm_run(C.byref(c), C.c_int(nsteps), Ea, Ha, _ptr(tr)) != 0:
+        raise RuntimeError("orc_abm_run failed")
+    return tr[:len(observations)], E, H
+
+
+def abm_kmat(lamped1):
+    K = np.zeros(144)
+    lib().orc_abm_kmat(_ptr(np.ascontiguousarray(lamped1, np.float64)), _ptr(K))
+    return K.reshape(12, 12)

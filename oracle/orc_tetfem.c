@@ -567,3 +567,15 @@ void orc_tet_pec_mask(int nx, int ny, int nz, unsigned char *mask)
     memcpy(mask, m.pec, m.nslot);
     free_tetmesh(&m);
 }
+
+/* f = K x (the stiffness operator alone). */
+int orc_tet_apply_K(int nx, int ny, int nz, const double *x, double *f)
+{
+    tetmesh m;
+    build_tetmesh(&m, nx, ny, nz);
+    double *cb = malloc(sizeof(double) * 3 * m.ntet);
+    apply_K_tet(&m, NULL, x, f, cb);
+    free(cb);
+    free_tetmesh(&m);
+    return 0;
+}

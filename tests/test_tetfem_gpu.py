@@ -126,3 +126,19 @@ def test_save_results_writes_reference_trace_format(tmp_path):
     lines = fn.read_text().splitlines()
     assert lines[0] == "time,Ex,Ey,Ez" and len(lines) == 21
     assert (tmp_path / "tet_1.csv").exists()
+
+
+@pytest.mark.parametrize("precision,tol", [(ems.FP64, 1e-13), (ems.FP32, 1e-6)])
+def test_apply_stiffness_matches_oracle(precision, tol):
+    n = (7, 6, 5)
+    _, nslot, ntet = oracle.tet_sizes(n)
+    rng = np.random.default_rng(13)
+    u = rng.standard_normal(nslot)
+    s = ems.TetFemSimulation(n, H, 1, ems.SYMP2, precision, dt=1e-13)
+    f = s.apply_stiffness(u)
+    f_o = oracle.tet_apply_K(n, u)
+    assert rel_l2(f, f_o) < tol
+    pec = oracle.tet_pec_mask(n)
+    assert np.all(f[pec] == 0.0)
+    # the solver state is untouched
+    assert np.all(s.get_field(0) == 0.0)
