@@ -17,6 +17,7 @@ $CXX -I"$REF/fdtd" "$HERE/ref_drivers/fdtd_ref_main.cpp" "$REF/fdtd/fdtd_simulat
 for v in fem_v2 symplectic_2 symplectic_4; do
   $CXX -I"$REF/$v" "$HERE/ref_drivers/femv2_ref_main.cpp" "$REF/$v/fem_simulation.cpp" -o "$OUT/${v}_ref" & pids+=($!)
 done
+$CXX -I"$REF/fem_abm" "$HERE/ref_drivers/abm_ref_main.cpp" "$REF/fem_abm/fem_simulation.cpp" -o "$OUT/fem_abm_ref" & pids+=($!)
 rc=0
 for p in "${pids[@]}"; do wait "$p" || rc=1; done
 exit $rc

@@ -41,6 +41,13 @@ FDTD_CASES = [
       ([(5, 5, 5)], [(5, 5, 5)], [(5, 5, 5), (6, 6, 5)])]),
 ]
 
+ABM_CASES = [
+    ("box9x8x7_point_and_dipole", (9, 8, 7), 0.1, 0.4, 2, 40, [(0, (3, 4, 3)), (2, (5, 4, 4))], [(4, 3, 3)],
+     [([(4, 4, 4)], [(3, 3, 4), (3, 4, 4), (4, 3, 4), (4, 4, 4)], [(3, 4, 3), (3, 4, 4), (4, 4, 3), (4, 4, 4)])]),
+    ("cube8_dipole", (8, 8, 8), 0.05, 0.6, 1, 30, [], [(3, 3, 3)],
+     [([(4, 4, 4), (3, 4, 4)], [(4, 4, 4)], [(4, 4, 4)])]),
+]
+
 FEM_CASES = []
 for variant in ("fem_v2", "symplectic_2", "symplectic_4"):
     for order, ofem in ((1, 1), (1, 0), (2, 1), (3, 1)):
@@ -85,6 +92,20 @@ def main():
                          eps=EPS0_FEM, mu=MU0, tf=2, nsteps=40, source=[src[0], list(src[1])], observation=list(obs)))
     out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
     np.savez_compressed(os.path.join(HERE, "femv2_cases.npz"), **out)
+    out = {}
+    meta = []
+    for name, g, h, dtf, tf, ns, src, dip, obs in ABM_CASES:
+        dt = dtf * h / (2.998e8 * np.sqrt(3))
+        tr, E, Hh = refrun.abm(g, h, dt, EPS0_FDTD, MU0, tf, ns, src, dip, obs)
+        out[f"{name}/traces"] = tr
+        for q in range(3):
+            out[f"{name}/E{q}"] = E[q]
+            out[f"{name}/H{q}"] = Hh[q]
+        meta.append(dict(name=name, grid=list(g), h=h, dt=float(dt), eps=EPS0_FDTD, mu=MU0, tf=tf, nsteps=ns,
+                         sources=[[c, list(p)] for c, p in src], dipoles=[list(p) for p in dip],
+                         observations=[[list(map(list, l)) for l in o] for o in obs]))
+    out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "abm_cases.npz"), **out)
     print("golden fixtures written to", HERE)
 
 

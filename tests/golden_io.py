@@ -29,3 +29,10 @@ def femv2_cases():
 
 def kmat_path(order, use_ofem):
     return os.path.join(KMAT_DIR, f"{order}.csv" if use_ofem else f"lamped{order}.csv")
+
+
+def abm_cases():
+    z, meta = load("abm_cases.npz")
+    for m in meta:
+        n = m["name"]
+        yield m, z[f"{n}/traces"], [z[f"{n}/E{q}"] for q in range(3)], [z[f"{n}/H{q}"] for q in range(3)]

@@ -70,3 +70,35 @@ def femv2(variant, order, use_ofem, grid, h, dt, eps, mu, tf, nsteps, src, obs):
         ef.append(np.frombuffer(raw[off:off + 8 * int(n)]).copy())
         off += 8 * int(n)
     return tr, ef
+
+
+def abm(grid, h, dt, eps, mu, tf, nsteps, sources, dipoles, observations):
+    """Reference fem_abm run.  sources: [(comp, (i,j,k))]; dipoles: [(i,j,k)]."""
+    gx, gy, gz = grid
+    lines = [f"{gx} {gy} {gz} {float(h)!r} {float(dt)!r} {float(eps)!r} {float(mu)!r} {tf} {nsteps}", str(len(sources))]
+    lines += [f"{c} {i} {j} {k}" for c, (i, j, k) in sources]
+    lines.append(str(len(dipoles)))
+    lines += [f"{i} {j} {k}" for (i, j, k) in dipoles]
+    lines.append(str(len(observations)))
+    for o in observations:
+        toks = []
+        for lst in o:
+            toks.append(str(len(lst)))
+            toks += [f"{i} {j} {k}" for (i, j, k) in lst]
+        lines.append(" ".join(toks))
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "o.bin")
+        subprocess.run([os.path.join(REF_BIN, "fem_abm_ref"), out], input="\n".join(lines) + "\n",
+                       text=True, check=True, stderr=subprocess.DEVNULL, stdout=subprocess.DEVNULL)
+        raw = open(out, "rb").read()
+    nobs, ns = np.frombuffer(raw[:8], np.int32)
+    off = 8
+    tr = np.frombuffer(raw[off:off + 8 * nobs * ns * 3]).reshape(nobs, ns, 3).copy()
+    off += 8 * nobs * ns * 3
+    sz = [gx * (gy + 1) * (gz + 1), (gx + 1) * gy * (gz + 1), (gx + 1) * (gy + 1) * gz]
+    fields = []
+    for q in range(6):
+        n = 4 * sz[q % 3]
+        fields.append(np.frombuffer(raw[off:off + 8 * n]).copy())
+        off += 8 * n
+    return tr, fields[:3], fields[3:]
