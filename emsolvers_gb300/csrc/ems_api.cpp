@@ -14,6 +14,11 @@ using ems::Sim;
 
 static thread_local std::string g_create_error;
 
+namespace ems {
+// Message for calls that have no handle; read back with ems_last_error(NULL).
+void record_error(const std::string &msg) { g_create_error = msg; }
+}  // namespace ems
+
 template <class F> static int guard(ems_sim *s, F &&f)
 {
     try {

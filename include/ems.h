@@ -144,6 +144,21 @@ int ems_tetfem_time_step(const ems_sim *sim, double *dt, double *dt_limit);
  * :603-639 applies the hexahedral counterpart).  Computed in the handle's
  * precision; PEC and unused slots of f are zero.  Does not touch the state. */
 int ems_tetfem_apply_stiffness(ems_sim *sim, const double *u, double *f, size_t n);
+/* The same f = K u for callers that cannot allocate device memory (their
+ * device memory belongs to another allocator, or they run in loops where
+ * cudaMalloc/cudaFree must not occur): FP32, on device arrays u and f of
+ * 7*(nx+1)(ny+1)(nz+1) floats owned by the caller, enqueued on `stream`
+ * (a cudaStream_t; NULL = the default stream).  This entry point has no
+ * counterpart in the reference.  It allocates nothing: the per-tetrahedron
+ * scratch is a fixed file-scope device array of 2^20 tetrahedra x 3 floats
+ * (12 MiB, held on every device that loads the library until exit); larger
+ * meshes are rejected with EMS_ERR_INVALID_ARGUMENT.  The first call on a
+ * device looks up the scratch address for that device (make that first call
+ * before any stream capture).  Every call shares the one scratch array, so
+ * calls that overlap on the GPU race; the scratch is fully overwritten before
+ * it is read, so nothing needs clearing between calls.  Errors are reported
+ * through ems_last_error(NULL). */
+int ems_tet_stiffness_apply_static(const int cells[3], const float *u, float *f, void *stream);
 
 /* ------------------------------------------------------ common operations */
 /* Replaces FemSimulation::run (fdtd :242-306, fem_v2 :1249-1320,
