@@ -77,16 +77,11 @@ int dir_index(int dx, int dy, int dz)
 
 // Shape tables in constant memory: curl of the six Whitney functions of each
 // of the six Kuhn tetrahedron types (scaled by nothing: unit cube).
-__constant__ float c_curl_f[6][6][3];
-__constant__ double c_curl_d[6][6][3];
 __constant__ double c_wint[6][6][3];
 __constant__ double c_wsq[6][6];
 __constant__ int c_dir[7][3];
 __constant__ unsigned char c_pack[7][7];   // packed symmetric index of (r,c)
 
-template <class T> __device__ __forceinline__ T curl_tab(int p, int l, int q);
-template <> __device__ __forceinline__ float curl_tab<float>(int p, int l, int q) { return c_curl_f[p][l][q]; }
-template <> __device__ __forceinline__ double curl_tab<double>(int p, int l, int q) { return c_curl_d[p][l][q]; }
 
 // ---------------------------------------------------------------- setup
 __device__ void sym3_eig(double A[3][3], double w[3], double V[3][3])
@@ -231,85 +226,161 @@ __global__ void tet_pack_minv_kernel(size_t nnode, const double *__restrict__ fu
 }
 
 // ---------------------------------------------------------------- time step
+template <class T> struct alignas(4 * sizeof(T)) vec4 {
+    T x, y, z, w;
+};
+
+__constant__ vec4<float> c_curl4_f[36];    // curl(w_l) of tetrahedron type p at [6p + l]
+__constant__ vec4<double> c_curl4_d[36];
+
+template <class T> __device__ __forceinline__ const vec4<T> *curl4_table();
+template <> __device__ __forceinline__ const vec4<float> *curl4_table<float>() { return c_curl4_f; }
+template <> __device__ __forceinline__ const vec4<double> *curl4_table<double>() { return c_curl4_d; }
+
+// The 36 curl vectors in shared memory: the lanes of a warp index them with
+// different (type, edge) pairs, which constant memory would serialise.
+template <class T> __device__ __forceinline__ void load_curl_table(vec4<T> *sc)
+{
+    if (threadIdx.x < 36) sc[threadIdx.x] = curl4_table<T>()[threadIdx.x];
+    __syncthreads();
+}
+
+// packed upper-triangle index of (r, c) in a symmetric 7x7 block
+__device__ __forceinline__ int pk7(int r, int c)
+{
+    int a = r < c ? r : c, b = r < c ? c : r;
+    return a * (13 - a) / 2 + b;
+}
+
 // B_T = |T|/mu_T * sum_l U_l curl(w_l)   (|T| = 1/6 on the unit cube)
 template <class T>
 __global__ void __launch_bounds__(256) tet_curl_kernel(size_t ntet, const int *__restrict__ tet_edge, const T *__restrict__ U,
-                                                       const T *__restrict__ mu_inv, T *__restrict__ Bx, T *__restrict__ By,
-                                                       T *__restrict__ Bz)
+                                                       const T *__restrict__ mu_inv, vec4<T> *__restrict__ B)
 {
+    __shared__ vec4<T> sc[36];
+    load_curl_table<T>(sc);
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntet) return;
     const int p = (int)(t % 6);
-    const int *e = tet_edge + 6 * t;
+    const int2 *e2 = reinterpret_cast<const int2 *>(tet_edge + 6 * t);
+    const int2 a = e2[0], b = e2[1], c = e2[2];
+    const int e[6] = {a.x, a.y, b.x, b.y, c.x, c.y};
     T c0 = 0, c1 = 0, c2 = 0;
 #pragma unroll
     for (int l = 0; l < 6; ++l) {
         T u = U[e[l]];
-        c0 = fma(u, curl_tab<T>(p, l, 0), c0);
-        c1 = fma(u, curl_tab<T>(p, l, 1), c1);
-        c2 = fma(u, curl_tab<T>(p, l, 2), c2);
+        vec4<T> cr = sc[6 * p + l];
+        c0 = fma(u, cr.x, c0);
+        c1 = fma(u, cr.y, c1);
+        c2 = fma(u, cr.z, c2);
     }
     T s = T(1.0 / 6.0);
     if (mu_inv) s *= mu_inv[t];
-    Bx[t] = s * c0;
-    By[t] = s * c1;
-    Bz[t] = s * c2;
+    vec4<T> o;
+    o.x = s * c0; o.y = s * c1; o.z = s * c2; o.w = T(0);
+    B[t] = o;
 }
 
-// Curl-transpose gathered for slot e: F_e = sum over (t,l) in inc(e) of B_t . curl(w_l).
+// Curl-transpose gathered for slot e over its incidence list (ascending
+// tetrahedron order): F_e = sum B_t . curl(w_l).  Up to six incidences are
+// issued unrolled (the Kuhn mesh has at most six); longer lists continue.
 template <class T>
 __device__ __forceinline__ T gather_force(size_t e, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
-                                          const T *__restrict__ Bx, const T *__restrict__ By, const T *__restrict__ Bz)
+                                          const vec4<T> *__restrict__ B, const vec4<T> *sc)
 {
+    const int s0 = inc_ptr[e], s1 = inc_ptr[e + 1];
     T f = 0;
-    const int s1 = inc_ptr[e + 1];
-    for (int s = inc_ptr[e]; s < s1; ++s) {
-        int code = inc[s];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        int s = s0 + k;
+        if (s < s1) {
+            int code = __ldg(inc + s);
+            int t = code >> 3, l = code & 7, p = t % 6;
+            vec4<T> b = B[t];
+            vec4<T> cr = sc[6 * p + l];
+            f = fma(b.x, cr.x, f);
+            f = fma(b.y, cr.y, f);
+            f = fma(b.z, cr.z, f);
+        }
+    }
+    for (int s = s0 + 6; s < s1; ++s) {
+        int code = __ldg(inc + s);
         int t = code >> 3, l = code & 7, p = t % 6;
-        f = fma(Bx[t], curl_tab<T>(p, l, 0), f);
-        f = fma(By[t], curl_tab<T>(p, l, 1), f);
-        f = fma(Bz[t], curl_tab<T>(p, l, 2), f);
+        vec4<T> b = B[t];
+        vec4<T> cr = sc[6 * p + l];
+        f = fma(b.x, cr.x, f);
+        f = fma(b.y, cr.y, f);
+        f = fma(b.z, cr.z, f);
     }
     return f;
 }
 
 // (Minv_v x)_d with x_j held by lane j of the node's 8-lane group.
 template <class T>
-__device__ __forceinline__ T block_apply(const T *__restrict__ mv, int d, T x, unsigned mask)
+__device__ __forceinline__ T block_apply(const T *__restrict__ mv, int d, T x)
 {
     T y = 0;
 #pragma unroll
     for (int j = 0; j < 7; ++j) {
-        T xj = __shfl_sync(mask, x, j, 8);
-        if (d < 7) y = fma(mv[c_pack[d < j ? d : j][d < j ? j : d]], xj, y);
+        T xj = __shfl_sync(0xffffffffu, x, j, 8);
+        if (d < 7) y = fma(mv[pk7(d, j)], xj, y);
     }
     return y;
 }
 
+// Point-dipole loads fused into the step kernels: entry k adds
+// coef[k] * g[dipole(k)] to slot[k]; g for this (step, substep) is read at
+// g + ((ctl[0]-1)*nsub + q)*nd (the step counter was advanced at the start of
+// the step by the receiver kernel).
+struct SrcArgs {
+    int n;
+    const int *slot;
+    const double *coef;
+    const double *g;
+    const int *ctl;
+    int nd, nsub, q;
+};
+
+__device__ __forceinline__ double source_load(const SrcArgs &s, size_t e)
+{
+    double f = 0.0;
+    if (s.n == 0) return f;
+    const double *g = s.g + ((size_t)(s.ctl[0] - 1) * s.nsub + s.q) * s.nd;
+    for (int k = 0; k < s.n; ++k)
+        if ((size_t)s.slot[k] == e) f += s.coef[k] * g[k / 6];
+    return f;
+}
+
 // Kick + drift, eight lanes per node (lane 7 idle):
-//   P_e -= a * F_e (F = K U gathered, zero on PEC slots),
+//   P_e -= a * (F_e - f_e)   (F = K U gathered, f the dipole load; PEC slots keep F = 0),
 //   U_e += c * (Minv_v P)_e.
+// With minv == nullptr only P is written (P -= a F): the stiffness apply.
 template <class T>
 __global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
-                                                       const unsigned char *__restrict__ pec, const T *__restrict__ Bx,
-                                                       const T *__restrict__ By, const T *__restrict__ Bz,
-                                                       const T *__restrict__ minv, T *__restrict__ P, T *__restrict__ U, T a, T c)
+                                                       const unsigned char *__restrict__ pec, const vec4<T> *__restrict__ B,
+                                                       const T *__restrict__ minv, T *__restrict__ P, T *__restrict__ U, T a, T c,
+                                                       SrcArgs src)
 {
+    __shared__ vec4<T> sc[36];
+    load_curl_table<T>(sc);
     size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t v = g >> 3;
     int d = (int)(g & 7);
-    const unsigned mask = 0xffffffffu;
     bool live = v < nnode && d < 7;
     size_t e = 7 * v + d;
     T p = 0;
     if (live) {
         p = P[e];
-        if (!pec[e]) p = fma(-a, gather_force<T>(e, inc_ptr, inc, Bx, By, Bz), p);
+        if (!pec[e]) {
+            T f = gather_force<T>(e, inc_ptr, inc, B, sc);
+            p = fma(-a, f, p);
+            if (src.n) p = fma(a, (T)source_load(src, e), p);
+        }
         P[e] = p;
     }
     if (minv == nullptr) return;     // force-only use (uniform across the grid)
     if (v >= nnode) v = nnode - 1;   // keep the whole warp in the shuffles
-    T y = block_apply<T>(minv + 28 * v, d, p, mask);
+    T y = block_apply<T>(minv + 28 * v, d, p);
     if (live && c != T(0)) U[e] = fma(c, y, U[e]);
 }
 
@@ -325,64 +396,63 @@ __global__ void __launch_bounds__(256) tet_drift_kernel(size_t nnode, const T *_
     size_t e = 7 * v + d;
     T p = live ? P[e] : T(0);
     if (v >= nnode) v = nnode - 1;
-    T y = block_apply<T>(minv + 28 * v, d, p, 0xffffffffu);
+    T y = block_apply<T>(minv + 28 * v, d, p);
     if (live) U[e] = fma(c, y, U[e]);
 }
 
-// Leapfrog: Unew = 2U - Uold - dt^2 Minv (K U); PEC slots stay zero.
+// Leapfrog: Unew = 2U - Uold - dt^2 Minv (K U - f); PEC slots stay zero.
 template <class T>
 __global__ void __launch_bounds__(256) tet_leapfrog_kernel(size_t nnode, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
-                                                           const unsigned char *__restrict__ pec, const T *__restrict__ Bx,
-                                                           const T *__restrict__ By, const T *__restrict__ Bz,
+                                                           const unsigned char *__restrict__ pec, const vec4<T> *__restrict__ B,
                                                            const T *__restrict__ minv, const T *__restrict__ U,
-                                                           const T *__restrict__ Uold, T *__restrict__ Unew, T dt2)
+                                                           const T *__restrict__ Uold, T *__restrict__ Unew, T dt2, SrcArgs src)
 {
+    __shared__ vec4<T> sc[36];
+    load_curl_table<T>(sc);
     size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t v = g >> 3;
     int d = (int)(g & 7);
     bool live = v < nnode && d < 7;
     size_t e = 7 * v + d;
     T f = 0;
-    if (live && !pec[e]) f = gather_force<T>(e, inc_ptr, inc, Bx, By, Bz);
+    if (live && !pec[e]) {
+        f = gather_force<T>(e, inc_ptr, inc, B, sc);
+        if (src.n) f -= (T)source_load(src, e);
+    }
     if (v >= nnode) v = nnode - 1;
-    T y = block_apply<T>(minv + 28 * v, d, f, 0xffffffffu);
+    T y = block_apply<T>(minv + 28 * v, d, f);
     if (live) Unew[e] = pec[e] ? T(0) : fma(-dt2, y, T(2) * U[e] - Uold[e]);
 }
 
-// Point-dipole load, added by one thread in a fixed order:
-//   symplectic: P_e += a * f_e ;  leapfrog: Unew += dt^2 Minv f.
+// Receivers and step counter, one block: at the start of step n = ctl[0],
+// record E(x) = sum_l w_l(x) U_l if n is a sampling step, then advance ctl.
+// With the symplectic drifts merged across steps the state holds
+// W = U + h Minv P; the receivers undo that half drift on their six slots.
 template <class T>
-__global__ void tet_source_kernel(int n, const int *__restrict__ slot, const double *__restrict__ coef, const double *__restrict__ g,
-                                  int ndip, T *__restrict__ P, T a, const T *__restrict__ minv, T *__restrict__ Unew, T dt2)
+__global__ void __launch_bounds__(1024) tet_receiver_kernel(int nrec, const int *__restrict__ edges, const double *__restrict__ w,
+                                                            const T *__restrict__ U, const T *__restrict__ P,
+                                                            const T *__restrict__ minv, T unmerge, double *__restrict__ tr,
+                                                            int nsamp, int tf, int *ctl)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int k = 0; k < n; ++k) {
-        double f = coef[k] * g[k / 6];
-        if (P) P[slot[k]] += a * (T)f;
-        if (Unew) {
-            int v = slot[k] / 7, dd = slot[k] % 7;
-            for (int j = 0; j < 7; ++j) {
-                T m = minv[28 * (size_t)v + c_pack[dd < j ? dd : j][dd < j ? j : dd]];
-                if (m != T(0)) Unew[7 * (size_t)v + j] += dt2 * m * (T)f;
+    const int step = ctl[0];
+    for (int r = threadIdx.x; r < nrec && step % tf == 0; r += blockDim.x) {
+        double acc[3] = {0, 0, 0};
+        for (int l = 0; l < 6; ++l) {
+            int e = edges[6 * r + l];
+            T u = U[e];
+            if (unmerge != T(0)) {
+                int v = e / 7, dd = e % 7;
+                T mp = 0;
+                for (int j = 0; j < 7; ++j) mp = fma(minv[28 * (size_t)v + pk7(dd, j)], P[7 * (size_t)v + j], mp);
+                u = fma(-unmerge, mp, u);
             }
+            for (int q = 0; q < 3; ++q) acc[q] += (double)u * w[18 * r + 3 * l + q];
         }
+        double *o = tr + ((size_t)r * nsamp + step / tf) * 4;
+        o[1] = acc[0]; o[2] = acc[1]; o[3] = acc[2];
     }
-}
-
-// Receivers: E(x) = sum_l U[e_l] w_l(x), written as (Ex, Ey, Ez) at sample s.
-template <class T>
-__global__ void tet_receiver_kernel(int nrec, const int *__restrict__ edges, const double *__restrict__ w, const T *__restrict__ U,
-                                    double *__restrict__ tr, int nsamp, int s)
-{
-    int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nrec) return;
-    double e[3] = {0, 0, 0};
-    for (int l = 0; l < 6; ++l) {
-        double u = (double)U[edges[6 * r + l]];
-        for (int q = 0; q < 3; ++q) e[q] += u * w[18 * r + 3 * l + q];
-    }
-    double *o = tr + ((size_t)r * nsamp + s) * 4;
-    o[1] = e[0]; o[2] = e[1]; o[3] = e[2];
+    __syncthreads();
+    if (threadIdx.x == 0) ctl[0] = step + 1;
 }
 
 // Block partial sums of x.y (deterministic two-pass reduction, FP64).
@@ -467,7 +537,7 @@ struct TetFemSim : Sim {
     std::vector<Dipole> dips;
     std::vector<std::array<int, 6>> rec_edges;
     std::vector<std::array<double, 18>> rec_w;
-    DevBuf d_src_slot, d_src_coef, d_src_g, d_rec_e, d_rec_w, d_tr;
+    DevBuf d_src_slot, d_src_coef, d_src_g, d_rec_e, d_rec_w, d_tr, d_ctl;
     bool ready = false;
     double cur_time = 0.0;          // normalised
 
@@ -554,8 +624,15 @@ struct TetFemSim : Sim {
         int q = 0;
         for (int r = 0; r < 7; ++r)
             for (int c = r; c < 7; ++c) pk[r][c] = pk[c][r] = (unsigned char)q++;
-        EMS_CUDA(cudaMemcpyToSymbol(c_curl_f, cf, sizeof(cf)));
-        EMS_CUDA(cudaMemcpyToSymbol(c_curl_d, cd, sizeof(cd)));
+        vec4<float> c4f[36];
+        vec4<double> c4d[36];
+        for (int p = 0; p < 6; ++p)
+            for (int l = 0; l < 6; ++l) {
+                c4f[6 * p + l] = vec4<float>{cf[p][l][0], cf[p][l][1], cf[p][l][2], 0.f};
+                c4d[6 * p + l] = vec4<double>{cd[p][l][0], cd[p][l][1], cd[p][l][2], 0.0};
+            }
+        EMS_CUDA(cudaMemcpyToSymbol(c_curl4_f, c4f, sizeof(c4f)));
+        EMS_CUDA(cudaMemcpyToSymbol(c_curl4_d, c4d, sizeof(c4d)));
         EMS_CUDA(cudaMemcpyToSymbol(c_wint, wi, sizeof(wi)));
         EMS_CUDA(cudaMemcpyToSymbol(c_wsq, ws, sizeof(ws)));
         EMS_CUDA(cudaMemcpyToSymbol(c_dir, kDir, sizeof(kDir)));
@@ -578,7 +655,7 @@ struct TetFemSim : Sim {
         d_U.alloc(nslot * w); d_U.zero(stream);
         d_P.alloc(nslot * w); d_P.zero(stream);
         d_Uold.alloc(nslot * w); d_Uold.zero(stream);
-        d_B.alloc(3 * ntet * w);
+        d_B.alloc(4 * ntet * w);
         d_minv.alloc(28 * nnode * w);
         EMS_CUDA(cudaStreamSynchronize(stream));
     }
@@ -645,24 +722,21 @@ struct TetFemSim : Sim {
         return s;
     }
 
-    // y = K x in FP64 through the curl kernel and a gather (kick with a = -1 on zero P)
+    // y = K x in FP64 through the curl kernel and the force-only kick (P = 0, a = -1)
     void applyK64(const DevBuf &x, DevBuf &z, DevBuf &B)
     {
         unsigned nbt = (unsigned)((ntet + 255) / 256);
-        tet_curl_kernel<double><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), x.as<double>(), nullptr, B.as<double>(),
-                                                         B.as<double>() + ntet, B.as<double>() + 2 * ntet);
+        tet_curl_kernel<double><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), x.as<double>(), nullptr, B.as<vec4<double>>());
         z.zero(stream);
         unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
-        // P = 0, a = -1: P becomes +F; c = 0 leaves U untouched
         tet_kick_kernel<double><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                         B.as<double>(), B.as<double>() + ntet, B.as<double>() + 2 * ntet,
-                                                         nullptr, z.as<double>(), nullptr, -1.0, 0.0);
+                                                         B.as<vec4<double>>(), nullptr, z.as<double>(), nullptr, -1.0, 0.0, SrcArgs{});
     }
 
     double power_iteration(const DevBuf &minv_d, int iters)
     {
         DevBuf x, z, p, B, part;
-        x.alloc(nslot * 8); z.alloc(nslot * 8); p.alloc(nslot * 8); B.alloc(3 * ntet * 8); part.alloc(512 * 8);
+        x.alloc(nslot * 8); z.alloc(nslot * 8); p.alloc(nslot * 8); B.alloc(4 * ntet * 8); part.alloc(512 * 8);
         std::vector<double> x0(nslot);
         unsigned long long st = 0x9E3779B97F4A7C15ull;
         for (size_t e = 0; e < nslot; ++e) {
@@ -717,6 +791,38 @@ struct TetFemSim : Sim {
         }
     }
 
+    // One time step: receivers (and the step counter), then for the
+    // symplectic steps curl + kick per substep with the drifts merged (the
+    // last one also carries the first half drift of the next step), or for
+    // leapfrog curl + leapfrog update.  Returns the number of launches.
+    template <class T>
+    int enqueue_step(T *Uc, T *Pc, T *Uo, const double *sub, int nsub, double hfirst, const SrcArgs &sa0, bool symp)
+    {
+        const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
+        vec4<T> *B = d_B.as<vec4<T>>();
+        tet_receiver_kernel<T><<<1, 256, 0, stream>>>(nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), Uc, Pc, d_minv.as<T>(),
+                                                      symp ? (T)hfirst : T(0), d_tr.as<double>(), nsamp, P.time_frequency,
+                                                      d_ctl.as<int>());
+        int nl = 1;
+        if (symp) {
+            for (int q = 0; q < nsub; ++q) {
+                SrcArgs sa = sa0;
+                sa.q = q;
+                double c = q + 1 < nsub ? 0.5 * (sub[q] + sub[q + 1]) : 0.5 * (sub[q] + sub[0]);
+                tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Uc, nullptr, B);
+                tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+                                                            B, d_minv.as<T>(), Pc, Uc, (T)sub[q], (T)c, sa);
+                nl += 2;
+            }
+        } else {
+            tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Uc, nullptr, B);
+            tet_leapfrog_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+                                                            B, d_minv.as<T>(), Uc, Pc, Uo, (T)(dtn * dtn), sa0);
+            nl += 2;
+        }
+        return nl;
+    }
+
     template <class T> void run_t(int nsteps)
     {
         if (!ready) setup();
@@ -724,7 +830,6 @@ struct TetFemSim : Sim {
         nobs = (int)rec_edges.size();
         nsamp = nsteps > 0 ? (nsteps - 1) / tf + 1 : 0;
         ncols = 4;
-        // receivers
         std::vector<int> re;
         std::vector<double> rw;
         for (int r = 0; r < nobs; ++r) {
@@ -737,7 +842,6 @@ struct TetFemSim : Sim {
         size_t ntr = (size_t)std::max(nobs, 1) * std::max(nsamp, 1) * 4;
         d_tr.alloc(ntr * 8);
         d_tr.zero(stream);
-        // sources: (slot, coef) pairs and per-substep waveform values
         std::vector<int> sslot;
         std::vector<double> scoef;
         for (auto &d : dips)
@@ -747,6 +851,7 @@ struct TetFemSim : Sim {
         up(d_src_slot, sslot);
         up(d_src_coef, scoef);
         const double x1 = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0)), x2 = 1.0 - 2.0 * x1;
+        const bool symp = P.integrator != EMS_LEAPFROG;
         int nsub = P.integrator == EMS_SYMP4 ? 3 : 1;
         double sub[3] = {dtn, 0, 0}, off[3] = {0, 0, 0};
         if (nsub == 3) { sub[0] = x1 * dtn; sub[1] = x2 * dtn; sub[2] = x1 * dtn; off[1] = x1 * dtn; off[2] = (x1 + x2) * dtn; }
@@ -757,64 +862,68 @@ struct TetFemSim : Sim {
         for (int st = 0; st < nsteps; ++st) {
             for (int q = 0; q < nsub; ++q)
                 for (size_t k = 0; k < dips.size(); ++k) {
-                    double tt = P.integrator == EMS_LEAPFROG ? t : t + off[q] + 0.5 * sub[q];
+                    double tt = symp ? t + off[q] + 0.5 * sub[q] : t;
                     gv[((size_t)st * nsub + q) * nd + k] = tet_wave(dips[k].kind, dips[k].f0n, tt);
                 }
             if (st % tf == 0) times[st / tf] = t;
             t += dtn;
         }
         up(d_src_g, gv);
-
-        const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
-        T *Bx = d_B.as<T>(), *By = Bx + ntet, *Bz = By + ntet;
+        d_ctl.alloc(16);
+        d_ctl.zero(stream);
+        SrcArgs sa{nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(), d_src_g.as<double>(), d_ctl.as<int>(), (int)nd, nsub, 0};
+        const double hfirst = 0.5 * sub[0];
+        const unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
+        // leapfrog ring: Uc = E^n, Pc = E^{n-1}, Uo = scratch for E^{n+1}
+        T *Uc = d_U.as<T>(), *Pc = d_P.as<T>(), *Uo = d_Uold.as<T>();
+        // one CUDA graph of kGraphSteps steps (a multiple of 3, so the
+        // leapfrog ring returns to the same assignment), replayed
+        constexpr int kGraphSteps = 12;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        int per_graph = 0;
+        const int nrep = nsteps / kGraphSteps;
+        if (nrep > 0) {
+            EMS_CUDA(cudaStreamSynchronize(stream));
+            EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            T *u = Uc, *p = Pc, *o = Uo;
+            for (int st = 0; st < kGraphSteps; ++st) {
+                per_graph += enqueue_step<T>(u, p, o, sub, nsub, hfirst, sa, symp);
+                if (!symp) { T *tmp = p; p = u; u = o; o = tmp; }
+            }
+            cudaError_t ce = cudaStreamEndCapture(stream, &graph);
+            if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
+            ce = cudaGraphInstantiate(&exec, graph, 0);
+            if (ce != cudaSuccess) {
+                cudaGraphDestroy(graph);
+                throw Error{EMS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+            }
+        }
         long long launches = 0;
         EMS_CUDA(cudaEventRecord(ev0, stream));
-        for (int st = 0; st < nsteps; ++st) {
-            if (nobs > 0 && st % tf == 0) {
-                tet_receiver_kernel<T><<<(nobs + 63) / 64, 64, 0, stream>>>(nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), d_U.as<T>(),
-                                                                           d_tr.as<double>(), nsamp, st / tf);
-                ++launches;
-            }
-            if (P.integrator == EMS_LEAPFROG) {
-                tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), d_U.as<T>(), nullptr, Bx, By, Bz);
-                tet_leapfrog_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                                Bx, By, Bz, d_minv.as<T>(), d_U.as<T>(), d_P.as<T>(), d_Uold.as<T>(),
-                                                                (T)(dtn * dtn));
-                launches += 2;
-                if (nsrc) {
-                    tet_source_kernel<T><<<1, 32, 0, stream>>>(nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(),
-                                                               d_src_g.as<double>() + (size_t)st * nd, (int)dips.size(), nullptr, T(0),
-                                                               d_minv.as<T>(), d_Uold.as<T>(), (T)(dtn * dtn));
-                    ++launches;
-                }
-                // ring: P holds E^{n-1}; new level written into Uold
-                std::swap(d_P.p, d_U.p);      // P <- E^n
-                std::swap(d_U.p, d_Uold.p);   // U <- E^{n+1}, Uold <- E^{n-1} storage (overwritten next step)
-            } else {
-                for (int q = 0; q < nsub; ++q) {
-                    double a = sub[q];
-                    if (q == 0) {
-                        tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(), (T)(0.5 * a));
-                        ++launches;
-                    }
-                    tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), d_U.as<T>(), nullptr, Bx, By, Bz);
-                    ++launches;
-                    if (nsrc) {
-                        tet_source_kernel<T><<<1, 32, 0, stream>>>(nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(),
-                                                                   d_src_g.as<double>() + ((size_t)st * nsub + q) * nd,
-                                                                   (int)dips.size(), d_P.as<T>(), (T)a, nullptr, nullptr, T(0));
-                        ++launches;
-                    }
-                    double c = q + 1 < nsub ? 0.5 * a + 0.5 * sub[q + 1] : 0.5 * a;
-                    tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                                Bx, By, Bz, d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(), (T)a, (T)c);
-                    ++launches;
-                }
-            }
+        if (symp) {
+            tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)hfirst);
+            ++launches;
+        }
+        for (int r = 0; r < nrep; ++r) EMS_CUDA(cudaGraphLaunch(exec, stream));
+        launches += (long long)nrep * per_graph;
+        for (int st = nrep * kGraphSteps; st < nsteps; ++st) {
+            launches += enqueue_step<T>(Uc, Pc, Uo, sub, nsub, hfirst, sa, symp);
+            if (!symp) { T *tmp = Pc; Pc = Uc; Uc = Uo; Uo = tmp; }
+        }
+        if (symp) {
+            tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)(-hfirst));
+            ++launches;
         }
         EMS_CUDA(cudaGetLastError());
         EMS_CUDA(cudaEventRecord(ev1, stream));
         EMS_CUDA(cudaStreamSynchronize(stream));
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (!symp) {   // keep the buffers in ring order: U = E^n, P = E^{n-1}
+            void *u = Uc, *p = Pc, *o = Uo;
+            d_U.p = u; d_P.p = p; d_Uold.p = o;
+        }
         float ms = 0;
         EMS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
         last_ms = ms;
@@ -893,10 +1002,10 @@ struct TetFemSim : Sim {
             using T = decltype(tag);
             std::vector<T> h(u, u + nslot);
             EMS_CUDA(cudaMemcpyAsync(in.p, h.data(), nslot * w, cudaMemcpyHostToDevice, stream));
-            T *Bx = d_B.as<T>(), *By = Bx + ntet, *Bz = By + ntet;
-            tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), in.as<T>(), nullptr, Bx, By, Bz);
+            vec4<T> *B = d_B.as<vec4<T>>();
+            tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), in.as<T>(), nullptr, B);
             tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                        Bx, By, Bz, nullptr, out.as<T>(), nullptr, T(-1), T(0));
+                                                        B, nullptr, out.as<T>(), nullptr, T(-1), T(0), SrcArgs{});
             EMS_CUDA(cudaGetLastError());
             EMS_CUDA(cudaMemcpyAsync(h.data(), out.p, nslot * w, cudaMemcpyDeviceToHost, stream));
             EMS_CUDA(cudaStreamSynchronize(stream));
@@ -923,11 +1032,11 @@ struct TetFemSim : Sim {
         const unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
         auto body = [&](auto tag) {
             using T = decltype(tag);
-            T *Bx = d_B.as<T>(), *By = Bx + ntet, *Bz = By + ntet;
+            vec4<T> *B = d_B.as<vec4<T>>();
             for (int r = 0; r <= launches; ++r) {
                 if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
                 tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                            Bx, By, Bz, d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(), T(0), T(0));
+                                                            B, d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(), T(0), T(0), SrcArgs{});
             }
         };
         if (fp64) body(double()); else body(float());
@@ -941,7 +1050,7 @@ struct TetFemSim : Sim {
         *ms = t / launches;
         // unique bytes of one kick: incidence list + row pointers + B (3 per
         // tet) + P read/write + U read/write + packed mass blocks + PEC flags
-        *bytes = (double)(6 * ntet) * 4 + (double)(nslot + 1) * 4 + (double)(3 * ntet) * w + (double)nslot * 4 * w +
+        *bytes = (double)(6 * ntet) * 4 + (double)(nslot + 1) * 4 + (double)(4 * ntet) * w + (double)nslot * 4 * w +
                  (double)(28 * nnode) * w + (double)nslot;
         *name = fp64 ? "tet_kick_kernel<double>" : "tet_kick_kernel<float>";
     }
