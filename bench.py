@@ -14,7 +14,8 @@ receivers, FP32 fields.  Metric: DOF-updates/s (edges x time steps / time).
 `roofline` the dominant kernel (tet_kick_kernel) timed alone on the same state.
 `cpu_baseline` the FP64 oracle on the host cores over a bounded sample.
 A secondary object `fdtd_512` times the 512^3 FP32 Yee update with a 10-cell
-CPML (HBM-bound) for a bounded number of steps.
+CPML (HBM-bound) for a bounded number of steps; `batch64` times 64 batched
+shots of uneven size (FP32) against the per-shot FP64 GPU path.
 
 `--impl reference` times the FP64 CPU oracle (the reference has no
 tetrahedral solver; this is the restated algorithm) with all host threads.
@@ -172,6 +173,58 @@ def fdtd_512(steps=60):
             "kernel": kname, "kernel_ms": kms, "kernel_bytes": kbytes, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
 
 
+def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
+    """Batched forward shots: nshots cubes of side n ~ U[12,40] (6 n^3
+    tetrahedra each), eps_r ~ U[1,6] per tet, one Ricker dipole each, 4th-order
+    symplectic, `steps` steps, FP32, all shots advanced by the same kernels.
+    Compared with the plain per-shot FP64 GPU path on `sample` of the shots
+    (same time step, `sample_steps` steps, scaled to `steps`)."""
+    import emsolvers_gb300 as ems
+    rng = np.random.default_rng(SEED + 4)
+    sides = rng.integers(12, 41, nshots)
+    cells = [(int(n), int(n), int(n)) for n in sides]
+    eps = [rng.uniform(1.0, 6.0, 6 * n ** 3) for n in sides]
+    pos = [np.array([n, n, n]) * rng.uniform(0.3, 0.7, 3) * H for n in sides]
+    rec = [np.array([n, n, n]) * rng.uniform(0.2, 0.8, 3) * H for n in sides]
+    f0 = C0 / (10 * H * np.sqrt(3.5))
+    b = ems.TetFemBatch(cells, H, integrator=ems.SYMP4, precision=ems.FP32, dt=0.0, cfl_fraction=0.9)
+    b.set_material(np.concatenate(eps))
+    for s in range(nshots):
+        b.add_dipole(s, pos[s], (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
+        b.add_receiver(s, rec[s])
+    dt, _ = b.time_step()
+    b.run(20)
+    b.reset()
+    b.run(steps)
+    ms_batch, launches = b.run_stats()
+    kms, kbytes, kname = b.time_dominant_kernel(20)
+    edges = sum(n_edges(int(n)) for n in sides)
+    b.close()
+    per = {ems.FP64: [], ems.FP32: []}
+    pick = rng.choice(nshots, size=min(sample, nshots), replace=False)
+    for prec in (ems.FP64, ems.FP32):
+        for s in pick:
+            one = ems.TetFemSimulation(cells[s], H, 1, ems.SYMP4, prec, dt=dt)
+            one.set_material(eps[s])
+            one.add_dipole(pos[s], (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
+            one.add_receiver(rec[s])
+            one.run(5)
+            one.reset()
+            one.run(sample_steps)
+            per[prec].append(one.run_stats()[0] * steps / sample_steps)
+            one.close()
+    shots_batch = nshots / (ms_batch * 1e-3)
+    shots_fp64 = 1.0 / (np.mean(per[ems.FP64]) * 1e-3)
+    shots_fp32 = 1.0 / (np.mean(per[ems.FP32]) * 1e-3)
+    return {"workload": "tet_batch64_symp4_3000", "shots": nshots, "steps": steps, "tets": int(sum(6 * sides ** 3)),
+            "edges": int(edges), "order": 1, "dt_s": dt, "batch_ms": ms_batch, "launches": int(launches),
+            "shots_per_s_fp32_batched": shots_batch, "shots_per_s_fp64_per_shot": shots_fp64,
+            "shots_per_s_fp32_per_shot": shots_fp32, "speedup_vs_fp64_per_shot": shots_batch / shots_fp64,
+            "dof_updates_per_s": edges * steps / (ms_batch * 1e-3),
+            "per_shot_sample": f"{len(pick)} shots x {sample_steps} steps, scaled to {steps}",
+            "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
+
+
 def run_gpu(args):
     import torch
     import emsolvers_gb300 as ems
@@ -260,6 +313,11 @@ def run_gpu(args):
             r, s = cpu_oracle_rate(20, os.cpu_count() or 1)
             out["cpu_baseline"] = {"value": r, "unit": "DOF-updates/s", "cores": os.cpu_count() or 1, "kind": "port",
                                    "sample": f"20 of {STEPS_PER_SOLVE} time steps, FP64 oracle, {s:.1f} s"}
+        if not args.no_batch:
+            try:
+                out["batch64"] = batch64()
+            except Exception as e:  # secondary measurement only
+                out["batch64"] = {"error": str(e)}
         if not args.no_fdtd:
             try:
                 out["fdtd_512"] = fdtd_512()
@@ -279,6 +337,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fdtd", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

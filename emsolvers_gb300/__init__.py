@@ -6,7 +6,7 @@ front end that mirrors the reference's solver classes.
 """
 from ._lib import (ABM, FP32, FP64, LEAPFROG, SYMP2, SYMP4, WAVE_REFERENCE, WAVE_RICKER, EmsError,  # noqa: F401
                    declared_functions, lib)
-from .solvers import FdtdSimulation, HexFemSimulation, TetFemSimulation  # noqa: F401
+from .solvers import FdtdSimulation, HexFemSimulation, TetFemBatch, TetFemSimulation  # noqa: F401
 
-__all__ = ["FdtdSimulation", "HexFemSimulation", "TetFemSimulation", "EmsError", "lib", "declared_functions",
+__all__ = ["FdtdSimulation", "HexFemSimulation", "TetFemSimulation", "TetFemBatch", "EmsError", "lib", "declared_functions",
            "FP32", "FP64", "LEAPFROG", "SYMP2", "SYMP4", "ABM", "WAVE_REFERENCE", "WAVE_RICKER"]

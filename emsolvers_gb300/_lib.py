@@ -76,7 +76,12 @@ def lib():
         "ems_hexfem_create": (C.c_int, [C.POINTER(HexFemParams), C.POINTER(vp)]),
         "ems_hexfem_set_source": (C.c_int, [vp, C.c_int, ip]),
         "ems_hexfem_add_observation": (C.c_int, [vp, ip]),
+        "ems_hexfem_add_dipole": (C.c_int, [vp, ip]),
+        "ems_hexfem_add_observation_edges": (C.c_int, [vp, ip, C.c_int, ip, C.c_int, ip, C.c_int]),
         "ems_tetfem_create": (C.c_int, [C.POINTER(TetFemParams), C.POINTER(vp)]),
+        "ems_tetbatch_create": (C.c_int, [C.POINTER(TetFemParams), C.c_int, ip, C.POINTER(vp)]),
+        "ems_tetbatch_add_dipole": (C.c_int, [vp, C.c_int, dp, dp, C.c_int, C.c_double, C.c_double]),
+        "ems_tetbatch_add_receiver": (C.c_int, [vp, C.c_int, dp]),
         "ems_tetfem_set_material": (C.c_int, [vp, dp, dp]),
         "ems_tetfem_add_dipole": (C.c_int, [vp, dp, dp, C.c_int, C.c_double, C.c_double]),
         "ems_tetfem_add_receiver": (C.c_int, [vp, dp]),

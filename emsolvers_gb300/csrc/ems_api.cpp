@@ -113,23 +113,62 @@ int ems_fdtd_set_material(ems_sim *s, const double *eps, const double *sigma)
 int ems_hexfem_create(const ems_hexfem_params *p, ems_sim **out)
 {
     if (!p) return EMS_ERR_INVALID_ARGUMENT;
-    return create(out, [&] { return ems::make_hexfem(p); });
+    return create(out, [&] { return p->integrator == EMS_ABM ? ems::make_abm(p) : ems::make_hexfem(p); });
 }
 int ems_hexfem_set_source(ems_sim *s, int comp, const int ijk[3])
 {
     NEED(s, ems::Kind::HEXFEM);
-    return guard(s, [&] { ems::hexfem_set_source(s->impl, comp, ijk); });
+    return guard(s, [&] {
+        if (comp < 0 || comp > 2 || !ijk) throw Error{EMS_ERR_INVALID_ARGUMENT, "component must be 0, 1 or 2"};
+        if (ems::is_abm(s->impl)) ems::abm_set_source(s->impl, comp, ijk);
+        else ems::hexfem_set_source(s->impl, comp, ijk);
+    });
 }
 int ems_hexfem_add_observation(ems_sim *s, const int ijk[3])
 {
     NEED(s, ems::Kind::HEXFEM);
-    return guard(s, [&] { ems::hexfem_add_observation(s->impl, ijk); });
+    return guard(s, [&] {
+        if (ems::is_abm(s->impl))
+            throw Error{EMS_ERR_STATE, "Adams-Bashforth-Moulton receivers take edge lists (ems_hexfem_add_observation_edges)"};
+        ems::hexfem_add_observation(s->impl, ijk);
+    });
+}
+int ems_hexfem_add_dipole(ems_sim *s, const int ijk[3])
+{
+    NEED(s, ems::Kind::HEXFEM);
+    return guard(s, [&] {
+        if (!ems::is_abm(s->impl)) throw Error{EMS_ERR_STATE, "Hertz dipoles belong to the Adams-Bashforth-Moulton solver"};
+        ems::abm_add_dipole(s->impl, ijk);
+    });
+}
+int ems_hexfem_add_observation_edges(ems_sim *s, const int *x, int nx, const int *y, int ny, const int *z, int nz)
+{
+    NEED(s, ems::Kind::HEXFEM);
+    return guard(s, [&] {
+        if (!ems::is_abm(s->impl)) throw Error{EMS_ERR_STATE, "edge-list receivers belong to the Adams-Bashforth-Moulton solver"};
+        ems::abm_add_observation(s->impl, x, nx, y, ny, z, nz);
+    });
 }
 
 int ems_tetfem_create(const ems_tetfem_params *p, ems_sim **out)
 {
     if (!p) return EMS_ERR_INVALID_ARGUMENT;
     return create(out, [&] { return ems::make_tetfem(p); });
+}
+int ems_tetbatch_create(const ems_tetfem_params *p, int nshots, const int *cells, ems_sim **out)
+{
+    if (!p) return EMS_ERR_INVALID_ARGUMENT;
+    return create(out, [&] { return ems::make_tetbatch(p, nshots, cells); });
+}
+int ems_tetbatch_add_dipole(ems_sim *s, int shot, const double pos[3], const double dir[3], int wf, double f0, double amp)
+{
+    NEED(s, ems::Kind::TETFEM);
+    return guard(s, [&] { ems::tetbatch_add_dipole(s->impl, shot, pos, dir, wf, f0, amp); });
+}
+int ems_tetbatch_add_receiver(ems_sim *s, int shot, const double pos[3])
+{
+    NEED(s, ems::Kind::TETFEM);
+    return guard(s, [&] { ems::tetbatch_add_receiver(s->impl, shot, pos); });
 }
 int ems_tetfem_set_material(ems_sim *s, const double *eps_r, const double *sigma)
 {

@@ -80,6 +80,14 @@ std::string compress_number(double v);
 Sim *make_fdtd(const ems_fdtd_params *p);
 Sim *make_hexfem(const ems_hexfem_params *p);
 Sim *make_tetfem(const ems_tetfem_params *p);
+Sim *make_abm(const ems_hexfem_params *p);
+Sim *make_tetbatch(const ems_tetfem_params *p, int nshots, const int *cells);
+void tetbatch_add_dipole(Sim *s, int shot, const double pos[3], const double dir[3], int waveform, double f0, double amp);
+void tetbatch_add_receiver(Sim *s, int shot, const double pos[3]);
+bool is_abm(const Sim *s);
+void abm_set_source(Sim *s, int comp, const int ijk[3]);
+void abm_add_dipole(Sim *s, const int ijk[3]);
+void abm_add_observation(Sim *s, const int *x, int nx, const int *y, int ny, const int *z, int nz);
 
 // per-kind setters (throw Error on misuse)
 void fdtd_set_source(Sim *s, int comp, const int ijk[3], int waveform, double f0, double amp);

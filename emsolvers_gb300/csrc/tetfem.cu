@@ -522,9 +522,17 @@ struct Dipole {
     double f0n;   // normalised frequency
 };
 
+// One shot of a batch: a cube of cells whose nodes and tetrahedra occupy
+// the ranges starting at node0 / tet0 of the concatenated mesh.
+struct Shot {
+    int nx, ny, nz;
+    size_t node0, tet0;
+};
+
 struct TetFemSim : Sim {
     ems_tetfem_params P;
-    int nx, ny, nz;
+    int nx, ny, nz;                 // the first shot (single-shot handles)
+    std::vector<Shot> shots;
     size_t nnode, nslot, ntet;
     bool fp64;
     double c0 = 299792458.0;
@@ -541,10 +549,19 @@ struct TetFemSim : Sim {
     bool ready = false;
     double cur_time = 0.0;          // normalised
 
-    explicit TetFemSim(const ems_tetfem_params *p) : Sim(Kind::TETFEM), P(*p)
+    // cells: 3 per shot.  Every shot is an independent cube mesh; the shots
+    // are concatenated so each kernel launch advances all of them.
+    TetFemSim(const ems_tetfem_params *p, const std::vector<std::array<int, 3>> &cells) : Sim(Kind::TETFEM), P(*p)
     {
-        nx = P.cells[0]; ny = P.cells[1]; nz = P.cells[2];
-        EMS_CHECK_ARG(nx > 0 && ny > 0 && nz > 0, "cell counts must be positive");
+        EMS_CHECK_ARG(!cells.empty(), "at least one shot");
+        size_t n0 = 0, t0 = 0;
+        for (auto &c : cells) {
+            EMS_CHECK_ARG(c[0] > 0 && c[1] > 0 && c[2] > 0, "cell counts must be positive");
+            shots.push_back(Shot{c[0], c[1], c[2], n0, t0});
+            n0 += (size_t)(c[0] + 1) * (c[1] + 1) * (c[2] + 1);
+            t0 += 6 * (size_t)c[0] * c[1] * c[2];
+        }
+        nx = shots[0].nx; ny = shots[0].ny; nz = shots[0].nz;
         EMS_CHECK_ARG(P.h > 0, "h must be positive");
         EMS_CHECK_ARG(P.order == 1, "only lowest-order (order 1) Nedelec tetrahedra are implemented");
         EMS_CHECK_ARG(P.integrator == EMS_LEAPFROG || P.integrator == EMS_SYMP2 || P.integrator == EMS_SYMP4,
@@ -555,10 +572,11 @@ struct TetFemSim : Sim {
         EMS_CHECK_ARG(P.cfl_fraction < 1.0, "cfl_fraction must be below 1");
         fp64 = P.precision == EMS_FP64;
         tscale = P.h / c0;
-        nnode = (size_t)(nx + 1) * (ny + 1) * (nz + 1);
+        nnode = n0;
         nslot = 7 * nnode;
-        ntet = 6 * (size_t)nx * ny * nz;
+        ntet = t0;
         EMS_CHECK_ARG(ntet < (size_t)1 << 28, "mesh too large for 28-bit element indices");
+        EMS_CHECK_ARG(nslot < (size_t)1 << 31, "mesh too large for 32-bit slot indices");
         build_mesh();
         eps_h.assign(ntet, 1.0);
         init_stream();
@@ -566,36 +584,43 @@ struct TetFemSim : Sim {
         upload_mesh();
     }
 
-    size_t node(int i, int j, int k) const { return (size_t)i + (size_t)(nx + 1) * ((size_t)j + (size_t)(ny + 1) * k); }
+    size_t node(const Shot &s, int i, int j, int k) const
+    {
+        return s.node0 + (size_t)i + (size_t)(s.nx + 1) * ((size_t)j + (size_t)(s.ny + 1) * k);
+    }
+    size_t node(int i, int j, int k) const { return node(shots[0], i, j, k); }
 
     void build_mesh()
     {
         Shape sh[6];
         for (int p = 0; p < 6; ++p) sh[p] = make_shape(p);
         tet_edge_h.resize(6 * ntet);
-        for (int k = 0; k < nz; ++k)
-            for (int j = 0; j < ny; ++j)
-                for (int i = 0; i < nx; ++i)
-                    for (int p = 0; p < 6; ++p) {
-                        size_t t = 6 * ((size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)) + p;
-                        for (int l = 0; l < 6; ++l) {
-                            const int *vm = sh[p].vert[kLoc[l][0]], *vn = sh[p].vert[kLoc[l][1]];
-                            int d = dir_index(vn[0] - vm[0], vn[1] - vm[1], vn[2] - vm[2]);
-                            tet_edge_h[6 * t + l] = (int)(7 * node(i + vm[0], j + vm[1], k + vm[2]) + d);
-                        }
-                    }
         pec_h.assign(nslot, 0);
-        const int lim[3] = {nx, ny, nz};
-        for (int k = 0; k <= nz; ++k)
-            for (int j = 0; j <= ny; ++j)
-                for (int i = 0; i <= nx; ++i)
-                    for (int d = 0; d < 7; ++d) {
-                        int a[3] = {i, j, k}, b[3] = {i + kDir[d][0], j + kDir[d][1], k + kDir[d][2]};
-                        bool bad = b[0] > nx || b[1] > ny || b[2] > nz;
-                        for (int q = 0; q < 3 && !bad; ++q)
-                            if (a[q] == b[q] && (a[q] == 0 || a[q] == lim[q])) bad = true;
-                        pec_h[7 * node(i, j, k) + d] = bad ? 1 : 0;
-                    }
+        for (const Shot &S : shots) {
+            const int nx = S.nx, ny = S.ny, nz = S.nz;
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i)
+                        for (int p = 0; p < 6; ++p) {
+                            size_t t = S.tet0 + 6 * ((size_t)i + (size_t)nx * ((size_t)j + (size_t)ny * k)) + p;
+                            for (int l = 0; l < 6; ++l) {
+                                const int *vm = sh[p].vert[kLoc[l][0]], *vn = sh[p].vert[kLoc[l][1]];
+                                int d = dir_index(vn[0] - vm[0], vn[1] - vm[1], vn[2] - vm[2]);
+                                tet_edge_h[6 * t + l] = (int)(7 * node(S, i + vm[0], j + vm[1], k + vm[2]) + d);
+                            }
+                        }
+            const int lim[3] = {nx, ny, nz};
+            for (int k = 0; k <= nz; ++k)
+                for (int j = 0; j <= ny; ++j)
+                    for (int i = 0; i <= nx; ++i)
+                        for (int d = 0; d < 7; ++d) {
+                            int a[3] = {i, j, k}, b[3] = {i + kDir[d][0], j + kDir[d][1], k + kDir[d][2]};
+                            bool bad = b[0] > nx || b[1] > ny || b[2] > nz;
+                            for (int q = 0; q < 3 && !bad; ++q)
+                                if (a[q] == b[q] && (a[q] == 0 || a[q] == lim[q])) bad = true;
+                            pec_h[7 * node(S, i, j, k) + d] = bad ? 1 : 0;
+                        }
+        }
         inc_ptr_h.assign(nslot + 1, 0);
         for (size_t t = 0; t < ntet; ++t)
             for (int l = 0; l < 6; ++l) inc_ptr_h[tet_edge_h[6 * t + l] + 1]++;
@@ -764,9 +789,9 @@ struct TetFemSim : Sim {
         return lam;
     }
 
-    void locate(const double xn[3], double w[6][3], int edges[6]) const
+    void locate(const Shot &S, const double xn[3], double w[6][3], int edges[6]) const
     {
-        int cell[3], lim[3] = {nx, ny, nz};
+        int cell[3], lim[3] = {S.nx, S.ny, S.nz};
         double s[3];
         for (int q = 0; q < 3; ++q) {
             int c = (int)std::floor(xn[q]);
@@ -787,7 +812,7 @@ struct TetFemSim : Sim {
             for (int q = 0; q < 3; ++q) w[l][q] = lam[a] * sh.grad[b][q] - lam[b] * sh.grad[a][q];
             const int *vm = sh.vert[a], *vn = sh.vert[b];
             int d = dir_index(vn[0] - vm[0], vn[1] - vm[1], vn[2] - vm[2]);
-            edges[l] = (int)(7 * node(cell[0] + vm[0], cell[1] + vm[1], cell[2] + vm[2]) + d);
+            edges[l] = (int)(7 * node(S, cell[0] + vm[0], cell[1] + vm[1], cell[2] + vm[2]) + d);
         }
     }
 
@@ -1056,23 +1081,41 @@ struct TetFemSim : Sim {
     }
 };
 
-Sim *make_tetfem(const ems_tetfem_params *p) { return new TetFemSim(p); }
+Sim *make_tetfem(const ems_tetfem_params *p)
+{
+    return new TetFemSim(p, {std::array<int, 3>{p->cells[0], p->cells[1], p->cells[2]}});
+}
+
+Sim *make_tetbatch(const ems_tetfem_params *p, int nshots, const int *cells)
+{
+    EMS_CHECK_ARG(nshots >= 1 && cells != nullptr, "need at least one shot");
+    std::vector<std::array<int, 3>> c(nshots);
+    for (int s = 0; s < nshots; ++s) c[s] = {cells[3 * s], cells[3 * s + 1], cells[3 * s + 2]};
+    return new TetFemSim(p, c);
+}
 
 void tetfem_set_material(Sim *s, const double *eps_r, const double *sigma) { static_cast<TetFemSim *>(s)->set_material(eps_r, sigma); }
 
 void tetfem_add_dipole(Sim *s, const double pos[3], const double dir[3], int waveform, double f0, double amp)
 {
+    tetbatch_add_dipole(s, 0, pos, dir, waveform, f0, amp);
+}
+
+void tetbatch_add_dipole(Sim *s, int shot, const double pos[3], const double dir[3], int waveform, double f0, double amp)
+{
     auto *f = static_cast<TetFemSim *>(s);
+    EMS_CHECK_ARG(shot >= 0 && shot < (int)f->shots.size(), "shot index out of range");
+    const Shot &S = f->shots[shot];
     EMS_CHECK_ARG(pos && dir, "position and direction required");
     EMS_CHECK_ARG(waveform == EMS_WAVE_REFERENCE || waveform == EMS_WAVE_RICKER, "unknown waveform");
     EMS_CHECK_ARG(f0 > 0 && std::isfinite(amp), "f0 must be positive");
     double xn[3] = {pos[0] / f->P.h, pos[1] / f->P.h, pos[2] / f->P.h};
-    const int lim[3] = {f->nx, f->ny, f->nz};
+    const int lim[3] = {S.nx, S.ny, S.nz};
     for (int q = 0; q < 3; ++q) EMS_CHECK_ARG(xn[q] >= 0 && xn[q] <= lim[q], "dipole outside the domain");
-    EMS_CHECK_ARG(f->dips.size() < 64, "at most 64 dipoles");
+    EMS_CHECK_ARG(f->dips.size() < 4096, "at most 4096 dipoles");
     double w[6][3];
     Dipole d{};
-    f->locate(xn, w, d.slot);
+    f->locate(S, xn, w, d.slot);
     // loads on PEC slots vanish (the force is zero there)
     for (int l = 0; l < 6; ++l)
         d.coef[l] = f->pec_h[d.slot[l]] ? 0.0 : (w[l][0] * dir[0] + w[l][1] * dir[1] + w[l][2] * dir[2]) * amp;
@@ -1081,16 +1124,20 @@ void tetfem_add_dipole(Sim *s, const double pos[3], const double dir[3], int wav
     f->dips.push_back(d);
 }
 
-void tetfem_add_receiver(Sim *s, const double pos[3])
+void tetfem_add_receiver(Sim *s, const double pos[3]) { tetbatch_add_receiver(s, 0, pos); }
+
+void tetbatch_add_receiver(Sim *s, int shot, const double pos[3])
 {
     auto *f = static_cast<TetFemSim *>(s);
     EMS_CHECK_ARG(pos != nullptr, "position required");
+    EMS_CHECK_ARG(shot >= 0 && shot < (int)f->shots.size(), "shot index out of range");
+    const Shot &S = f->shots[shot];
     double xn[3] = {pos[0] / f->P.h, pos[1] / f->P.h, pos[2] / f->P.h};
-    const int lim[3] = {f->nx, f->ny, f->nz};
+    const int lim[3] = {S.nx, S.ny, S.nz};
     for (int q = 0; q < 3; ++q) EMS_CHECK_ARG(xn[q] >= 0 && xn[q] <= lim[q], "receiver outside the domain");
     double w[6][3];
     std::array<int, 6> e;
-    f->locate(xn, w, e.data());
+    f->locate(S, xn, w, e.data());
     std::array<double, 18> ww;
     for (int l = 0; l < 6; ++l)
         for (int q = 0; q < 3; ++q) ww[3 * l + q] = w[l][q];

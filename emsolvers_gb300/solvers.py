@@ -175,8 +175,21 @@ class HexFemSimulation(_Sim):
         self._src(2, position)
 
     def setObservationPoint(self, position):
+        """fem_v2 family: a node (i, j, k).  Adams-Bashforth-Moulton
+        (fem_abm): three lists of (i, j, k) edges of Ex, Ey and Ez."""
+        if len(position) == 3 and all(np.isscalar(v) for v in position):
+            ijk = (C.c_int * 3)(*[int(v) for v in position])
+            self._check(lib().ems_hexfem_add_observation(self._h, ijk))
+            return
+        arrs = [np.ascontiguousarray(np.array(l, np.int32).reshape(-1)) for l in position]
+        ptrs = [a.ctypes.data_as(_ip) for a in arrs]
+        self._check(lib().ems_hexfem_add_observation_edges(self._h, ptrs[0], len(position[0]), ptrs[1], len(position[1]),
+                                                           ptrs[2], len(position[2])))
+
+    def setSourceDipole_x(self, position):
+        """fem_abm setSourceDipole_x: Hertz dipole over cells (i, j..j+1, k..k+1)."""
         ijk = (C.c_int * 3)(*[int(v) for v in position])
-        self._check(lib().ems_hexfem_add_observation(self._h, ijk))
+        self._check(lib().ems_hexfem_add_dipole(self._h, ijk))
 
     def levels(self):
         return [self.get_field(q) for q in range(3)]
@@ -223,3 +236,29 @@ class TetFemSimulation(_Sim):
         dt, lim = C.c_double(), C.c_double()
         self._check(lib().ems_tetfem_time_step(self._h, C.byref(dt), C.byref(lim)))
         return dt.value, lim.value
+
+
+class TetFemBatch(TetFemSimulation):
+    """Independent shots (cubes of cells[s] cells) advanced together by the
+    same kernels; materials and fields are the shots' arrays concatenated."""
+
+    def __init__(self, cells, h, order=1, integrator=SYMP4, precision=FP32, dt=0.0, cfl_fraction=0.9,
+                 time_frequency=1):
+        _Sim.__init__(self)
+        p = _lib.TetFemParams()
+        p.cells[:] = list(cells[0])
+        p.h, p.order, p.integrator, p.precision = h, order, integrator, precision
+        p.dt, p.cfl_fraction, p.time_frequency = dt, cfl_fraction, time_frequency
+        self.params = p
+        flat = np.ascontiguousarray(np.array(cells, np.int32).reshape(-1))
+        self.cells = [tuple(c) for c in cells]
+        check(lib().ems_tetbatch_create(C.byref(p), len(cells), flat.ctypes.data_as(_ip), C.byref(self._h)))
+
+    def add_dipole(self, shot, pos, direction=(0.0, 0.0, 1.0), waveform=WAVE_RICKER, f0=1.0, amplitude=1.0):
+        a = np.ascontiguousarray(pos, dtype=np.float64)
+        d = np.ascontiguousarray(direction, dtype=np.float64)
+        self._check(lib().ems_tetbatch_add_dipole(self._h, shot, _dptr(a), _dptr(d), waveform, f0, amplitude))
+
+    def add_receiver(self, shot, pos):
+        a = np.ascontiguousarray(pos, dtype=np.float64)
+        self._check(lib().ems_tetbatch_add_receiver(self._h, shot, _dptr(a)))

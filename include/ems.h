@@ -113,6 +113,15 @@ int ems_hexfem_create(const ems_hexfem_params *params, ems_sim **out);
 int ems_hexfem_set_source(ems_sim *sim, int component, const int ijk[3]);
 /* Replaces setObservationPoint (fem_v2/fem_simulation.cpp:547-563). */
 int ems_hexfem_add_observation(ems_sim *sim, const int ijk[3]);
+/* EMS_ABM handles (fem_abm): replaces setSourceDipole_x
+ * (fem_abm/fem_simulation.cpp:266-269; injection 407-481, 758-833): an
+ * x-directed Hertz dipole spread over the cells (i, j..j+1, k..k+1). */
+int ems_hexfem_add_dipole(ems_sim *sim, const int ijk[3]);
+/* EMS_ABM handles: replaces setObservationPoint with edge lists
+ * (fem_abm/fem_simulation.cpp:271-276, sampling 972-1013): one receiver
+ * averaging n_x x-edges, n_y y-edges and n_z z-edges of E. */
+int ems_hexfem_add_observation_edges(ems_sim *sim, const int *x_ijk, int n_x, const int *y_ijk, int n_y, const int *z_ijk,
+                                     int n_z);
 
 /* -------------------------------------------------------- tetrahedral FEM */
 typedef struct {
@@ -159,6 +168,18 @@ int ems_tetfem_apply_stiffness(ems_sim *sim, const double *u, double *f, size_t 
  * it is read, so nothing needs clearing between calls.  Errors are reported
  * through ems_last_error(NULL). */
 int ems_tet_stiffness_apply_static(const int cells[3], const float *u, float *f, void *stream);
+
+/* Batch of independent shots (configurations that differ in mesh size,
+ * material, source and receivers) advanced together: shot s is a cube of
+ * cells[3s..3s+2] cells split into tetrahedra; all shots share the time step
+ * (with dt == 0, cfl_fraction x the stability limit of the stiffest shot).
+ * Fields, materials (ems_tetfem_set_material) and edge-slot vectors are the
+ * shots' arrays concatenated in shot order.  New: the reference runs one
+ * configuration per process. */
+int ems_tetbatch_create(const ems_tetfem_params *params, int nshots, const int *cells, ems_sim **out);
+int ems_tetbatch_add_dipole(ems_sim *sim, int shot, const double pos[3], const double dir[3], int waveform, double f0,
+                            double amplitude);
+int ems_tetbatch_add_receiver(ems_sim *sim, int shot, const double pos[3]);
 
 /* ------------------------------------------------------ common operations */
 /* Replaces FemSimulation::run (fdtd :242-306, fem_v2 :1249-1320,
