@@ -142,10 +142,11 @@ def run_reference(args):
     }))
 
 
-def fdtd_512(steps=60):
-    """512^3 FP32 Yee step with a 10-cell CPML: device rate and roofline of the E kernel."""
+def fdtd_512(steps=60, n=512):
+    """n^3 (512^3 by default) FP32 Yee step with a 10-cell CPML: device rate
+    and roofline of the E kernel."""
     import emsolvers_gb300 as ems
-    n, h = 512, 1e-3
+    h = 1e-3
     eps0, mu0 = 8.854187817e-12, 1.25663706212e-6
     dt = 0.99 * h / (C0 * np.sqrt(3))
     rng = np.random.default_rng(SEED)
@@ -167,7 +168,7 @@ def fdtd_512(steps=60):
     kms, kbytes, kname = s.time_dominant_kernel(10)
     cells = n ** 3
     s.close()
-    return {"workload": "fdtd512_fp32_cpml10", "steps": steps, "ms_per_step": ms / steps,
+    return {"workload": f"fdtd{n}_fp32_cpml10", "steps": steps, "ms_per_step": ms / steps,
             "cell_updates_per_s": cells * steps / (ms * 1e-3),
             "dof_updates_per_s": 6 * cells * steps / (ms * 1e-3),
             "kernel": kname, "kernel_ms": kms, "kernel_bytes": kbytes, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
@@ -303,7 +304,10 @@ def run_gpu(args):
                 "d2h_bytes_per_step": int(tr.nbytes)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": kname, "kernel_us": kms * 1e3, "bytes_per_launch": kbytes,
+                     # DRAM bytes of one kick launch from the ncu capture in
+                     # profiles/tet_kick_tet32_symp4.md (cold fill: the 17 MB
+                     # working set is L2-resident in the timed loop)
+                     "traffic": 15054080, "kernel": kname, "kernel_us": kms * 1e3, "bytes_per_launch": kbytes,
                      "peak_source": peak_kind},
         "clocks": clk,
         "wall_s": wall,
@@ -338,10 +342,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fdtd", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--only", choices=["batch", "fdtd"],
+                    help="run one secondary workload alone and print its JSON (for profiling)")
+    ap.add_argument("--fdtd-n", type=int, default=512, help="FDTD cube side for --only fdtd")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.only:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps(batch64() if args.only == "batch" else fdtd_512(n=args.fdtd_n)))
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

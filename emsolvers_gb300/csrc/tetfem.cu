@@ -33,6 +33,9 @@ namespace {
 const int kPerm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
 const int kLoc[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
 const int kDir[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+// Per-slot flag byte: the slot is PEC or unused (no DOF), or it carries a
+// dipole load (only those slots search the source list).
+constexpr unsigned char kPecBit = 1, kSrcBit = 2;
 
 struct Shape {
     double grad[4][3];
@@ -148,7 +151,7 @@ __global__ void tet_minv_setup_kernel(size_t nnode, const unsigned char *__restr
     for (int q = 0; q < 49; ++q) B[q] = 0.0;
     int slot[7], k = 0;
     for (int d = 0; d < 7; ++d)
-        if (!pec[7 * v + d]) slot[k++] = d;
+        if (!(pec[7 * v + d] & kPecBit)) slot[k++] = d;
     if (k == 0) return;
     double W[7][3], D[7][3], diag[7];
     for (int r = 0; r < k; ++r) {
@@ -371,10 +374,11 @@ __global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *
     T p = 0;
     if (live) {
         p = P[e];
-        if (!pec[e]) {
+        const unsigned char m = pec[e];
+        if (!(m & kPecBit)) {
             T f = gather_force<T>(e, inc_ptr, inc, B, sc);
             p = fma(-a, f, p);
-            if (src.n) p = fma(a, (T)source_load(src, e), p);
+            if (m & kSrcBit) p = fma(a, (T)source_load(src, e), p);
         }
         P[e] = p;
     }
@@ -415,13 +419,14 @@ __global__ void __launch_bounds__(256) tet_leapfrog_kernel(size_t nnode, const i
     bool live = v < nnode && d < 7;
     size_t e = 7 * v + d;
     T f = 0;
-    if (live && !pec[e]) {
+    const unsigned char m = live ? pec[e] : (unsigned char)kPecBit;
+    if (!(m & kPecBit)) {
         f = gather_force<T>(e, inc_ptr, inc, B, sc);
-        if (src.n) f -= (T)source_load(src, e);
+        if (m & kSrcBit) f -= (T)source_load(src, e);
     }
     if (v >= nnode) v = nnode - 1;
     T y = block_apply<T>(minv + 28 * v, d, f);
-    if (live) Unew[e] = pec[e] ? T(0) : fma(-dt2, y, T(2) * U[e] - Uold[e]);
+    if (live) Unew[e] = (m & kPecBit) ? T(0) : fma(-dt2, y, T(2) * U[e] - Uold[e]);
 }
 
 // Receivers and step counter, one block: at the start of step n = ctl[0],
@@ -547,6 +552,7 @@ struct TetFemSim : Sim {
     std::vector<std::array<double, 18>> rec_w;
     DevBuf d_src_slot, d_src_coef, d_src_g, d_rec_e, d_rec_w, d_tr, d_ctl;
     bool ready = false;
+    bool flags_dirty = false;       // pec_h gained source bits not yet on the device
     double cur_time = 0.0;          // normalised
 
     // cells: 3 per shot.  Every shot is an independent cube mesh; the shots
@@ -766,7 +772,7 @@ struct TetFemSim : Sim {
         unsigned long long st = 0x9E3779B97F4A7C15ull;
         for (size_t e = 0; e < nslot; ++e) {
             st ^= st << 13; st ^= st >> 7; st ^= st << 17;
-            x0[e] = pec_h[e] ? 0.0 : ((double)(st >> 11) / 9007199254740992.0 - 0.5);
+            x0[e] = (pec_h[e] & kPecBit) ? 0.0 : ((double)(st >> 11) / 9007199254740992.0 - 0.5);
         }
         EMS_CUDA(cudaMemcpyAsync(x.p, x0.data(), nslot * 8, cudaMemcpyHostToDevice, stream));
         unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
@@ -875,6 +881,10 @@ struct TetFemSim : Sim {
         if (sslot.empty()) { sslot.push_back(0); scoef.push_back(0.0); }
         up(d_src_slot, sslot);
         up(d_src_coef, scoef);
+        if (flags_dirty) {
+            EMS_CUDA(cudaMemcpyAsync(d_pec.p, pec_h.data(), nslot, cudaMemcpyHostToDevice, stream));
+            flags_dirty = false;
+        }
         const double x1 = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0)), x2 = 1.0 - 2.0 * x1;
         const bool symp = P.integrator != EMS_LEAPFROG;
         int nsub = P.integrator == EMS_SYMP4 ? 3 : 1;
@@ -1118,10 +1128,13 @@ void tetbatch_add_dipole(Sim *s, int shot, const double pos[3], const double dir
     f->locate(S, xn, w, d.slot);
     // loads on PEC slots vanish (the force is zero there)
     for (int l = 0; l < 6; ++l)
-        d.coef[l] = f->pec_h[d.slot[l]] ? 0.0 : (w[l][0] * dir[0] + w[l][1] * dir[1] + w[l][2] * dir[2]) * amp;
+        d.coef[l] = (f->pec_h[d.slot[l]] & kPecBit) ? 0.0 : (w[l][0] * dir[0] + w[l][1] * dir[1] + w[l][2] * dir[2]) * amp;
     d.kind = waveform;
     d.f0n = f0 * f->tscale;
     f->dips.push_back(d);
+    for (int l = 0; l < 6; ++l)
+        if (d.coef[l] != 0.0) f->pec_h[d.slot[l]] |= kSrcBit;
+    f->flags_dirty = true;
 }
 
 void tetfem_add_receiver(Sim *s, const double pos[3]) { tetbatch_add_receiver(s, 0, pos); }
