@@ -99,6 +99,8 @@ int orc_spd_inverse7(double *A, int k);
 int orc_tet_apply_op(int nx, int ny, int nz, const double *eps_r, const double *x, double *y);
 void orc_tet_pec_mask(int nx, int ny, int nz, unsigned char *mask);
 int orc_tet_apply_K(int nx, int ny, int nz, const double *x, double *f);
+int orc_tet_mass_block(int nx, int ny, int nz, const double *eps_r, long v, long t, double *M, double *dM);
+int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad, double *grad_eps);
 
 /* ----------------------------------------- Adams-Bashforth-Moulton (hex) --- */
 typedef struct {

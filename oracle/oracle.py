@@ -184,6 +184,10 @@ class _TetCase(C.Structure):
                 ("dip_kind", _ip), ("nrec", C.c_int), ("rec_pos", _dp)]
 
 
+# integrators of orc_tet_case (ORC_LEAPFROG / ORC_SYMP2 / ORC_SYMP4 in ems_oracle.h)
+ORC_LEAPFROG, ORC_SYMP2, ORC_SYMP4 = 0, 1, 2
+
+
 def tet_sizes(n):
     nx, ny, nz = n
     nnode = (nx + 1) * (ny + 1) * (nz + 1)
@@ -201,16 +205,12 @@ def _tlib():
     return L
 
 
-def tet_run(n, eps_r, integrator, dt, nsteps, tf=1, dipoles=(), receivers=(), mu_r=None, U=None, P=None):
-    """FP64 oracle of the tetrahedral solver in normalised units (cube edge 1,
-    c0 = 1).  dipoles: [(pos, dir, kind, f0, amp)]; receivers: [pos].
-    Returns (traces[nrec, nsamp, 4], U, P)."""
-    nnode, nslot, ntet = tet_sizes(n)
+def _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r):
+    """orc_tet_case for the arguments of tet_run; returns (case, arrays kept alive)."""
+    _, _, ntet = tet_sizes(n)
     eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
     assert eps.size == ntet
     mu = None if mu_r is None else np.ascontiguousarray(mu_r, dtype=np.float64).reshape(-1)
-    U = np.zeros(nslot) if U is None else np.ascontiguousarray(U, dtype=np.float64).copy()
-    P = np.zeros(nslot) if P is None else np.ascontiguousarray(P, dtype=np.float64).copy()
     c = _TetCase()
     c.nx, c.ny, c.nz = n
     c.eps_r, c.mu_r = _ptr(eps), _ptr(mu) if mu is not None else None
@@ -223,12 +223,51 @@ def tet_run(n, eps_r, integrator, dt, nsteps, tf=1, dipoles=(), receivers=(), mu
     rp = np.array(list(receivers) or [(0, 0, 0)], np.float64).reshape(-1)
     c.ndip, c.dip_pos, c.dip_dir, c.dip_kind, c.dip_f0, c.dip_amp = len(dipoles), _ptr(dp), _ptr(dd), _ptr(dk, _ip), _ptr(df), _ptr(da)
     c.nrec, c.rec_pos = len(receivers), _ptr(rp)
+    return c, (eps, mu, dp, dd, dk, df, da, rp)
+
+
+def tet_run(n, eps_r, integrator, dt, nsteps, tf=1, dipoles=(), receivers=(), mu_r=None, U=None, P=None):
+    """FP64 oracle of the tetrahedral solver in normalised units (cube edge 1,
+    c0 = 1).  dipoles: [(pos, dir, kind, f0, amp)]; receivers: [pos].
+    Returns (traces[nrec, nsamp, 4], U, P)."""
+    _, nslot, _ = tet_sizes(n)
+    U = np.zeros(nslot) if U is None else np.ascontiguousarray(U, dtype=np.float64).copy()
+    P = np.zeros(nslot) if P is None else np.ascontiguousarray(P, dtype=np.float64).copy()
+    c, keep = _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r)
     nsamp = (nsteps - 1) // tf + 1 if nsteps > 0 else 0
     tr = np.zeros((max(len(receivers), 1), max(nsamp, 1), 4))
     rc = _tlib().orc_tet_run(C.byref(c), C.c_int(nsteps), _ptr(U), _ptr(P), _ptr(tr))
     if rc != 0:
         raise RuntimeError(f"orc_tet_run failed: {rc}")
     return tr[:len(receivers), :nsamp], U, P
+
+
+def tet_gradient(n, eps_r, integrator, dt, nsteps, trace_grad, tf=1, dipoles=(), receivers=(), mu_r=None):
+    """dJ/deps_r per tetrahedron by the FP64 discrete adjoint of tet_run
+    (symplectic integrators, zero initial fields).  trace_grad: dJ/dtraces,
+    shaped like tet_run's traces (column 0, the time, is ignored)."""
+    _, _, ntet = tet_sizes(n)
+    nsamp = (nsteps - 1) // tf + 1 if nsteps > 0 else 0
+    g = np.zeros((max(len(receivers), 1), max(nsamp, 1), 4))
+    tg = np.asarray(trace_grad, np.float64)
+    if len(receivers):
+        g[:len(receivers), :nsamp] = tg.reshape(len(receivers), nsamp, 4)
+    c, keep = _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r)
+    out = np.zeros(ntet)
+    rc = _tlib().orc_tet_gradient(C.byref(c), C.c_int(nsteps), _ptr(g), _ptr(out))
+    if rc != 0:
+        raise RuntimeError(f"orc_tet_gradient failed: {rc}")
+    return out
+
+
+def tet_mass_block(n, eps_r, v, t=-1):
+    """Mass block M_v (7x7 over the node's slots) and, for t >= 0, dM_v/deps_t."""
+    eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
+    M, dM = np.zeros((7, 7)), np.zeros((7, 7))
+    if _tlib().orc_tet_mass_block(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(eps), C.c_long(v), C.c_long(t),
+                                  _ptr(M), _ptr(dM)) != 0:
+        raise ValueError("node or tetrahedron index out of range")
+    return M, dM
 
 
 def tet_minv(n, eps_r):

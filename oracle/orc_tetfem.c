@@ -221,54 +221,75 @@ int orc_spd_inverse7(double *A, int k)
     return 0;
 }
 
+/* Parts of the mass block of node v: live slots, W, D, diag, S = sym(D^T W)
+ * with its pseudo-inverse, G = D^T D with its pseudo-inverse, alpha. */
+typedef struct {
+    int k, slot[7];
+    double W[7][3], D[7][3], diag[7], S[3][3], Sp[3][3], G[3][3], Gp[3][3], alpha;
+} massparts;
+
+static void mass_parts(const tetmesh *m, const double *eps_r, size_t v, massparts *b)
+{
+    int k = 0;
+    for (int d = 0; d < 7; ++d)
+        if (!m->pec[7 * v + d]) b->slot[k++] = d;
+    b->k = k;
+    memset(b->W, 0, sizeof(b->W));
+    memset(b->diag, 0, sizeof(b->diag));
+    for (int r = 0; r < k; ++r) {
+        int e = (int)(7 * v + b->slot[r]);
+        for (int q = 0; q < 3; ++q) b->D[r][q] = DIRV[b->slot[r]][q];
+        for (int s = m->inc_ptr[e]; s < m->inc_ptr[e + 1]; ++s) {
+            int t = m->inc[s] >> 3, l = m->inc[s] & 7, p = t % 6;
+            double ep = eps_r[t];
+            for (int q = 0; q < 3; ++q) b->W[r][q] += ep * m->shape_wint[p][l][q];
+            b->diag[r] += ep * m->shape_wsq[p][l];
+        }
+    }
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) {
+            double s1 = 0.0, s2 = 0.0, g = 0.0;
+            for (int r = 0; r < k; ++r) { s1 += b->D[r][a] * b->W[r][c]; s2 += b->W[r][a] * b->D[r][c]; g += b->D[r][a] * b->D[r][c]; }
+            b->S[a][c] = 0.5 * (s1 + s2);
+            b->G[a][c] = g;
+        }
+    orc_sym3_pinv(b->S, b->Sp);
+    orc_sym3_pinv(b->G, b->Gp);
+    double alpha = 0.0;
+    for (int r = 0; r < k; ++r) alpha += b->diag[r];
+    b->alpha = k ? alpha / k : 0.0;
+}
+
+/* The mass block M_v = W S^+ W^T + alpha (I - D G^+ D^T) over the live slots
+ * (k x k, row stride 7). */
+static void mass_block(const massparts *b, double *M)
+{
+    for (int r = 0; r < b->k; ++r)
+        for (int c = 0; c < b->k; ++c) {
+            double ws = 0.0, dq = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int e = 0; e < 3; ++e) {
+                    ws += b->W[r][a] * b->Sp[a][e] * b->W[c][e];
+                    dq += b->D[r][a] * b->Gp[a][e] * b->D[c][e];
+                }
+            M[r * 7 + c] = ws + b->alpha * ((r == c ? 1.0 : 0.0) - dq);
+        }
+}
+
 /* Per-node inverse mass blocks (7x7 each, zero rows/cols for PEC/unused slots). */
 static int build_minv(const tetmesh *m, const double *eps_r, double *minv)
 {
     for (size_t v = 0; v < m->nnode; ++v) {
-        int slot[7], k = 0;
-        for (int d = 0; d < 7; ++d)
-            if (!m->pec[7 * v + d]) slot[k++] = d;
+        massparts b;
+        mass_parts(m, eps_r, v, &b);
         double *B = minv + 49 * v;
         memset(B, 0, sizeof(double) * 49);
-        if (k == 0) continue;
-        double W[7][3] = {{0}}, D[7][3], diag[7] = {0};
-        for (int r = 0; r < k; ++r) {
-            int e = (int)(7 * v + slot[r]);
-            for (int q = 0; q < 3; ++q) D[r][q] = DIRV[slot[r]][q];
-            for (int s = m->inc_ptr[e]; s < m->inc_ptr[e + 1]; ++s) {
-                int t = m->inc[s] >> 3, l = m->inc[s] & 7, p = t % 6;
-                double ep = eps_r[t];
-                for (int q = 0; q < 3; ++q) W[r][q] += ep * m->shape_wint[p][l][q];
-                diag[r] += ep * m->shape_wsq[p][l];
-            }
-        }
-        double S[3][3], G[3][3], Sp[3][3], Gp[3][3];
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) {
-                double s1 = 0.0, s2 = 0.0, g = 0.0;
-                for (int r = 0; r < k; ++r) { s1 += D[r][a] * W[r][b]; s2 += W[r][a] * D[r][b]; g += D[r][a] * D[r][b]; }
-                S[a][b] = 0.5 * (s1 + s2);
-                G[a][b] = g;
-            }
-        orc_sym3_pinv(S, Sp);
-        orc_sym3_pinv(G, Gp);
-        double alpha = 0.0;
-        for (int r = 0; r < k; ++r) alpha += diag[r];
-        alpha /= k;
+        if (b.k == 0) continue;
         double M[49] = {0};
-        for (int r = 0; r < k; ++r)
-            for (int c = 0; c < k; ++c) {
-                double ws = 0.0, dq = 0.0;
-                for (int a = 0; a < 3; ++a)
-                    for (int b = 0; b < 3; ++b) {
-                        ws += W[r][a] * Sp[a][b] * W[c][b];
-                        dq += D[r][a] * Gp[a][b] * D[c][b];
-                    }
-                M[r * 7 + c] = ws + alpha * ((r == c ? 1.0 : 0.0) - dq);
-            }
-        if (orc_spd_inverse7(M, k) != 0) return -1;
-        for (int r = 0; r < k; ++r)
-            for (int c = 0; c < k; ++c) B[slot[r] * 7 + slot[c]] = M[r * 7 + c];
+        mass_block(&b, M);
+        if (orc_spd_inverse7(M, b.k) != 0) return -1;
+        for (int r = 0; r < b.k; ++r)
+            for (int c = 0; c < b.k; ++c) B[b.slot[r] * 7 + b.slot[c]] = M[r * 7 + c];
     }
     return 0;
 }
@@ -576,6 +597,249 @@ int orc_tet_apply_K(int nx, int ny, int nz, const double *x, double *f)
     double *cb = malloc(sizeof(double) * 3 * m.ntet);
     apply_K_tet(&m, NULL, x, f, cb);
     free(cb);
+    free_tetmesh(&m);
+    return 0;
+}
+
+/* ------------------------------------------------------------ adjoint ---
+ * Gradient of a receiver-trace functional J with respect to the per-tet
+ * permittivity, by the discrete adjoint of the symplectic loop of
+ * orc_tet_run.  Only the mass blocks depend on eps, so every drift
+ * U += c M^-1 P contributes -c (M^-1 Ubar)^T (dM/deps_t) (M^-1 P); these
+ * outer products are summed per node (Q_v) over the whole run and
+ * contracted with dM_v/deps_t at the end.  All forward P vectors are kept
+ * (small cases only). */
+
+/* dM_v/deps_t over the live slots of v (k x k, row stride 7):
+ *   dM = dW S^+ W^T + W S^+ dW^T + W d(S^+) W^T + dalpha (I - D G^+ D^T).
+ * S^+ keeps the eigenvalues above 1e-10 max|lambda| (orc_sym3_pinv), so at
+ * edge and corner nodes, where S is indefinite, it is the spectral function
+ * f(lambda) = 1/lambda on the kept eigenvalues and 0 elsewhere; its
+ * derivative is V (F o (V^T dS V)) V^T with the divided differences
+ * F_ij = (f(l_i) - f(l_j)) / (l_i - l_j), F_ii = f'(l_i) (Daleckii-Krein). */
+static void sym3_pinv_deriv(const double S[3][3], const double dS[3][3], double dSp[3][3])
+{
+    double w[3], V[3][3];
+    orc_sym3_eig(S, w, V);
+    double mx = fmax(fabs(w[0]), fmax(fabs(w[1]), fabs(w[2])));
+    int keep[3];
+    for (int i = 0; i < 3; ++i) keep[i] = w[i] > 1e-10 * mx;
+    double A[3][3], B[3][3];
+    for (int i = 0; i < 3; ++i)          /* A = V^T dS V */
+        for (int j = 0; j < 3; ++j) {
+            double x = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int c = 0; c < 3; ++c) x += V[a][i] * dS[a][c] * V[c][j];
+            A[i][j] = x;
+        }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double F;
+            if (keep[i] && keep[j]) F = -1.0 / (w[i] * w[j]);
+            else if (keep[i]) F = 1.0 / (w[i] * (w[i] - w[j]));
+            else if (keep[j]) F = 1.0 / (w[j] * (w[j] - w[i]));
+            else F = 0.0;
+            B[i][j] = F * A[i][j];
+        }
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) {
+            double x = 0.0;
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) x += V[a][i] * B[i][j] * V[c][j];
+            dSp[a][c] = x;
+        }
+}
+
+static void mass_block_deriv(const tetmesh *m, const massparts *b, size_t v, size_t t, double *dM)
+{
+    const int k = b->k, p = (int)(t % 6);
+    double dW[7][3] = {{0}}, dd[7] = {0};
+    for (int r = 0; r < k; ++r) {
+        int e = (int)(7 * v + b->slot[r]);
+        for (int s = m->inc_ptr[e]; s < m->inc_ptr[e + 1]; ++s)
+            if ((size_t)(m->inc[s] >> 3) == t) {
+                int l = m->inc[s] & 7;
+                for (int q = 0; q < 3; ++q) dW[r][q] += m->shape_wint[p][l][q];
+                dd[r] += m->shape_wsq[p][l];
+            }
+    }
+    double dalpha = 0.0;
+    for (int r = 0; r < k; ++r) dalpha += dd[r];
+    dalpha = k ? dalpha / k : 0.0;
+    double dS[3][3], dSp[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) {
+            double x = 0.0;
+            for (int r = 0; r < k; ++r) x += b->D[r][a] * dW[r][c] + dW[r][a] * b->D[r][c];
+            dS[a][c] = 0.5 * x;
+        }
+    sym3_pinv_deriv(b->S, dS, dSp);
+    for (int r = 0; r < k; ++r)
+        for (int c = 0; c < k; ++c) {
+            double x = 0.0, dq = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int e = 0; e < 3; ++e) {
+                    x += dW[r][a] * b->Sp[a][e] * b->W[c][e] + b->W[r][a] * b->Sp[a][e] * dW[c][e] +
+                         b->W[r][a] * dSp[a][e] * b->W[c][e];
+                    dq += b->D[r][a] * b->Gp[a][e] * b->D[c][e];
+                }
+            dM[r * 7 + c] = x + dalpha * ((r == c ? 1.0 : 0.0) - dq);
+        }
+}
+
+/* The mass block of node v (7 x 7 over all slots, zero rows/cols for dead
+ * slots) and, when t >= 0, its derivative with respect to eps_t. */
+int orc_tet_mass_block(int nx, int ny, int nz, const double *eps_r, long v, long t, double *M, double *dM)
+{
+    tetmesh m;
+    build_tetmesh(&m, nx, ny, nz);
+    if (v < 0 || (size_t)v >= m.nnode || t >= (long)m.ntet) { free_tetmesh(&m); return -1; }
+    massparts b;
+    mass_parts(&m, eps_r, (size_t)v, &b);
+    double Mk[49] = {0}, dMk[49] = {0};
+    mass_block(&b, Mk);
+    if (t >= 0) mass_block_deriv(&m, &b, (size_t)v, (size_t)t, dMk);
+    memset(M, 0, sizeof(double) * 49);
+    if (dM) memset(dM, 0, sizeof(double) * 49);
+    for (int r = 0; r < b.k; ++r)
+        for (int c = 0; c < b.k; ++c) {
+            M[b.slot[r] * 7 + b.slot[c]] = Mk[r * 7 + c];
+            if (dM) dM[b.slot[r] * 7 + b.slot[c]] = dMk[r * 7 + c];
+        }
+    free_tetmesh(&m);
+    return 0;
+}
+
+/* Q_v += c/2 (y z^T + z y^T) over every node (y, z: nslot vectors). */
+static void accumulate_outer(const tetmesh *m, double c, const double *y, const double *z, double *Q)
+{
+#pragma omp parallel for schedule(static)
+    for (long v = 0; v < (long)m->nnode; ++v)
+        for (int r = 0; r < 7; ++r)
+            for (int s = 0; s < 7; ++s)
+                Q[49 * v + 7 * r + s] += 0.5 * c * (y[7 * v + r] * z[7 * v + s] + z[7 * v + r] * y[7 * v + s]);
+}
+
+/* dJ/deps for the symplectic integrators.  trace_grad: dJ/dtraces in the
+ * layout of orc_tet_run's traces (nrec * nsamp * 4, column 0 ignored).  The
+ * run starts from zero fields at t = 0. */
+int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad, double *grad_eps)
+{
+    if (c->integrator == ORC_LEAPFROG) return -2;
+    tetmesh m;
+    build_tetmesh(&m, c->nx, c->ny, c->nz);
+    const size_t ns = m.nslot;
+    double *minv = malloc(sizeof(double) * 49 * m.nnode);
+    if (build_minv(&m, c->eps_r, minv) != 0) { free(minv); free_tetmesh(&m); return -1; }
+    double *mu_inv = NULL;
+    if (c->mu_r) {
+        mu_inv = malloc(sizeof(double) * m.ntet);
+        for (size_t t = 0; t < m.ntet; ++t) mu_inv[t] = 1.0 / c->mu_r[t];
+    }
+    int nd = c->ndip;
+    double (*dw)[6] = malloc(sizeof(double) * 6 * (nd > 0 ? nd : 1));
+    int (*de)[6] = malloc(sizeof(int) * 6 * (nd > 0 ? nd : 1));
+    for (int s = 0; s < nd; ++s) {
+        double w[6][3];
+        orc_tet_locate(c->nx, c->ny, c->nz, c->dip_pos + 3 * s, w, de[s]);
+        const double *dir = c->dip_dir + 3 * s;
+        for (int l = 0; l < 6; ++l) dw[s][l] = (w[l][0] * dir[0] + w[l][1] * dir[1] + w[l][2] * dir[2]) * c->dip_amp[s];
+    }
+    int nr = c->nrec;
+    double (*rw)[6][3] = malloc(sizeof(double) * 18 * (nr > 0 ? nr : 1));
+    int (*re)[6] = malloc(sizeof(int) * 6 * (nr > 0 ? nr : 1));
+    for (int r = 0; r < nr; ++r) orc_tet_locate(c->nx, c->ny, c->nz, c->rec_pos + 3 * r, rw[r], re[r]);
+    const int tf = c->time_frequency;
+    const int nsamp = nsteps > 0 ? (nsteps - 1) / tf + 1 : 0;
+    const double dt = c->dt, x1 = 1.0 / (2.0 - pow(2.0, 1.0 / 3.0)), x2 = 1.0 - 2.0 * x1;
+    double sub[3] = {dt, 0, 0}, off[3] = {0, 0, 0};
+    int nsub = 1;
+    if (c->integrator == ORC_SYMP4) { nsub = 3; sub[0] = x1 * dt; sub[1] = x2 * dt; sub[2] = x1 * dt; off[1] = x1 * dt; off[2] = (x1 + x2) * dt; }
+
+    /* forward: Pk[i] = P after kick i (i = 0 .. nsteps*nsub-1), Pk[-1] = 0 */
+    const size_t nk = (size_t)nsteps * nsub;
+    double *Pstore = calloc((nk + 1) * ns, sizeof(double));
+    double *U = calloc(ns, sizeof(double)), *P = calloc(ns, sizeof(double));
+    double *F = calloc(ns, sizeof(double)), *Y = calloc(ns, sizeof(double)), *Z = calloc(ns, sizeof(double));
+    double *cb = malloc(sizeof(double) * 3 * m.ntet);
+    double t = 0.0;
+    for (int step = 0; step < nsteps; ++step) {
+        for (int q = 0; q < nsub; ++q) {
+            double a = sub[q];
+            apply_minv(&m, minv, P, Y);
+            for (size_t e = 0; e < ns; ++e) U[e] += 0.5 * a * Y[e];
+            apply_K_tet(&m, mu_inv, U, F, cb);
+            for (int s = 0; s < nd; ++s) {
+                double g = orc_tet_wave(c->dip_kind[s], c->dip_f0[s], t + off[q] + 0.5 * a);
+                for (int l = 0; l < 6; ++l) F[de[s][l]] -= dw[s][l] * g;
+            }
+            for (size_t e = 0; e < ns; ++e) {
+                if (m.pec[e]) F[e] = 0.0;
+                P[e] -= a * F[e];
+            }
+            memcpy(Pstore + (1 + (size_t)step * nsub + q) * ns, P, sizeof(double) * ns);
+            apply_minv(&m, minv, P, Y);
+            for (size_t e = 0; e < ns; ++e) U[e] += 0.5 * a * Y[e];
+        }
+        t += dt;
+    }
+    /* reverse */
+    double *Ub = calloc(ns, sizeof(double)), *Pb = calloc(ns, sizeof(double));
+    double *Q = calloc(49 * m.nnode, sizeof(double));
+    for (int step = nsteps - 1; step >= 0; --step) {
+        for (int q = nsub - 1; q >= 0; --q) {
+            double a = sub[q];
+            size_t i = (size_t)step * nsub + q;
+            /* second half drift, with P after kick i */
+            apply_minv(&m, minv, Ub, Y);
+            for (size_t e = 0; e < ns; ++e) Pb[e] += 0.5 * a * Y[e];
+            apply_minv(&m, minv, Pstore + (1 + i) * ns, Z);
+            accumulate_outer(&m, 0.5 * a, Y, Z, Q);
+            /* kick: P -= a Pi K U  =>  Ubar -= a K Pi Pbar */
+            for (size_t e = 0; e < ns; ++e) Y[e] = m.pec[e] ? 0.0 : Pb[e];
+            apply_K_tet(&m, mu_inv, Y, F, cb);
+            for (size_t e = 0; e < ns; ++e) Ub[e] -= a * F[e];
+            /* first half drift, with P before kick i */
+            apply_minv(&m, minv, Ub, Y);
+            for (size_t e = 0; e < ns; ++e) Pb[e] += 0.5 * a * Y[e];
+            apply_minv(&m, minv, Pstore + i * ns, Z);
+            accumulate_outer(&m, 0.5 * a, Y, Z, Q);
+        }
+        if (step % tf == 0)
+            for (int r = 0; r < nr; ++r) {
+                const double *g = trace_grad + ((size_t)r * nsamp + step / tf) * 4;
+                for (int l = 0; l < 6; ++l)
+                    Ub[re[r][l]] += rw[r][l][0] * g[1] + rw[r][l][1] * g[2] + rw[r][l][2] * g[3];
+            }
+    }
+    /* contraction: grad_t = -sum_v <dM_v/deps_t, Q_v> over the nodes whose
+     * blocks depend on eps_t (the tails of t's edges) */
+    memset(grad_eps, 0, sizeof(double) * m.ntet);
+    for (size_t v = 0; v < m.nnode; ++v) {
+        massparts b;
+        mass_parts(&m, c->eps_r, v, &b);
+        if (b.k == 0) continue;
+        long seen[64];
+        int nseen = 0;
+        for (int r = 0; r < b.k; ++r) {
+            int e = (int)(7 * v + b.slot[r]);
+            for (int s = m.inc_ptr[e]; s < m.inc_ptr[e + 1]; ++s) {
+                long tt = m.inc[s] >> 3;
+                int dup = 0;
+                for (int u = 0; u < nseen; ++u) dup |= seen[u] == tt;
+                if (dup || nseen == 64) continue;
+                seen[nseen++] = tt;
+                double dM[49];
+                mass_block_deriv(&m, &b, v, (size_t)tt, dM);
+                double acc = 0.0;
+                for (int i = 0; i < b.k; ++i)
+                    for (int j = 0; j < b.k; ++j) acc += dM[i * 7 + j] * Q[49 * v + 7 * b.slot[i] + b.slot[j]];
+                grad_eps[tt] -= acc;
+            }
+        }
+    }
+    free(Pstore); free(U); free(P); free(F); free(Y); free(Z); free(cb); free(Ub); free(Pb); free(Q);
+    free(mu_inv); free(minv); free(dw); free(de); free(rw); free(re);
     free_tetmesh(&m);
     return 0;
 }
