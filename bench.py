@@ -15,7 +15,9 @@ receivers, FP32 fields.  Metric: DOF-updates/s (edges x time steps / time).
 `cpu_baseline` the FP64 oracle on the host cores over a bounded sample.
 A secondary object `fdtd_512` times the 512^3 FP32 Yee update with a 10-cell
 CPML (HBM-bound) for a bounded number of steps; `batch64` times 64 batched
-shots of uneven size (FP32) against the per-shot FP64 GPU path.
+shots of uneven size (FP32) against the per-shot FP64 GPU path; `adjoint16`
+times the forward + adjoint misfit gradient of 16 shots on a 48^3 x 6 tet
+cube (FP32 batched against the per-shot FP64 GPU path).
 
 `--impl reference` times the FP64 CPU oracle (the reference has no
 tetrahedral solver; this is the restated algorithm) with all host threads.
@@ -226,6 +228,104 @@ def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
             "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
 
 
+def blob_model(n, rng, background=2.0, nblob=3):
+    """Per-tet eps_r: background plus nblob Gaussian blobs (amplitude U[1,3],
+    width U[4,8] cells) evaluated at the tetrahedron centroids."""
+    # centroid of Kuhn tetrahedron p of cell (i,j,k): cell corner + (3/4, 2/4, 1/4) along its axis order
+    perm = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    off = np.zeros((6, 3))
+    for p, (a, b, c) in enumerate(perm):
+        off[p, a], off[p, b], off[p, c] = 0.75, 0.5, 0.25
+    k, j, i = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    corner = np.stack([i.ravel(), j.ravel(), k.ravel()], 1).astype(float)
+    cen = (corner[:, None, :] + off[None, :, :]).reshape(-1, 3)
+    eps = np.full(cen.shape[0], background)
+    for _ in range(nblob):
+        c = rng.uniform(0.25, 0.75, 3) * n
+        amp, width = rng.uniform(1.0, 3.0), rng.uniform(4.0, 8.0)
+        eps += amp * np.exp(-np.sum((cen - c) ** 2, 1) / (2 * width ** 2))
+    return eps
+
+
+def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, sample_steps=400):
+    """Forward + adjoint misfit gradient: nshots Ricker dipole shots on an
+    n^3 x 6 tet cube (true eps_r = 2 + 3 Gaussian blobs, start model 2), nrec
+    receivers per shot, symp4, `steps` steps, L2 trace misfit, nsnap
+    snapshots.  FP32 batched (all shots in one handle) against the plain
+    per-shot FP64 GPU path, the latter timed on one shot over
+    `sample_steps` steps (same segment length) and scaled to `steps`."""
+    import emsolvers_gb300 as ems
+    rng = np.random.default_rng(SEED + 5)
+    true = blob_model(n, rng)
+    start = np.full(true.size, 2.0)
+    f0 = C0 / (10 * H * np.sqrt(2.0))
+    src = [rng.uniform(0.2, 0.8, 3) * n * H for _ in range(nshots)]
+    rec = [rng.uniform(0.1, 0.9, 3) * n * H for _ in range(nrec)]
+    probe = ems.TetFemSimulation((n, n, n), H, 1, ems.SYMP4, ems.FP32, dt=0.0, cfl_fraction=0.9)
+    probe.set_material(start)
+    dt, _ = probe.time_step()
+    probe.close()
+
+    def handle(precision, shots, model):
+        b = ems.TetFemBatch([(n, n, n)] * len(shots), H, integrator=ems.SYMP4, precision=precision, dt=dt)
+        b.set_material(np.tile(model, len(shots)))
+        for k, s in enumerate(shots):
+            b.add_dipole(k, src[s], (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
+            for r in rec:
+                b.add_receiver(k, r)
+        return b
+
+    shots = list(range(nshots))
+    b = handle(ems.FP32, shots, true)
+    b.run(steps)
+    obs = b.traces()
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.set_material(np.tile(start, nshots))
+    b.set_checkpoints(nsnap)
+    b.reset()
+    b.run(steps)
+    fwd_ms, _ = b.run_stats()
+    J, tg = ems.trace_misfit(b.traces(), obs, ems.MISFIT_L2)
+    g32 = b.backward(tg).reshape(nshots, -1).sum(0)
+    wall32 = time.perf_counter() - t0
+    b.close()
+    # per-shot FP64 sample with the same segment length
+    seg = -(-steps // nsnap)
+    one = handle(ems.FP64, [0], start)
+    one.set_checkpoints(-(-sample_steps // seg))
+    obs0 = obs[:nrec, :sample_steps]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    one.set_material(start)
+    one.reset()
+    one.run(sample_steps)
+    _, tg0 = ems.trace_misfit(one.traces(), obs0, ems.MISFIT_L2)
+    g64_0 = one.backward(tg0)
+    wall64 = (time.perf_counter() - t0) * steps / sample_steps
+    tr64 = one.traces()
+    one.close()
+    # FP32 against FP64 on the same sampled shot
+    one32 = handle(ems.FP32, [0], start)
+    one32.set_checkpoints(-(-sample_steps // seg))
+    one32.reset()
+    one32.run(sample_steps)
+    g32_0 = one32.backward(tg0)
+    tr_err = float(np.linalg.norm(one32.traces()[..., 1:] - tr64[..., 1:]) / np.linalg.norm(tr64[..., 1:]))
+    one32.close()
+    g_err = float(np.linalg.norm(g32_0 - g64_0) / np.linalg.norm(g64_0))
+    return {"workload": f"tet{n}_adjoint_{nshots}shots_symp4_{steps}", "tets_per_shot": int(true.size),
+            "shots": nshots, "receivers_per_shot": nrec, "steps": steps, "snapshots": nsnap, "misfit": "L2",
+            "order": 1, "dt_s": dt, "misfit_value": J, "grad_norm": float(np.linalg.norm(g32)),
+            "fp32_batched_s": wall32, "fp32_forward_ms": fwd_ms,
+            "shots_per_s_fp32_batched": nshots / wall32, "shots_per_s_fp64_per_shot": 1.0 / wall64,
+            "speedup_vs_fp64_per_shot": (nshots / wall32) * wall64,
+            "fp64_sample": f"1 shot x {sample_steps} steps, scaled to {steps}",
+            "fp32_vs_fp64_trace_rel_l2": tr_err, "fp32_vs_fp64_grad_rel_l2": g_err,
+            "timing": "wall clock: material upload + FP64 mass setup + recorded forward + misfit + backward"}
+
+
 def run_gpu(args):
     import torch
     import emsolvers_gb300 as ems
@@ -322,6 +422,11 @@ def run_gpu(args):
                 out["batch64"] = batch64()
             except Exception as e:  # secondary measurement only
                 out["batch64"] = {"error": str(e)}
+        if not args.no_adjoint:
+            try:
+                out["adjoint16"] = adjoint16()
+            except Exception as e:  # secondary measurement only
+                out["adjoint16"] = {"error": str(e)}
         if not args.no_fdtd:
             try:
                 out["fdtd_512"] = fdtd_512()
@@ -342,7 +447,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fdtd", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
-    ap.add_argument("--only", choices=["batch", "fdtd"],
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--only", choices=["batch", "fdtd", "adjoint"],
                     help="run one secondary workload alone and print its JSON (for profiling)")
     ap.add_argument("--fdtd-n", type=int, default=512, help="FDTD cube side for --only fdtd")
     args = ap.parse_args()
@@ -351,7 +457,8 @@ def main():
     if args.only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps(batch64() if args.only == "batch" else fdtd_512(n=args.fdtd_n)))
+        fn = {"batch": batch64, "fdtd": lambda: fdtd_512(n=args.fdtd_n), "adjoint": adjoint16}[args.only]
+        print(json.dumps(fn()))
     elif args.impl == "reference":
         run_reference(args)
     else:

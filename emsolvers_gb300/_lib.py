@@ -87,6 +87,9 @@ def lib():
         "ems_tetfem_add_receiver": (C.c_int, [vp, dp]),
         "ems_tetfem_time_step": (C.c_int, [vp, dp, dp]),
         "ems_tetfem_apply_stiffness": (C.c_int, [vp, dp, dp, C.c_size_t]),
+        "ems_tetfem_set_checkpoints": (C.c_int, [vp, C.c_int]),
+        "ems_tetfem_backward": (C.c_int, [vp, dp, C.c_size_t, dp, C.c_size_t]),
+        "ems_trace_misfit": (C.c_int, [C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp]),
         "ems_tet_stiffness_apply_static": (C.c_int, [ip, vp, vp, vp]),
         "ems_run": (C.c_int, [vp, C.c_int]),
         "ems_trace_shape": (C.c_int, [vp, ip, ip, ip]),

@@ -197,6 +197,22 @@ int ems_tetfem_apply_stiffness(ems_sim *s, const double *u, double *f, size_t n)
     return guard(s, [&] { ems::tetfem_apply_stiffness(s->impl, u, f, n); });
 }
 
+int ems_tetfem_set_checkpoints(ems_sim *s, int nsnap)
+{
+    NEED(s, ems::Kind::TETFEM);
+    return guard(s, [&] { ems::tetfem_set_checkpoints(s->impl, nsnap); });
+}
+int ems_tetfem_backward(ems_sim *s, const double *tg, size_t n, double *grad, size_t ntet)
+{
+    NEED(s, ems::Kind::TETFEM);
+    return guard(s, [&] { ems::tetfem_backward(s->impl, tg, n, grad, ntet); });
+}
+int ems_trace_misfit(int kind, int nobs, int nsamp, const double *tr, const double *obs, const double *band, double *misfit,
+                     double *tg)
+{
+    return guard(nullptr, [&] { ems::trace_misfit(kind, nobs, nsamp, tr, obs, misfit, tg, band); });
+}
+
 int ems_run(ems_sim *s, int n)
 {
     if (!s) return EMS_ERR_INVALID_ARGUMENT;

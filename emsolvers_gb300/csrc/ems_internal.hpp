@@ -100,6 +100,10 @@ void tetfem_add_dipole(Sim *s, const double pos[3], const double dir[3], int wav
 void tetfem_add_receiver(Sim *s, const double pos[3]);
 void tetfem_time_step(const Sim *s, double *dt, double *lim);
 void tetfem_apply_stiffness(Sim *s, const double *u, double *f, size_t n);
+void tetfem_set_checkpoints(Sim *s, int nsnap);
+void tetfem_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, size_t ngrad);
+void trace_misfit(int kind, int nobs, int nsamp, const double *traces, const double *observed, double *misfit,
+                  double *trace_grad, const double *tf_band);
 
 // Source waveforms evaluated on the host in FP64.
 double fdtd_source_value(int kind, double f0, double t, double h);

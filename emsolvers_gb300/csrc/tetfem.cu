@@ -23,6 +23,7 @@
 #include <cstring>
 #include <fstream>
 #include <iomanip>
+#include <unordered_map>
 
 #include "ems_internal.hpp"
 
@@ -356,13 +357,13 @@ __device__ __forceinline__ double source_load(const SrcArgs &s, size_t e)
 
 // Kick + drift, eight lanes per node (lane 7 idle):
 //   P_e -= a * (F_e - f_e)   (F = K U gathered, f the dipole load; PEC slots keep F = 0),
-//   U_e += c * (Minv_v P)_e.
+//   U_e += c * (Minv_v P)_e,  and zout_e = (Minv_v P)_e when zout is given.
 // With minv == nullptr only P is written (P -= a F): the stiffness apply.
 template <class T>
 __global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
                                                        const unsigned char *__restrict__ pec, const vec4<T> *__restrict__ B,
                                                        const T *__restrict__ minv, T *__restrict__ P, T *__restrict__ U, T a, T c,
-                                                       SrcArgs src)
+                                                       SrcArgs src, T *__restrict__ zout)
 {
     __shared__ vec4<T> sc[36];
     load_curl_table<T>(sc);
@@ -386,6 +387,7 @@ __global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *
     if (v >= nnode) v = nnode - 1;   // keep the whole warp in the shuffles
     T y = block_apply<T>(minv + 28 * v, d, p);
     if (live && c != T(0)) U[e] = fma(c, y, U[e]);
+    if (zout && live) zout[e] = y;   // Minv P of this drift, kept for the adjoint
 }
 
 // U += c * Minv P (drift alone).
@@ -458,6 +460,227 @@ __global__ void __launch_bounds__(1024) tet_receiver_kernel(int nrec, const int 
     }
     __syncthreads();
     if (threadIdx.x == 0) ctl[0] = step + 1;
+}
+
+// ---------------------------------------------------------------- adjoint
+// The discrete adjoint of the merged symplectic loop runs the same two
+// launches per substep backward in time, with the roles of the fields
+// swapped: tet_curl_kernel on Pbar, then the adjoint kick below.  Only the
+// mass blocks depend on eps, so each drift U += c Minv P adds
+// -c (Minv Ubar)^T dM (Minv P) to dJ/deps; the outer products are summed per
+// node in FP64 (Q_v, packed symmetric like the mass blocks) and contracted
+// with dM_v/deps once at the end (tet_grad_node_kernel).
+
+// Adjoint kick (eight lanes per node):
+//   Wb_e -= a * F_e        (F = K Pbar gathered from B; PEC slots keep F = 0)
+//   y = Minv_v Wb,  Pb_e += c * y_e,  Q_v += c * sym(y z^T)
+// with z = Minv P of the forward drift being reversed.
+template <class T>
+__global__ void __launch_bounds__(256) tet_adjoint_kick_kernel(size_t nnode, const int *__restrict__ inc_ptr,
+                                                               const int *__restrict__ inc, const unsigned char *__restrict__ pec,
+                                                               const vec4<T> *__restrict__ B, const T *__restrict__ minv,
+                                                               T *__restrict__ Wb, T *__restrict__ Pb, const T *__restrict__ z,
+                                                               double *__restrict__ Q, T a, T c)
+{
+    __shared__ vec4<T> sc[36];
+    load_curl_table<T>(sc);
+    size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t v = g >> 3;
+    int d = (int)(g & 7);
+    bool live = v < nnode && d < 7;
+    size_t e = 7 * v + d;
+    T w = 0, zd = 0;
+    if (live) {
+        w = Wb[e];
+        if (!(pec[e] & kPecBit)) {
+            w = fma(-a, gather_force<T>(e, inc_ptr, inc, B, sc), w);
+            Wb[e] = w;
+        }
+        zd = z[e];
+    }
+    if (v >= nnode) v = nnode - 1;   // keep the whole warp in the shuffles
+    T y = block_apply<T>(minv + 28 * v, d, w);
+    if (live) Pb[e] = fma(c, y, Pb[e]);
+    double *q = Q + 28 * v;
+    const double hc = 0.5 * (double)c;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) {
+        T yj = __shfl_sync(0xffffffffu, y, j, 8), zj = __shfl_sync(0xffffffffu, zd, j, 8);
+        if (live && j >= d) q[pk7(d, j)] += hc * ((double)y * (double)zj + (double)yj * (double)zd);
+    }
+}
+
+// Receiver adjoint of one sample, one block.  The receivers' edge slots are
+// listed once each (slot k gathers w * r over its receiver terms), then
+// every node holding such a slot gets the half drift that the merged loop
+// folded into the sampling: Pbar += cc Minv a, Q += cc sym((Minv a) z^T).
+template <class T>
+__global__ void __launch_bounds__(1024) tet_receiver_adjoint_kernel(int nsl, const int *__restrict__ sl_slot,
+                                                                    const int *__restrict__ sl_ptr, const int *__restrict__ term_rc,
+                                                                    const double *__restrict__ term_w, const double *__restrict__ r,
+                                                                    int nnd, const int *__restrict__ nd_node,
+                                                                    const int *__restrict__ nd_map, double *__restrict__ a_scr,
+                                                                    T *__restrict__ Wb, T *__restrict__ Pb,
+                                                                    const T *__restrict__ minv, const T *__restrict__ z,
+                                                                    double *__restrict__ Q, double cc)
+{
+    for (int k = threadIdx.x; k < nsl; k += blockDim.x) {
+        double acc = 0.0;
+        for (int s = sl_ptr[k]; s < sl_ptr[k + 1]; ++s) acc += term_w[s] * r[term_rc[s]];
+        a_scr[k] = acc;
+        Wb[sl_slot[k]] += (T)acc;
+    }
+    if (cc == 0.0) return;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nnd; i += blockDim.x) {
+        const size_t v = (size_t)nd_node[i];
+        T x[7], y[7], zz[7];
+        for (int d = 0; d < 7; ++d) {
+            int k = nd_map[7 * i + d];
+            x[d] = k >= 0 ? (T)a_scr[k] : T(0);
+            zz[d] = z[7 * v + d];
+        }
+        for (int d = 0; d < 7; ++d) {
+            T s = 0;
+            for (int j = 0; j < 7; ++j) s = fma(minv[28 * v + pk7(d, j)], x[j], s);
+            y[d] = s;
+            Pb[7 * v + d] = fma((T)cc, s, Pb[7 * v + d]);
+        }
+        for (int d = 0; d < 7; ++d)
+            for (int j = d; j < 7; ++j)
+                Q[28 * v + pk7(d, j)] += 0.5 * cc * ((double)y[d] * (double)zz[j] + (double)y[j] * (double)zz[d]);
+    }
+}
+
+// dJ/deps contributions of node v, FP64.  With M_v = W S^+ W^T +
+// alpha (I - D G^+ D^T) and Q_v over the live slots,
+//   -<dM_v/deps_t, Q_v> = -sum over the incidences (slot r, tet t, edge l) of
+//       2 wint_l . Z_r + D_r^T Y wint_l + wsq_l pq,
+//   Z = Q W S^+,  pq = <I - D G^+ D^T, Q> / k,  Y = V (F o V^T (W^T Q W) V) V^T,
+// where V, lambda diagonalise S, S^+ keeps lambda > 1e-10 max|lambda|, and
+// F holds the divided differences of f(lambda) = 1/lambda (kept) or 0
+// (dropped), the derivative of that spectral function.  One value per
+// incidence entry, written to contrib at the entry's position.
+__global__ void tet_grad_node_kernel(size_t nnode, const unsigned char *__restrict__ pec, const int *__restrict__ inc_ptr,
+                                     const int *__restrict__ inc, const double *__restrict__ eps,
+                                     const double *__restrict__ Q, double *__restrict__ contrib)
+{
+    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nnode) return;
+    int slot[7], k = 0;
+    for (int d = 0; d < 7; ++d)
+        if (!(pec[7 * v + d] & kPecBit)) slot[k++] = d;
+    if (k == 0) return;
+    double W[7][3], D[7][3];
+    for (int r = 0; r < k; ++r) {
+        size_t e = 7 * v + slot[r];
+        W[r][0] = W[r][1] = W[r][2] = 0.0;
+        for (int q = 0; q < 3; ++q) D[r][q] = c_dir[slot[r]][q];
+        for (int s = inc_ptr[e]; s < inc_ptr[e + 1]; ++s) {
+            int t = inc[s] >> 3, l = inc[s] & 7, p = t % 6;
+            double ep = eps[t];
+            for (int q = 0; q < 3; ++q) W[r][q] += ep * c_wint[p][l][q];
+        }
+    }
+    double S[3][3], G[3][3], Gp[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            double s1 = 0.0, s2 = 0.0, g = 0.0;
+            for (int r = 0; r < k; ++r) { s1 += D[r][a] * W[r][b]; s2 += W[r][a] * D[r][b]; g += D[r][a] * D[r][b]; }
+            S[a][b] = 0.5 * (s1 + s2);
+            G[a][b] = g;
+        }
+    sym3_pinv(G, Gp);
+    double lam[3], V[3][3], A[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) A[a][b] = S[a][b];
+    sym3_eig(A, lam, V);
+    const double mx = fmax(fabs(lam[0]), fmax(fabs(lam[1]), fabs(lam[2])));
+    bool keep[3];
+    for (int i = 0; i < 3; ++i) keep[i] = lam[i] > 1e-10 * mx;
+    double Sp[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            double s = 0.0;
+            for (int i = 0; i < 3; ++i)
+                if (keep[i]) s += V[a][i] * V[b][i] / lam[i];
+            Sp[a][b] = s;
+        }
+    // QW (k x 3), then Z = QW S^+, X = W^T QW, pq
+    double QW[7][3], pq = 0.0;
+    for (int r = 0; r < k; ++r) {
+        double q0 = 0.0, q1 = 0.0, q2 = 0.0;
+        for (int c = 0; c < k; ++c) {
+            double qrc = Q[28 * v + pk7(slot[r], slot[c])];
+            q0 += qrc * W[c][0]; q1 += qrc * W[c][1]; q2 += qrc * W[c][2];
+            double dq = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) dq += D[r][a] * Gp[a][b] * D[c][b];
+            pq += ((r == c ? 1.0 : 0.0) - dq) * qrc;
+        }
+        QW[r][0] = q0; QW[r][1] = q1; QW[r][2] = q2;
+    }
+    pq /= k;
+    double X[3][3], Xt[3][3], Y[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            double s = 0.0;
+            for (int r = 0; r < k; ++r) s += W[r][a] * QW[r][b];
+            X[a][b] = s;
+        }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double s = 0.0;
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) s += V[a][i] * X[a][b] * V[b][j];
+            double F;
+            if (keep[i] && keep[j]) F = -1.0 / (lam[i] * lam[j]);
+            else if (keep[i]) F = 1.0 / (lam[i] * (lam[i] - lam[j]));
+            else if (keep[j]) F = 1.0 / (lam[j] * (lam[j] - lam[i]));
+            else F = 0.0;
+            Xt[i][j] = F * s;
+        }
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            double s = 0.0;
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) s += V[a][i] * Xt[i][j] * V[b][j];
+            Y[a][b] = s;
+        }
+    for (int r = 0; r < k; ++r) {
+        double Z[3], DY[3];
+        for (int b = 0; b < 3; ++b) {
+            Z[b] = QW[r][0] * Sp[0][b] + QW[r][1] * Sp[1][b] + QW[r][2] * Sp[2][b];
+            DY[b] = D[r][0] * Y[0][b] + D[r][1] * Y[1][b] + D[r][2] * Y[2][b];
+        }
+        size_t e = 7 * v + slot[r];
+        for (int s = inc_ptr[e]; s < inc_ptr[e + 1]; ++s) {
+            int t = inc[s] >> 3, l = inc[s] & 7, p = t % 6;
+            const double *wi = c_wint[p][l];
+            double val = 0.0;
+            for (int b = 0; b < 3; ++b) val += (2.0 * Z[b] + DY[b]) * wi[b];
+            contrib[s] = -(val + c_wsq[p][l] * pq);
+        }
+    }
+}
+
+// dJ/deps_t: sum of the contributions at the incidence entries of t's six
+// edges (PEC and unused slots carry none).
+__global__ void tet_grad_gather_kernel(size_t ntet, const int *__restrict__ tet_edge, const unsigned char *__restrict__ pec,
+                                       const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                                       const double *__restrict__ contrib, double *__restrict__ grad)
+{
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntet) return;
+    double g = 0.0;
+    for (int l = 0; l < 6; ++l) {
+        int e = tet_edge[6 * t + l];
+        if (pec[e] & kPecBit) continue;
+        const int code = (int)(t * 8 + l);
+        for (int s = inc_ptr[e]; s < inc_ptr[e + 1]; ++s)
+            if (inc[s] == code) g += contrib[s];
+    }
+    grad[t] = g;
 }
 
 // Block partial sums of x.y (deterministic two-pass reduction, FP64).
@@ -553,6 +776,13 @@ struct TetFemSim : Sim {
     DevBuf d_src_slot, d_src_coef, d_src_g, d_rec_e, d_rec_w, d_tr, d_ctl;
     bool ready = false;
     bool flags_dirty = false;       // pec_h gained source bits not yet on the device
+    // recording for the adjoint: snapshots of the merged state (U, P) at the
+    // start of every segment of rec_seg steps of the last run, if that run
+    // started from the reset state with ckpt_nsnap > 0
+    int ckpt_nsnap = 0, rec_nsteps = -1, rec_seg = 0;
+    bool fresh = true;              // zero fields at t = 0
+    DevBuf d_snap;
+    SrcArgs rec_sa{};
     double cur_time = 0.0;          // normalised
 
     // cells: 3 per shot.  Every shot is an independent cube mesh; the shots
@@ -700,6 +930,16 @@ struct TetFemSim : Sim {
                 if (sigma[t] != 0.0) throw Error{EMS_ERR_UNSUPPORTED, "conductivity in the tetrahedral solver is not supported"};
         eps_h.assign(eps_r, eps_r + ntet);
         ready = false;
+        rec_nsteps = -1;   // the recorded run used the old mass blocks
+    }
+
+    void set_checkpoints(int nsnap)
+    {
+        EMS_CHECK_ARG(nsnap >= 0, "snapshot count must be >= 0");
+        if (nsnap > 0 && P.integrator == EMS_LEAPFROG)
+            throw Error{EMS_ERR_UNSUPPORTED, "the adjoint is implemented for the symplectic integrators only"};
+        ckpt_nsnap = nsnap;
+        if (nsnap == 0) { rec_nsteps = -1; d_snap.release(); }
     }
 
     // FP64 mass-inverse setup on the GPU, then the stability limit by power
@@ -761,7 +1001,8 @@ struct TetFemSim : Sim {
         z.zero(stream);
         unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
         tet_kick_kernel<double><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                         B.as<vec4<double>>(), nullptr, z.as<double>(), nullptr, -1.0, 0.0, SrcArgs{});
+                                                         B.as<vec4<double>>(), nullptr, z.as<double>(), nullptr, -1.0, 0.0, SrcArgs{},
+                                                         nullptr);
     }
 
     double power_iteration(const DevBuf &minv_d, int iters)
@@ -822,27 +1063,53 @@ struct TetFemSim : Sim {
         }
     }
 
+    // Substeps of one time step in normalised units: kick lengths sub[q],
+    // source-time offsets off[q], merged drift lengths c[q] (the second half
+    // of substep q plus the first half of the next one) and the first half
+    // drift hfirst.
+    struct Schedule {
+        bool symp;
+        int nsub;
+        double sub[3], off[3], c[3], hfirst;
+    };
+    Schedule schedule() const
+    {
+        Schedule s{};
+        s.symp = P.integrator != EMS_LEAPFROG;
+        s.nsub = P.integrator == EMS_SYMP4 ? 3 : 1;
+        s.sub[0] = dtn;
+        if (s.nsub == 3) {
+            const double x1 = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0)), x2 = 1.0 - 2.0 * x1;
+            s.sub[0] = x1 * dtn; s.sub[1] = x2 * dtn; s.sub[2] = x1 * dtn;
+            s.off[1] = x1 * dtn; s.off[2] = (x1 + x2) * dtn;
+        }
+        for (int q = 0; q < s.nsub; ++q) s.c[q] = 0.5 * (s.sub[q] + s.sub[q + 1 < s.nsub ? q + 1 : 0]);
+        s.hfirst = 0.5 * s.sub[0];
+        return s;
+    }
+
     // One time step: receivers (and the step counter), then for the
     // symplectic steps curl + kick per substep with the drifts merged (the
     // last one also carries the first half drift of the next step), or for
-    // leapfrog curl + leapfrog update.  Returns the number of launches.
+    // leapfrog curl + leapfrog update.  zout (symplectic only): Minv P of
+    // substep q goes to zout + q * nslot.  Returns the number of launches.
     template <class T>
-    int enqueue_step(T *Uc, T *Pc, T *Uo, const double *sub, int nsub, double hfirst, const SrcArgs &sa0, bool symp)
+    int enqueue_step(T *Uc, T *Pc, T *Uo, const Schedule &sc, const SrcArgs &sa0, T *zout)
     {
         const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
         vec4<T> *B = d_B.as<vec4<T>>();
         tet_receiver_kernel<T><<<1, 256, 0, stream>>>(nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), Uc, Pc, d_minv.as<T>(),
-                                                      symp ? (T)hfirst : T(0), d_tr.as<double>(), nsamp, P.time_frequency,
-                                                      d_ctl.as<int>());
+                                                      sc.symp ? (T)sc.hfirst : T(0), d_tr.as<double>(), nsamp,
+                                                      P.time_frequency, d_ctl.as<int>());
         int nl = 1;
-        if (symp) {
-            for (int q = 0; q < nsub; ++q) {
+        if (sc.symp) {
+            for (int q = 0; q < sc.nsub; ++q) {
                 SrcArgs sa = sa0;
                 sa.q = q;
-                double c = q + 1 < nsub ? 0.5 * (sub[q] + sub[q + 1]) : 0.5 * (sub[q] + sub[0]);
                 tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Uc, nullptr, B);
                 tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                            B, d_minv.as<T>(), Pc, Uc, (T)sub[q], (T)c, sa);
+                                                            B, d_minv.as<T>(), Pc, Uc, (T)sc.sub[q], (T)sc.c[q], sa,
+                                                            zout ? zout + (size_t)q * nslot : nullptr);
                 nl += 2;
             }
         } else {
@@ -854,9 +1121,11 @@ struct TetFemSim : Sim {
         return nl;
     }
 
-    template <class T> void run_t(int nsteps)
+    // Uploads the receivers, the dipole table and the per-substep source
+    // values of an nsteps run from the current time; returns the source
+    // arguments of the step kernels and fills the sample times.
+    SrcArgs prepare_run(int nsteps, const Schedule &sc, std::vector<double> &times, double &t_end)
     {
-        if (!ready) setup();
         const int tf = P.time_frequency;
         nobs = (int)rec_edges.size();
         nsamp = nsteps > 0 ? (nsteps - 1) / tf + 1 : 0;
@@ -885,29 +1154,38 @@ struct TetFemSim : Sim {
             EMS_CUDA(cudaMemcpyAsync(d_pec.p, pec_h.data(), nslot, cudaMemcpyHostToDevice, stream));
             flags_dirty = false;
         }
-        const double x1 = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0)), x2 = 1.0 - 2.0 * x1;
-        const bool symp = P.integrator != EMS_LEAPFROG;
-        int nsub = P.integrator == EMS_SYMP4 ? 3 : 1;
-        double sub[3] = {dtn, 0, 0}, off[3] = {0, 0, 0};
-        if (nsub == 3) { sub[0] = x1 * dtn; sub[1] = x2 * dtn; sub[2] = x1 * dtn; off[1] = x1 * dtn; off[2] = (x1 + x2) * dtn; }
         size_t nd = std::max<size_t>(dips.size(), 1);
-        std::vector<double> gv((size_t)std::max(nsteps, 1) * nsub * nd, 0.0);
-        std::vector<double> times(std::max(nsamp, 1), 0.0);
+        std::vector<double> gv((size_t)std::max(nsteps, 1) * sc.nsub * nd, 0.0);
+        times.assign(std::max(nsamp, 1), 0.0);
         double t = cur_time;
         for (int st = 0; st < nsteps; ++st) {
-            for (int q = 0; q < nsub; ++q)
+            for (int q = 0; q < sc.nsub; ++q)
                 for (size_t k = 0; k < dips.size(); ++k) {
-                    double tt = symp ? t + off[q] + 0.5 * sub[q] : t;
-                    gv[((size_t)st * nsub + q) * nd + k] = tet_wave(dips[k].kind, dips[k].f0n, tt);
+                    double tt = sc.symp ? t + sc.off[q] + 0.5 * sc.sub[q] : t;
+                    gv[((size_t)st * sc.nsub + q) * nd + k] = tet_wave(dips[k].kind, dips[k].f0n, tt);
                 }
             if (st % tf == 0) times[st / tf] = t;
             t += dtn;
         }
+        t_end = t;
         up(d_src_g, gv);
         d_ctl.alloc(16);
         d_ctl.zero(stream);
-        SrcArgs sa{nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(), d_src_g.as<double>(), d_ctl.as<int>(), (int)nd, nsub, 0};
-        const double hfirst = 0.5 * sub[0];
+        return SrcArgs{nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(), d_src_g.as<double>(), d_ctl.as<int>(), (int)nd,
+                       sc.nsub, 0};
+    }
+
+    template <class T> void run_t(int nsteps)
+    {
+        if (!ready) setup();
+        const Schedule sc = schedule();
+        const bool symp = sc.symp;
+        // record for ems_tetfem_backward: symplectic runs from the reset state
+        const bool record = ckpt_nsnap > 0 && symp && fresh && nsteps > 0;
+        rec_nsteps = -1;
+        std::vector<double> times;
+        double t_end = 0.0;
+        const SrcArgs sa = prepare_run(nsteps, sc, times, t_end);
         const unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
         // leapfrog ring: Uc = E^n, Pc = E^{n-1}, Uo = scratch for E^{n+1}
         T *Uc = d_U.as<T>(), *Pc = d_P.as<T>(), *Uo = d_Uold.as<T>();
@@ -917,13 +1195,12 @@ struct TetFemSim : Sim {
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
         int per_graph = 0;
-        const int nrep = nsteps / kGraphSteps;
-        if (nrep > 0) {
+        if (nsteps >= kGraphSteps) {
             EMS_CUDA(cudaStreamSynchronize(stream));
             EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
             T *u = Uc, *p = Pc, *o = Uo;
             for (int st = 0; st < kGraphSteps; ++st) {
-                per_graph += enqueue_step<T>(u, p, o, sub, nsub, hfirst, sa, symp);
+                per_graph += enqueue_step<T>(u, p, o, sc, sa, nullptr);
                 if (!symp) { T *tmp = p; p = u; u = o; o = tmp; }
             }
             cudaError_t ce = cudaStreamEndCapture(stream, &graph);
@@ -935,19 +1212,39 @@ struct TetFemSim : Sim {
             }
         }
         long long launches = 0;
+        auto advance = [&](int k) {
+            const int nrep = exec ? k / kGraphSteps : 0;
+            for (int r = 0; r < nrep; ++r) EMS_CUDA(cudaGraphLaunch(exec, stream));
+            launches += (long long)nrep * per_graph;
+            for (int st = nrep * kGraphSteps; st < k; ++st) {
+                launches += enqueue_step<T>(Uc, Pc, Uo, sc, sa, nullptr);
+                if (!symp) { T *tmp = Pc; Pc = Uc; Uc = Uo; Uo = tmp; }
+            }
+        };
+        int seg_len = 0, nseg = 0;
+        if (record) {
+            seg_len = (nsteps + ckpt_nsnap - 1) / ckpt_nsnap;
+            nseg = (nsteps + seg_len - 1) / seg_len;
+            d_snap.alloc((size_t)nseg * 2 * nslot * sizeof(T));
+        }
         EMS_CUDA(cudaEventRecord(ev0, stream));
         if (symp) {
-            tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)hfirst);
+            tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)sc.hfirst);
             ++launches;
         }
-        for (int r = 0; r < nrep; ++r) EMS_CUDA(cudaGraphLaunch(exec, stream));
-        launches += (long long)nrep * per_graph;
-        for (int st = nrep * kGraphSteps; st < nsteps; ++st) {
-            launches += enqueue_step<T>(Uc, Pc, Uo, sub, nsub, hfirst, sa, symp);
-            if (!symp) { T *tmp = Pc; Pc = Uc; Uc = Uo; Uo = tmp; }
+        if (record) {
+            // snapshot of the merged state at the start of every segment
+            for (int s = 0; s < nseg; ++s) {
+                T *snap = d_snap.as<T>() + (size_t)s * 2 * nslot;
+                EMS_CUDA(cudaMemcpyAsync(snap, Uc, nslot * sizeof(T), cudaMemcpyDeviceToDevice, stream));
+                EMS_CUDA(cudaMemcpyAsync(snap + nslot, Pc, nslot * sizeof(T), cudaMemcpyDeviceToDevice, stream));
+                advance(std::min(seg_len, nsteps - s * seg_len));
+            }
+        } else {
+            advance(nsteps);
         }
         if (symp) {
-            tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)(-hfirst));
+            tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)(-sc.hfirst));
             ++launches;
         }
         EMS_CUDA(cudaGetLastError());
@@ -963,12 +1260,151 @@ struct TetFemSim : Sim {
         EMS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
         last_ms = ms;
         last_launches = launches;
-        cur_time = t;
+        cur_time = t_end;
+        fresh = nsteps == 0 && fresh;
+        if (record) { rec_nsteps = nsteps; rec_seg = seg_len; rec_sa = sa; }
+        const size_t ntr = (size_t)std::max(nobs, 1) * std::max(nsamp, 1) * 4;
         traces.assign(ntr, 0.0);
         EMS_CUDA(cudaMemcpy(traces.data(), d_tr.p, ntr * 8, cudaMemcpyDeviceToHost));
         traces.resize((size_t)nobs * nsamp * 4);
         for (int r = 0; r < nobs; ++r)
             for (int s = 0; s < nsamp; ++s) traces[((size_t)r * nsamp + s) * 4] = times[s] * tscale;
+    }
+
+    // ---- discrete adjoint of the recorded run
+    // Receiver terms grouped by edge slot and by node for
+    // tet_receiver_adjoint_kernel.
+    struct RecAdj {
+        DevBuf sl_slot, sl_ptr, term_rc, term_w, nd_node, nd_map, a_scr;
+        int nsl = 0, nnd = 0;
+    };
+    void build_receiver_adjoint(RecAdj &ra)
+    {
+        std::vector<int> sl_slot, sl_ptr{0}, term_rc, nd_node, nd_map;
+        std::vector<double> term_w;
+        std::vector<std::vector<std::pair<int, double>>> terms;
+        std::unordered_map<int, int> slot_idx, node_idx;
+        for (int r = 0; r < nobs; ++r)
+            for (int l = 0; l < 6; ++l) {
+                const int e = rec_edges[r][l];
+                auto it = slot_idx.find(e);
+                int k;
+                if (it == slot_idx.end()) {
+                    k = (int)sl_slot.size();
+                    slot_idx[e] = k;
+                    sl_slot.push_back(e);
+                    terms.emplace_back();
+                } else {
+                    k = it->second;
+                }
+                for (int c = 0; c < 3; ++c) terms[k].push_back({3 * r + c, rec_w[r][3 * l + c]});
+            }
+        for (size_t k = 0; k < sl_slot.size(); ++k) {
+            for (auto &tm : terms[k]) { term_rc.push_back(tm.first); term_w.push_back(tm.second); }
+            sl_ptr.push_back((int)term_rc.size());
+            const int v = sl_slot[k] / 7, d = sl_slot[k] % 7;
+            auto it = node_idx.find(v);
+            int i;
+            if (it == node_idx.end()) {
+                i = (int)nd_node.size();
+                node_idx[v] = i;
+                nd_node.push_back(v);
+                nd_map.insert(nd_map.end(), 7, -1);
+            } else {
+                i = it->second;
+            }
+            nd_map[7 * i + d] = (int)k;
+        }
+        ra.nsl = (int)sl_slot.size();
+        ra.nnd = (int)nd_node.size();
+        if (sl_slot.empty()) { sl_slot.push_back(0); term_rc.push_back(0); term_w.push_back(0.0); nd_node.push_back(0); nd_map.assign(7, -1); }
+        up(ra.sl_slot, sl_slot); up(ra.sl_ptr, sl_ptr); up(ra.term_rc, term_rc); up(ra.term_w, term_w);
+        up(ra.nd_node, nd_node); up(ra.nd_map, nd_map);
+        ra.a_scr.alloc(std::max(ra.nsl, 1) * sizeof(double));
+    }
+
+    // dJ/deps per tetrahedron (FP64) for dJ/dtraces tg (nobs x nsamp x 4,
+    // column 0 ignored) of the recorded run.  Segments are recomputed from
+    // their snapshots (keeping Minv P of every substep), then swept backward.
+    template <class T> void backward_t(const double *tg, double *grad)
+    {
+        const Schedule sc = schedule();
+        const int N = rec_nsteps, L = rec_seg, nseg = (N + L - 1) / L, tf = P.time_frequency, nsub = sc.nsub;
+        const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
+        const unsigned nbv = (unsigned)((nnode + 127) / 128);
+        // adjoint sources per sample: r[s][rec][c]
+        std::vector<double> rs((size_t)std::max(nsamp, 1) * std::max(nobs, 1) * 3, 0.0);
+        for (int r = 0; r < nobs; ++r)
+            for (int s = 0; s < nsamp; ++s)
+                for (int c = 0; c < 3; ++c) rs[((size_t)s * nobs + r) * 3 + c] = tg[((size_t)r * nsamp + s) * 4 + 1 + c];
+        DevBuf d_rs, Wb, Pb, Q, zbuf, Uw, Pw, contrib, d_grad;
+        up(d_rs, rs);
+        RecAdj ra;
+        build_receiver_adjoint(ra);
+        const size_t w = sizeof(T);
+        Wb.alloc(nslot * w); Wb.zero(stream);
+        Pb.alloc(nslot * w); Pb.zero(stream);
+        Q.alloc(28 * nnode * 8); Q.zero(stream);
+        zbuf.alloc(((size_t)L * nsub + 1) * nslot * w);
+        Uw.alloc(nslot * w); Pw.alloc(nslot * w);
+        const SrcArgs sa = rec_sa;   // the recorded run's source tables are still on the device
+        vec4<T> *B = d_B.as<vec4<T>>();
+        T *zb = zbuf.as<T>();
+        for (int s = nseg - 1; s >= 0; --s) {
+            const int n0 = s * L, n1 = std::min(N, n0 + L);
+            const T *snap = d_snap.as<T>() + (size_t)s * 2 * nslot;
+            EMS_CUDA(cudaMemcpyAsync(Uw.p, snap, nslot * w, cudaMemcpyDeviceToDevice, stream));
+            EMS_CUDA(cudaMemcpyAsync(Pw.p, snap + nslot, nslot * w, cudaMemcpyDeviceToDevice, stream));
+            EMS_CUDA(cudaMemcpyAsync(d_ctl.p, &n0, sizeof(int), cudaMemcpyHostToDevice, stream));
+            // z[0] = Minv P at the start of step n0
+            EMS_CUDA(cudaMemsetAsync(zb, 0, nslot * w, stream));
+            tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pw.as<T>(), zb, T(1));
+            for (int n = n0; n < n1; ++n)
+                enqueue_step<T>(Uw.as<T>(), Pw.as<T>(), nullptr, sc, sa, zb + ((size_t)(n - n0) * nsub + 1) * nslot);
+            for (int n = n1 - 1; n >= n0; --n) {
+                for (int q = nsub - 1; q >= 0; --q) {
+                    // the drift before kick (n, q): same step (q > 0), the
+                    // previous step's last one, or the initial half drift
+                    const double c = q > 0 ? sc.c[q - 1] : (n > 0 ? sc.c[nsub - 1] : sc.hfirst);
+                    const T *z = zb + ((size_t)(n - n0) * nsub + q) * nslot;
+                    tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Pb.as<T>(), nullptr, B);
+                    tet_adjoint_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(),
+                                                                        d_pec.as<unsigned char>(), B, d_minv.as<T>(),
+                                                                        Wb.as<T>(), Pb.as<T>(), z, Q.as<double>(),
+                                                                        (T)sc.sub[q], (T)c);
+                }
+                if (n % tf == 0 && n > 0 && nobs > 0) {
+                    const T *z = zb + (size_t)(n - n0) * nsub * nslot;
+                    tet_receiver_adjoint_kernel<T><<<1, 1024, 0, stream>>>(
+                        ra.nsl, ra.sl_slot.as<int>(), ra.sl_ptr.as<int>(), ra.term_rc.as<int>(), ra.term_w.as<double>(),
+                        d_rs.as<double>() + (size_t)(n / tf) * nobs * 3, ra.nnd, ra.nd_node.as<int>(), ra.nd_map.as<int>(),
+                        ra.a_scr.as<double>(), Wb.as<T>(), Pb.as<T>(), d_minv.as<T>(), z, Q.as<double>(),
+                        0.5 * sc.sub[nsub - 1]);
+                }
+            }
+            EMS_CUDA(cudaGetLastError());
+        }
+        contrib.alloc(6 * ntet * 8);
+        contrib.zero(stream);
+        d_grad.alloc(ntet * 8);
+        tet_grad_node_kernel<<<nbv, 128, 0, stream>>>(nnode, d_pec.as<unsigned char>(), d_inc_ptr.as<int>(), d_inc.as<int>(),
+                                                      d_eps.as<double>(), Q.as<double>(), contrib.as<double>());
+        tet_grad_gather_kernel<<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), d_pec.as<unsigned char>(),
+                                                        d_inc_ptr.as<int>(), d_inc.as<int>(), contrib.as<double>(),
+                                                        d_grad.as<double>());
+        EMS_CUDA(cudaGetLastError());
+        EMS_CUDA(cudaMemcpyAsync(grad, d_grad.p, ntet * 8, cudaMemcpyDeviceToHost, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    void backward(const double *tg, size_t ntg, double *grad, size_t ngrad)
+    {
+        if (rec_nsteps < 0)
+            throw Error{EMS_ERR_STATE, "no recorded run: call ems_tetfem_set_checkpoints, ems_reset, then ems_run"};
+        EMS_CHECK_ARG(tg && grad, "trace gradient and output required");
+        EMS_CHECK_ARG(ntg == (size_t)nobs * nsamp * 4, "trace gradient must have nrec * nsamp * 4 values");
+        EMS_CHECK_ARG(ngrad == ntet, "gradient must have one value per tetrahedron");
+        if (fp64) backward_t<double>(tg, grad); else backward_t<float>(tg, grad);
     }
 
     void run(int nsteps) override
@@ -996,6 +1432,7 @@ struct TetFemSim : Sim {
     void set_field(int which, const double *in) override
     {
         DevBuf &b = which == 0 ? d_U : d_P;
+        fresh = false;
         if (fp64) {
             EMS_CUDA(cudaMemcpy(b.p, in, nslot * 8, cudaMemcpyHostToDevice));
         } else {
@@ -1040,7 +1477,7 @@ struct TetFemSim : Sim {
             vec4<T> *B = d_B.as<vec4<T>>();
             tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), in.as<T>(), nullptr, B);
             tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                        B, nullptr, out.as<T>(), nullptr, T(-1), T(0), SrcArgs{});
+                                                        B, nullptr, out.as<T>(), nullptr, T(-1), T(0), SrcArgs{}, nullptr);
             EMS_CUDA(cudaGetLastError());
             EMS_CUDA(cudaMemcpyAsync(h.data(), out.p, nslot * w, cudaMemcpyDeviceToHost, stream));
             EMS_CUDA(cudaStreamSynchronize(stream));
@@ -1053,6 +1490,7 @@ struct TetFemSim : Sim {
     {
         d_U.zero(stream); d_P.zero(stream); d_Uold.zero(stream);
         cur_time = 0.0;
+        fresh = true;
         EMS_CUDA(cudaStreamSynchronize(stream));
     }
 
@@ -1071,7 +1509,7 @@ struct TetFemSim : Sim {
             for (int r = 0; r <= launches; ++r) {
                 if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
                 tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                            B, d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(), T(0), T(0), SrcArgs{});
+                                                            B, d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(), T(0), T(0), SrcArgs{}, nullptr);
             }
         };
         if (fp64) body(double()); else body(float());
@@ -1132,6 +1570,7 @@ void tetbatch_add_dipole(Sim *s, int shot, const double pos[3], const double dir
     d.kind = waveform;
     d.f0n = f0 * f->tscale;
     f->dips.push_back(d);
+    f->rec_nsteps = -1;
     for (int l = 0; l < 6; ++l)
         if (d.coef[l] != 0.0) f->pec_h[d.slot[l]] |= kSrcBit;
     f->flags_dirty = true;
@@ -1156,6 +1595,7 @@ void tetbatch_add_receiver(Sim *s, int shot, const double pos[3])
         for (int q = 0; q < 3; ++q) ww[3 * l + q] = w[l][q];
     f->rec_edges.push_back(e);
     f->rec_w.push_back(ww);
+    f->rec_nsteps = -1;
 }
 
 void tetfem_apply_stiffness(Sim *s, const double *u, double *f, size_t n)
@@ -1164,6 +1604,13 @@ void tetfem_apply_stiffness(Sim *s, const double *u, double *f, size_t n)
     EMS_CHECK_ARG(u && f, "input and output required");
     EMS_CHECK_ARG(n == t->nslot, "vector length must be 7*(nx+1)*(ny+1)*(nz+1)");
     t->apply_stiffness(u, f);
+}
+
+void tetfem_set_checkpoints(Sim *s, int nsnap) { static_cast<TetFemSim *>(s)->set_checkpoints(nsnap); }
+
+void tetfem_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, size_t ngrad)
+{
+    static_cast<TetFemSim *>(s)->backward(trace_grad, ntg, grad_eps, ngrad);
 }
 
 void tetfem_time_step(const Sim *s, double *dt, double *lim)

@@ -237,6 +237,26 @@ class TetFemSimulation(_Sim):
         self._check(lib().ems_tetfem_time_step(self._h, C.byref(dt), C.byref(lim)))
         return dt.value, lim.value
 
+    def set_checkpoints(self, nsnap):
+        """Record the next run from the reset state for :meth:`backward`,
+        keeping nsnap snapshots on the device (0 stops recording)."""
+        self._check(lib().ems_tetfem_set_checkpoints(self._h, int(nsnap)))
+
+    def backward(self, trace_grad):
+        """dJ/deps_r per tetrahedron (FP64) of the recorded run, given
+        dJ/dtraces shaped like :meth:`traces` (column 0 ignored)."""
+        g = np.ascontiguousarray(trace_grad, dtype=np.float64).reshape(-1)
+        out = np.zeros(self.ntet)
+        self._check(lib().ems_tetfem_backward(self._h, _dptr(g), g.size, _dptr(out), out.size))
+        return out
+
+    @property
+    def ntet(self):
+        return sum(6 * c[0] * c[1] * c[2] for c in self._cells())
+
+    def _cells(self):
+        return [tuple(self.params.cells)]
+
 
 class TetFemBatch(TetFemSimulation):
     """Independent shots (cubes of cells[s] cells) advanced together by the
@@ -262,3 +282,27 @@ class TetFemBatch(TetFemSimulation):
     def add_receiver(self, shot, pos):
         a = np.ascontiguousarray(pos, dtype=np.float64)
         self._check(lib().ems_tetbatch_add_receiver(self._h, shot, _dptr(a)))
+
+    def _cells(self):
+        return self.cells
+
+
+MISFIT_L2, MISFIT_TF_ENVELOPE = 0, 1
+
+
+def trace_misfit(traces, observed, kind=MISFIT_L2, tf_band=None):
+    """Misfit J of traces against observed traces (both [nobs, nsamp, 4] as
+    returned by ``traces()``) and dJ/dtraces (same shape, column 0 zero).
+    kind: MISFIT_L2 (1/2 sum of squared differences) or MISFIT_TF_ENVELOPE
+    (1/2 sum of squared single-valued TF envelope misfits, Kristekova et al.
+    2006); tf_band = (fmin, fmax, nf) in the units of the time column."""
+    tr = np.ascontiguousarray(traces, dtype=np.float64)
+    ob = np.ascontiguousarray(observed, dtype=np.float64)
+    if tr.shape != ob.shape or tr.ndim != 3 or tr.shape[2] != 4:
+        raise ValueError("traces and observed must both be [nobs, nsamp, 4]")
+    g = np.zeros_like(tr)
+    J = C.c_double()
+    band = None if tf_band is None else np.ascontiguousarray(tf_band, dtype=np.float64)
+    check(lib().ems_trace_misfit(kind, tr.shape[0], tr.shape[1], _dptr(tr), _dptr(ob),
+                                 _dptr(band) if band is not None else None, C.byref(J), _dptr(g)))
+    return J.value, g

@@ -181,6 +181,42 @@ int ems_tetbatch_add_dipole(ems_sim *sim, int shot, const double pos[3], const d
                             double amplitude);
 int ems_tetbatch_add_receiver(ems_sim *sim, int shot, const double pos[3]);
 
+/* ------------------------------------------------ misfit gradient (adjoint)
+ * New: the reference has no adjoint.  The gradient of a receiver-trace
+ * functional J with respect to the per-tetrahedron permittivity comes from
+ * the discrete adjoint of the symplectic time loop (EMS_SYMP2, EMS_SYMP4):
+ *   ems_tetfem_set_checkpoints(sim, nsnap); ems_reset(sim); ems_run(sim, n);
+ *   ... dJ/dtraces from the traces (ems_trace_misfit or the caller) ...
+ *   ems_tetfem_backward(sim, dJ_dtraces, len, grad_eps, ntet);
+ * The recorded run keeps nsnap snapshots of the state on the device (one per
+ * segment of ceil(n / nsnap) steps); the backward sweep recomputes each
+ * segment from its snapshot and runs the reversed steps over it.  Fields are
+ * in the handle's precision, the gradient is accumulated in FP64.  Works on
+ * batch handles too (one gradient value per tetrahedron of every shot). */
+/* Record the next ems_run that starts from the reset state (nsnap > 0), or
+ * stop recording (nsnap = 0).  EMS_ERR_UNSUPPORTED for EMS_LEAPFROG. */
+int ems_tetfem_set_checkpoints(ems_sim *sim, int nsnap);
+/* dJ/deps_r per tetrahedron (ntet values) of the recorded run, given
+ * dJ/dtraces in the layout of ems_get_traces (nobs x nsamp x 4, column 0,
+ * the time, ignored; n = nobs * nsamp * 4).  EMS_ERR_STATE when there is no
+ * recorded run (or the material, dipoles or receivers changed since). */
+int ems_tetfem_backward(ems_sim *sim, const double *trace_grad, size_t n, double *grad_eps, size_t ntet);
+
+enum {
+    EMS_MISFIT_L2 = 0,          /* J = 1/2 sum (E - E_obs)^2 over receivers, samples, components */
+    EMS_MISFIT_TF_ENVELOPE = 1  /* single-valued time-frequency envelope misfit (Kristekova et al. 2006) */
+};
+/* Misfit of traces against observed traces (both nobs x nsamp x 4 in the
+ * ems_get_traces layout; column 0 holds the sample times) and its gradient
+ * with respect to the traces (same layout, column 0 zero; may be NULL).
+ * EMS_MISFIT_TF_ENVELOPE: J = 1/2 sum of EM^2 over receivers and components,
+ * EM the single-valued envelope misfit with the observed trace as reference
+ * (TF_MISFIT_GOF's IS_S2_REFERENCE = T, LOCAL_NORM = F, one component per
+ * pair); tf_band = {fmin, fmax, nf} in the units of the time column (NULL:
+ * 4/T .. 1/(4 dt), 32 log-spaced frequencies); ignored for EMS_MISFIT_L2. */
+int ems_trace_misfit(int kind, int nobs, int nsamp, const double *traces, const double *observed, const double *tf_band,
+                     double *misfit, double *trace_grad);
+
 /* ------------------------------------------------------ common operations */
 /* Replaces FemSimulation::run (fdtd :242-306, fem_v2 :1249-1320,
  * symplectic_2/4 :1278-1351): advance num_steps steps, recording receivers.
