@@ -90,6 +90,7 @@ def lib():
         "ems_tetfem_set_checkpoints": (C.c_int, [vp, C.c_int]),
         "ems_tetfem_backward": (C.c_int, [vp, dp, C.c_size_t, dp, C.c_size_t]),
         "ems_trace_misfit": (C.c_int, [C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp]),
+        "ems_tetfem_gradient": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, C.c_size_t]),
         "ems_tet_stiffness_apply_static": (C.c_int, [ip, vp, vp, vp]),
         "ems_run": (C.c_int, [vp, C.c_int]),
         "ems_trace_shape": (C.c_int, [vp, ip, ip, ip]),

@@ -207,6 +207,12 @@ int ems_tetfem_backward(ems_sim *s, const double *tg, size_t n, double *grad, si
     NEED(s, ems::Kind::TETFEM);
     return guard(s, [&] { ems::tetfem_backward(s->impl, tg, n, grad, ntet); });
 }
+int ems_tetfem_gradient(ems_sim *s, int nsteps, int nsnap, int kind, const double *obs, const double *band, double *misfit,
+                        double *grad, size_t ntet)
+{
+    NEED(s, ems::Kind::TETFEM);
+    return guard(s, [&] { ems::tetfem_gradient(s->impl, nsteps, nsnap, kind, obs, band, misfit, grad, ntet); });
+}
 int ems_trace_misfit(int kind, int nobs, int nsamp, const double *tr, const double *obs, const double *band, double *misfit,
                      double *tg)
 {

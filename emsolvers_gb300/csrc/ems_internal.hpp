@@ -102,6 +102,8 @@ void tetfem_time_step(const Sim *s, double *dt, double *lim);
 void tetfem_apply_stiffness(Sim *s, const double *u, double *f, size_t n);
 void tetfem_set_checkpoints(Sim *s, int nsnap);
 void tetfem_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, size_t ngrad);
+void tetfem_gradient(Sim *s, int nsteps, int nsnap, int kind, const double *observed, const double *tf_band, double *misfit,
+                     double *grad_eps, size_t ngrad);
 void trace_misfit(int kind, int nobs, int nsamp, const double *traces, const double *observed, double *misfit,
                   double *trace_grad, const double *tf_band);
 

@@ -15,6 +15,7 @@
 //                (tet_minv_setup_kernel), stored packed symmetric in the run
 //                precision; applied inside the kick kernel by eight lanes per
 //                node exchanging values with warp shuffles.
+//   adjoint      the same kernels run the reversed steps (see "adjoint").
 // Units are normalised (cube edge 1, c0 = 1); the API converts.
 #include <cuda_runtime.h>
 
@@ -357,13 +358,13 @@ __device__ __forceinline__ double source_load(const SrcArgs &s, size_t e)
 
 // Kick + drift, eight lanes per node (lane 7 idle):
 //   P_e -= a * (F_e - f_e)   (F = K U gathered, f the dipole load; PEC slots keep F = 0),
-//   U_e += c * (Minv_v P)_e,  and zout_e = (Minv_v P)_e when zout is given.
+//   Uout_e = Uin_e + c * (Minv_v P)_e,  and zout_e = (Minv_v P)_e when zout is given.
 // With minv == nullptr only P is written (P -= a F): the stiffness apply.
 template <class T>
 __global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
                                                        const unsigned char *__restrict__ pec, const vec4<T> *__restrict__ B,
-                                                       const T *__restrict__ minv, T *__restrict__ P, T *__restrict__ U, T a, T c,
-                                                       SrcArgs src, T *__restrict__ zout)
+                                                       const T *__restrict__ minv, T *__restrict__ P, const T *Uin, T *Uout,
+                                                       T a, T c, SrcArgs src, T *__restrict__ zout)
 {
     __shared__ vec4<T> sc[36];
     load_curl_table<T>(sc);
@@ -386,7 +387,7 @@ __global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *
     if (minv == nullptr) return;     // force-only use (uniform across the grid)
     if (v >= nnode) v = nnode - 1;   // keep the whole warp in the shuffles
     T y = block_apply<T>(minv + 28 * v, d, p);
-    if (live && c != T(0)) U[e] = fma(c, y, U[e]);
+    if (live) Uout[e] = fma(c, y, Uin[e]);
     if (zout && live) zout[e] = y;   // Minv P of this drift, kept for the adjoint
 }
 
@@ -464,50 +465,54 @@ __global__ void __launch_bounds__(1024) tet_receiver_kernel(int nrec, const int 
 
 // ---------------------------------------------------------------- adjoint
 // The discrete adjoint of the merged symplectic loop runs the same two
-// launches per substep backward in time, with the roles of the fields
-// swapped: tet_curl_kernel on Pbar, then the adjoint kick below.  Only the
-// mass blocks depend on eps, so each drift U += c Minv P adds
-// -c (Minv Ubar)^T dM (Minv P) to dJ/deps; the outer products are summed per
-// node in FP64 (Q_v, packed symmetric like the mass blocks) and contracted
-// with dM_v/deps once at the end (tet_grad_node_kernel).
+// launches per substep backward in time.  Only the mass blocks depend on
+// eps, so each drift U += c Minv P adds
+// -c (Minv Ubar)^T dM (Minv P) to dJ/deps.  The adjoint substep is the
+// forward one with the roles swapped (curl of Pbar, kick on Ubar, drift on
+// Pbar), storing y = Minv Ubar of every drift of a segment next to the
+// forward z = Minv P; tet_grad_accumulate_kernel then sums the outer products per node
+// (Q_v += c sym(y z^T), FP64, packed symmetric like the mass blocks) in one
+// streaming pass per segment, and tet_grad_node_kernel contracts Q with
+// dM_v/deps once at the end.
 
-// Adjoint kick (eight lanes per node):
-//   Wb_e -= a * F_e        (F = K Pbar gathered from B; PEC slots keep F = 0)
-//   y = Minv_v Wb,  Pb_e += c * y_e,  Q_v += c * sym(y z^T)
-// with z = Minv P of the forward drift being reversed.
+// Q_v += sum_k c_k sym(y_k z_k^T) over the nk drifts of one segment (eight
+// lanes per node; lane d owns the entries (d, j >= d)).  Drift k = nsub * i
+// + q of the segment starting at step n0 has the coefficient cq[q - 1]
+// (q > 0), cq[nsub - 1] (q = 0, step > 0) or hfirst (the initial half
+// drift).  The products of a time step are summed in T, the steps in FP64.
 template <class T>
-__global__ void __launch_bounds__(256) tet_adjoint_kick_kernel(size_t nnode, const int *__restrict__ inc_ptr,
-                                                               const int *__restrict__ inc, const unsigned char *__restrict__ pec,
-                                                               const vec4<T> *__restrict__ B, const T *__restrict__ minv,
-                                                               T *__restrict__ Wb, T *__restrict__ Pb, const T *__restrict__ z,
-                                                               double *__restrict__ Q, T a, T c)
+__global__ void __launch_bounds__(256) tet_grad_accumulate_kernel(size_t nnode, size_t nslot, int nk, int nsub, int n0,
+                                                                  T c0, T c1, T c2, T hfirst, const T *__restrict__ ybuf,
+                                                                  const T *__restrict__ zbuf, double *__restrict__ Q)
 {
-    __shared__ vec4<T> sc[36];
-    load_curl_table<T>(sc);
     size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t v = g >> 3;
     int d = (int)(g & 7);
     bool live = v < nnode && d < 7;
-    size_t e = 7 * v + d;
-    T w = 0, zd = 0;
-    if (live) {
-        w = Wb[e];
-        if (!(pec[e] & kPecBit)) {
-            w = fma(-a, gather_force<T>(e, inc_ptr, inc, B, sc), w);
-            Wb[e] = w;
-        }
-        zd = z[e];
-    }
-    if (v >= nnode) v = nnode - 1;   // keep the whole warp in the shuffles
-    T y = block_apply<T>(minv + 28 * v, d, w);
-    if (live) Pb[e] = fma(c, y, Pb[e]);
-    double *q = Q + 28 * v;
-    const double hc = 0.5 * (double)c;
+    if (v >= nnode) v = nnode - 1;
+    const size_t e = 7 * v + (d < 7 ? d : 6);
+    const T cq[3] = {c0, c1, c2};
+    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+    T part[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < nk; ++k) {
+        const int q = k % nsub;
+        const T c = q > 0 ? cq[q - 1] : (n0 + k / nsub > 0 ? cq[nsub - 1] : hfirst);
+        const T y = live ? ybuf[(size_t)k * nslot + e] : T(0), z = live ? zbuf[(size_t)k * nslot + e] : T(0);
 #pragma unroll
-    for (int j = 0; j < 7; ++j) {
-        T yj = __shfl_sync(0xffffffffu, y, j, 8), zj = __shfl_sync(0xffffffffu, zd, j, 8);
-        if (live && j >= d) q[pk7(d, j)] += hc * ((double)y * (double)zj + (double)yj * (double)zd);
+        for (int j = 0; j < 7; ++j) {
+            T yj = __shfl_sync(0xffffffffu, y, j, 8), zj = __shfl_sync(0xffffffffu, z, j, 8);
+            part[j] = fma(c, fma(y, zj, yj * z), part[j]);
+        }
+        if (q == nsub - 1 || k == nk - 1) {
+#pragma unroll
+            for (int j = 0; j < 7; ++j) { acc[j] += (double)part[j]; part[j] = T(0); }
+        }
     }
+    if (!live) return;
+    double *qv = Q + 28 * v;
+#pragma unroll
+    for (int j = 0; j < 7; ++j)
+        if (j >= d) qv[pk7(d, j)] += 0.5 * acc[j];
 }
 
 // Receiver adjoint of one sample, one block.  The receivers' edge slots are
@@ -1001,8 +1006,8 @@ struct TetFemSim : Sim {
         z.zero(stream);
         unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
         tet_kick_kernel<double><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                         B.as<vec4<double>>(), nullptr, z.as<double>(), nullptr, -1.0, 0.0, SrcArgs{},
-                                                         nullptr);
+                                                         B.as<vec4<double>>(), nullptr, z.as<double>(), nullptr, nullptr, -1.0, 0.0,
+                                                         SrcArgs{}, nullptr);
     }
 
     double power_iteration(const DevBuf &minv_d, int iters)
@@ -1088,16 +1093,34 @@ struct TetFemSim : Sim {
         return s;
     }
 
-    // One time step: receivers (and the step counter), then for the
-    // symplectic steps curl + kick per substep with the drifts merged (the
-    // last one also carries the first half drift of the next step), or for
-    // leapfrog curl + leapfrog update.  zout (symplectic only): Minv P of
-    // substep q goes to zout + q * nslot.  Returns the number of launches.
-    template <class T>
-    int enqueue_step(T *Uc, T *Pc, T *Uo, const Schedule &sc, const SrcArgs &sa0, T *zout)
+    // One substep: B = curl of Uin (tet_curl_kernel), then MODE 0
+    // (symplectic, tet_kick_kernel): P -= a (K Uin - f); Uout = Uin + c Minv P
+    // (zout = Minv P), or MODE 1 (leapfrog, tet_leapfrog_kernel):
+    // Uout = 2 Uin - Uold - c Minv (K Uin - f).  Returns the number of launches.
+    template <class T, int MODE>
+    int substep(const T *Uin, T *Uout, T *Pio, const T *Uold, T a, T c, const SrcArgs &sa, T *zout)
     {
         const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
         vec4<T> *B = d_B.as<vec4<T>>();
+        tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Uin, nullptr, B);
+        if (MODE == 0)
+            tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+                                                        B, d_minv.as<T>(), Pio, Uin, Uout, a, c, sa, zout);
+        else
+            tet_leapfrog_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+                                                            B, d_minv.as<T>(), Uin, Uold, Uout, c, sa);
+        return 2;
+    }
+
+    // One time step: receivers (and the step counter), then for the
+    // symplectic steps curl + kick per substep with the drifts merged (the
+    // last one also carries the first half drift of the next step), U and P
+    // updated in place; for leapfrog curl + update into Uo and the ring
+    // rotation (Uc, Pc, Uo) <- (Uo, Uc, Pc).  zout (symplectic only): Minv P
+    // of substep q goes to zout + q * nslot.  Returns the number of launches.
+    template <class T>
+    int enqueue_step(T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa0, T *zout)
+    {
         tet_receiver_kernel<T><<<1, 256, 0, stream>>>(nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), Uc, Pc, d_minv.as<T>(),
                                                       sc.symp ? (T)sc.hfirst : T(0), d_tr.as<double>(), nsamp,
                                                       P.time_frequency, d_ctl.as<int>());
@@ -1106,17 +1129,12 @@ struct TetFemSim : Sim {
             for (int q = 0; q < sc.nsub; ++q) {
                 SrcArgs sa = sa0;
                 sa.q = q;
-                tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Uc, nullptr, B);
-                tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                            B, d_minv.as<T>(), Pc, Uc, (T)sc.sub[q], (T)sc.c[q], sa,
-                                                            zout ? zout + (size_t)q * nslot : nullptr);
-                nl += 2;
+                nl += substep<T, 0>(Uc, Uc, Pc, nullptr, (T)sc.sub[q], (T)sc.c[q], sa,
+                                    zout ? zout + (size_t)q * nslot : nullptr);
             }
         } else {
-            tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Uc, nullptr, B);
-            tet_leapfrog_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                            B, d_minv.as<T>(), Uc, Pc, Uo, (T)(dtn * dtn), sa0);
-            nl += 2;
+            nl += substep<T, 1>(Uc, Uo, nullptr, Pc, T(0), (T)(dtn * dtn), sa0, nullptr);
+            T *tmp = Pc; Pc = Uc; Uc = Uo; Uo = tmp;
         }
         return nl;
     }
@@ -1187,39 +1205,39 @@ struct TetFemSim : Sim {
         double t_end = 0.0;
         const SrcArgs sa = prepare_run(nsteps, sc, times, t_end);
         const unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
-        // leapfrog ring: Uc = E^n, Pc = E^{n-1}, Uo = scratch for E^{n+1}
+        // symplectic: U and P updated in place; leapfrog ring: Uc = E^n,
+        // Pc = E^{n-1}, Uo = scratch for E^{n+1}
         T *Uc = d_U.as<T>(), *Pc = d_P.as<T>(), *Uo = d_Uold.as<T>();
         // one CUDA graph of kGraphSteps steps (a multiple of 3, so the
-        // leapfrog ring returns to the same assignment), replayed
+        // leapfrog ring returns to the captured assignment), replayed
         constexpr int kGraphSteps = 12;
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
+        struct StepGraph {   // destroyed on every exit path
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            ~StepGraph()
+            {
+                if (exec) cudaGraphExecDestroy(exec);
+                if (g) cudaGraphDestroy(g);
+            }
+        } graph;
         int per_graph = 0;
-        if (nsteps >= kGraphSteps) {
+        auto capture = [&] {
+            T *u = Uc, *p = Pc, *o = Uo;
             EMS_CUDA(cudaStreamSynchronize(stream));
             EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-            T *u = Uc, *p = Pc, *o = Uo;
-            for (int st = 0; st < kGraphSteps; ++st) {
-                per_graph += enqueue_step<T>(u, p, o, sc, sa, nullptr);
-                if (!symp) { T *tmp = p; p = u; u = o; o = tmp; }
-            }
-            cudaError_t ce = cudaStreamEndCapture(stream, &graph);
+            for (int st = 0; st < kGraphSteps; ++st) per_graph += enqueue_step<T>(u, p, o, sc, sa, nullptr);
+            cudaError_t ce = cudaStreamEndCapture(stream, &graph.g);
             if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
-            ce = cudaGraphInstantiate(&exec, graph, 0);
-            if (ce != cudaSuccess) {
-                cudaGraphDestroy(graph);
-                throw Error{EMS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
-            }
-        }
+            ce = cudaGraphInstantiate(&graph.exec, graph.g, 0);
+            if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+        };
         long long launches = 0;
         auto advance = [&](int k) {
+            cudaGraphExec_t exec = graph.exec;
             const int nrep = exec ? k / kGraphSteps : 0;
             for (int r = 0; r < nrep; ++r) EMS_CUDA(cudaGraphLaunch(exec, stream));
             launches += (long long)nrep * per_graph;
-            for (int st = nrep * kGraphSteps; st < k; ++st) {
-                launches += enqueue_step<T>(Uc, Pc, Uo, sc, sa, nullptr);
-                if (!symp) { T *tmp = Pc; Pc = Uc; Uc = Uo; Uo = tmp; }
-            }
+            for (int st = nrep * kGraphSteps; st < k; ++st) launches += enqueue_step<T>(Uc, Pc, Uo, sc, sa, nullptr);
         };
         int seg_len = 0, nseg = 0;
         if (record) {
@@ -1227,6 +1245,7 @@ struct TetFemSim : Sim {
             nseg = (nsteps + seg_len - 1) / seg_len;
             d_snap.alloc((size_t)nseg * 2 * nslot * sizeof(T));
         }
+        if ((record ? seg_len : nsteps) >= kGraphSteps) capture();
         EMS_CUDA(cudaEventRecord(ev0, stream));
         if (symp) {
             tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)sc.hfirst);
@@ -1250,9 +1269,7 @@ struct TetFemSim : Sim {
         EMS_CUDA(cudaGetLastError());
         EMS_CUDA(cudaEventRecord(ev1, stream));
         EMS_CUDA(cudaStreamSynchronize(stream));
-        if (exec) cudaGraphExecDestroy(exec);
-        if (graph) cudaGraphDestroy(graph);
-        if (!symp) {   // keep the buffers in ring order: U = E^n, P = E^{n-1}
+        {   // keep the current buffers: U (symplectic) or the ring U = E^n, P = E^{n-1}
             void *u = Uc, *p = Pc, *o = Uo;
             d_U.p = u; d_P.p = p; d_Uold.p = o;
         }
@@ -1337,7 +1354,7 @@ struct TetFemSim : Sim {
         for (int r = 0; r < nobs; ++r)
             for (int s = 0; s < nsamp; ++s)
                 for (int c = 0; c < 3; ++c) rs[((size_t)s * nobs + r) * 3 + c] = tg[((size_t)r * nsamp + s) * 4 + 1 + c];
-        DevBuf d_rs, Wb, Pb, Q, zbuf, Uw, Pw, contrib, d_grad;
+        DevBuf d_rs, Wb, Pb, Q, zbuf, ybuf, Uw, Pw, contrib, d_grad;
         up(d_rs, rs);
         RecAdj ra;
         build_receiver_adjoint(ra);
@@ -1346,10 +1363,11 @@ struct TetFemSim : Sim {
         Pb.alloc(nslot * w); Pb.zero(stream);
         Q.alloc(28 * nnode * 8); Q.zero(stream);
         zbuf.alloc(((size_t)L * nsub + 1) * nslot * w);
+        ybuf.alloc((size_t)L * nsub * nslot * w);
         Uw.alloc(nslot * w); Pw.alloc(nslot * w);
         const SrcArgs sa = rec_sa;   // the recorded run's source tables are still on the device
-        vec4<T> *B = d_B.as<vec4<T>>();
-        T *zb = zbuf.as<T>();
+        T *zb = zbuf.as<T>(), *yb = ybuf.as<T>();
+        T *pb = Pb.as<T>();
         for (int s = nseg - 1; s >= 0; --s) {
             const int n0 = s * L, n1 = std::min(N, n0 + L);
             const T *snap = d_snap.as<T>() + (size_t)s * 2 * nslot;
@@ -1359,29 +1377,31 @@ struct TetFemSim : Sim {
             // z[0] = Minv P at the start of step n0
             EMS_CUDA(cudaMemsetAsync(zb, 0, nslot * w, stream));
             tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pw.as<T>(), zb, T(1));
+            T *uc = Uw.as<T>(), *pc = Pw.as<T>(), *unused = nullptr;
             for (int n = n0; n < n1; ++n)
-                enqueue_step<T>(Uw.as<T>(), Pw.as<T>(), nullptr, sc, sa, zb + ((size_t)(n - n0) * nsub + 1) * nslot);
+                enqueue_step<T>(uc, pc, unused, sc, sa, zb + ((size_t)(n - n0) * nsub + 1) * nslot);
             for (int n = n1 - 1; n >= n0; --n) {
                 for (int q = nsub - 1; q >= 0; --q) {
                     // the drift before kick (n, q): same step (q > 0), the
                     // previous step's last one, or the initial half drift
                     const double c = q > 0 ? sc.c[q - 1] : (n > 0 ? sc.c[nsub - 1] : sc.hfirst);
-                    const T *z = zb + ((size_t)(n - n0) * nsub + q) * nslot;
-                    tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Pb.as<T>(), nullptr, B);
-                    tet_adjoint_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(),
-                                                                        d_pec.as<unsigned char>(), B, d_minv.as<T>(),
-                                                                        Wb.as<T>(), Pb.as<T>(), z, Q.as<double>(),
-                                                                        (T)sc.sub[q], (T)c);
+                    T *y = yb + ((size_t)(n - n0) * nsub + q) * nslot;
+                    // Wbar -= a K Pbar; Pbar += c Minv Wbar (y = Minv Wbar kept)
+                    substep<T, 0>(pb, pb, Wb.as<T>(), nullptr, (T)sc.sub[q], (T)c, SrcArgs{}, y);
                 }
                 if (n % tf == 0 && n > 0 && nobs > 0) {
                     const T *z = zb + (size_t)(n - n0) * nsub * nslot;
                     tet_receiver_adjoint_kernel<T><<<1, 1024, 0, stream>>>(
                         ra.nsl, ra.sl_slot.as<int>(), ra.sl_ptr.as<int>(), ra.term_rc.as<int>(), ra.term_w.as<double>(),
                         d_rs.as<double>() + (size_t)(n / tf) * nobs * 3, ra.nnd, ra.nd_node.as<int>(), ra.nd_map.as<int>(),
-                        ra.a_scr.as<double>(), Wb.as<T>(), Pb.as<T>(), d_minv.as<T>(), z, Q.as<double>(),
+                        ra.a_scr.as<double>(), Wb.as<T>(), pb, d_minv.as<T>(), z, Q.as<double>(),
                         0.5 * sc.sub[nsub - 1]);
                 }
             }
+            // the drifts of this segment: y at [k], z at [k] (k = nsub (n - n0) + q)
+            tet_grad_accumulate_kernel<T><<<nbn, 256, 0, stream>>>(nnode, nslot, (n1 - n0) * nsub, nsub, n0, (T)sc.c[0],
+                                                                   (T)sc.c[1], (T)sc.c[2], (T)sc.hfirst, yb, zb,
+                                                                   Q.as<double>());
             EMS_CUDA(cudaGetLastError());
         }
         contrib.alloc(6 * ntet * 8);
@@ -1477,7 +1497,8 @@ struct TetFemSim : Sim {
             vec4<T> *B = d_B.as<vec4<T>>();
             tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), in.as<T>(), nullptr, B);
             tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                        B, nullptr, out.as<T>(), nullptr, T(-1), T(0), SrcArgs{}, nullptr);
+                                                        B, nullptr, out.as<T>(), nullptr, nullptr, T(-1), T(0), SrcArgs{},
+                                                        nullptr);
             EMS_CUDA(cudaGetLastError());
             EMS_CUDA(cudaMemcpyAsync(h.data(), out.p, nslot * w, cudaMemcpyDeviceToHost, stream));
             EMS_CUDA(cudaStreamSynchronize(stream));
@@ -1497,32 +1518,30 @@ struct TetFemSim : Sim {
     void time_dominant(int launches, double *ms, double *bytes, std::string *name) override
     {
         if (!ready) setup();
-        size_t w = fp64 ? 8 : 4;
-        DevBuf saveU, saveP;
-        saveU.alloc(d_U.bytes); saveP.alloc(d_P.bytes);
-        EMS_CUDA(cudaMemcpyAsync(saveU.p, d_U.p, d_U.bytes, cudaMemcpyDeviceToDevice, stream));
-        EMS_CUDA(cudaMemcpyAsync(saveP.p, d_P.p, d_P.bytes, cudaMemcpyDeviceToDevice, stream));
+        const size_t w = fp64 ? 8 : 4;
         const unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
+        // the kick of a substep; a = c = 0 leaves P unchanged and copies U
+        // into the spare buffer
         auto body = [&](auto tag) {
             using T = decltype(tag);
-            vec4<T> *B = d_B.as<vec4<T>>();
             for (int r = 0; r <= launches; ++r) {
                 if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
-                tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
-                                                            B, d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(), T(0), T(0), SrcArgs{}, nullptr);
+                tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(),
+                                                            d_pec.as<unsigned char>(), d_B.as<vec4<T>>(), d_minv.as<T>(),
+                                                            d_P.as<T>(), d_U.as<T>(), d_Uold.as<T>(), T(0), T(0), SrcArgs{},
+                                                            nullptr);
             }
         };
         if (fp64) body(double()); else body(float());
+        EMS_CUDA(cudaGetLastError());
         EMS_CUDA(cudaEventRecord(ev1, stream));
         EMS_CUDA(cudaStreamSynchronize(stream));
         float t = 0;
         EMS_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
-        EMS_CUDA(cudaMemcpyAsync(d_U.p, saveU.p, d_U.bytes, cudaMemcpyDeviceToDevice, stream));
-        EMS_CUDA(cudaMemcpyAsync(d_P.p, saveP.p, d_P.bytes, cudaMemcpyDeviceToDevice, stream));
-        EMS_CUDA(cudaStreamSynchronize(stream));
         *ms = t / launches;
-        // unique bytes of one kick: incidence list + row pointers + B (3 per
-        // tet) + P read/write + U read/write + packed mass blocks + PEC flags
+        // unique bytes of one kick: incidence list + row pointers + B (3
+        // values per tetrahedron, stored as 4) + P read and written + U read
+        // + U written + packed mass blocks + slot flags
         *bytes = (double)(6 * ntet) * 4 + (double)(nslot + 1) * 4 + (double)(4 * ntet) * w + (double)nslot * 4 * w +
                  (double)(28 * nnode) * w + (double)nslot;
         *name = fp64 ? "tet_kick_kernel<double>" : "tet_kick_kernel<float>";
@@ -1611,6 +1630,21 @@ void tetfem_set_checkpoints(Sim *s, int nsnap) { static_cast<TetFemSim *>(s)->se
 void tetfem_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, size_t ngrad)
 {
     static_cast<TetFemSim *>(s)->backward(trace_grad, ntg, grad_eps, ngrad);
+}
+
+void tetfem_gradient(Sim *s, int nsteps, int nsnap, int kind, const double *obs, const double *band, double *misfit,
+                     double *grad, size_t ngrad)
+{
+    auto *f = static_cast<TetFemSim *>(s);
+    EMS_CHECK_ARG(nsteps > 0 && nsnap > 0, "nsteps and nsnap must be positive");
+    EMS_CHECK_ARG(obs && misfit && grad, "observed traces, misfit and gradient required");
+    EMS_CHECK_ARG(ngrad == f->ntet, "gradient must have one value per tetrahedron");
+    f->set_checkpoints(nsnap);
+    f->reset();
+    f->run(nsteps);
+    std::vector<double> tg(f->traces.size());
+    trace_misfit(kind, f->nobs, f->nsamp, f->traces.data(), obs, misfit, tg.data(), band);
+    f->backward(tg.data(), tg.size(), grad, ngrad);
 }
 
 void tetfem_time_step(const Sim *s, double *dt, double *lim)

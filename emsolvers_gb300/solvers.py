@@ -250,6 +250,18 @@ class TetFemSimulation(_Sim):
         self._check(lib().ems_tetfem_backward(self._h, _dptr(g), g.size, _dptr(out), out.size))
         return out
 
+    def gradient(self, nsteps, observed, kind=0, nsnap=64, tf_band=None):
+        """Misfit J of an nsteps run from the reset state against `observed`
+        traces and dJ/deps_r per tetrahedron (one call of ems_tetfem_gradient)."""
+        ob = np.ascontiguousarray(observed, dtype=np.float64)
+        band = None if tf_band is None else np.ascontiguousarray(tf_band, dtype=np.float64)
+        J = C.c_double()
+        out = np.zeros(self.ntet)
+        self._check(lib().ems_tetfem_gradient(self._h, int(nsteps), int(nsnap), int(kind), _dptr(ob),
+                                              _dptr(band) if band is not None else None, C.byref(J), _dptr(out),
+                                              out.size))
+        return J.value, out
+
     @property
     def ntet(self):
         return sum(6 * c[0] * c[1] * c[2] for c in self._cells())

@@ -202,6 +202,13 @@ int ems_tetfem_set_checkpoints(ems_sim *sim, int nsnap);
  * recorded run (or the material, dipoles or receivers changed since). */
 int ems_tetfem_backward(ems_sim *sim, const double *trace_grad, size_t n, double *grad_eps, size_t ntet);
 
+/* The whole gradient in one call (the pipeline above with ems_trace_misfit):
+ * reset, record nsteps steps with nsnap snapshots, misfit of the traces
+ * against `observed` (nobs x nsamp x 4), dJ/deps_r into grad_eps (ntet).
+ * The fields end in the state after the forward run. */
+int ems_tetfem_gradient(ems_sim *sim, int nsteps, int nsnap, int misfit_kind, const double *observed,
+                        const double *tf_band, double *misfit, double *grad_eps, size_t ntet);
+
 enum {
     EMS_MISFIT_L2 = 0,          /* J = 1/2 sum (E - E_obs)^2 over receivers, samples, components */
     EMS_MISFIT_TF_ENVELOPE = 1  /* single-valued time-frequency envelope misfit (Kristekova et al. 2006) */

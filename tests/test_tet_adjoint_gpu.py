@@ -52,7 +52,8 @@ def _residual(traces, seed):
 
 
 @pytest.mark.parametrize("integ", [oracle.SYMP2, oracle.SYMP4], ids=["symp2", "symp4"])
-@pytest.mark.parametrize("nsnap", [1, 5, 37], ids=["one_segment", "uneven_segments", "step_per_segment"])
+@pytest.mark.parametrize("nsnap", [1, 2, 5, 37],
+                         ids=["one_segment", "odd_graph_remainder", "uneven_segments", "step_per_segment"])
 def test_fp64_gradient_matches_oracle_adjoint(integ, nsnap):
     n, nsteps, tf = (4, 3, 5), 37, 2
     eps, dips, recs, dtn = _case(n, 5, integ)
@@ -65,6 +66,22 @@ def test_fp64_gradient_matches_oracle_adjoint(integ, nsnap):
     assert rel_l2(s.traces()[..., 1:], tr_o[..., 1:]) < 1e-10
     g = s.backward(resid)
     assert rel_l2(g, g_o) < 1e-9
+
+
+@pytest.mark.parametrize("nsnap", [3, 7, 40])
+def test_recorded_forward_equals_plain_forward(nsnap):
+    # a recorded run advances segment by segment (graph replays plus single
+    # steps); it must give the same fields and traces bit for bit
+    integ, n, nsteps = oracle.SYMP4, (9, 8, 7), 121
+    eps, dips, recs, dtn = _case(n, 12, integ, cfl=0.9)
+    plain = _sim(n, eps, dips, recs, integ, dtn, ems.FP32, 1, 0)
+    plain.run(nsteps)
+    rec = _sim(n, eps, dips, recs, integ, dtn, ems.FP32, 1, nsnap)
+    rec.reset()
+    rec.run(nsteps)
+    assert np.array_equal(plain.traces(), rec.traces())
+    assert np.array_equal(plain.get_field(0), rec.get_field(0))
+    assert np.array_equal(plain.get_field(1), rec.get_field(1))
 
 
 def test_fp32_gradient_within_1e3_of_fp64_oracle():
@@ -195,3 +212,20 @@ def test_backward_error_paths():
     with pytest.raises(ems.EmsError) as e:
         lf.set_checkpoints(2)
     assert e.value.status == -8
+
+
+def test_one_call_gradient_equals_the_pipeline():
+    integ, n, nsteps = oracle.SYMP4, (5, 4, 4), 50
+    eps, dips, recs, dtn = _case(n, 14, integ)
+    s = _sim(n, eps * 1.1, dips, recs, integ, dtn, ems.FP32, 1, 5)
+    s.reset()
+    s.run(nsteps)
+    obs = s.traces()
+    s.set_material(eps)
+    J1, g1 = s.gradient(nsteps, obs, ems.MISFIT_TF_ENVELOPE, nsnap=5)
+    s.set_checkpoints(5)
+    s.reset()
+    s.run(nsteps)
+    J2, tg = ems.trace_misfit(s.traces(), obs, ems.MISFIT_TF_ENVELOPE)
+    g2 = s.backward(tg)
+    assert J1 == J2 and np.array_equal(g1, g2)
