@@ -436,6 +436,8 @@ __global__ void __launch_bounds__(256) tet_leapfrog_kernel(size_t nnode, const i
 // record E(x) = sum_l w_l(x) U_l if n is a sampling step, then advance ctl.
 // With the symplectic drifts merged across steps the state holds
 // W = U + h Minv P; the receivers undo that half drift on their six slots.
+// Eight lanes per receiver: lane l < 6 forms its slot's terms, lane 0 sums
+// them in slot order.
 template <class T>
 __global__ void __launch_bounds__(1024) tet_receiver_kernel(int nrec, const int *__restrict__ edges, const double *__restrict__ w,
                                                             const T *__restrict__ U, const T *__restrict__ P,
@@ -443,21 +445,28 @@ __global__ void __launch_bounds__(1024) tet_receiver_kernel(int nrec, const int 
                                                             int nsamp, int tf, int *ctl)
 {
     const int step = ctl[0];
-    for (int r = threadIdx.x; r < nrec && step % tf == 0; r += blockDim.x) {
-        double acc[3] = {0, 0, 0};
-        for (int l = 0; l < 6; ++l) {
-            int e = edges[6 * r + l];
+    const int l = threadIdx.x & 7;
+    for (int r0 = 0; r0 < nrec && step % tf == 0; r0 += blockDim.x >> 3) {
+        const int r = r0 + (threadIdx.x >> 3);
+        double c[3] = {0, 0, 0};
+        if (r < nrec && l < 6) {
+            const int e = edges[6 * r + l];
             T u = U[e];
             if (unmerge != T(0)) {
-                int v = e / 7, dd = e % 7;
+                const int v = e / 7, dd = e % 7;
                 T mp = 0;
                 for (int j = 0; j < 7; ++j) mp = fma(minv[28 * (size_t)v + pk7(dd, j)], P[7 * (size_t)v + j], mp);
                 u = fma(-unmerge, mp, u);
             }
-            for (int q = 0; q < 3; ++q) acc[q] += (double)u * w[18 * r + 3 * l + q];
+            for (int q = 0; q < 3; ++q) c[q] = (double)u * w[18 * r + 3 * l + q];
         }
-        double *o = tr + ((size_t)r * nsamp + step / tf) * 4;
-        o[1] = acc[0]; o[2] = acc[1]; o[3] = acc[2];
+        double acc[3] = {0, 0, 0};
+        for (int j = 0; j < 6; ++j)
+            for (int q = 0; q < 3; ++q) acc[q] += __shfl_sync(0xffffffffu, c[q], j, 8);
+        if (r < nrec && l == 0) {
+            double *o = tr + ((size_t)r * nsamp + step / tf) * 4;
+            o[1] = acc[0]; o[2] = acc[1]; o[3] = acc[2];
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) ctl[0] = step + 1;
@@ -1121,7 +1130,7 @@ struct TetFemSim : Sim {
     template <class T>
     int enqueue_step(T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa0, T *zout)
     {
-        tet_receiver_kernel<T><<<1, 256, 0, stream>>>(nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), Uc, Pc, d_minv.as<T>(),
+        tet_receiver_kernel<T><<<1, 512, 0, stream>>>(nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), Uc, Pc, d_minv.as<T>(),
                                                       sc.symp ? (T)sc.hfirst : T(0), d_tr.as<double>(), nsamp,
                                                       P.time_frequency, d_ctl.as<int>());
         int nl = 1;
