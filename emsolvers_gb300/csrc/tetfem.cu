@@ -320,6 +320,34 @@ __device__ __forceinline__ T gather_force(size_t e, const int *__restrict__ inc_
     return f;
 }
 
+// The same sum over the fixed-width incidence table of the time step: six
+// entries per slot (t*8 + l in ascending t, -1 after the last), read with
+// three 8-byte loads; the B loads of the incident tetrahedra are issued
+// together before the sum, which keeps the order of gather_force.
+template <class T>
+__device__ __forceinline__ T gather_force6(size_t e, const int *__restrict__ inc6, const vec4<T> *__restrict__ B,
+                                           const vec4<T> *sc)
+{
+    const int2 *p2 = reinterpret_cast<const int2 *>(inc6 + 6 * e);
+    const int2 c01 = __ldg(p2), c23 = __ldg(p2 + 1), c45 = __ldg(p2 + 2);
+    const int code[6] = {c01.x, c01.y, c23.x, c23.y, c45.x, c45.y};
+    vec4<T> b[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        if (code[k] >= 0) b[k] = B[code[k] >> 3];
+    T f = 0;
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        if (code[k] >= 0) {
+            const int t = code[k] >> 3, l = code[k] & 7;
+            const vec4<T> cr = sc[6 * (t % 6) + l];
+            f = fma(b[k].x, cr.x, f);
+            f = fma(b[k].y, cr.y, f);
+            f = fma(b[k].z, cr.z, f);
+        }
+    return f;
+}
+
 // (Minv_v x)_d with x_j held by lane j of the node's 8-lane group.
 template <class T>
 __device__ __forceinline__ T block_apply(const T *__restrict__ mv, int d, T x)
@@ -330,6 +358,16 @@ __device__ __forceinline__ T block_apply(const T *__restrict__ mv, int d, T x)
         T xj = __shfl_sync(0xffffffffu, x, j, 8);
         if (d < 7) y = fma(mv[pk7(d, j)], xj, y);
     }
+    return y;
+}
+
+// block_apply with the lane's mass-block row already in registers.
+template <class T>
+__device__ __forceinline__ T block_apply_row(const T (&row)[7], T x)
+{
+    T y = 0;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) y = fma(row[j], __shfl_sync(0xffffffffu, x, j, 8), y);
     return y;
 }
 
@@ -361,7 +399,7 @@ __device__ __forceinline__ double source_load(const SrcArgs &s, size_t e)
 //   Uout_e = Uin_e + c * (Minv_v P)_e,  and zout_e = (Minv_v P)_e when zout is given.
 // With minv == nullptr only P is written (P -= a F): the stiffness apply.
 template <class T>
-__global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+__global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *__restrict__ inc6,
                                                        const unsigned char *__restrict__ pec, const vec4<T> *__restrict__ B,
                                                        const T *__restrict__ minv, T *__restrict__ P, const T *Uin, T *Uout,
                                                        T a, T c, SrcArgs src, T *__restrict__ zout)
@@ -371,23 +409,28 @@ __global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *
     size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t v = g >> 3;
     int d = (int)(g & 7);
-    bool live = v < nnode && d < 7;
-    size_t e = 7 * v + d;
-    T p = 0;
+    const bool live = v < nnode && d < 7;
+    const size_t e = 7 * v + d;
+    const size_t vc = v < nnode ? v : nnode - 1;   // keep the whole warp in the shuffles
+    // the mass-block row and the old U do not depend on the gather: load them first
+    T row[7];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) row[j] = (minv && d < 7) ? __ldg(minv + 28 * vc + pk7(d, j)) : T(0);
+    T p = 0, u = 0;
     if (live) {
         p = P[e];
+        if (minv) u = Uin[e];
         const unsigned char m = pec[e];
         if (!(m & kPecBit)) {
-            T f = gather_force<T>(e, inc_ptr, inc, B, sc);
+            T f = gather_force6<T>(e, inc6, B, sc);
             p = fma(-a, f, p);
             if (m & kSrcBit) p = fma(a, (T)source_load(src, e), p);
         }
         P[e] = p;
     }
     if (minv == nullptr) return;     // force-only use (uniform across the grid)
-    if (v >= nnode) v = nnode - 1;   // keep the whole warp in the shuffles
-    T y = block_apply<T>(minv + 28 * v, d, p);
-    if (live) Uout[e] = fma(c, y, Uin[e]);
+    T y = block_apply_row<T>(row, p);
+    if (live) Uout[e] = fma(c, y, u);
     if (zout && live) zout[e] = y;   // Minv P of this drift, kept for the adjoint
 }
 
@@ -409,7 +452,7 @@ __global__ void __launch_bounds__(256) tet_drift_kernel(size_t nnode, const T *_
 
 // Leapfrog: Unew = 2U - Uold - dt^2 Minv (K U - f); PEC slots stay zero.
 template <class T>
-__global__ void __launch_bounds__(256) tet_leapfrog_kernel(size_t nnode, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+__global__ void __launch_bounds__(256) tet_leapfrog_kernel(size_t nnode, const int *__restrict__ inc6,
                                                            const unsigned char *__restrict__ pec, const vec4<T> *__restrict__ B,
                                                            const T *__restrict__ minv, const T *__restrict__ U,
                                                            const T *__restrict__ Uold, T *__restrict__ Unew, T dt2, SrcArgs src)
@@ -419,17 +462,21 @@ __global__ void __launch_bounds__(256) tet_leapfrog_kernel(size_t nnode, const i
     size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t v = g >> 3;
     int d = (int)(g & 7);
-    bool live = v < nnode && d < 7;
-    size_t e = 7 * v + d;
-    T f = 0;
+    const bool live = v < nnode && d < 7;
+    const size_t e = 7 * v + d;
+    const size_t vc = v < nnode ? v : nnode - 1;
+    T row[7];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) row[j] = d < 7 ? __ldg(minv + 28 * vc + pk7(d, j)) : T(0);
+    T f = 0, u = 0, uo = 0;
     const unsigned char m = live ? pec[e] : (unsigned char)kPecBit;
+    if (live) { u = U[e]; uo = Uold[e]; }
     if (!(m & kPecBit)) {
-        f = gather_force<T>(e, inc_ptr, inc, B, sc);
+        f = gather_force6<T>(e, inc6, B, sc);
         if (m & kSrcBit) f -= (T)source_load(src, e);
     }
-    if (v >= nnode) v = nnode - 1;
-    T y = block_apply<T>(minv + 28 * v, d, f);
-    if (live) Unew[e] = (m & kPecBit) ? T(0) : fma(-dt2, y, T(2) * U[e] - Uold[e]);
+    T y = block_apply_row<T>(row, f);
+    if (live) Unew[e] = (m & kPecBit) ? T(0) : fma(-dt2, y, T(2) * u - uo);
 }
 
 // Receivers and step counter, one block: at the start of step n = ctl[0],
@@ -780,10 +827,10 @@ struct TetFemSim : Sim {
     double c0 = 299792458.0;
     double tscale;                  // seconds per normalised time unit (h / c0)
     double dtn = 0.0, dt_lim_n = 0.0, lambda_max = 0.0;
-    std::vector<int> tet_edge_h, inc_ptr_h, inc_h;
+    std::vector<int> tet_edge_h, inc_ptr_h, inc_h, inc6_h;
     std::vector<unsigned char> pec_h;
     std::vector<double> eps_h;
-    DevBuf d_tet_edge, d_inc_ptr, d_inc, d_pec, d_eps, d_minv64, d_minv, d_B, d_U, d_P, d_Uold, d_status;
+    DevBuf d_tet_edge, d_inc_ptr, d_inc, d_inc6, d_pec, d_eps, d_minv64, d_minv, d_B, d_U, d_P, d_Uold, d_status;
     std::vector<Dipole> dips;
     std::vector<std::array<int, 6>> rec_edges;
     std::vector<std::array<double, 18>> rec_w;
@@ -882,6 +929,14 @@ struct TetFemSim : Sim {
                 int e = tet_edge_h[6 * t + l];
                 inc_h[inc_ptr_h[e] + fill[e]++] = (int)(t * 8 + l);
             }
+        // the same lists at a fixed width of six for the time step (the Kuhn
+        // mesh has at most six tetrahedra on an edge), padded with -1
+        inc6_h.assign(6 * nslot, -1);
+        for (size_t e = 0; e < nslot; ++e) {
+            const int n = inc_ptr_h[e + 1] - inc_ptr_h[e];
+            if (n > 6) throw Error{EMS_ERR_INVALID_ARGUMENT, "edge with more than six tetrahedra"};
+            for (int k = 0; k < n; ++k) inc6_h[6 * e + k] = inc_h[inc_ptr_h[e] + k];
+        }
     }
 
     void upload_tables()
@@ -925,6 +980,7 @@ struct TetFemSim : Sim {
         up(d_tet_edge, tet_edge_h);
         up(d_inc_ptr, inc_ptr_h);
         up(d_inc, inc_h);
+        up(d_inc6, inc6_h);
         up(d_pec, pec_h);
         size_t w = fp64 ? 8 : 4;
         d_U.alloc(nslot * w); d_U.zero(stream);
@@ -1014,7 +1070,7 @@ struct TetFemSim : Sim {
         tet_curl_kernel<double><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), x.as<double>(), nullptr, B.as<vec4<double>>());
         z.zero(stream);
         unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
-        tet_kick_kernel<double><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+        tet_kick_kernel<double><<<nbn, 256, 0, stream>>>(nnode, d_inc6.as<int>(), d_pec.as<unsigned char>(),
                                                          B.as<vec4<double>>(), nullptr, z.as<double>(), nullptr, nullptr, -1.0, 0.0,
                                                          SrcArgs{}, nullptr);
     }
@@ -1113,10 +1169,10 @@ struct TetFemSim : Sim {
         vec4<T> *B = d_B.as<vec4<T>>();
         tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Uin, nullptr, B);
         if (MODE == 0)
-            tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+            tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc6.as<int>(), d_pec.as<unsigned char>(),
                                                         B, d_minv.as<T>(), Pio, Uin, Uout, a, c, sa, zout);
         else
-            tet_leapfrog_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+            tet_leapfrog_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc6.as<int>(), d_pec.as<unsigned char>(),
                                                             B, d_minv.as<T>(), Uin, Uold, Uout, c, sa);
         return 2;
     }
@@ -1505,7 +1561,7 @@ struct TetFemSim : Sim {
             EMS_CUDA(cudaMemcpyAsync(in.p, h.data(), nslot * w, cudaMemcpyHostToDevice, stream));
             vec4<T> *B = d_B.as<vec4<T>>();
             tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), in.as<T>(), nullptr, B);
-            tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(), d_pec.as<unsigned char>(),
+            tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc6.as<int>(), d_pec.as<unsigned char>(),
                                                         B, nullptr, out.as<T>(), nullptr, nullptr, T(-1), T(0), SrcArgs{},
                                                         nullptr);
             EMS_CUDA(cudaGetLastError());
@@ -1535,8 +1591,7 @@ struct TetFemSim : Sim {
             using T = decltype(tag);
             for (int r = 0; r <= launches; ++r) {
                 if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
-                tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc_ptr.as<int>(), d_inc.as<int>(),
-                                                            d_pec.as<unsigned char>(), d_B.as<vec4<T>>(), d_minv.as<T>(),
+                tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc6.as<int>(), d_pec.as<unsigned char>(), d_B.as<vec4<T>>(), d_minv.as<T>(),
                                                             d_P.as<T>(), d_U.as<T>(), d_Uold.as<T>(), T(0), T(0), SrcArgs{},
                                                             nullptr);
             }
@@ -1548,11 +1603,11 @@ struct TetFemSim : Sim {
         float t = 0;
         EMS_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
         *ms = t / launches;
-        // unique bytes of one kick: incidence list + row pointers + B (3
-        // values per tetrahedron, stored as 4) + P read and written + U read
-        // + U written + packed mass blocks + slot flags
-        *bytes = (double)(6 * ntet) * 4 + (double)(nslot + 1) * 4 + (double)(4 * ntet) * w + (double)nslot * 4 * w +
-                 (double)(28 * nnode) * w + (double)nslot;
+        // unique bytes of one kick: fixed-width incidence table (6 ints per
+        // slot) + B (3 values per tetrahedron, stored as 4) + P read and
+        // written + U read + U written + packed mass blocks + slot flags
+        *bytes = (double)nslot * 24 + (double)(4 * ntet) * w + (double)nslot * 4 * w + (double)(28 * nnode) * w +
+                 (double)nslot;
         *name = fp64 ? "tet_kick_kernel<double>" : "tet_kick_kernel<float>";
     }
 };
