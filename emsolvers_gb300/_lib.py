@@ -96,6 +96,7 @@ def lib():
         "ems_trace_shape": (C.c_int, [vp, ip, ip, ip]),
         "ems_get_traces": (C.c_int, [vp, dp, C.c_size_t]),
         "ems_save_results": (C.c_int, [vp, C.c_char_p]),
+        "ems_save_trace_component": (C.c_int, [vp, C.c_int, C.c_int, C.c_char_p]),
         "ems_field_size": (C.c_int, [vp, C.c_int, C.POINTER(C.c_size_t)]),
         "ems_get_field": (C.c_int, [vp, C.c_int, dp, C.c_size_t]),
         "ems_set_field": (C.c_int, [vp, C.c_int, dp, C.c_size_t]),

@@ -103,4 +103,17 @@ std::string compress_number(double v)
     return mant + ex;
 }
 
+void Sim::save_component(int receiver, int component, const char *path) const
+{
+    EMS_CHECK_ARG(path && *path, "file name required");
+    EMS_CHECK_ARG(receiver >= 0 && receiver < nobs, "receiver index out of range");
+    EMS_CHECK_ARG(component >= 0 && component < 3, "component must be 0 (x), 1 (y) or 2 (z)");
+    std::ofstream f(path);
+    if (!f.is_open()) throw Error{EMS_ERR_IO, std::string("cannot open ") + path};
+    const int off = ncols == 4 ? 1 : 0;   // FEM tables: t, Ex, Ey, Ez; FDTD: Ex, Ey, Ez
+    f << std::setprecision(15) << std::scientific << "t,u" << std::endl;
+    for (int j = 0; j < nsamp; ++j)
+        f << sample_time(j) << "," << traces[((size_t)receiver * nsamp + j) * ncols + off + component] << std::endl;
+}
+
 }  // namespace ems

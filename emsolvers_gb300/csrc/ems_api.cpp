@@ -246,6 +246,11 @@ int ems_save_results(const ems_sim *s, const char *path)
     if (!s) return EMS_ERR_INVALID_ARGUMENT;
     return guard(const_cast<ems_sim *>(s), [&] { s->impl->save(path); });
 }
+int ems_save_trace_component(const ems_sim *s, int receiver, int component, const char *path)
+{
+    if (!s) return EMS_ERR_INVALID_ARGUMENT;
+    return guard(const_cast<ems_sim *>(s), [&] { s->impl->save_component(receiver, component, path); });
+}
 int ems_field_size(const ems_sim *s, int which, size_t *n)
 {
     if (!s || !n) return EMS_ERR_INVALID_ARGUMENT;

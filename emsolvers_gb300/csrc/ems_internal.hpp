@@ -69,6 +69,11 @@ struct Sim {
     virtual void save(const char *path) const = 0;
     virtual void time_dominant(int launches, double *ms, double *bytes, std::string *name) = 0;
     virtual void reset() = 0;
+    // Time [s] of sample j of the last run (FEM tables carry it in column 0).
+    virtual double sample_time(int j) const { return traces[(size_t)j * ncols]; }
+    // One receiver component as the `t,u` CSV that
+    // TF_MISFIT_GOF_master/main.py:6-40 reads.
+    void save_component(int receiver, int component, const char *path) const;
 };
 
 // CSV element matrices in the reference format (fem_v2/fem_simulation.cpp:1477-1524).

@@ -34,9 +34,16 @@ template <class T> struct Prof {
     const unsigned char *on;
 };
 
+// Row (y) and plane (z) strides of the padded arrays and of the material
+// grid, in elements (all arrays hold fewer than 2^32 elements).
+struct FdtdStrides {
+    unsigned ex_y, ex_z, ey_y, ey_z, ez_y, ez_z, hx_y, hx_z, hy_y, hy_z, hz_y, hz_z, m_y, m_z;
+};
+
 template <class T> struct FdtdArgs {
     T *Ex, *Ey, *Ez, *Hx, *Hy, *Hz;
     int nx, ny, nz;
+    FdtdStrides st;
     T ch, ce;                      // uniform update coefficients dt/mu/h, dt/eps/h
     const uint16_t *mat;           // per-cell material id (MAT)
     const T *ca, *cb;              // per-material E coefficients (MAT)
@@ -66,7 +73,9 @@ __device__ __forceinline__ T pml_curl(T d1, T d2, const Prof<T> &p1, int s1, con
     return rsub(radd(rsub(rmul(p1.kinv[s1], d1), rmul(p2.kinv[s2], d2)), q1), q2);
 }
 
-// H from curl E at cell (i,j,k): fdtd_simulation.cpp:119-169.
+// H from curl E at cell (i,j,k): fdtd_simulation.cpp:119-169.  Offsets are
+// 32-bit, formed once per array and moved by the strides; E values shared
+// by two components are loaded once.
 template <class T, bool PML>
 __global__ void __launch_bounds__(256) fdtd_h_kernel(FdtdArgs<T> a)
 {
@@ -74,10 +83,18 @@ __global__ void __launch_bounds__(256) fdtd_h_kernel(FdtdArgs<T> a)
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z;
     if (i > a.nx || j > a.ny || k > a.nz) return;
-    if (i < a.nx) {
-        size_t p = IHX(i, j, k);
-        T e1 = a.Ez[IEZ(i + 1, j + 1, k)], e2 = a.Ez[IEZ(i + 1, j, k)];
-        T e3 = a.Ey[IEY(i + 1, j, k + 1)], e4 = a.Ey[IEY(i + 1, j, k)];
+    const FdtdStrides &st = a.st;
+    const unsigned oEx = i + j * st.ex_y + k * st.ex_z, oEy = i + j * st.ey_y + k * st.ey_z;
+    const unsigned oEz = i + j * st.ez_y + k * st.ez_z;
+    const bool hx = i < a.nx, hy = j < a.ny, hz = k < a.nz;
+    T ez11 = 0, ey1k = 0, ex1k = 0;   // Ez(i+1,j+1,k), Ey(i+1,j,k+1), Ex(i,j+1,k+1)
+    if (hx || hy) ez11 = __ldg(a.Ez + oEz + 1 + st.ez_y);
+    if (hx || hz) ey1k = __ldg(a.Ey + oEy + 1 + st.ey_z);
+    if (hy || hz) ex1k = __ldg(a.Ex + oEx + st.ex_y + st.ex_z);
+    if (hx) {
+        const unsigned p = i + j * st.hx_y + k * st.hx_z;
+        const T e1 = ez11, e2 = __ldg(a.Ez + oEz + 1);
+        const T e3 = ey1k, e4 = __ldg(a.Ey + oEy + 1);
         if (PML && (a.ph[1].on[j] | a.ph[2].on[k])) {
             T c = pml_curl(rsub(e1, e2), rsub(e3, e4), a.ph[1], j, a.ph[2], k, &a.psiH[0][0][p], &a.psiH[0][1][p]);
             a.Hx[p] = rsub(a.Hx[p], rmul(a.ch, c));
@@ -85,10 +102,10 @@ __global__ void __launch_bounds__(256) fdtd_h_kernel(FdtdArgs<T> a)
             a.Hx[p] = rsub(a.Hx[p], rmul(a.ch, curl4(e1, e2, e3, e4)));
         }
     }
-    if (j < a.ny) {
-        size_t p = IHY(i, j, k);
-        T e1 = a.Ex[IEX(i, j + 1, k + 1)], e2 = a.Ex[IEX(i, j + 1, k)];
-        T e3 = a.Ez[IEZ(i + 1, j + 1, k)], e4 = a.Ez[IEZ(i, j + 1, k)];
+    if (hy) {
+        const unsigned p = i + j * st.hy_y + k * st.hy_z;
+        const T e1 = ex1k, e2 = __ldg(a.Ex + oEx + st.ex_y);
+        const T e3 = ez11, e4 = __ldg(a.Ez + oEz + st.ez_y);
         if (PML && (a.ph[2].on[k] | a.ph[0].on[i])) {
             T c = pml_curl(rsub(e1, e2), rsub(e3, e4), a.ph[2], k, a.ph[0], i, &a.psiH[1][0][p], &a.psiH[1][1][p]);
             a.Hy[p] = rsub(a.Hy[p], rmul(a.ch, c));
@@ -96,10 +113,10 @@ __global__ void __launch_bounds__(256) fdtd_h_kernel(FdtdArgs<T> a)
             a.Hy[p] = rsub(a.Hy[p], rmul(a.ch, curl4(e1, e2, e3, e4)));
         }
     }
-    if (k < a.nz) {
-        size_t p = IHZ(i, j, k);
-        T e1 = a.Ey[IEY(i + 1, j, k + 1)], e2 = a.Ey[IEY(i, j, k + 1)];
-        T e3 = a.Ex[IEX(i, j + 1, k + 1)], e4 = a.Ex[IEX(i, j, k + 1)];
+    if (hz) {
+        const unsigned p = i + j * st.hz_y + k * st.hz_z;
+        const T e1 = ey1k, e2 = __ldg(a.Ey + oEy + st.ey_z);
+        const T e3 = ex1k, e4 = __ldg(a.Ex + oEx + st.ex_z);
         if (PML && (a.ph[0].on[i] | a.ph[1].on[j])) {
             T c = pml_curl(rsub(e1, e2), rsub(e3, e4), a.ph[0], i, a.ph[1], j, &a.psiH[2][0][p], &a.psiH[2][1][p]);
             a.Hz[p] = rsub(a.Hz[p], rmul(a.ch, c));
@@ -109,7 +126,8 @@ __global__ void __launch_bounds__(256) fdtd_h_kernel(FdtdArgs<T> a)
     }
 }
 
-// E from curl H at (i,j,k): fdtd_simulation.cpp:170-220, E = ca E + cb curl.
+// E from curl H at (i,j,k): fdtd_simulation.cpp:170-220, E = ca E + cb curl
+// (ca, cb of the cell's material; uniform: E += ce curl).
 template <class T, bool MAT, bool PML>
 __global__ void __launch_bounds__(256) fdtd_e_kernel(FdtdArgs<T> a)
 {
@@ -118,17 +136,29 @@ __global__ void __launch_bounds__(256) fdtd_e_kernel(FdtdArgs<T> a)
     const int k = blockIdx.z;
     if (i > a.nx || j > a.ny || k > a.nz) return;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
-    auto cell = [&](int ci, int cj, int ck) { return a.mat[(size_t)ci + (size_t)cj * nx + (size_t)ck * nx * ny]; };
-    auto upd = [&](T *f, size_t p, T ca, T cb, T c) {
+    const FdtdStrides &st = a.st;
+    const unsigned oHx = i + j * st.hx_y + k * st.hx_z, oHy = i + j * st.hy_y + k * st.hy_z;
+    const unsigned oHz = i + j * st.hz_y + k * st.hz_z;
+    const bool ex = j >= 1 && k >= 1, ey = i >= 1 && k >= 1, ez = i >= 1 && j >= 1;
+    T hz_k = 0, hy_j = 0, hx_i = 0;   // Hz(i,j,k-1), Hy(i,j-1,k), Hx(i-1,j,k)
+    if (ex || ey) hz_k = __ldg(a.Hz + oHz - st.hz_z);
+    if (ex || ez) hy_j = __ldg(a.Hy + oHy - st.hy_y);
+    if (ey || ez) hx_i = __ldg(a.Hx + oHx - 1);
+    auto upd = [&](T *f, unsigned p, T ca, T cb, T c) {
         if (MAT) f[p] = radd(rmul(ca, f[p]), rmul(cb, c));
         else f[p] = radd(f[p], rmul(a.ce, c));
     };
-    if (j >= 1 && k >= 1) {  // Ex, i in [0,nx]
-        size_t p = IEX(i, j, k);
+    auto coef = [&](int ci, int cj, int ck, T &ca, T &cb) {
+        const int m = __ldg(a.mat + (unsigned)ci + (unsigned)cj * st.m_y + (unsigned)ck * st.m_z);
+        ca = __ldg(a.ca + m);
+        cb = __ldg(a.cb + m);
+    };
+    if (ex) {  // Ex, i in [0,nx]
+        const unsigned p = i + j * st.ex_y + k * st.ex_z;
         T ca = 1, cb = 0;
-        if (MAT) { int m = cell(i < nx ? i : nx - 1, j - 1, k - 1); ca = a.ca[m]; cb = a.cb[m]; }
-        T h1 = a.Hz[IHZ(i, j, k - 1)], h2 = a.Hz[IHZ(i, j - 1, k - 1)];
-        T h3 = a.Hy[IHY(i, j - 1, k)], h4 = a.Hy[IHY(i, j - 1, k - 1)];
+        if (MAT) coef(i < nx ? i : nx - 1, j - 1, k - 1, ca, cb);
+        const T h1 = hz_k, h2 = __ldg(a.Hz + oHz - st.hz_y - st.hz_z);
+        const T h3 = hy_j, h4 = __ldg(a.Hy + oHy - st.hy_y - st.hy_z);
         if (PML && (a.pe[1].on[j] | a.pe[2].on[k])) {
             T c = pml_curl(rsub(h1, h2), rsub(h3, h4), a.pe[1], j, a.pe[2], k, &a.psiE[0][0][p], &a.psiE[0][1][p]);
             T cbb = MAT ? cb : a.ce;
@@ -138,12 +168,12 @@ __global__ void __launch_bounds__(256) fdtd_e_kernel(FdtdArgs<T> a)
             upd(a.Ex, p, ca, cb, curl4(h1, h2, h3, h4));
         }
     }
-    if (i >= 1 && k >= 1) {  // Ey, j in [0,ny]
-        size_t p = IEY(i, j, k);
+    if (ey) {  // Ey, j in [0,ny]
+        const unsigned p = i + j * st.ey_y + k * st.ey_z;
         T ca = 1, cb = 0;
-        if (MAT) { int m = cell(i - 1, j < ny ? j : ny - 1, k - 1); ca = a.ca[m]; cb = a.cb[m]; }
-        T h1 = a.Hx[IHX(i - 1, j, k)], h2 = a.Hx[IHX(i - 1, j, k - 1)];
-        T h3 = a.Hz[IHZ(i, j, k - 1)], h4 = a.Hz[IHZ(i - 1, j, k - 1)];
+        if (MAT) coef(i - 1, j < ny ? j : ny - 1, k - 1, ca, cb);
+        const T h1 = hx_i, h2 = __ldg(a.Hx + oHx - 1 - st.hx_z);
+        const T h3 = hz_k, h4 = __ldg(a.Hz + oHz - 1 - st.hz_z);
         if (PML && (a.pe[2].on[k] | a.pe[0].on[i])) {
             T c = pml_curl(rsub(h1, h2), rsub(h3, h4), a.pe[2], k, a.pe[0], i, &a.psiE[1][0][p], &a.psiE[1][1][p]);
             T cbb = MAT ? cb : a.ce;
@@ -153,12 +183,12 @@ __global__ void __launch_bounds__(256) fdtd_e_kernel(FdtdArgs<T> a)
             upd(a.Ey, p, ca, cb, curl4(h1, h2, h3, h4));
         }
     }
-    if (i >= 1 && j >= 1) {  // Ez, k in [0,nz]
-        size_t p = IEZ(i, j, k);
+    if (ez) {  // Ez, k in [0,nz]
+        const unsigned p = i + j * st.ez_y + k * st.ez_z;
         T ca = 1, cb = 0;
-        if (MAT) { int m = cell(i - 1, j - 1, k < nz ? k : nz - 1); ca = a.ca[m]; cb = a.cb[m]; }
-        T h1 = a.Hy[IHY(i, j - 1, k)], h2 = a.Hy[IHY(i - 1, j - 1, k)];
-        T h3 = a.Hx[IHX(i - 1, j, k)], h4 = a.Hx[IHX(i - 1, j - 1, k)];
+        if (MAT) coef(i - 1, j - 1, k < nz ? k : nz - 1, ca, cb);
+        const T h1 = hy_j, h2 = __ldg(a.Hy + oHy - 1 - st.hy_y);
+        const T h3 = hx_i, h4 = __ldg(a.Hx + oHx - 1 - st.hx_y);
         if (PML && (a.pe[0].on[i] | a.pe[1].on[j])) {
             T c = pml_curl(rsub(h1, h2), rsub(h3, h4), a.pe[0], i, a.pe[1], j, &a.psiE[2][0][p], &a.psiE[2][1][p]);
             T cbb = MAT ? cb : a.ce;
@@ -241,6 +271,7 @@ struct FdtdSim : Sim {
     {
         nx = P.grid[0]; ny = P.grid[1]; nz = P.grid[2];
         EMS_CHECK_ARG(nx > 0 && ny > 0 && nz > 0, "grid sizes must be positive");
+        EMS_CHECK_ARG((double)(nx + 2) * (ny + 2) * (nz + 2) < 4294967296.0, "grid too large for 32-bit array offsets");
         EMS_CHECK_ARG(P.h > 0 && P.dt > 0 && P.permittivity > 0 && P.permeability > 0, "h, dt, eps, mu must be positive");
         EMS_CHECK_ARG(P.time_frequency > 0, "time_frequency must be positive");
         EMS_CHECK_ARG(P.precision == EMS_FP64 || P.precision == EMS_FP32, "precision must be EMS_FP64 or EMS_FP32");
@@ -380,6 +411,9 @@ struct FdtdSim : Sim {
         a.Ex = F[0].as<T>(); a.Ey = F[1].as<T>(); a.Ez = F[2].as<T>();
         a.Hx = F[3].as<T>(); a.Hy = F[4].as<T>(); a.Hz = F[5].as<T>();
         a.nx = nx; a.ny = ny; a.nz = nz;
+        const unsigned X = nx, Y = ny;
+        a.st = FdtdStrides{X + 1, (X + 1) * (Y + 2), X + 2, (X + 2) * (Y + 1), X + 2, (X + 2) * (Y + 2),
+                           X, X * (Y + 1), X + 1, (X + 1) * Y, X + 1, (X + 1) * (Y + 1), X, X * Y};
         a.ch = (T)(P.dt / P.permeability / P.h);
         a.ce = (T)(P.dt / P.permittivity / P.h);
         a.mat = d_mat.as<uint16_t>();
@@ -549,6 +583,8 @@ struct FdtdSim : Sim {
             }
         }
     }
+
+    double sample_time(int j) const override { return j * P.time_frequency * P.dt; }
 
     void reset() override
     {

@@ -16,13 +16,14 @@
 // scales of the lowest frequency, so the circular convolution equals the
 // linear one to exp(-32)); the envelope difference
 // dE(t, f) = |W(t, f)| - |W_ref(t, f)| gives the single-valued envelope
-// misfit EM = sqrt(sum dE^2 / sum |W_ref|^2) (components whose reference
-// has no energy in the band are skipped).  The constant factors of the
-// transform cancel in EM and are left out.  Here J = 1/2 sum EM^2 over
-// receivers and components (smooth where EM = 0, unlike EM itself), and
-//     dJ/ds = (1/sum|W_ref|^2) sum_f Re(A_f^H (dE_f W_f / |W_f|)),
-// A_f the discrete transform at frequency f and A_f^H its adjoint
-// (zero-pad, FFT, window, inverse FFT, crop).
+// misfit EM = sqrt(sum dE^2 / sum |W_ref|^2); the phase difference
+// dP(t, f) = |W_ref| (Arg W - Arg W_ref) / pi gives the phase misfit PM in
+// the same way (components whose reference has no energy in the band are
+// skipped).  The constant factors of the transform cancel and are left
+// out.  Here J = 1/2 sum EM^2 (or PM^2) over receivers and components
+// (smooth where the misfit vanishes, unlike EM itself), and its gradient
+// follows through the adjoint A_f^H of the discrete transform at each
+// frequency (zero-pad, FFT, window, inverse FFT, crop).
 #include <cmath>
 #include <complex>
 #include <thread>
@@ -108,17 +109,30 @@ void tf_transform(const TfPlan &p, const double *s, std::vector<std::vector<cplx
     }
 }
 
-// EM^2 of s against s_ref and, when g is given, d(EM^2 / 2)/ds.
-double tf_envelope_misfit(const TfPlan &p, const double *s, const double *sref, double *g)
+// EM^2 (phase = false) or PM^2 (phase = true) of s against s_ref and, when
+// g is given, its half derivative d(X^2 / 2)/ds.
+//   envelope: dE = |W| - |W_ref|,           R = dE W / |W|,                 g = Re(A^H R) / N
+//   phase:    dP = |W_ref| dphi / pi,       R = |W_ref|^2 dphi W / (pi^2 |W|^2), g = -Im(A^H R) / N
+// with dphi = Arg W - Arg W_ref wrapped to (-pi, pi], N = sum |W_ref|^2, and
+// A^H R = crop(IFFT(window * FFT(pad(R)))) carrying the 1/n2 of the forward
+// transform's inverse FFT.
+double tf_misfit(const TfPlan &p, const double *s, const double *sref, double *g, bool phase)
 {
     std::vector<std::vector<cplx>> W, Wr;
     tf_transform(p, s, W);
     tf_transform(p, sref, Wr);
+    auto dphi = [](const cplx &w, const cplx &wr) {
+        double d = std::arg(w) - std::arg(wr);
+        if (d > M_PI) d -= 2.0 * M_PI;
+        if (d <= -M_PI) d += 2.0 * M_PI;
+        return d;
+    };
     double num = 0.0, den = 0.0;
     for (size_t k = 0; k < W.size(); ++k)
         for (int i = 0; i < p.nsamp; ++i) {
-            double dE = std::abs(W[k][i]) - std::abs(Wr[k][i]);
-            num += dE * dE;
+            const double dX = phase ? std::abs(Wr[k][i]) * dphi(W[k][i], Wr[k][i]) / M_PI
+                                    : std::abs(W[k][i]) - std::abs(Wr[k][i]);
+            num += dX * dX;
             den += std::norm(Wr[k][i]);
         }
     if (den == 0.0) {   // no reference energy in the band: the component is skipped
@@ -132,15 +146,17 @@ double tf_envelope_misfit(const TfPlan &p, const double *s, const double *sref, 
         for (size_t k = 0; k < W.size(); ++k) {
             std::fill(tmp.begin(), tmp.end(), cplx(0.0, 0.0));
             for (int i = 0; i < p.nsamp; ++i) {
-                double m = std::abs(W[k][i]);
-                if (m > 0.0) tmp[i] = (m - std::abs(Wr[k][i])) * W[k][i] / m;
+                const double m = std::abs(W[k][i]);
+                if (m == 0.0) continue;
+                if (phase)
+                    tmp[i] = std::norm(Wr[k][i]) * dphi(W[k][i], Wr[k][i]) / (M_PI * M_PI * m * m) * W[k][i];
+                else
+                    tmp[i] = (m - std::abs(Wr[k][i])) * W[k][i] / m;
             }
-            // A^H R = crop(IFFT(window * FFT(pad(R)))) with the 1/n2 of the
-            // forward transform's inverse FFT
             fft(tmp, -1);
             for (size_t m = 0; m < p.n2; ++m) tmp[m] *= p.window[k][m];
             fft(tmp, +1);
-            for (int i = 0; i < p.nsamp; ++i) acc[i] += tmp[i].real() / (double)p.n2;
+            for (int i = 0; i < p.nsamp; ++i) acc[i] += (phase ? -tmp[i].imag() : tmp[i].real()) / (double)p.n2;
         }
         for (int i = 0; i < p.nsamp; ++i) g[i] = acc[i] / den;
     }
@@ -172,7 +188,9 @@ void trace_misfit(int kind, int nobs, int nsamp, const double *tr, const double 
         if (misfit) *misfit = J;
         return;
     }
-    if (kind != EMS_MISFIT_TF_ENVELOPE) throw Error{EMS_ERR_INVALID_ARGUMENT, "unknown misfit kind"};
+    if (kind != EMS_MISFIT_TF_ENVELOPE && kind != EMS_MISFIT_TF_PHASE)
+        throw Error{EMS_ERR_INVALID_ARGUMENT, "unknown misfit kind"};
+    const bool phase = kind == EMS_MISFIT_TF_PHASE;
     EMS_CHECK_ARG(nsamp >= 4, "the TF envelope misfit needs at least 4 samples");
     const double dt = tr[4] - tr[0];
     EMS_CHECK_ARG(dt > 0 && std::isfinite(dt), "column 0 must hold increasing sample times");
@@ -199,7 +217,7 @@ void trace_misfit(int kind, int nobs, int nsamp, const double *tr, const double 
                         s[i] = tr[((size_t)r * nsamp + i) * 4 + 1 + c];
                         sr[i] = obs[((size_t)r * nsamp + i) * 4 + 1 + c];
                     }
-                    em2[task] = tf_envelope_misfit(plan, s.data(), sr.data(), tg ? g.data() : nullptr);
+                    em2[task] = tf_misfit(plan, s.data(), sr.data(), tg ? g.data() : nullptr, phase);
                     if (tg)
                         for (int i = 0; i < nsamp; ++i) tg[((size_t)r * nsamp + i) * 4 + 1 + c] = g[i];
                 }

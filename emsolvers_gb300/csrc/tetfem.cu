@@ -421,8 +421,10 @@ __global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *
         p = P[e];
         if (minv) u = Uin[e];
         const unsigned char m = pec[e];
+        // gathered for every live slot (PEC and unused slots list no or
+        // unused incidences), so its loads do not wait for the flag byte
+        const T f = gather_force6<T>(e, inc6, B, sc);
         if (!(m & kPecBit)) {
-            T f = gather_force6<T>(e, inc6, B, sc);
             p = fma(-a, f, p);
             if (m & kSrcBit) p = fma(a, (T)source_load(src, e), p);
         }
@@ -470,10 +472,14 @@ __global__ void __launch_bounds__(256) tet_leapfrog_kernel(size_t nnode, const i
     for (int j = 0; j < 7; ++j) row[j] = d < 7 ? __ldg(minv + 28 * vc + pk7(d, j)) : T(0);
     T f = 0, u = 0, uo = 0;
     const unsigned char m = live ? pec[e] : (unsigned char)kPecBit;
-    if (live) { u = U[e]; uo = Uold[e]; }
-    if (!(m & kPecBit)) {
-        f = gather_force6<T>(e, inc6, B, sc);
-        if (m & kSrcBit) f -= (T)source_load(src, e);
+    if (live) {
+        u = U[e];
+        uo = Uold[e];
+        const T g = gather_force6<T>(e, inc6, B, sc);   // issued before the flag test, as in the kick
+        if (!(m & kPecBit)) {
+            f = g;
+            if (m & kSrcBit) f -= (T)source_load(src, e);
+        }
     }
     T y = block_apply_row<T>(row, f);
     if (live) Unew[e] = (m & kPecBit) ? T(0) : fma(-dt2, y, T(2) * u - uo);

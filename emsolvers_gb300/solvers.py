@@ -55,6 +55,11 @@ class _Sim:
         a = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
         self._check(lib().ems_set_field(self._h, which, _dptr(a), a.size))
 
+    def save_component(self, receiver, component, path):
+        """One receiver component as the `t,u` CSV read by the reference's
+        TF_MISFIT_GOF_master/main.py."""
+        self._check(lib().ems_save_trace_component(self._h, int(receiver), int(component), str(path).encode()))
+
     def run_stats(self):
         ms, n = C.c_double(), C.c_longlong()
         self._check(lib().ems_last_run_stats(self._h, C.byref(ms), C.byref(n)))
@@ -299,15 +304,16 @@ class TetFemBatch(TetFemSimulation):
         return self.cells
 
 
-MISFIT_L2, MISFIT_TF_ENVELOPE = 0, 1
+MISFIT_L2, MISFIT_TF_ENVELOPE, MISFIT_TF_PHASE = 0, 1, 2
 
 
 def trace_misfit(traces, observed, kind=MISFIT_L2, tf_band=None):
     """Misfit J of traces against observed traces (both [nobs, nsamp, 4] as
     returned by ``traces()``) and dJ/dtraces (same shape, column 0 zero).
-    kind: MISFIT_L2 (1/2 sum of squared differences) or MISFIT_TF_ENVELOPE
-    (1/2 sum of squared single-valued TF envelope misfits, Kristekova et al.
-    2006); tf_band = (fmin, fmax, nf) in the units of the time column."""
+    kind: MISFIT_L2 (1/2 sum of squared differences), MISFIT_TF_ENVELOPE or
+    MISFIT_TF_PHASE (1/2 sum of squared single-valued TF envelope / phase
+    misfits, Kristekova et al. 2006); tf_band = (fmin, fmax, nf) in the units
+    of the time column."""
     tr = np.ascontiguousarray(traces, dtype=np.float64)
     ob = np.ascontiguousarray(observed, dtype=np.float64)
     if tr.shape != ob.shape or tr.ndim != 3 or tr.shape[2] != 4:

@@ -211,13 +211,15 @@ int ems_tetfem_gradient(ems_sim *sim, int nsteps, int nsnap, int misfit_kind, co
 
 enum {
     EMS_MISFIT_L2 = 0,          /* J = 1/2 sum (E - E_obs)^2 over receivers, samples, components */
-    EMS_MISFIT_TF_ENVELOPE = 1  /* single-valued time-frequency envelope misfit (Kristekova et al. 2006) */
+    EMS_MISFIT_TF_ENVELOPE = 1, /* single-valued time-frequency envelope misfit EM (Kristekova et al. 2006) */
+    EMS_MISFIT_TF_PHASE = 2     /* single-valued time-frequency phase misfit PM (same paper) */
 };
 /* Misfit of traces against observed traces (both nobs x nsamp x 4 in the
  * ems_get_traces layout; column 0 holds the sample times) and its gradient
  * with respect to the traces (same layout, column 0 zero; may be NULL).
- * EMS_MISFIT_TF_ENVELOPE: J = 1/2 sum of EM^2 over receivers and components,
- * EM the single-valued envelope misfit with the observed trace as reference
+ * EMS_MISFIT_TF_ENVELOPE / _PHASE: J = 1/2 sum of EM^2 / PM^2 over receivers
+ * and components, EM / PM the single-valued envelope / phase misfit with the
+ * observed trace as reference
  * (TF_MISFIT_GOF's IS_S2_REFERENCE = T, LOCAL_NORM = F, one component per
  * pair); tf_band = {fmin, fmax, nf} in the units of the time column (NULL:
  * 4/T .. 1/(4 dt), 32 log-spaced frequencies); ignored for EMS_MISFIT_L2. */
@@ -237,6 +239,10 @@ int ems_get_traces(const ems_sim *sim, double *out, size_t n);
  * fem_v2 :1322-1344 writes the given file name, one file per receiver with
  * suffix _<i> when there is more than one). */
 int ems_save_results(const ems_sim *sim, const char *path);
+/* One component (0 = x, 1 = y, 2 = z) of one receiver of the last run as the
+ * `t,u` CSV that TF_MISFIT_GOF_master/main.py:6-40 converts for the
+ * third-party misfit program (header t,u; 15 significant digits). */
+int ems_save_trace_component(const ems_sim *sim, int receiver, int component, const char *path);
 /* Field access in the reference layout, converted to/from double.
  * FDTD: which 0..5 = Ex,Ey,Ez,Hx,Hy,Hz.  Hex FEM: which 0..2 = component
  * x,y,z (all levels).  Tet FEM: 0 = U (edge values), 1 = P. */

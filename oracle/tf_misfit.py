@@ -10,9 +10,12 @@ exp(-x^2/2), w0 = 6 (constant factors dropped: they cancel in the misfit):
 
     W(t_j, f) = a^{-1/2} sum_i s(t_i) conj(psi((t_i - t_j) / a)) dt,   a = w0 / (2 pi f)
 
-and the single-valued envelope misfit of s against the reference s_ref
+and the single-valued envelope and phase misfits of s against the
+reference s_ref
 
-    EM = sqrt( sum_{j,f} (|W(t_j,f)| - |W_ref(t_j,f)|)^2 / sum_{j,f} |W_ref(t_j,f)|^2 ).
+    EM = sqrt( sum_{j,f} (|W(t_j,f)| - |W_ref(t_j,f)|)^2 / sum_{j,f} |W_ref(t_j,f)|^2 ),
+    PM = sqrt( sum_{j,f} (|W_ref| dphi / pi)^2 / sum_{j,f} |W_ref|^2 ),
+    dphi = Arg W - Arg W_ref wrapped to (-pi, pi].
 """
 import numpy as np
 
@@ -47,3 +50,16 @@ def envelope_misfit(s, s_ref, dt, fmin, fmax, nf):
     if den == 0.0:
         return 0.0
     return float(np.sqrt(np.sum((np.abs(W) - np.abs(Wr)) ** 2) / den))
+
+
+def phase_misfit(s, s_ref, dt, fmin, fmax, nf):
+    """PM of s against s_ref (0 when s_ref has no energy in the band)."""
+    fr = frequencies(fmin, fmax, nf)
+    W, Wr = cwt_morlet(s, dt, fr), cwt_morlet(s_ref, dt, fr)
+    den = np.sum(np.abs(Wr) ** 2)
+    if den == 0.0:
+        return 0.0
+    d = np.angle(W) - np.angle(Wr)
+    d = np.where(d > np.pi, d - 2 * np.pi, d)
+    d = np.where(d <= -np.pi, d + 2 * np.pi, d)
+    return float(np.sqrt(np.sum((np.abs(Wr) * d / np.pi) ** 2) / den))

@@ -126,6 +126,12 @@ def test_save_results_matches_reference_format(tmp_path):
     assert lines[0] == "time,Ex,Ey,Ez"
     assert len(lines) == m["nsteps"] // m["tf"] + 2
     assert lines[1].startswith("0,0,0,0")
+    s.save_component(0, 1, tmp_path / "ey.csv")
+    rows = (tmp_path / "ey.csv").read_text().splitlines()
+    tu = np.array([[float(x) for x in r.split(",")] for r in rows[1:]])
+    assert rows[0] == "t,u"
+    np.testing.assert_allclose(tu[:, 0], np.arange(len(tu)) * m["tf"] * m["dt"], rtol=1e-14)
+    np.testing.assert_allclose(tu[:, 1], s.traces()[0, :, 1], rtol=1e-14)
 
 
 def test_runs_are_deterministic():

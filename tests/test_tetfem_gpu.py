@@ -126,6 +126,16 @@ def test_save_results_writes_reference_trace_format(tmp_path):
     lines = fn.read_text().splitlines()
     assert lines[0] == "time,Ex,Ey,Ez" and len(lines) == 21
     assert (tmp_path / "tet_1.csv").exists()
+    # per-component t,u file for the TF misfit pipeline
+    tr = s.traces()
+    s.save_component(1, 2, tmp_path / "u.csv")
+    rows = (tmp_path / "u.csv").read_text().splitlines()
+    assert rows[0] == "t,u" and len(rows) == tr.shape[1] + 1
+    tu = np.array([[float(x) for x in r.split(",")] for r in rows[1:]])
+    np.testing.assert_allclose(tu[:, 0], tr[1, :, 0], rtol=1e-14)
+    np.testing.assert_allclose(tu[:, 1], tr[1, :, 3], rtol=1e-14)
+    with pytest.raises(ems.EmsError):
+        s.save_component(5, 0, tmp_path / "bad.csv")
 
 
 @pytest.mark.parametrize("precision,tol", [(ems.FP64, 1e-13), (ems.FP32, 1e-6)])
