@@ -228,6 +228,41 @@ def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
             "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
 
 
+def hex72(steps=200, order=2, sample_steps=10):
+    """The reference's own solver family: symplectic_4, OFEM order 2 on a
+    72^3 fine grid (1,151,064 edge DOFs; the element size and time step of
+    the symplectic_4 order-2 golden case), FP64 (bit-identical to the
+    reference) and FP32 device rates, against the FP64 oracle port of the
+    reference's loop on the host cores (`sample_steps` steps)."""
+    import emsolvers_gb300 as ems
+    import oracle
+    g = 72
+    h, dt, eps0, mu0 = 0.1, 9.629166007732144e-11, 8.8541878128e-12, 1.25663706212e-06
+    kdir = os.path.join(ROOT, "tests", "golden", "kmat")
+    dofs = 3 * g * (g + 1) ** 2
+    out = {"workload": f"hex{g}_symp4_o{order}_ofem", "dofs": dofs, "steps": steps, "order": order}
+    for prec, name in ((ems.FP64, "fp64"), (ems.FP32, "fp32")):
+        s = ems.HexFemSimulation(order, (g, g, g), h, dt, eps0, mu0, 2, 1, integrator=ems.SYMP4, precision=prec,
+                                 kmat_dir=kdir)
+        s.setSource_z((g // 2, g // 2, g // 2))
+        s.setObservationPoint((g // 2 + 6, g // 2 - 4, g // 2 + 2))
+        s.run(5)
+        s.reset()
+        s.run(steps)
+        ms, _ = s.run_stats()
+        out[f"dof_updates_per_s_{name}"] = dofs * steps / (ms * 1e-3)
+        s.close()
+    kmat = oracle.load_kmat(os.path.join(kdir, f"{order}.csv"))
+    t0 = time.perf_counter()
+    oracle.hexfem_run(order, (g, g, g), h, dt, eps0, mu0, 2, oracle.SYMP4, kmat, sample_steps,
+                      sources=[(2, (g // 2, g // 2, g // 2))], observations=[(g // 2 + 6, g // 2 - 4, g // 2 + 2)])
+    cpu = dofs * sample_steps / (time.perf_counter() - t0)
+    out["cpu_baseline"] = {"value": cpu, "unit": "DOF-updates/s", "cores": os.cpu_count() or 1, "kind": "port",
+                           "sample": f"{sample_steps} steps, FP64 oracle of the reference loop (bit-identical to it)"}
+    out["speedup_fp64_vs_cpu"] = out["dof_updates_per_s_fp64"] / cpu
+    return out
+
+
 def blob_model(n, rng, background=2.0, nblob=3):
     """Per-tet eps_r: background plus nblob Gaussian blobs (amplitude U[1,3],
     width U[4,8] cells) evaluated at the tetrahedron centroids."""
@@ -432,6 +467,11 @@ def run_gpu(args):
                 out["batch64"] = batch64()
             except Exception as e:  # secondary measurement only
                 out["batch64"] = {"error": str(e)}
+        if not args.no_hex:
+            try:
+                out["hex72"] = hex72()
+            except Exception as e:  # secondary measurement only
+                out["hex72"] = {"error": str(e)}
         if not args.no_adjoint:
             try:
                 out["adjoint16"] = adjoint16()
@@ -458,7 +498,8 @@ def main():
     ap.add_argument("--no-fdtd", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--only", choices=["batch", "fdtd", "adjoint"],
+    ap.add_argument("--no-hex", action="store_true")
+    ap.add_argument("--only", choices=["batch", "fdtd", "adjoint", "hex"],
                     help="run one secondary workload alone and print its JSON (for profiling)")
     ap.add_argument("--fdtd-n", type=int, default=512, help="FDTD cube side for --only fdtd")
     ap.add_argument("--adj-n", type=int, default=48, help="cube side for --only adjoint")
@@ -470,7 +511,7 @@ def main():
     if args.only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        fn = {"batch": batch64, "fdtd": lambda: fdtd_512(n=args.fdtd_n), "adjoint": lambda: adjoint16(n=args.adj_n, nshots=args.adj_shots, steps=args.adj_steps,
+        fn = {"batch": batch64, "fdtd": lambda: fdtd_512(n=args.fdtd_n), "hex": hex72, "adjoint": lambda: adjoint16(n=args.adj_n, nshots=args.adj_shots, steps=args.adj_steps,
                                              sample_steps=min(400, args.adj_steps))}[args.only]
         print(json.dumps(fn()))
     elif args.impl == "reference":

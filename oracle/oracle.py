@@ -184,10 +184,6 @@ class _TetCase(C.Structure):
                 ("dip_kind", _ip), ("nrec", C.c_int), ("rec_pos", _dp)]
 
 
-# integrators of orc_tet_case (ORC_LEAPFROG / ORC_SYMP2 / ORC_SYMP4 in ems_oracle.h)
-ORC_LEAPFROG, ORC_SYMP2, ORC_SYMP4 = 0, 1, 2
-
-
 def tet_sizes(n):
     nx, ny, nz = n
     nnode = (nx + 1) * (ny + 1) * (nz + 1)

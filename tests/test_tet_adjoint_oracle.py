@@ -55,7 +55,7 @@ def _misfit_setup(integrator, steps=40, dt=0.3):
     return eps, J, resid, dt, steps
 
 
-@pytest.mark.parametrize("integrator", [oracle.ORC_SYMP2, oracle.ORC_SYMP4], ids=["symp2", "symp4"])
+@pytest.mark.parametrize("integrator", [oracle.SYMP2, oracle.SYMP4], ids=["symp2", "symp4"])
 def test_oracle_gradient_matches_finite_differences(integrator):
     eps, J, resid, dt, steps = _misfit_setup(integrator)
     g = oracle.tet_gradient(N, eps, integrator, dt, steps, resid, 1, DIPOLES, RECEIVERS)
@@ -71,10 +71,10 @@ def test_oracle_gradient_matches_finite_differences(integrator):
 
 
 def test_oracle_gradient_is_linear_in_the_trace_weights():
-    eps, _, resid, dt, steps = _misfit_setup(oracle.ORC_SYMP4, steps=25)
+    eps, _, resid, dt, steps = _misfit_setup(oracle.SYMP4, steps=25)
     rng = np.random.default_rng(3)
     r2 = rng.standard_normal(resid.shape)
-    g1 = oracle.tet_gradient(N, eps, oracle.ORC_SYMP4, dt, steps, resid, 1, DIPOLES, RECEIVERS)
-    g2 = oracle.tet_gradient(N, eps, oracle.ORC_SYMP4, dt, steps, r2, 1, DIPOLES, RECEIVERS)
-    g12 = oracle.tet_gradient(N, eps, oracle.ORC_SYMP4, dt, steps, 2.0 * resid - 0.5 * r2, 1, DIPOLES, RECEIVERS)
+    g1 = oracle.tet_gradient(N, eps, oracle.SYMP4, dt, steps, resid, 1, DIPOLES, RECEIVERS)
+    g2 = oracle.tet_gradient(N, eps, oracle.SYMP4, dt, steps, r2, 1, DIPOLES, RECEIVERS)
+    g12 = oracle.tet_gradient(N, eps, oracle.SYMP4, dt, steps, 2.0 * resid - 0.5 * r2, 1, DIPOLES, RECEIVERS)
     assert np.allclose(g12, 2.0 * g1 - 0.5 * g2, rtol=1e-10, atol=1e-14 * np.abs(g12).max())
