@@ -259,6 +259,7 @@ struct FdtdSim : Sim {
     DevBuf d_mat, d_ca, d_cb;
     // CPML
     DevBuf d_prof[2][3][4];   // [E/H][axis][b,a,kinv,on]
+    std::vector<unsigned char> pml_on[2][3];   // host copies of the "on" flags
     DevBuf d_psiE[3][2], d_psiH[3][2];
     // sources, receivers
     std::vector<FdtdSource> srcs;
@@ -326,6 +327,7 @@ struct FdtdSim : Sim {
                 upload_real(d_prof[eh][d][2], kinv);
                 d_prof[eh][d][3].alloc(cnt);
                 EMS_CUDA(cudaMemcpyAsync(d_prof[eh][d][3].p, on.data(), cnt, cudaMemcpyHostToDevice, stream));
+                pml_on[eh][d] = on;
             }
         size_t w = fp64 ? 8 : 4;
         for (int c = 0; c < 3; ++c)
@@ -595,12 +597,26 @@ struct FdtdSim : Sim {
         EMS_CUDA(cudaStreamSynchronize(stream));
     }
 
+    // E points whose update runs the CPML recursion (two psi values each).
+    double pml_e_points() const
+    {
+        if (P.pml_cells <= 0) return 0.0;
+        auto pairs = [&](int d1, int n1, int d2, int n2) {
+            double c = 0.0;
+            for (int a = 1; a <= n1; ++a)
+                for (int b = 1; b <= n2; ++b) c += (pml_on[0][d1][a] | pml_on[0][d2][b]) ? 1.0 : 0.0;
+            return c;
+        };
+        return (nx + 1.0) * pairs(1, ny, 2, nz) + (ny + 1.0) * pairs(2, nz, 0, nx) + (nz + 1.0) * pairs(0, nx, 1, ny);
+    }
+
     void time_dominant(int launches, double *ms, double *bytes, std::string *name) override
     {
-        // E update: reads H (3), reads and writes E (3), plus the material id
+        // E update: reads H (3), reads and writes E (3), the material id, and
+        // reads and writes two psi values per point inside the CPML
         size_t w = fp64 ? 8 : 4;
         size_t cells = (size_t)nx * ny * nz;
-        double b = (double)cells * 9.0 * w + (mat_host.empty() ? 0.0 : 2.0 * cells);
+        double b = (double)cells * 9.0 * w + (mat_host.empty() ? 0.0 : 2.0 * cells) + pml_e_points() * 4.0 * w;
         std::vector<DevBuf> save(3);
         for (int q = 0; q < 3; ++q) {
             save[q].alloc(F[q].bytes);
