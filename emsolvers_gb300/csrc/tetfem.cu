@@ -286,44 +286,12 @@ __global__ void __launch_bounds__(256) tet_curl_kernel(size_t ntet, const int *_
     B[t] = o;
 }
 
-// Curl-transpose gathered for slot e over its incidence list (ascending
-// tetrahedron order): F_e = sum B_t . curl(w_l).  Up to six incidences are
-// issued unrolled (the Kuhn mesh has at most six); longer lists continue.
-template <class T>
-__device__ __forceinline__ T gather_force(size_t e, const int *__restrict__ inc_ptr, const int *__restrict__ inc,
-                                          const vec4<T> *__restrict__ B, const vec4<T> *sc)
-{
-    const int s0 = inc_ptr[e], s1 = inc_ptr[e + 1];
-    T f = 0;
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        int s = s0 + k;
-        if (s < s1) {
-            int code = __ldg(inc + s);
-            int t = code >> 3, l = code & 7, p = t % 6;
-            vec4<T> b = B[t];
-            vec4<T> cr = sc[6 * p + l];
-            f = fma(b.x, cr.x, f);
-            f = fma(b.y, cr.y, f);
-            f = fma(b.z, cr.z, f);
-        }
-    }
-    for (int s = s0 + 6; s < s1; ++s) {
-        int code = __ldg(inc + s);
-        int t = code >> 3, l = code & 7, p = t % 6;
-        vec4<T> b = B[t];
-        vec4<T> cr = sc[6 * p + l];
-        f = fma(b.x, cr.x, f);
-        f = fma(b.y, cr.y, f);
-        f = fma(b.z, cr.z, f);
-    }
-    return f;
-}
-
-// The same sum over the fixed-width incidence table of the time step: six
-// entries per slot (t*8 + l in ascending t, -1 after the last), read with
-// three 8-byte loads; the B loads of the incident tetrahedra are issued
-// together before the sum, which keeps the order of gather_force.
+// Curl-transpose gathered for slot e over its incidences: F_e = sum_T
+// B_T . curl(w_l), in ascending tetrahedron order (deterministic, no
+// atomics).  The incidences come from a fixed-width table of six entries per
+// slot (t*8 + l, -1 after the last; the Kuhn mesh has at most six
+// tetrahedra on an edge) read with three 8-byte loads, and the B loads of
+// all incident tetrahedra are issued before the sum.
 template <class T>
 __device__ __forceinline__ T gather_force6(size_t e, const int *__restrict__ inc6, const vec4<T> *__restrict__ B,
                                            const vec4<T> *sc)
@@ -765,10 +733,36 @@ __global__ void dot_partial_kernel(size_t n, const double *__restrict__ x, const
     if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
-__global__ void scale_kernel(size_t n, double *x, double *y, double s)
+// *out = the partial sums added in index order (one thread: the same
+// order as a host loop over them).
+__global__ void dot_finish_kernel(int nb, const double *__restrict__ part, double *__restrict__ out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0;
+    for (int i = 0; i < nb; ++i) s += part[i];
+    *out = s;
+}
+
+// x, y *= 1 / sqrt(*nrm)
+__global__ void scale_kernel(size_t n, double *x, double *y, const double *__restrict__ nrm)
 {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const double s = 1.0 / sqrt(*nrm);
     if (i < n) { x[i] *= s; y[i] *= s; }
+}
+
+// Lanczos three-term step on a vector and its mass image:
+// w -= alpha v + beta vp,  Mw -= alpha Mv + beta Mvp  (alpha = *a, beta = sqrt(*b2)).
+__global__ void lanczos_step_kernel(size_t n, double *__restrict__ w, double *__restrict__ Mw, const double *__restrict__ v,
+                                    const double *__restrict__ Mv, const double *__restrict__ vp,
+                                    const double *__restrict__ Mvp, const double *__restrict__ a,
+                                    const double *__restrict__ b2)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double al = *a, be = b2 ? sqrt(*b2) : 0.0;
+    w[i] = w[i] - al * v[i] - be * (vp ? vp[i] : 0.0);
+    Mw[i] = Mw[i] - al * Mv[i] - be * (Mvp ? Mvp[i] : 0.0);
 }
 
 // -------------------------------------------------------------- host side
@@ -1045,10 +1039,10 @@ struct TetFemSim : Sim {
         EMS_CUDA(cudaGetLastError());
         if (P.dt > 0) {
             dtn = P.dt / tscale;
-            lambda_max = power_iteration(minv_d, 300);
+            lambda_max = lambda_max_lanczos(minv_d, 400);
             dt_lim_n = stability_constant(P.integrator) / std::sqrt(lambda_max);
         } else {
-            lambda_max = power_iteration(minv_d, 300);
+            lambda_max = lambda_max_lanczos(minv_d, 400);
             dt_lim_n = stability_constant(P.integrator) / std::sqrt(lambda_max);
             dtn = P.cfl_fraction * dt_lim_n;
         }
@@ -1057,16 +1051,13 @@ struct TetFemSim : Sim {
         ready = true;
     }
 
-    double dot(const DevBuf &x, const DevBuf &y, DevBuf &part)
+    // *out = x.y on the device (deterministic: block partials, then their
+    // sum in order)
+    void dot(const DevBuf &x, const DevBuf &y, DevBuf &part, double *out)
     {
         const int nb = 512;
         dot_partial_kernel<<<nb, 256, 0, stream>>>(nslot, x.as<double>(), y.as<double>(), part.as<double>());
-        std::vector<double> h(nb);
-        EMS_CUDA(cudaMemcpyAsync(h.data(), part.p, nb * 8, cudaMemcpyDeviceToHost, stream));
-        EMS_CUDA(cudaStreamSynchronize(stream));
-        double s = 0.0;
-        for (double v : h) s += v;
-        return s;
+        dot_finish_kernel<<<1, 32, 0, stream>>>(nb, part.as<double>(), out);
     }
 
     // y = K x in FP64 through the curl kernel and the force-only kick (P = 0, a = -1)
@@ -1081,35 +1072,96 @@ struct TetFemSim : Sim {
                                                          SrcArgs{}, nullptr);
     }
 
-    double power_iteration(const DevBuf &minv_d, int iters)
+    // Largest eigenvalue of Minv K by Lanczos in the M inner product.  Minv K
+    // is self-adjoint there, and every Lanczos vector v travels with its mass
+    // image Mv: K v is the mass image of w = Minv K v, so <v, w>_M = v.K v and
+    // <w, w>_M = w.(M w) need no M.  The start pair is x = Minv K x0, Mx =
+    // K x0.  The tridiagonal coefficients stay on the device; every 20 steps
+    // the largest eigenvalue of the tridiagonal matrix (Sturm bisection) is
+    // checked and the iteration stops once it changes by less than 1e-10.
+    // Without reorthogonalisation converged Ritz values repeat, which does
+    // not move the largest one.
+    double lambda_max_lanczos(const DevBuf &minv_d, int max_iters)
     {
-        DevBuf x, z, p, B, part;
-        x.alloc(nslot * 8); z.alloc(nslot * 8); p.alloc(nslot * 8); B.alloc(4 * ntet * 8); part.alloc(512 * 8);
+        DevBuf vb[3], mb[3], B, part, coef;
+        for (int q = 0; q < 3; ++q) { vb[q].alloc(nslot * 8); mb[q].alloc(nslot * 8); }
+        B.alloc(4 * ntet * 8);
+        part.alloc(512 * 8);
+        coef.alloc(2 * (max_iters + 2) * 8);   // alpha_j at [2j], beta_{j+1}^2 at [2j+1]
         std::vector<double> x0(nslot);
         unsigned long long st = 0x9E3779B97F4A7C15ull;
         for (size_t e = 0; e < nslot; ++e) {
             st ^= st << 13; st ^= st >> 7; st ^= st << 17;
             x0[e] = (pec_h[e] & kPecBit) ? 0.0 : ((double)(st >> 11) / 9007199254740992.0 - 0.5);
         }
-        EMS_CUDA(cudaMemcpyAsync(x.p, x0.data(), nslot * 8, cudaMemcpyHostToDevice, stream));
-        unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
-        applyK64(x, p, B);                   // p = K x0
-        x.zero(stream);
-        tet_drift_kernel<double><<<nbn, 256, 0, stream>>>(nnode, minv_d.as<double>(), p.as<double>(), x.as<double>(), 1.0);
-        double lam = 0.0;
-        for (int it = 0; it < iters; ++it) {
-            applyK64(x, z, B);
-            double num = dot(x, z, part), den = dot(x, p, part);
-            lam = num / den;
-            EMS_CUDA(cudaMemcpyAsync(p.p, z.p, nslot * 8, cudaMemcpyDeviceToDevice, stream));
-            x.zero(stream);
-            tet_drift_kernel<double><<<nbn, 256, 0, stream>>>(nnode, minv_d.as<double>(), p.as<double>(), x.as<double>(), 1.0);
-            double nrm = dot(x, x, part);
-            scale_kernel<<<(unsigned)((nslot + 255) / 256), 256, 0, stream>>>(nslot, x.as<double>(), p.as<double>(), 1.0 / std::sqrt(nrm));
+        const unsigned nbn = (unsigned)((8 * nnode + 255) / 256), nbs = (unsigned)((nslot + 255) / 256);
+        double *cf = coef.as<double>();
+        // start pair (v1, Mv1) = (Minv K x0, K x0) / |.|_M, in buffers 1
+        EMS_CUDA(cudaMemcpyAsync(vb[0].p, x0.data(), nslot * 8, cudaMemcpyHostToDevice, stream));
+        applyK64(vb[0], mb[1], B);
+        vb[1].zero(stream);
+        tet_drift_kernel<double><<<nbn, 256, 0, stream>>>(nnode, minv_d.as<double>(), mb[1].as<double>(), vb[1].as<double>(), 1.0);
+        dot(vb[1], mb[1], part, cf + 2 * max_iters + 2);
+        scale_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), cf + 2 * max_iters + 2);
+        int prev = -1, cur = 1, nxt = 2;
+        std::vector<double> h;
+        double lam = 0.0, lam_old = -1.0;
+        int j = 0;
+        for (; j < max_iters; ++j) {
+            // w = Minv K v (mass image K v), alpha = v.K v
+            applyK64(vb[cur], mb[nxt], B);
+            dot(vb[cur], mb[nxt], part, cf + 2 * j);
+            vb[nxt].zero(stream);
+            tet_drift_kernel<double><<<nbn, 256, 0, stream>>>(nnode, minv_d.as<double>(), mb[nxt].as<double>(),
+                                                              vb[nxt].as<double>(), 1.0);
+            lanczos_step_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(), vb[cur].as<double>(),
+                                                         mb[cur].as<double>(), prev >= 0 ? vb[prev].as<double>() : nullptr,
+                                                         prev >= 0 ? mb[prev].as<double>() : nullptr, cf + 2 * j,
+                                                         j > 0 ? cf + 2 * j - 1 : nullptr);
+            dot(vb[nxt], mb[nxt], part, cf + 2 * j + 1);   // beta_{j+1}^2
+            scale_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(), cf + 2 * j + 1);
+            const int t = prev < 0 ? 0 : prev;
+            prev = cur; cur = nxt; nxt = t;
+            if ((j + 1) % 20 == 0 || j + 1 == max_iters) {
+                h.resize(2 * (j + 1));
+                EMS_CUDA(cudaMemcpyAsync(h.data(), cf, h.size() * 8, cudaMemcpyDeviceToHost, stream));
+                EMS_CUDA(cudaStreamSynchronize(stream));
+                lam = tridiag_max_eig(h, j + 1);
+                const bool breakdown = !(h[2 * j + 1] > 1e-300);
+                if (breakdown || std::fabs(lam - lam_old) <= 1e-10 * lam) break;
+                lam_old = lam;
+            }
         }
         EMS_CUDA(cudaGetLastError());
-        EMS_CUDA(cudaStreamSynchronize(stream));
         return lam;
+    }
+
+    // Largest eigenvalue of the symmetric tridiagonal matrix with diagonal
+    // h[0], h[2], ... and squared off-diagonals h[1], h[3], ... (m x m), by
+    // bisection on the Sturm count of eigenvalues below x.
+    static double tridiag_max_eig(const std::vector<double> &h, int m)
+    {
+        double lo = 1e300, hi = -1e300;
+        for (int i = 0; i < m; ++i) {
+            const double r = (i > 0 ? std::sqrt(h[2 * i - 1]) : 0.0) + (i + 1 < m ? std::sqrt(h[2 * i + 1]) : 0.0);
+            lo = std::min(lo, h[2 * i] - r);
+            hi = std::max(hi, h[2 * i] + r);
+        }
+        auto below = [&](double x) {   // eigenvalues < x
+            int c = 0;
+            double d = 1.0;
+            for (int i = 0; i < m; ++i) {
+                d = h[2 * i] - x - (i > 0 ? h[2 * i - 1] / d : 0.0);
+                if (d == 0.0) d = -1e-300;
+                if (d < 0.0) ++c;
+            }
+            return c;
+        };
+        for (int it = 0; it < 200 && hi - lo > 1e-15 * std::fabs(hi); ++it) {
+            const double mid = 0.5 * (lo + hi);
+            if (below(mid) >= m) hi = mid; else lo = mid;
+        }
+        return hi;
     }
 
     void locate(const Shot &S, const double xn[3], double w[6][3], int edges[6]) const
