@@ -733,14 +733,19 @@ __global__ void dot_partial_kernel(size_t n, const double *__restrict__ x, const
     if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
-// *out = the partial sums added in index order (one thread: the same
-// order as a host loop over them).
-__global__ void dot_finish_kernel(int nb, const double *__restrict__ part, double *__restrict__ out)
+// *out = sum of the nb <= 512 partial sums, by a fixed-shape tree (one
+// block of 512 threads; deterministic).
+__global__ void __launch_bounds__(512) dot_finish_kernel(int nb, const double *__restrict__ part, double *__restrict__ out)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double s = 0.0;
-    for (int i = 0; i < nb; ++i) s += part[i];
-    *out = s;
+    __shared__ double sh[512];
+    const int t = threadIdx.x;
+    sh[t] = t < nb ? part[t] : 0.0;
+    __syncthreads();
+    for (int w = 256; w > 0; w >>= 1) {
+        if (t < w) sh[t] += sh[t + w];
+        __syncthreads();
+    }
+    if (t == 0) *out = sh[0];
 }
 
 // x, y *= 1 / sqrt(*nrm)
@@ -1057,7 +1062,7 @@ struct TetFemSim : Sim {
     {
         const int nb = 512;
         dot_partial_kernel<<<nb, 256, 0, stream>>>(nslot, x.as<double>(), y.as<double>(), part.as<double>());
-        dot_finish_kernel<<<1, 32, 0, stream>>>(nb, part.as<double>(), out);
+        dot_finish_kernel<<<1, 512, 0, stream>>>(nb, part.as<double>(), out);
     }
 
     // y = K x in FP64 through the curl kernel and the force-only kick (P = 0, a = -1)
