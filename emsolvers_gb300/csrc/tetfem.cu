@@ -362,6 +362,177 @@ __device__ __forceinline__ double source_load(const SrcArgs &s, size_t e)
     return f;
 }
 
+// ------------------------------------------------------ node-centric step
+// Each thread owns one node and its seven edge slots.  The tetrahedra that
+// hold the node as vertex 0, 1 or 2 (the tails of its slots) sit at fixed
+// cell offsets o in {-1, 0}^3 and types p: 18 around an interior node.
+// Listed in ascending tetrahedron order, each feeds one to three of the
+// node's slots, so every B is loaded once per node and each slot's sum runs
+// over its incidences in ascending tetrahedron order (the order of the
+// incidence lists).  The table is built at compile time from the Kuhn split.
+struct NodeTab {
+    int o[18][3], p[18];
+    int ne[18], d[18][3], l[18][3];   // slots (directions) fed by entry q and their local edges
+    int curl[6][6][3];                 // 2 grad(l_m) x grad(l_n) of local edge l of type p
+};
+
+constexpr NodeTab make_node_tab()
+{
+    NodeTab t{};
+    const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    const int loc[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+    const int dirs[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+    int vert[6][4][3] = {}, grad[6][4][3] = {};
+    for (int p = 0; p < 6; ++p) {
+        const int a = perm[p][0], b = perm[p][1], c = perm[p][2];
+        vert[p][1][a] = 1;
+        vert[p][2][a] = 1; vert[p][2][b] = 1;
+        vert[p][3][0] = vert[p][3][1] = vert[p][3][2] = 1;
+        grad[p][0][a] = -1;
+        grad[p][1][a] = 1; grad[p][1][b] = -1;
+        grad[p][2][b] = 1; grad[p][2][c] = -1;
+        grad[p][3][c] = 1;
+        for (int l = 0; l < 6; ++l) {
+            const int *gm = grad[p][loc[l][0]], *gn = grad[p][loc[l][1]];
+            t.curl[p][l][0] = 2 * (gm[1] * gn[2] - gm[2] * gn[1]);
+            t.curl[p][l][1] = 2 * (gm[2] * gn[0] - gm[0] * gn[2]);
+            t.curl[p][l][2] = 2 * (gm[0] * gn[1] - gm[1] * gn[0]);
+        }
+    }
+    int eo[18][3] = {}, ep[18] = {}, em[18] = {};
+    int n = 0;
+    for (int p = 0; p < 6; ++p)
+        for (int m = 0; m < 3; ++m) {
+            for (int x = 0; x < 3; ++x) eo[n][x] = -vert[p][m][x];
+            ep[n] = p;
+            em[n] = m;
+            ++n;
+        }
+    int idx[18] = {};
+    for (int q = 0; q < 18; ++q) idx[q] = q;
+    auto before = [&](int u, int w) {   // ascending tetrahedron index: cell (z, y, x), then type
+        if (eo[u][2] != eo[w][2]) return eo[u][2] < eo[w][2];
+        if (eo[u][1] != eo[w][1]) return eo[u][1] < eo[w][1];
+        if (eo[u][0] != eo[w][0]) return eo[u][0] < eo[w][0];
+        return ep[u] < ep[w];
+    };
+    for (int q = 1; q < 18; ++q)
+        for (int r = q; r > 0 && before(idx[r], idx[r - 1]); --r) {
+            const int tmp = idx[r];
+            idx[r] = idx[r - 1];
+            idx[r - 1] = tmp;
+        }
+    for (int q = 0; q < 18; ++q) {
+        const int s = idx[q], p = ep[s], m = em[s];
+        for (int x = 0; x < 3; ++x) t.o[q][x] = eo[s][x];
+        t.p[q] = p;
+        int k = 0;
+        for (int l = 0; l < 6; ++l) {
+            if (loc[l][0] != m) continue;
+            const int *vm = vert[p][m], *vn = vert[p][loc[l][1]];
+            int dd = 0;
+            for (int c = 0; c < 7; ++c)
+                if (dirs[c][0] == vn[0] - vm[0] && dirs[c][1] == vn[1] - vm[1] && dirs[c][2] == vn[2] - vm[2]) dd = c;
+            t.d[q][k] = dd;
+            t.l[q][k] = l;
+            ++k;
+        }
+        t.ne[q] = k;
+    }
+    return t;
+}
+
+// MODE 0 (symplectic): P_e -= a (F_e - f_e) on non-PEC slots, then
+// Uout = Uin + c Minv P (zout = Minv P); with minv == nullptr only P is
+// written (the stiffness apply).  MODE 1 (leapfrog): Uout = 2 Uin - Uold -
+// c Minv (F - f), PEC slots zero.  ntets: the 18 tetrahedron indices of each
+// node in table order, -1 where the cell is outside the mesh.
+template <class T, int MODE>
+__global__ void __launch_bounds__(128) tet_node_kernel(size_t nnode, const int *__restrict__ ntets,
+                                                       const unsigned char *__restrict__ pec, const vec4<T> *__restrict__ B,
+                                                       const T *__restrict__ minv, T *__restrict__ P, const T *Uin, T *Uout,
+                                                       const T *__restrict__ Uold, T a, T c, SrcArgs src,
+                                                       T *__restrict__ zout)
+{
+    constexpr NodeTab tab = make_node_tab();
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nnode) return;
+    const int2 *l2 = reinterpret_cast<const int2 *>(ntets + 18 * v);
+    int code[18];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const int2 x = __ldg(l2 + q);
+        code[2 * q] = x.x;
+        code[2 * q + 1] = x.y;
+    }
+    T f[7] = {0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int q = 0; q < 18; ++q)
+        if (code[q] >= 0) {
+            const vec4<T> b = B[code[q]];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                if (k < tab.ne[q]) {
+                    const int d = tab.d[q][k], l = tab.l[q][k], p = tab.p[q];
+                    f[d] = fma(b.x, (T)tab.curl[p][l][0], f[d]);
+                    f[d] = fma(b.y, (T)tab.curl[p][l][1], f[d]);
+                    f[d] = fma(b.z, (T)tab.curl[p][l][2], f[d]);
+                }
+        }
+    const size_t e0 = 7 * v;
+    unsigned char m[7];
+    T x[7], u[7];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) {
+        m[d] = pec[e0 + d];
+        if (MODE == 0) {
+            x[d] = P[e0 + d];
+            u[d] = minv ? Uin[e0 + d] : T(0);
+        } else {
+            u[d] = Uin[e0 + d];
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < 7; ++d) {
+        if (MODE == 0) {
+            if (!(m[d] & kPecBit)) {
+                x[d] = fma(-a, f[d], x[d]);
+                if (m[d] & kSrcBit) x[d] = fma(a, (T)source_load(src, e0 + d), x[d]);
+            }
+            P[e0 + d] = x[d];
+        } else {
+            x[d] = T(0);
+            if (!(m[d] & kPecBit)) {
+                x[d] = f[d];
+                if (m[d] & kSrcBit) x[d] -= (T)source_load(src, e0 + d);
+            }
+        }
+    }
+    if (minv == nullptr) return;   // force-only use (uniform across the grid)
+    T mv[28];
+    const vec4<T> *m4 = reinterpret_cast<const vec4<T> *>(minv + 28 * v);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        const vec4<T> w = m4[q];
+        mv[4 * q] = w.x; mv[4 * q + 1] = w.y; mv[4 * q + 2] = w.z; mv[4 * q + 3] = w.w;
+    }
+#pragma unroll
+    for (int d = 0; d < 7; ++d) {
+        T y = 0;
+#pragma unroll
+        for (int j = 0; j < 7; ++j) {
+            const int r = d < j ? d : j, s = d < j ? j : d;
+            y = fma(mv[r * (13 - r) / 2 + s], x[j], y);
+        }
+        if (MODE == 0) {
+            Uout[e0 + d] = fma(c, y, u[d]);
+            if (zout) zout[e0 + d] = y;
+        } else {
+            Uout[e0 + d] = (m[d] & kPecBit) ? T(0) : fma(-c, y, T(2) * u[d] - Uold[e0 + d]);
+        }
+    }
+}
+
 // Kick + drift, eight lanes per node (lane 7 idle):
 //   P_e -= a * (F_e - f_e)   (F = K U gathered, f the dipole load; PEC slots keep F = 0),
 //   Uout_e = Uin_e + c * (Minv_v P)_e,  and zout_e = (Minv_v P)_e when zout is given.
@@ -832,10 +1003,10 @@ struct TetFemSim : Sim {
     double c0 = 299792458.0;
     double tscale;                  // seconds per normalised time unit (h / c0)
     double dtn = 0.0, dt_lim_n = 0.0, lambda_max = 0.0;
-    std::vector<int> tet_edge_h, inc_ptr_h, inc_h, inc6_h;
+    std::vector<int> tet_edge_h, inc_ptr_h, inc_h, inc6_h, ntet_h;
     std::vector<unsigned char> pec_h;
     std::vector<double> eps_h;
-    DevBuf d_tet_edge, d_inc_ptr, d_inc, d_inc6, d_pec, d_eps, d_minv64, d_minv, d_B, d_U, d_P, d_Uold, d_status;
+    DevBuf d_tet_edge, d_inc_ptr, d_inc, d_inc6, d_ntet, d_pec, d_eps, d_minv64, d_minv, d_B, d_U, d_P, d_Uold, d_status;
     std::vector<Dipole> dips;
     std::vector<std::array<int, 6>> rec_edges;
     std::vector<std::array<double, 18>> rec_w;
@@ -934,6 +1105,24 @@ struct TetFemSim : Sim {
                 int e = tet_edge_h[6 * t + l];
                 inc_h[inc_ptr_h[e] + fill[e]++] = (int)(t * 8 + l);
             }
+        // the 18 tetrahedra around every node in node-table order (-1 where
+        // the cell is outside the mesh) for the node-centric step
+        {
+            constexpr NodeTab tab = make_node_tab();
+            ntet_h.assign(18 * nnode, -1);
+            for (const Shot &S : shots)
+                for (int k = 0; k <= S.nz; ++k)
+                    for (int j = 0; j <= S.ny; ++j)
+                        for (int i = 0; i <= S.nx; ++i) {
+                            const size_t v = node(S, i, j, k);
+                            for (int q = 0; q < 18; ++q) {
+                                const int ci = i + tab.o[q][0], cj = j + tab.o[q][1], ck = k + tab.o[q][2];
+                                if (ci < 0 || cj < 0 || ck < 0 || ci >= S.nx || cj >= S.ny || ck >= S.nz) continue;
+                                ntet_h[18 * v + q] =
+                                    (int)(S.tet0 + 6 * ((size_t)ci + (size_t)S.nx * ((size_t)cj + (size_t)S.ny * ck)) + tab.p[q]);
+                            }
+                        }
+        }
         // the same lists at a fixed width of six for the time step (the Kuhn
         // mesh has at most six tetrahedra on an edge), padded with -1
         inc6_h.assign(6 * nslot, -1);
@@ -986,6 +1175,7 @@ struct TetFemSim : Sim {
         up(d_inc_ptr, inc_ptr_h);
         up(d_inc, inc_h);
         up(d_inc6, inc6_h);
+        up(d_ntet, ntet_h);
         up(d_pec, pec_h);
         size_t w = fp64 ? 8 : 4;
         d_U.alloc(nslot * w); d_U.zero(stream);
@@ -1230,13 +1420,11 @@ struct TetFemSim : Sim {
     {
         const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
         vec4<T> *B = d_B.as<vec4<T>>();
+        const unsigned nbv = (unsigned)((nnode + 127) / 128);
+        (void)nbn;
         tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Uin, nullptr, B);
-        if (MODE == 0)
-            tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc6.as<int>(), d_pec.as<unsigned char>(),
-                                                        B, d_minv.as<T>(), Pio, Uin, Uout, a, c, sa, zout);
-        else
-            tet_leapfrog_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc6.as<int>(), d_pec.as<unsigned char>(),
-                                                            B, d_minv.as<T>(), Uin, Uold, Uout, c, sa);
+        tet_node_kernel<T, MODE><<<nbv, 128, 0, stream>>>(nnode, d_ntet.as<int>(), d_pec.as<unsigned char>(), B, d_minv.as<T>(),
+                                                          Pio, Uin, Uout, Uold, a, c, sa, zout);
         return 2;
     }
 
@@ -1647,16 +1835,16 @@ struct TetFemSim : Sim {
     {
         if (!ready) setup();
         const size_t w = fp64 ? 8 : 4;
-        const unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
-        // the kick of a substep; a = c = 0 leaves P unchanged and copies U
-        // into the spare buffer
+        const unsigned nbv = (unsigned)((nnode + 127) / 128);
+        // the node-centric kick of a substep; a = c = 0 leaves P unchanged
+        // and copies U into the spare buffer
         auto body = [&](auto tag) {
             using T = decltype(tag);
             for (int r = 0; r <= launches; ++r) {
                 if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
-                tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc6.as<int>(), d_pec.as<unsigned char>(), d_B.as<vec4<T>>(), d_minv.as<T>(),
-                                                            d_P.as<T>(), d_U.as<T>(), d_Uold.as<T>(), T(0), T(0), SrcArgs{},
-                                                            nullptr);
+                tet_node_kernel<T, 0><<<nbv, 128, 0, stream>>>(nnode, d_ntet.as<int>(), d_pec.as<unsigned char>(),
+                                                               d_B.as<vec4<T>>(), d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(),
+                                                               d_Uold.as<T>(), nullptr, T(0), T(0), SrcArgs{}, nullptr);
             }
         };
         if (fp64) body(double()); else body(float());
@@ -1666,12 +1854,12 @@ struct TetFemSim : Sim {
         float t = 0;
         EMS_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
         *ms = t / launches;
-        // unique bytes of one kick: fixed-width incidence table (6 ints per
-        // slot) + B (3 values per tetrahedron, stored as 4) + P read and
-        // written + U read + U written + packed mass blocks + slot flags
-        *bytes = (double)nslot * 24 + (double)(4 * ntet) * w + (double)nslot * 4 * w + (double)(28 * nnode) * w +
+        // unique bytes of one kick: node tetrahedron lists (18 ints per node)
+        // + B (3 values per tetrahedron, stored as 4) + P read and written +
+        // U read + U written + packed mass blocks + slot flags
+        *bytes = (double)nnode * 72 + (double)(4 * ntet) * w + (double)nslot * 4 * w + (double)(28 * nnode) * w +
                  (double)nslot;
-        *name = fp64 ? "tet_kick_kernel<double>" : "tet_kick_kernel<float>";
+        *name = fp64 ? "tet_node_kernel<double>" : "tet_node_kernel<float>";
     }
 };
 
