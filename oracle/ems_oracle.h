@@ -82,6 +82,7 @@ typedef struct {
     const int *dip_kind;          /* 1 = Ricker, 0 = Gaussian second derivative */
     int nrec;
     const double *rec_pos;
+    const double *sigma;          /* conductivity per tetrahedron or NULL (= 0) */
 } orc_tet_case;
 
 int orc_tet_run(const orc_tet_case *c, int nsteps, double *U, double *P, double *traces);
@@ -100,7 +101,8 @@ int orc_tet_apply_op(int nx, int ny, int nz, const double *eps_r, const double *
 void orc_tet_pec_mask(int nx, int ny, int nz, unsigned char *mask);
 int orc_tet_apply_K(int nx, int ny, int nz, const double *x, double *f);
 int orc_tet_mass_block(int nx, int ny, int nz, const double *eps_r, long v, long t, double *M, double *dM);
-int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad, double *grad_eps);
+int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad, double *grad_eps, double *grad_sigma);
+int orc_tet_loss_rate(int nx, int ny, int nz, const double *eps_r, const double *sigma, double *rho);
 
 /* ----------------------------------------- Adams-Bashforth-Moulton (hex) --- */
 typedef struct {

@@ -181,7 +181,7 @@ class _TetCase(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("eps_r", _dp), ("mu_r", _dp),
                 ("integrator", C.c_int), ("dt", C.c_double), ("time_frequency", C.c_int),
                 ("ndip", C.c_int), ("dip_pos", _dp), ("dip_dir", _dp), ("dip_f0", _dp), ("dip_amp", _dp),
-                ("dip_kind", _ip), ("nrec", C.c_int), ("rec_pos", _dp)]
+                ("dip_kind", _ip), ("nrec", C.c_int), ("rec_pos", _dp), ("sigma", _dp)]
 
 
 def tet_sizes(n):
@@ -201,15 +201,18 @@ def _tlib():
     return L
 
 
-def _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r):
+def _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r, sigma=None):
     """orc_tet_case for the arguments of tet_run; returns (case, arrays kept alive)."""
     _, _, ntet = tet_sizes(n)
     eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
     assert eps.size == ntet
     mu = None if mu_r is None else np.ascontiguousarray(mu_r, dtype=np.float64).reshape(-1)
+    sg = None if sigma is None else np.ascontiguousarray(sigma, dtype=np.float64).reshape(-1)
+    assert sg is None or sg.size == ntet
     c = _TetCase()
     c.nx, c.ny, c.nz = n
     c.eps_r, c.mu_r = _ptr(eps), _ptr(mu) if mu is not None else None
+    c.sigma = _ptr(sg) if sg is not None else None
     c.integrator, c.dt, c.time_frequency = integrator, dt, tf
     dp = np.array([d[0] for d in dipoles] or [(0, 0, 0)], np.float64).reshape(-1)
     dd = np.array([d[1] for d in dipoles] or [(0, 0, 1)], np.float64).reshape(-1)
@@ -219,17 +222,18 @@ def _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r):
     rp = np.array(list(receivers) or [(0, 0, 0)], np.float64).reshape(-1)
     c.ndip, c.dip_pos, c.dip_dir, c.dip_kind, c.dip_f0, c.dip_amp = len(dipoles), _ptr(dp), _ptr(dd), _ptr(dk, _ip), _ptr(df), _ptr(da)
     c.nrec, c.rec_pos = len(receivers), _ptr(rp)
-    return c, (eps, mu, dp, dd, dk, df, da, rp)
+    return c, (eps, mu, sg, dp, dd, dk, df, da, rp)
 
 
-def tet_run(n, eps_r, integrator, dt, nsteps, tf=1, dipoles=(), receivers=(), mu_r=None, U=None, P=None):
+def tet_run(n, eps_r, integrator, dt, nsteps, tf=1, dipoles=(), receivers=(), mu_r=None, U=None, P=None, sigma=None):
     """FP64 oracle of the tetrahedral solver in normalised units (cube edge 1,
-    c0 = 1).  dipoles: [(pos, dir, kind, f0, amp)]; receivers: [pos].
+    c0 = 1).  dipoles: [(pos, dir, kind, f0, amp)]; receivers: [pos];
+    sigma: conductivity per tetrahedron (normalised, a loss rate) or None.
     Returns (traces[nrec, nsamp, 4], U, P)."""
     _, nslot, _ = tet_sizes(n)
     U = np.zeros(nslot) if U is None else np.ascontiguousarray(U, dtype=np.float64).copy()
     P = np.zeros(nslot) if P is None else np.ascontiguousarray(P, dtype=np.float64).copy()
-    c, keep = _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r)
+    c, keep = _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r, sigma)
     nsamp = (nsteps - 1) // tf + 1 if nsteps > 0 else 0
     tr = np.zeros((max(len(receivers), 1), max(nsamp, 1), 4))
     rc = _tlib().orc_tet_run(C.byref(c), C.c_int(nsteps), _ptr(U), _ptr(P), _ptr(tr))
@@ -238,22 +242,33 @@ def tet_run(n, eps_r, integrator, dt, nsteps, tf=1, dipoles=(), receivers=(), mu
     return tr[:len(receivers), :nsamp], U, P
 
 
-def tet_gradient(n, eps_r, integrator, dt, nsteps, trace_grad, tf=1, dipoles=(), receivers=(), mu_r=None):
+def tet_gradient(n, eps_r, integrator, dt, nsteps, trace_grad, tf=1, dipoles=(), receivers=(), mu_r=None, sigma=None):
     """dJ/deps_r per tetrahedron by the FP64 discrete adjoint of tet_run
     (symplectic integrators, zero initial fields).  trace_grad: dJ/dtraces,
-    shaped like tet_run's traces (column 0, the time, is ignored)."""
+    shaped like tet_run's traces (column 0, the time, is ignored).  With
+    sigma given, returns (dJ/deps_r, dJ/dsigma)."""
     _, _, ntet = tet_sizes(n)
     nsamp = (nsteps - 1) // tf + 1 if nsteps > 0 else 0
     g = np.zeros((max(len(receivers), 1), max(nsamp, 1), 4))
     tg = np.asarray(trace_grad, np.float64)
     if len(receivers):
         g[:len(receivers), :nsamp] = tg.reshape(len(receivers), nsamp, 4)
-    c, keep = _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r)
+    c, keep = _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r, sigma)
     out = np.zeros(ntet)
-    rc = _tlib().orc_tet_gradient(C.byref(c), C.c_int(nsteps), _ptr(g), _ptr(out))
+    gs = np.zeros(ntet)
+    rc = _tlib().orc_tet_gradient(C.byref(c), C.c_int(nsteps), _ptr(g), _ptr(out), _ptr(gs))
     if rc != 0:
         raise RuntimeError(f"orc_tet_gradient failed: {rc}")
-    return out
+    return out if sigma is None else (out, gs)
+
+
+def tet_loss_rate(n, eps_r, sigma):
+    """Per-node loss rate rho_v of the conductivity model."""
+    nnode, _, _ = tet_sizes(n)
+    rho = np.zeros(nnode)
+    _tlib().orc_tet_loss_rate(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(np.ascontiguousarray(eps_r, np.float64)),
+                              _ptr(np.ascontiguousarray(sigma, np.float64)), _ptr(rho))
+    return rho
 
 
 def tet_mass_block(n, eps_r, v, t=-1):

@@ -461,6 +461,42 @@ double orc_stability_constant(int integrator)
     return lo;
 }
 
+/* Conductivity as a per-node loss rate: rho_v = sum sigma_T w / sum eps_T w
+ * over the incidences (T, l) of the node's live slots, w = |w_l|^2 integral
+ * (the weights of the mass block's alpha term), so that M_sigma,v =
+ * rho_v M_eps,v and the loss term M_sigma dU/dt of the momentum equation is
+ * rho_v P.  The symplectic loop applies its flow dP/dt = -rho P exactly,
+ * P *= exp(-rho dt/2), on each side of the middle kick of every step (a
+ * time-symmetric composition, second order when sigma != 0); leapfrog uses
+ * the centred difference of the loss term.  den (if given) gets the
+ * denominators.  New: the reference has no conductivity in its FEM. */
+static void loss_rate(const tetmesh *m, const double *eps_r, const double *sigma, double *rho, double *den)
+{
+    for (size_t v = 0; v < m->nnode; ++v) {
+        double num = 0.0, dd = 0.0;
+        for (int d = 0; d < 7; ++d) {
+            size_t e = 7 * v + d;
+            if (m->pec[e]) continue;
+            for (int s = m->inc_ptr[e]; s < m->inc_ptr[e + 1]; ++s) {
+                int t = m->inc[s] >> 3, l = m->inc[s] & 7, p = t % 6;
+                num += sigma[t] * m->shape_wsq[p][l];
+                dd += eps_r[t] * m->shape_wsq[p][l];
+            }
+        }
+        rho[v] = dd > 0.0 ? num / dd : 0.0;
+        if (den) den[v] = dd;
+    }
+}
+
+int orc_tet_loss_rate(int nx, int ny, int nz, const double *eps_r, const double *sigma, double *rho)
+{
+    tetmesh m;
+    build_tetmesh(&m, nx, ny, nz);
+    loss_rate(&m, eps_r, sigma, rho, NULL);
+    free_tetmesh(&m);
+    return 0;
+}
+
 /* Time loop.  U, P: nslot values (in/out).  traces: nrec * nsamp * 4
  * (t, Ex, Ey, Ez), sampled before the step every tf steps (symplectic) or
  * E^n at step n (leapfrog, which uses U as E^n and P as E^{n-1}). */
@@ -495,6 +531,11 @@ int orc_tet_run(const orc_tet_case *c, int nsteps, double *U, double *P, double 
     const int nsamp = nsteps > 0 ? (nsteps - 1) / tf + 1 : 0;
     double t = 0.0, dt = c->dt;
     const double x1 = 1.0 / (2.0 - pow(2.0, 1.0 / 3.0)), x2 = 1.0 - 2.0 * x1;
+    double *rho = NULL;
+    if (c->sigma) {
+        rho = malloc(sizeof(double) * m.nnode);
+        loss_rate(&m, c->eps_r, c->sigma, rho, NULL);
+    }
 
 #define ADD_SOURCE(vec, time, sign)                                                             \
     for (int s = 0; s < nd; ++s) {                                                              \
@@ -517,7 +558,12 @@ int orc_tet_run(const orc_tet_case *c, int nsteps, double *U, double *P, double 
             apply_minv(&m, minv, F, Y);
             for (size_t e = 0; e < m.nslot; ++e) {
                 double en = U[e];
-                U[e] = m.pec[e] ? 0.0 : 2.0 * en - P[e] - dt * dt * Y[e];
+                if (rho) {   /* (1 + r) E^{n+1} = 2 E^n - (1 - r) E^{n-1} - dt^2 Y,  r = rho dt / 2 */
+                    double r = 0.5 * rho[e / 7] * dt;
+                    U[e] = m.pec[e] ? 0.0 : (2.0 * en - (1.0 - r) * P[e] - dt * dt * Y[e]) / (1.0 + r);
+                } else {
+                    U[e] = m.pec[e] ? 0.0 : 2.0 * en - P[e] - dt * dt * Y[e];
+                }
                 P[e] = en;
             }
         } else {
@@ -530,10 +576,15 @@ int orc_tet_run(const orc_tet_case *c, int nsteps, double *U, double *P, double 
                 for (size_t e = 0; e < m.nslot; ++e) U[e] += 0.5 * a * Y[e];
                 apply_K_tet(&m, mu_inv, U, F, cb);
                 ADD_SOURCE(F, t + off[q] + 0.5 * a, -1.0)
+                const int damp = rho && q == nsub / 2;
+                if (damp)
+                    for (size_t e = 0; e < m.nslot; ++e) P[e] *= exp(-0.5 * dt * rho[e / 7]);
                 for (size_t e = 0; e < m.nslot; ++e) {
                     if (m.pec[e]) F[e] = 0.0;
                     P[e] -= a * F[e];
                 }
+                if (damp)
+                    for (size_t e = 0; e < m.nslot; ++e) P[e] *= exp(-0.5 * dt * rho[e / 7]);
                 apply_minv(&m, minv, P, Y);
                 for (size_t e = 0; e < m.nslot; ++e) U[e] += 0.5 * a * Y[e];
             }
@@ -541,7 +592,7 @@ int orc_tet_run(const orc_tet_case *c, int nsteps, double *U, double *P, double 
         t += dt;
     }
 #undef ADD_SOURCE
-    free(F); free(Y); free(cb); free(mu_inv); free(minv);
+    free(F); free(Y); free(cb); free(mu_inv); free(minv); free(rho);
     free(dw); free(de); free(rw); free(re);
     free_tetmesh(&m);
     return 0;
@@ -720,10 +771,16 @@ static void accumulate_outer(const tetmesh *m, double c, const double *y, const 
                 Q[49 * v + 7 * r + s] += 0.5 * c * (y[7 * v + r] * z[7 * v + s] + z[7 * v + r] * y[7 * v + s]);
 }
 
-/* dJ/deps for the symplectic integrators.  trace_grad: dJ/dtraces in the
- * layout of orc_tet_run's traces (nrec * nsamp * 4, column 0 ignored).  The
- * run starts from zero fields at t = 0. */
-int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad, double *grad_eps)
+/* dJ/deps (and dJ/dsigma when grad_sigma is given) for the symplectic
+ * integrators.  trace_grad: dJ/dtraces in the layout of orc_tet_run's traces
+ * (nrec * nsamp * 4, column 0 ignored).  The run starts from zero fields at
+ * t = 0.  With conductivity, each loss factor g_v = exp(-rho_v dt/2) acts
+ * twice per step (P_out = g P_in at the middle kick); the adjoint collects
+ * zr_v = sum Pbar_out,v . P_in,v, so dJ/drho_v = -(dt/2) g_v zr_v, and rho_v
+ * = sum sigma_T c_Tv / sum eps_T c_Tv (c_Tv the loss weights of T at v)
+ * gives dJ/dsigma_T = sum_v dJ/drho_v c_Tv / den_v and the extra
+ * dJ/deps_T = -sum_v dJ/drho_v rho_v c_Tv / den_v. */
+int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad, double *grad_eps, double *grad_sigma)
 {
     if (c->integrator == ORC_LEAPFROG) return -2;
     tetmesh m;
@@ -756,9 +813,21 @@ int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad
     int nsub = 1;
     if (c->integrator == ORC_SYMP4) { nsub = 3; sub[0] = x1 * dt; sub[1] = x2 * dt; sub[2] = x1 * dt; off[1] = x1 * dt; off[2] = (x1 + x2) * dt; }
 
-    /* forward: Pk[i] = P after kick i (i = 0 .. nsteps*nsub-1), Pk[-1] = 0 */
+    double *rho = NULL, *den = NULL, *gl = NULL;
+    if (c->sigma) {
+        rho = malloc(sizeof(double) * m.nnode);
+        den = malloc(sizeof(double) * m.nnode);
+        gl = malloc(sizeof(double) * m.nnode);
+        loss_rate(&m, c->eps_r, c->sigma, rho, den);
+        for (size_t v = 0; v < m.nnode; ++v) gl[v] = exp(-0.5 * dt * rho[v]);
+    }
+    const int qm = nsub / 2;
+
+    /* forward: Pk[i] = P after kick i (i = 0 .. nsteps*nsub-1), Pk[-1] = 0;
+     * Pmid[step] = P after the middle kick, before its second loss factor */
     const size_t nk = (size_t)nsteps * nsub;
     double *Pstore = calloc((nk + 1) * ns, sizeof(double));
+    double *Pmid = rho ? calloc((size_t)(nsteps > 0 ? nsteps : 1) * ns, sizeof(double)) : NULL;
     double *U = calloc(ns, sizeof(double)), *P = calloc(ns, sizeof(double));
     double *F = calloc(ns, sizeof(double)), *Y = calloc(ns, sizeof(double)), *Z = calloc(ns, sizeof(double));
     double *cb = malloc(sizeof(double) * 3 * m.ntet);
@@ -773,9 +842,16 @@ int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad
                 double g = orc_tet_wave(c->dip_kind[s], c->dip_f0[s], t + off[q] + 0.5 * a);
                 for (int l = 0; l < 6; ++l) F[de[s][l]] -= dw[s][l] * g;
             }
+            const int damp = rho && q == qm;
+            if (damp)
+                for (size_t e = 0; e < ns; ++e) P[e] *= gl[e / 7];
             for (size_t e = 0; e < ns; ++e) {
                 if (m.pec[e]) F[e] = 0.0;
                 P[e] -= a * F[e];
+            }
+            if (damp) {
+                memcpy(Pmid + (size_t)step * ns, P, sizeof(double) * ns);
+                for (size_t e = 0; e < ns; ++e) P[e] *= gl[e / 7];
             }
             memcpy(Pstore + (1 + (size_t)step * nsub + q) * ns, P, sizeof(double) * ns);
             apply_minv(&m, minv, P, Y);
@@ -786,6 +862,7 @@ int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad
     /* reverse */
     double *Ub = calloc(ns, sizeof(double)), *Pb = calloc(ns, sizeof(double));
     double *Q = calloc(49 * m.nnode, sizeof(double));
+    double *zr = calloc(m.nnode, sizeof(double));
     for (int step = nsteps - 1; step >= 0; --step) {
         for (int q = nsub - 1; q >= 0; --q) {
             double a = sub[q];
@@ -795,10 +872,21 @@ int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad
             for (size_t e = 0; e < ns; ++e) Pb[e] += 0.5 * a * Y[e];
             apply_minv(&m, minv, Pstore + (1 + i) * ns, Z);
             accumulate_outer(&m, 0.5 * a, Y, Z, Q);
+            const int damp = rho && q == qm;
+            if (damp)   /* second loss factor: P = g Pmid */
+                for (size_t e = 0; e < ns; ++e) {
+                    zr[e / 7] += Pb[e] * Pmid[(size_t)step * ns + e];
+                    Pb[e] *= gl[e / 7];
+                }
             /* kick: P -= a Pi K U  =>  Ubar -= a K Pi Pbar */
             for (size_t e = 0; e < ns; ++e) Y[e] = m.pec[e] ? 0.0 : Pb[e];
             apply_K_tet(&m, mu_inv, Y, F, cb);
             for (size_t e = 0; e < ns; ++e) Ub[e] -= a * F[e];
+            if (damp)   /* first loss factor: P = g P_before */
+                for (size_t e = 0; e < ns; ++e) {
+                    zr[e / 7] += Pb[e] * Pstore[i * ns + e];
+                    Pb[e] *= gl[e / 7];
+                }
             /* first half drift, with P before kick i */
             apply_minv(&m, minv, Ub, Y);
             for (size_t e = 0; e < ns; ++e) Pb[e] += 0.5 * a * Y[e];
@@ -838,7 +926,25 @@ int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad
             }
         }
     }
+    /* loss-rate terms */
+    if (grad_sigma) memset(grad_sigma, 0, sizeof(double) * m.ntet);
+    if (rho)
+        for (size_t v = 0; v < m.nnode; ++v) {
+            if (den[v] <= 0.0) continue;
+            const double gr = -0.5 * dt * gl[v] * zr[v];   /* dJ/drho_v */
+            for (int d = 0; d < 7; ++d) {
+                size_t e = 7 * v + d;
+                if (m.pec[e]) continue;
+                for (int s = m.inc_ptr[e]; s < m.inc_ptr[e + 1]; ++s) {
+                    int tt = m.inc[s] >> 3, l = m.inc[s] & 7, p = tt % 6;
+                    const double w = m.shape_wsq[p][l] / den[v];
+                    if (grad_sigma) grad_sigma[tt] += gr * w;
+                    grad_eps[tt] -= gr * rho[v] * w;
+                }
+            }
+        }
     free(Pstore); free(U); free(P); free(F); free(Y); free(Z); free(cb); free(Ub); free(Pb); free(Q);
+    free(zr); free(Pmid); free(rho); free(den); free(gl);
     free(mu_inv); free(minv); free(dw); free(de); free(rw); free(re);
     free_tetmesh(&m);
     return 0;
