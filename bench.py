@@ -11,7 +11,9 @@ receivers, FP32 fields.  Metric: DOF-updates/s (edges x time steps / time).
           inputs resident, L2 flushed between solves.
 `e2e`     the same solve through the C ABI from host buffers: material upload,
           FP64 mass-block setup and stability limit, time loop, trace download.
-`roofline` the dominant kernel (tet_kick_kernel) timed alone on the same state.
+`roofline` the dominant kernel (tet_step_kernel, the fused kick + drift of one
+          substep) timed alone on the same state, alternating the two U
+          buffers as the time loop does.
 `cpu_baseline` the FP64 oracle on the host cores over a bounded sample.
 A secondary object `fdtd_512` times the 512^3 FP32 Yee update with a 10-cell
 CPML (HBM-bound) for a bounded number of steps; `batch64` times 64 batched
@@ -164,13 +166,15 @@ def fdtd_512(steps=60, n=512):
     for q in range(4):
         c = rng.integers(20, n - 20, 3)
         s.setSource_z(tuple(int(v) for v in c), waveform=ems.WAVE_RICKER, f0=float(rng.uniform(5e9, 15e9)))
-    s.run(2)
+    s.run(24)          # warm-up; the handle's first run of >= 24 steps picks the launch shape
     s.run(steps)
     ms, launches = s.run_stats()
     kms, kbytes, kname = s.time_dominant_kernel(10)
+    shape = s.launch_shape()
     cells = n ** 3
     s.close()
     return {"workload": f"fdtd{n}_fp32_cpml10", "steps": steps, "ms_per_step": ms / steps,
+            "launch_shape": list(shape[:2]),
             "cell_updates_per_s": cells * steps / (ms * 1e-3),
             "dof_updates_per_s": 6 * cells * steps / (ms * 1e-3),
             "kernel": kname, "kernel_ms": kms, "kernel_bytes": kbytes, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
@@ -201,6 +205,7 @@ def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
     b.run(steps)
     ms_batch, launches = b.run_stats()
     kms, kbytes, kname = b.time_dominant_kernel(20)
+    block = b.launch_shape()[0]
     edges = sum(n_edges(int(n)) for n in sides)
     b.close()
     per = {ems.FP64: [], ems.FP32: []}
@@ -225,7 +230,7 @@ def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
             "shots_per_s_fp32_per_shot": shots_fp32, "speedup_vs_fp64_per_shot": shots_batch / shots_fp64,
             "dof_updates_per_s": edges * steps / (ms_batch * 1e-3),
             "per_shot_sample": f"{len(pick)} shots x {sample_steps} steps, scaled to {steps}",
-            "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
+            "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9, "threads_per_block": block}
 
 
 def hex72(steps=200, order=2, sample_steps=10):
@@ -436,6 +441,7 @@ def run_gpu(args):
     e2e = world * dofs * STEPS_PER_SOLVE * args.steps / (np.sum(e2e_ms) * 1e-3)
     # ---- dominant kernel roofline
     kms, kbytes, kname = sim.time_dominant_kernel(200)
+    block = sim.launch_shape()[0]
     peak, peak_kind = peaks()
     achieved = kbytes / (kms * 1e-3) / 1e9
     out = {
@@ -454,7 +460,7 @@ def run_gpu(args):
                      # profiles/tet_kick_tet32_symp4.md (cold fill: the 17 MB
                      # working set is L2-resident in the timed loop)
                      "traffic": 15486208, "kernel": kname, "kernel_us": kms * 1e3, "bytes_per_launch": kbytes,
-                     "peak_source": peak_kind},
+                     "threads_per_block": block, "peak_source": peak_kind},
         "clocks": clk,
         "wall_s": wall,
     }

@@ -88,9 +88,11 @@ def lib():
         "ems_tetfem_time_step": (C.c_int, [vp, dp, dp]),
         "ems_tetfem_apply_stiffness": (C.c_int, [vp, dp, dp, C.c_size_t]),
         "ems_tetfem_set_checkpoints": (C.c_int, [vp, C.c_int]),
-        "ems_tetfem_backward": (C.c_int, [vp, dp, C.c_size_t, dp, C.c_size_t]),
+        "ems_tetfem_backward": (C.c_int, [vp, dp, C.c_size_t, dp, dp, C.c_size_t]),
+        "ems_tetfem_energy": (C.c_int, [vp, dp, C.c_int]),
+
         "ems_trace_misfit": (C.c_int, [C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp]),
-        "ems_tetfem_gradient": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, C.c_size_t]),
+        "ems_tetfem_gradient": (C.c_int, [vp, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, C.c_size_t]),
         "ems_tet_stiffness_apply_static": (C.c_int, [ip, vp, vp, vp]),
         "ems_run": (C.c_int, [vp, C.c_int]),
         "ems_trace_shape": (C.c_int, [vp, ip, ip, ip]),
@@ -102,6 +104,7 @@ def lib():
         "ems_set_field": (C.c_int, [vp, C.c_int, dp, C.c_size_t]),
         "ems_last_run_stats": (C.c_int, [vp, dp, C.POINTER(C.c_longlong)]),
         "ems_time_dominant_kernel": (C.c_int, [vp, C.c_int, dp, dp, C.c_char_p, C.c_size_t]),
+        "ems_launch_shape": (C.c_int, [vp, C.POINTER(C.c_int)]),
         "ems_reset": (C.c_int, [vp]),
         "ems_destroy": (C.c_int, [vp]),
     }

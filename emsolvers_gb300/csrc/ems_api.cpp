@@ -202,16 +202,21 @@ int ems_tetfem_set_checkpoints(ems_sim *s, int nsnap)
     NEED(s, ems::Kind::TETFEM);
     return guard(s, [&] { ems::tetfem_set_checkpoints(s->impl, nsnap); });
 }
-int ems_tetfem_backward(ems_sim *s, const double *tg, size_t n, double *grad, size_t ntet)
+int ems_tetfem_energy(ems_sim *s, double *energy, int nshots)
 {
     NEED(s, ems::Kind::TETFEM);
-    return guard(s, [&] { ems::tetfem_backward(s->impl, tg, n, grad, ntet); });
+    return guard(s, [&] { ems::tetfem_energy(s->impl, energy, nshots); });
+}
+int ems_tetfem_backward(ems_sim *s, const double *tg, size_t n, double *grad, double *grad_sigma, size_t ntet)
+{
+    NEED(s, ems::Kind::TETFEM);
+    return guard(s, [&] { ems::tetfem_backward(s->impl, tg, n, grad, grad_sigma, ntet); });
 }
 int ems_tetfem_gradient(ems_sim *s, int nsteps, int nsnap, int kind, const double *obs, const double *band, double *misfit,
-                        double *grad, size_t ntet)
+                        double *grad, double *grad_sigma, size_t ntet)
 {
     NEED(s, ems::Kind::TETFEM);
-    return guard(s, [&] { ems::tetfem_gradient(s->impl, nsteps, nsnap, kind, obs, band, misfit, grad, ntet); });
+    return guard(s, [&] { ems::tetfem_gradient(s->impl, nsteps, nsnap, kind, obs, band, misfit, grad, grad_sigma, ntet); });
 }
 int ems_trace_misfit(int kind, int nobs, int nsamp, const double *tr, const double *obs, const double *band, double *misfit,
                      double *tg)
@@ -290,6 +295,11 @@ int ems_time_dominant_kernel(ems_sim *s, int launches, double *ms, double *bytes
             name[cap - 1] = 0;
         }
     });
+}
+int ems_launch_shape(ems_sim *s, int block[3])
+{
+    if (!s || !block) return EMS_ERR_INVALID_ARGUMENT;
+    return guard(s, [&] { s->impl->launch_shape(block); });
 }
 int ems_reset(ems_sim *s)
 {

@@ -69,6 +69,9 @@ struct Sim {
     virtual void save(const char *path) const = 0;
     virtual void time_dominant(int launches, double *ms, double *bytes, std::string *name) = 0;
     virtual void reset() = 0;
+    // Threads per block (x, y, z) of the solver's main kernels as its
+    // autotuner chose them; zeros where a solver has fixed shapes.
+    virtual void launch_shape(int b[3]) { b[0] = b[1] = b[2] = 0; }
     // Time [s] of sample j of the last run (FEM tables carry it in column 0).
     virtual double sample_time(int j) const { return traces[(size_t)j * ncols]; }
     // One receiver component as the `t,u` CSV that
@@ -106,9 +109,10 @@ void tetfem_add_receiver(Sim *s, const double pos[3]);
 void tetfem_time_step(const Sim *s, double *dt, double *lim);
 void tetfem_apply_stiffness(Sim *s, const double *u, double *f, size_t n);
 void tetfem_set_checkpoints(Sim *s, int nsnap);
-void tetfem_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, size_t ngrad);
+void tetfem_energy(Sim *s, double *out, int n);
+void tetfem_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, double *grad_sigma, size_t ngrad);
 void tetfem_gradient(Sim *s, int nsteps, int nsnap, int kind, const double *observed, const double *tf_band, double *misfit,
-                     double *grad_eps, size_t ngrad);
+                     double *grad_eps, double *grad_sigma, size_t ngrad);
 void trace_misfit(int kind, int nobs, int nsamp, const double *traces, const double *observed, double *misfit,
                   double *trace_grad, const double *tf_band);
 

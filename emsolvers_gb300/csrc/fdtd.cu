@@ -11,6 +11,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -429,8 +431,35 @@ struct FdtdSim : Sim {
         return a;
     }
 
-    dim3 block() const { return dim3(32, 8, 1); }
-    dim3 grid() const { return dim3((nx + 1 + 31) / 32, (ny + 1 + 7) / 8, nz + 1); }
+    // Launch shape of the H and E kernels (x, y threads; one z plane per
+    // block row), chosen by tune_shape on the handle's first run of at least
+    // kTuneMinSteps steps.  Every cell is one thread whatever the shape, so
+    // the shape changes no result.
+    dim3 blk{32, 8, 1};
+    bool tuned = false;
+    dim3 block() const { return blk; }
+    void launch_shape(int b[3]) override { b[0] = (int)blk.x; b[1] = (int)blk.y; b[2] = 1; }
+    dim3 grid() const { return dim3((nx + 1 + blk.x - 1) / blk.x, (ny + 1 + blk.y - 1) / blk.y, nz + 1); }
+
+    static constexpr int kShapes = 6, kTuneSteps = 3, kTuneMinSteps = 24;
+    static constexpr unsigned kShape[kShapes][2] = {{32, 8}, {32, 4}, {64, 4}, {128, 2}, {256, 1}, {64, 2}};
+
+    // Steps of this run spent tuning: the environment variable
+    // EMS_FDTD_BLOCK="XxY" forces one of the shapes; otherwise the first run
+    // of at least kTuneMinSteps steps advances kTuneSteps steps with each
+    // shape (one warm-up, two timed) and keeps the fastest.
+    int tune_steps(int nsteps)
+    {
+        if (tuned) return 0;
+        if (const char *env = std::getenv("EMS_FDTD_BLOCK")) {
+            unsigned x = 0, y = 0;
+            if (std::sscanf(env, "%ux%u", &x, &y) == 2)
+                for (auto &sh : kShape)
+                    if (sh[0] == x && sh[1] == y) { blk = dim3(x, y, 1); tuned = true; return 0; }
+            throw Error{EMS_ERR_INVALID_ARGUMENT, "EMS_FDTD_BLOCK must be one of 32x8 32x4 64x4 128x2 256x1 64x2"};
+        }
+        return nsteps >= kTuneMinSteps ? kShapes * kTuneSteps : 0;
+    }
 
     template <class T> void launch_h(const FdtdArgs<T> &a)
     {
@@ -504,8 +533,24 @@ struct FdtdSim : Sim {
 
         FdtdArgs<T> a = args<T>();
         long long launches = 0;
+        const int tune = tune_steps(nsteps);
+        struct TuneEvents {   // destroyed on every exit path
+            cudaEvent_t e[2 * kShapes] = {};
+            ~TuneEvents()
+            {
+                for (cudaEvent_t x : e)
+                    if (x) cudaEventDestroy(x);
+            }
+        } tev;
+        if (tune)
+            for (cudaEvent_t &x : tev.e) EMS_CUDA(cudaEventCreate(&x));
         EMS_CUDA(cudaEventRecord(ev0, stream));
         for (int step = 1; step < nsteps + 1; ++step) {
+            const int ts = step - 1, c = ts / kTuneSteps, r = ts % kTuneSteps;
+            if (ts < tune) {
+                blk = dim3(kShape[c][0], kShape[c][1], 1);
+                if (r == 1) EMS_CUDA(cudaEventRecord(tev.e[2 * c], stream));
+            }
             launch_h<T>(a);
             launch_e<T>(a);
             launches += 2;
@@ -519,6 +564,19 @@ struct FdtdSim : Sim {
                     a.Ex, a.Ey, a.Ez, nobs, d_obs_cnt.as<int>(), d_obs_start.as<int>(), d_obs_off.as<size_t>(),
                     d_traces.as<double>() + (size_t)(step / tf) * 3, nsamp);
                 ++launches;
+            }
+            if (ts < tune && r == kTuneSteps - 1) EMS_CUDA(cudaEventRecord(tev.e[2 * c + 1], stream));
+            if (tune && step == tune) {   // all shapes timed: keep the fastest
+                EMS_CUDA(cudaEventSynchronize(tev.e[2 * kShapes - 1]));
+                float best = 0.0f;
+                int pick = 0;
+                for (int k = 0; k < kShapes; ++k) {
+                    float ms = 0.0f;
+                    EMS_CUDA(cudaEventElapsedTime(&ms, tev.e[2 * k], tev.e[2 * k + 1]));
+                    if (k == 0 || ms < best) { best = ms; pick = k; }
+                }
+                blk = dim3(kShape[pick][0], kShape[pick][1], 1);
+                tuned = true;
             }
         }
         EMS_CUDA(cudaGetLastError());

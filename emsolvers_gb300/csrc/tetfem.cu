@@ -8,23 +8,25 @@
 //   DOF layout   edge slot 7*node + d, d over the 7 edge directions leaving a
 //                node; node-major, so the 7 edges of a node are contiguous.
 //   K apply      tet_curl_kernel: per tetrahedron, B_T = |T|/mu_T curl(E|_T)
-//                (3 values); tet_kick_kernel: per edge slot, the curl-
-//                transpose gathered over the slot's edge->element incidence
-//                list (deterministic, no atomics).
+//                (3 values); tet_node_kernel: one thread per node gathers
+//                the curl-transpose of its 7 slots from the node's 18
+//                incident tetrahedra (each B read once per node, in
+//                ascending tetrahedron order: deterministic, no atomics).
 //   mass inverse per-node 7x7 blocks, built and inverted in FP64 on the GPU
 //                (tet_minv_setup_kernel), stored packed symmetric in the run
-//                precision; applied inside the kick kernel by eight lanes per
-//                node exchanging values with warp shuffles.
+//                precision; applied inside tet_node_kernel from registers.
 //   adjoint      the same kernels run the reversed steps (see "adjoint").
 // Units are normalised (cube edge 1, c0 = 1); the API converts.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iomanip>
 #include <unordered_map>
+#include <utility>
 
 #include "ems_internal.hpp"
 
@@ -38,6 +40,7 @@ const int kDir[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0}, {1, 0, 1}, {
 // Per-slot flag byte: the slot is PEC or unused (no DOF), or it carries a
 // dipole load (only those slots search the source list).
 constexpr unsigned char kPecBit = 1, kSrcBit = 2;
+constexpr double kEps0 = 8.8541878128e-12;   // vacuum permittivity, F/m
 
 struct Shape {
     double grad[4][3];
@@ -235,85 +238,11 @@ template <class T> struct alignas(4 * sizeof(T)) vec4 {
     T x, y, z, w;
 };
 
-__constant__ vec4<float> c_curl4_f[36];    // curl(w_l) of tetrahedron type p at [6p + l]
-__constant__ vec4<double> c_curl4_d[36];
-
-template <class T> __device__ __forceinline__ const vec4<T> *curl4_table();
-template <> __device__ __forceinline__ const vec4<float> *curl4_table<float>() { return c_curl4_f; }
-template <> __device__ __forceinline__ const vec4<double> *curl4_table<double>() { return c_curl4_d; }
-
-// The 36 curl vectors in shared memory: the lanes of a warp index them with
-// different (type, edge) pairs, which constant memory would serialise.
-template <class T> __device__ __forceinline__ void load_curl_table(vec4<T> *sc)
-{
-    if (threadIdx.x < 36) sc[threadIdx.x] = curl4_table<T>()[threadIdx.x];
-    __syncthreads();
-}
-
 // packed upper-triangle index of (r, c) in a symmetric 7x7 block
 __device__ __forceinline__ int pk7(int r, int c)
 {
     int a = r < c ? r : c, b = r < c ? c : r;
     return a * (13 - a) / 2 + b;
-}
-
-// B_T = |T|/mu_T * sum_l U_l curl(w_l)   (|T| = 1/6 on the unit cube)
-template <class T>
-__global__ void __launch_bounds__(256) tet_curl_kernel(size_t ntet, const int *__restrict__ tet_edge, const T *__restrict__ U,
-                                                       const T *__restrict__ mu_inv, vec4<T> *__restrict__ B)
-{
-    __shared__ vec4<T> sc[36];
-    load_curl_table<T>(sc);
-    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntet) return;
-    const int p = (int)(t % 6);
-    const int2 *e2 = reinterpret_cast<const int2 *>(tet_edge + 6 * t);
-    const int2 a = e2[0], b = e2[1], c = e2[2];
-    const int e[6] = {a.x, a.y, b.x, b.y, c.x, c.y};
-    T c0 = 0, c1 = 0, c2 = 0;
-#pragma unroll
-    for (int l = 0; l < 6; ++l) {
-        T u = U[e[l]];
-        vec4<T> cr = sc[6 * p + l];
-        c0 = fma(u, cr.x, c0);
-        c1 = fma(u, cr.y, c1);
-        c2 = fma(u, cr.z, c2);
-    }
-    T s = T(1.0 / 6.0);
-    if (mu_inv) s *= mu_inv[t];
-    vec4<T> o;
-    o.x = s * c0; o.y = s * c1; o.z = s * c2; o.w = T(0);
-    B[t] = o;
-}
-
-// Curl-transpose gathered for slot e over its incidences: F_e = sum_T
-// B_T . curl(w_l), in ascending tetrahedron order (deterministic, no
-// atomics).  The incidences come from a fixed-width table of six entries per
-// slot (t*8 + l, -1 after the last; the Kuhn mesh has at most six
-// tetrahedra on an edge) read with three 8-byte loads, and the B loads of
-// all incident tetrahedra are issued before the sum.
-template <class T>
-__device__ __forceinline__ T gather_force6(size_t e, const int *__restrict__ inc6, const vec4<T> *__restrict__ B,
-                                           const vec4<T> *sc)
-{
-    const int2 *p2 = reinterpret_cast<const int2 *>(inc6 + 6 * e);
-    const int2 c01 = __ldg(p2), c23 = __ldg(p2 + 1), c45 = __ldg(p2 + 2);
-    const int code[6] = {c01.x, c01.y, c23.x, c23.y, c45.x, c45.y};
-    vec4<T> b[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k)
-        if (code[k] >= 0) b[k] = B[code[k] >> 3];
-    T f = 0;
-#pragma unroll
-    for (int k = 0; k < 6; ++k)
-        if (code[k] >= 0) {
-            const int t = code[k] >> 3, l = code[k] & 7;
-            const vec4<T> cr = sc[6 * (t % 6) + l];
-            f = fma(b[k].x, cr.x, f);
-            f = fma(b[k].y, cr.y, f);
-            f = fma(b[k].z, cr.z, f);
-        }
-    return f;
 }
 
 // (Minv_v x)_d with x_j held by lane j of the node's 8-lane group.
@@ -326,16 +255,6 @@ __device__ __forceinline__ T block_apply(const T *__restrict__ mv, int d, T x)
         T xj = __shfl_sync(0xffffffffu, x, j, 8);
         if (d < 7) y = fma(mv[pk7(d, j)], xj, y);
     }
-    return y;
-}
-
-// block_apply with the lane's mass-block row already in registers.
-template <class T>
-__device__ __forceinline__ T block_apply_row(const T (&row)[7], T x)
-{
-    T y = 0;
-#pragma unroll
-    for (int j = 0; j < 7; ++j) y = fma(row[j], __shfl_sync(0xffffffffu, x, j, 8), y);
     return y;
 }
 
@@ -442,62 +361,207 @@ constexpr NodeTab make_node_tab()
     return t;
 }
 
-// MODE 0 (symplectic): P_e -= a (F_e - f_e) on non-PEC slots, then
-// Uout = Uin + c Minv P (zout = Minv P); with minv == nullptr only P is
-// written (the stiffness apply).  MODE 1 (leapfrog): Uout = 2 Uin - Uold -
-// c Minv (F - f), PEC slots zero.  ntets: the 18 tetrahedron indices of each
-// node in table order, -1 where the cell is outside the mesh.
-template <class T, int MODE>
-__global__ void __launch_bounds__(128) tet_node_kernel(size_t nnode, const int *__restrict__ ntets,
-                                                       const unsigned char *__restrict__ pec, const vec4<T> *__restrict__ B,
-                                                       const T *__restrict__ minv, T *__restrict__ P, const T *Uin, T *Uout,
-                                                       const T *__restrict__ Uold, T a, T c, SrcArgs src,
-                                                       T *__restrict__ zout)
+// ------------------------------------------------------ fused step
+// The fused step recomputes the curls of a node's 18 tetrahedra from U
+// instead of reading them from a per-tetrahedron array.  Their 6 x 18 edges
+// are 43 distinct slots whose tails are 13 nodes at offsets in {-1,0,1}^3;
+// each thread loads those 43 values once (neighbouring threads share them
+// through L1/L2), so per node only U, P, the mass block, the flags and an
+// 8-byte record leave DRAM.  Mask bits of a node: 1 i > 0, 2 i < nx, 4 j > 0,
+// 8 j < ny, 16 k > 0, 32 k < nz; a tail node exists when the bits of its
+// offset are set, a tetrahedron when the bits of its cell are.
+struct StepTab {
+    NodeTab n;
+    int ntail, tail[13][3], treq[13];
+    int nedge, etail[43], edir[43];
+    int eidx[18][6];   // distinct-edge index of local edge l of entry q
+    int qreq[18];      // mask bits the cell of entry q needs
+    int own[7];        // distinct-edge index of the node's own slot d
+};
+
+constexpr int offset_bits(int x, int y, int z)
 {
-    constexpr NodeTab tab = make_node_tab();
+    return (x < 0 ? 1 : 0) | (x > 0 ? 2 : 0) | (y < 0 ? 4 : 0) | (y > 0 ? 8 : 0) | (z < 0 ? 16 : 0) | (z > 0 ? 32 : 0);
+}
+
+constexpr StepTab make_step_tab()
+{
+    StepTab s{};
+    s.n = make_node_tab();
+    const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+    const int loc[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+    const int dirs[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+    int vert[6][4][3] = {};
+    for (int p = 0; p < 6; ++p) {
+        const int a = perm[p][0], b = perm[p][1];
+        vert[p][1][a] = 1;
+        vert[p][2][a] = 1; vert[p][2][b] = 1;
+        vert[p][3][0] = vert[p][3][1] = vert[p][3][2] = 1;
+    }
+    // edge (tail offset, direction) of every local edge, and the tails in
+    // ascending node order (z, y, x)
+    int et[18][6][3] = {}, ed[18][6] = {};
+    for (int q = 0; q < 18; ++q) {
+        const int p = s.n.p[q];
+        for (int l = 0; l < 6; ++l) {
+            const int *vm = vert[p][loc[l][0]], *vn = vert[p][loc[l][1]];
+            for (int x = 0; x < 3; ++x) et[q][l][x] = s.n.o[q][x] + vm[x];
+            for (int c = 0; c < 7; ++c)
+                if (dirs[c][0] == vn[0] - vm[0] && dirs[c][1] == vn[1] - vm[1] && dirs[c][2] == vn[2] - vm[2]) ed[q][l] = c;
+        }
+    }
+    for (int z = -1; z <= 1; ++z)
+        for (int y = -1; y <= 1; ++y)
+            for (int x = -1; x <= 1; ++x) {
+                bool used = false;
+                for (int q = 0; q < 18; ++q)
+                    for (int l = 0; l < 6; ++l)
+                        if (et[q][l][0] == x && et[q][l][1] == y && et[q][l][2] == z) used = true;
+                if (!used) continue;
+                s.tail[s.ntail][0] = x; s.tail[s.ntail][1] = y; s.tail[s.ntail][2] = z;
+                s.treq[s.ntail] = offset_bits(x, y, z);
+                ++s.ntail;
+            }
+    for (int t = 0; t < s.ntail; ++t)
+        for (int c = 0; c < 7; ++c) {
+            bool used = false;
+            for (int q = 0; q < 18; ++q)
+                for (int l = 0; l < 6; ++l)
+                    if (ed[q][l] == c && et[q][l][0] == s.tail[t][0] && et[q][l][1] == s.tail[t][1] && et[q][l][2] == s.tail[t][2])
+                        used = true;
+            if (!used) continue;
+            s.etail[s.nedge] = t;
+            s.edir[s.nedge] = c;
+            if (s.tail[t][0] == 0 && s.tail[t][1] == 0 && s.tail[t][2] == 0) s.own[c] = s.nedge;
+            ++s.nedge;
+        }
+    for (int q = 0; q < 18; ++q) {
+        s.qreq[q] = (s.n.o[q][0] < 0 ? 1 : 2) | (s.n.o[q][1] < 0 ? 4 : 8) | (s.n.o[q][2] < 0 ? 16 : 32);
+        for (int l = 0; l < 6; ++l)
+            for (int k = 0; k < s.nedge; ++k) {
+                const int t = s.etail[k];
+                if (s.edir[k] == ed[q][l] && s.tail[t][0] == et[q][l][0] && s.tail[t][1] == et[q][l][1] &&
+                    s.tail[t][2] == et[q][l][2])
+                    s.eidx[q][l] = k;
+            }
+    }
+    return s;
+}
+
+// Table sizes the kernel relies on (every slot of the node is an edge of
+// one of its tetrahedra, so own[] is complete).
+static_assert(make_step_tab().ntail == 13 && make_step_tab().nedge == 43, "Kuhn split: 13 tails, 43 edges per node");
+
+// Contribution of entry Q of the node table (a template parameter, so every
+// table index below is a compile-time constant and ue, f stay in
+// registers): the curl of the tetrahedron from the edge values ue, B =
+// curl / 6, and B . curl(w_l) added to the node's slots it feeds.  Zero curl
+// entries are left out.
+template <class T, int Q>
+__device__ __forceinline__ void step_tet(const T (&ue)[43], T (&f)[7], int have)
+{
+    constexpr StepTab tab = make_step_tab();
+    constexpr int p = tab.n.p[Q];
+    if ((tab.qreq[Q] & ~have) != 0) return;   // cell outside the mesh
+    T c0 = 0, c1 = 0, c2 = 0;
+#pragma unroll
+    for (int l = 0; l < 6; ++l) {
+        const T u = ue[tab.eidx[Q][l]];
+        if (tab.n.curl[p][l][0] != 0) c0 = fma(u, (T)tab.n.curl[p][l][0], c0);
+        if (tab.n.curl[p][l][1] != 0) c1 = fma(u, (T)tab.n.curl[p][l][1], c1);
+        if (tab.n.curl[p][l][2] != 0) c2 = fma(u, (T)tab.n.curl[p][l][2], c2);
+    }
+    const T s6 = T(1.0 / 6.0);
+    const T bx = s6 * c0, by = s6 * c1, bz = s6 * c2;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        if (k < tab.n.ne[Q]) {
+            const int d = tab.n.d[Q][k], l = tab.n.l[Q][k];
+            if (tab.n.curl[p][l][0] != 0) f[d] = fma(bx, (T)tab.n.curl[p][l][0], f[d]);
+            if (tab.n.curl[p][l][1] != 0) f[d] = fma(by, (T)tab.n.curl[p][l][1], f[d]);
+            if (tab.n.curl[p][l][2] != 0) f[d] = fma(bz, (T)tab.n.curl[p][l][2], f[d]);
+        }
+}
+
+// All 18 entries in table order (ascending tetrahedron index).
+template <class T, int... Q>
+__device__ __forceinline__ void step_tets(const T (&ue)[43], T (&f)[7], int have, std::integer_sequence<int, Q...>)
+{
+    (step_tet<T, Q>(ue, f, have), ...);
+}
+
+// Node record of the fused step: x = y-stride | mask << 26, y = z-stride (in
+// nodes, within the node's shot).
+__host__ __device__ constexpr int step_record_x(int sy, int mask) { return sy | (mask << 26); }
+
+// One fused substep per node: F = K Uin gathered from the curls of its 18
+// tetrahedra recomputed from Uin (curl terms over local edges 0..5, B =
+// curl / 6, entries in ascending tetrahedron order, zero curl entries left
+// out), then MODE 0 (symplectic) P -= a (F - f) on non-PEC slots and Uout =
+// Uin + c Minv P (zout = Minv P; with minv == nullptr only P is written), or
+// MODE 1 (leapfrog) Uout = 2 Uin - Uold - c Minv (F - f), PEC slots zero.
+// Uout must not alias Uin: other threads read Uin around their node.
+// Losses (damp per node): DAMP 1 with MODE 0 is the middle kick of a lossy
+// step, P = g (g P - a (F - f)) with g = exp(-rho dt/2) (ppre, pmid, when
+// given, keep P before the first factor and after the kick); DAMP 2 with
+// MODE 0 is its adjoint, Uout = g Uin + c Minv P; DAMP 1 with MODE 1 is the
+// lossy leapfrog, Uout = (2 Uin - (1 - r) Uold - c Minv (F - f)) / (1 + r)
+// with r = rho dt / 2.
+// Threads per block of the fused step: chosen per handle by timing these
+// candidates on the handle's own mesh (TetFemSim::tune_step_block); small
+// meshes (a 32^3 mesh has 36k nodes) spread better over the 152 SMs in
+// small blocks.  The block size changes no arithmetic.
+constexpr int kStepBlocks[4] = {32, 64, 128, 256};
+constexpr int kStepBlockMax = 256;
+
+template <class T, int MODE, int DAMP>
+__global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, const int2 *__restrict__ nrec,
+                                                       const unsigned char *__restrict__ pec, const T *__restrict__ minv,
+                                                       T *__restrict__ P, const T *__restrict__ Uin, T *__restrict__ Uout,
+                                                       const T *__restrict__ Uold, T a, T c, SrcArgs src, T *__restrict__ zout,
+                                                       const T *__restrict__ damp, T *__restrict__ ppre, T *__restrict__ pmid)
+{
+    constexpr StepTab tab = make_step_tab();
     const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nnode) return;
-    const int2 *l2 = reinterpret_cast<const int2 *>(ntets + 18 * v);
-    int code[18];
+    const int2 r = __ldg(nrec + v);
+    const int have = (int)((unsigned)r.x >> 26), sy = r.x & 0x3ffffff, sz = r.y;
+    const T *u0 = Uin + 7 * v;
+    // a missing tail node only feeds missing tetrahedra: read the node's own
+    // slots instead (in bounds) and let the cell test drop them
+    int off[13];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        const int2 x = __ldg(l2 + q);
-        code[2 * q] = x.x;
-        code[2 * q + 1] = x.y;
-    }
+    for (int t = 0; t < 13; ++t)
+        off[t] = (tab.treq[t] & ~have) == 0 ? 7 * (tab.tail[t][0] + tab.tail[t][1] * sy + tab.tail[t][2] * sz) : 0;
+    T ue[43];
+#pragma unroll
+    for (int k = 0; k < 43; ++k) ue[k] = u0[off[tab.etail[k]] + tab.edir[k]];
     T f[7] = {0, 0, 0, 0, 0, 0, 0};
-#pragma unroll
-    for (int q = 0; q < 18; ++q)
-        if (code[q] >= 0) {
-            const vec4<T> b = B[code[q]];
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-                if (k < tab.ne[q]) {
-                    const int d = tab.d[q][k], l = tab.l[q][k], p = tab.p[q];
-                    f[d] = fma(b.x, (T)tab.curl[p][l][0], f[d]);
-                    f[d] = fma(b.y, (T)tab.curl[p][l][1], f[d]);
-                    f[d] = fma(b.z, (T)tab.curl[p][l][2], f[d]);
-                }
-        }
+    step_tets<T>(ue, f, have, std::make_integer_sequence<int, 18>{});
     const size_t e0 = 7 * v;
     unsigned char m[7];
     T x[7], u[7];
+    const T g = DAMP ? damp[v] : T(1);
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
         m[d] = pec[e0 + d];
-        if (MODE == 0) {
-            x[d] = P[e0 + d];
-            u[d] = minv ? Uin[e0 + d] : T(0);
-        } else {
-            u[d] = Uin[e0 + d];
-        }
+        u[d] = ue[tab.own[d]];
+        if (MODE == 0) x[d] = P[e0 + d];
     }
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
         if (MODE == 0) {
+            if (DAMP == 1) {
+                if (ppre) ppre[e0 + d] = x[d];
+                x[d] *= g;
+            }
             if (!(m[d] & kPecBit)) {
                 x[d] = fma(-a, f[d], x[d]);
                 if (m[d] & kSrcBit) x[d] = fma(a, (T)source_load(src, e0 + d), x[d]);
+            }
+            if (DAMP == 1) {
+                if (pmid) pmid[e0 + d] = x[d];
+                x[d] *= g;
             }
             P[e0 + d] = x[d];
         } else {
@@ -521,58 +585,43 @@ __global__ void __launch_bounds__(128) tet_node_kernel(size_t nnode, const int *
         T y = 0;
 #pragma unroll
         for (int j = 0; j < 7; ++j) {
-            const int r = d < j ? d : j, s = d < j ? j : d;
-            y = fma(mv[r * (13 - r) / 2 + s], x[j], y);
+            const int r7 = d < j ? d : j, s7 = d < j ? j : d;
+            y = fma(mv[r7 * (13 - r7) / 2 + s7], x[j], y);
         }
         if (MODE == 0) {
-            Uout[e0 + d] = fma(c, y, u[d]);
+            Uout[e0 + d] = fma(c, y, DAMP == 2 ? g * u[d] : u[d]);
             if (zout) zout[e0 + d] = y;
+        } else if (DAMP) {
+            Uout[e0 + d] = (m[d] & kPecBit) ? T(0) : (fma(-c, y, T(2) * u[d]) - (T(1) - g) * Uold[e0 + d]) / (T(1) + g);
         } else {
             Uout[e0 + d] = (m[d] & kPecBit) ? T(0) : fma(-c, y, T(2) * u[d] - Uold[e0 + d]);
         }
     }
 }
 
-// Kick + drift, eight lanes per node (lane 7 idle):
-//   P_e -= a * (F_e - f_e)   (F = K U gathered, f the dipole load; PEC slots keep F = 0),
-//   Uout_e = Uin_e + c * (Minv_v P)_e,  and zout_e = (Minv_v P)_e when zout is given.
-// With minv == nullptr only P is written (P -= a F): the stiffness apply.
+// Adjoint of the second loss factor of a lossy middle kick and the loss
+// sensitivities of both factors (node-local, before the adjoint kick):
+// with Pbar the sensitivity to P after the kick's second factor,
+// zr_v += Pbar . Pmid + (g Pbar) . Ppre in FP64 (the sensitivity after the
+// first factor is g Pbar, the adjoint kick leaves Pbar alone), Pbar = g Pbar.
 template <class T>
-__global__ void __launch_bounds__(256) tet_kick_kernel(size_t nnode, const int *__restrict__ inc6,
-                                                       const unsigned char *__restrict__ pec, const vec4<T> *__restrict__ B,
-                                                       const T *__restrict__ minv, T *__restrict__ P, const T *Uin, T *Uout,
-                                                       T a, T c, SrcArgs src, T *__restrict__ zout)
+__global__ void __launch_bounds__(128) tet_loss_adjoint_kernel(size_t nnode, const T *__restrict__ damp, T *__restrict__ Pb,
+                                                               const T *__restrict__ pmid, const T *__restrict__ ppre,
+                                                               double *__restrict__ zr)
 {
-    __shared__ vec4<T> sc[36];
-    load_curl_table<T>(sc);
-    size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t v = g >> 3;
-    int d = (int)(g & 7);
-    const bool live = v < nnode && d < 7;
-    const size_t e = 7 * v + d;
-    const size_t vc = v < nnode ? v : nnode - 1;   // keep the whole warp in the shuffles
-    // the mass-block row and the old U do not depend on the gather: load them first
-    T row[7];
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nnode) return;
+    const T g = damp[v];
+    double s = 0.0;
 #pragma unroll
-    for (int j = 0; j < 7; ++j) row[j] = (minv && d < 7) ? __ldg(minv + 28 * vc + pk7(d, j)) : T(0);
-    T p = 0, u = 0;
-    if (live) {
-        p = P[e];
-        if (minv) u = Uin[e];
-        const unsigned char m = pec[e];
-        // gathered for every live slot (PEC and unused slots list no or
-        // unused incidences), so its loads do not wait for the flag byte
-        const T f = gather_force6<T>(e, inc6, B, sc);
-        if (!(m & kPecBit)) {
-            p = fma(-a, f, p);
-            if (m & kSrcBit) p = fma(a, (T)source_load(src, e), p);
-        }
-        P[e] = p;
+    for (int d = 0; d < 7; ++d) {
+        const size_t e = 7 * v + d;
+        const T pb = Pb[e], pg = g * pb;
+        s = fma((double)pb, (double)pmid[e], s);
+        s = fma((double)pg, (double)ppre[e], s);
+        Pb[e] = pg;
     }
-    if (minv == nullptr) return;     // force-only use (uniform across the grid)
-    T y = block_apply_row<T>(row, p);
-    if (live) Uout[e] = fma(c, y, u);
-    if (zout && live) zout[e] = y;   // Minv P of this drift, kept for the adjoint
+    zr[v] += s;
 }
 
 // U += c * Minv P (drift alone).
@@ -589,39 +638,6 @@ __global__ void __launch_bounds__(256) tet_drift_kernel(size_t nnode, const T *_
     if (v >= nnode) v = nnode - 1;
     T y = block_apply<T>(minv + 28 * v, d, p);
     if (live) U[e] = fma(c, y, U[e]);
-}
-
-// Leapfrog: Unew = 2U - Uold - dt^2 Minv (K U - f); PEC slots stay zero.
-template <class T>
-__global__ void __launch_bounds__(256) tet_leapfrog_kernel(size_t nnode, const int *__restrict__ inc6,
-                                                           const unsigned char *__restrict__ pec, const vec4<T> *__restrict__ B,
-                                                           const T *__restrict__ minv, const T *__restrict__ U,
-                                                           const T *__restrict__ Uold, T *__restrict__ Unew, T dt2, SrcArgs src)
-{
-    __shared__ vec4<T> sc[36];
-    load_curl_table<T>(sc);
-    size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t v = g >> 3;
-    int d = (int)(g & 7);
-    const bool live = v < nnode && d < 7;
-    const size_t e = 7 * v + d;
-    const size_t vc = v < nnode ? v : nnode - 1;
-    T row[7];
-#pragma unroll
-    for (int j = 0; j < 7; ++j) row[j] = d < 7 ? __ldg(minv + 28 * vc + pk7(d, j)) : T(0);
-    T f = 0, u = 0, uo = 0;
-    const unsigned char m = live ? pec[e] : (unsigned char)kPecBit;
-    if (live) {
-        u = U[e];
-        uo = Uold[e];
-        const T g = gather_force6<T>(e, inc6, B, sc);   // issued before the flag test, as in the kick
-        if (!(m & kPecBit)) {
-            f = g;
-            if (m & kSrcBit) f -= (T)source_load(src, e);
-        }
-    }
-    T y = block_apply_row<T>(row, f);
-    if (live) Unew[e] = (m & kPecBit) ? T(0) : fma(-dt2, y, T(2) * u - uo);
 }
 
 // Receivers and step counter, one block: at the start of step n = ctl[0],
@@ -894,7 +910,8 @@ __global__ void dot_partial_kernel(size_t n, const double *__restrict__ x, const
 {
     __shared__ double sh[256];
     double s = 0.0;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) s += x[i] * y[i];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        s += y ? x[i] * y[i] : x[i];   // y == nullptr: the plain sum of x
     sh[threadIdx.x] = s;
     __syncthreads();
     for (int w = 128; w > 0; w >>= 1) {
@@ -902,6 +919,44 @@ __global__ void dot_partial_kernel(size_t n, const double *__restrict__ x, const
         __syncthreads();
     }
     if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// Discrete energy of the symplectic state per node, in FP64:
+// e_v = 1/2 P_v . (Minv_v P_v) + 1/2 U_v . F_v with F = K U (FP64); U, P and
+// the mass blocks are the run's values widened to FP64, so this is the
+// invariant of the system the run integrates.
+template <class T>
+__global__ void __launch_bounds__(128) tet_energy_node_kernel(size_t nnode, const T *__restrict__ minv, const T *__restrict__ P,
+                                                              const T *__restrict__ U, const double *__restrict__ F,
+                                                              double *__restrict__ e)
+{
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nnode) return;
+    double p[7], mv[28];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) p[d] = (double)P[7 * v + d];
+#pragma unroll
+    for (int q = 0; q < 28; ++q) mv[q] = (double)minv[28 * v + q];
+    double s = 0.0;
+#pragma unroll
+    for (int d = 0; d < 7; ++d) {
+        double y = 0.0;
+#pragma unroll
+        for (int j = 0; j < 7; ++j) {
+            const int r7 = d < j ? d : j, s7 = d < j ? j : d;
+            y = fma(mv[r7 * (13 - r7) / 2 + s7], p[j], y);
+        }
+        s = fma(0.5 * p[d], y, s);
+        s = fma(0.5 * (double)U[7 * v + d], F[7 * v + d], s);
+    }
+    e[v] = s;
+}
+
+// y = (double)x
+template <class T> __global__ void widen_kernel(size_t n, const T *__restrict__ x, double *__restrict__ y)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = (double)x[i];
 }
 
 // *out = sum of the nb <= 512 partial sums, by a fixed-shape tree (one
@@ -1003,10 +1058,17 @@ struct TetFemSim : Sim {
     double c0 = 299792458.0;
     double tscale;                  // seconds per normalised time unit (h / c0)
     double dtn = 0.0, dt_lim_n = 0.0, lambda_max = 0.0;
-    std::vector<int> tet_edge_h, inc_ptr_h, inc_h, inc6_h, ntet_h;
+    std::vector<int> tet_edge_h, inc_ptr_h, inc_h, nrec_h;
     std::vector<unsigned char> pec_h;
     std::vector<double> eps_h;
-    DevBuf d_tet_edge, d_inc_ptr, d_inc, d_inc6, d_ntet, d_pec, d_eps, d_minv64, d_minv, d_B, d_U, d_P, d_Uold, d_status;
+    // conductivity: normalised per tetrahedron (sigma h / (c0 eps0)), the
+    // per-node loss rate and its denominator, and the per-node loss factor
+    // of the time loop (exp(-rho dt/2) symplectic, rho dt/2 leapfrog)
+    std::vector<double> sig_h, rho_h, lden_h;
+    bool has_loss = false;
+    DevBuf d_damp;
+    int step_block = 64;            // threads per block of tet_step_kernel (tune_step_block)
+    DevBuf d_tet_edge, d_inc_ptr, d_inc, d_nrec, d_pec, d_eps, d_minv64, d_minv, d_U, d_P, d_Uold, d_status;
     std::vector<Dipole> dips;
     std::vector<std::array<int, 6>> rec_edges;
     std::vector<std::array<double, 18>> rec_w;
@@ -1105,42 +1167,32 @@ struct TetFemSim : Sim {
                 int e = tet_edge_h[6 * t + l];
                 inc_h[inc_ptr_h[e] + fill[e]++] = (int)(t * 8 + l);
             }
-        // the 18 tetrahedra around every node in node-table order (-1 where
-        // the cell is outside the mesh) for the node-centric step
-        {
-            constexpr NodeTab tab = make_node_tab();
-            ntet_h.assign(18 * nnode, -1);
-            for (const Shot &S : shots)
-                for (int k = 0; k <= S.nz; ++k)
-                    for (int j = 0; j <= S.ny; ++j)
-                        for (int i = 0; i <= S.nx; ++i) {
-                            const size_t v = node(S, i, j, k);
-                            for (int q = 0; q < 18; ++q) {
-                                const int ci = i + tab.o[q][0], cj = j + tab.o[q][1], ck = k + tab.o[q][2];
-                                if (ci < 0 || cj < 0 || ck < 0 || ci >= S.nx || cj >= S.ny || ck >= S.nz) continue;
-                                ntet_h[18 * v + q] =
-                                    (int)(S.tet0 + 6 * ((size_t)ci + (size_t)S.nx * ((size_t)cj + (size_t)S.ny * ck)) + tab.p[q]);
-                            }
-                        }
-        }
-        // the same lists at a fixed width of six for the time step (the Kuhn
-        // mesh has at most six tetrahedra on an edge), padded with -1
-        inc6_h.assign(6 * nslot, -1);
-        for (size_t e = 0; e < nslot; ++e) {
-            const int n = inc_ptr_h[e + 1] - inc_ptr_h[e];
-            if (n > 6) throw Error{EMS_ERR_INVALID_ARGUMENT, "edge with more than six tetrahedra"};
-            for (int k = 0; k < n; ++k) inc6_h[6 * e + k] = inc_h[inc_ptr_h[e] + k];
+        // per-node records of the fused step: strides to the neighbouring
+        // nodes and the mask of the neighbours that exist
+        nrec_h.assign(2 * nnode, 0);
+        for (const Shot &S : shots) {
+            const size_t sy = (size_t)S.nx + 1, sz = sy * ((size_t)S.ny + 1);
+            if (sy >= ((size_t)1 << 26) || sz > (size_t)0x7fffffff)
+                throw Error{EMS_ERR_INVALID_ARGUMENT, "mesh planes too large for the node records"};
+            for (int k = 0; k <= S.nz; ++k)
+                for (int j = 0; j <= S.ny; ++j)
+                    for (int i = 0; i <= S.nx; ++i) {
+                        const size_t v = node(S, i, j, k);
+                        const int mask = (i > 0 ? 1 : 0) | (i < S.nx ? 2 : 0) | (j > 0 ? 4 : 0) | (j < S.ny ? 8 : 0) |
+                                         (k > 0 ? 16 : 0) | (k < S.nz ? 32 : 0);
+                        nrec_h[2 * v] = step_record_x((int)sy, mask);
+                        nrec_h[2 * v + 1] = (int)sz;
+                    }
         }
     }
 
     void upload_tables()
     {
-        float cf[6][6][3];
-        double cd[6][6][3], wi[6][6][3], ws[6][6];
+        double wi[6][6][3], ws[6][6];
         for (int p = 0; p < 6; ++p) {
             Shape s = make_shape(p);
             for (int l = 0; l < 6; ++l) {
-                for (int q = 0; q < 3; ++q) { cd[p][l][q] = s.curl[l][q]; cf[p][l][q] = (float)s.curl[l][q]; wi[p][l][q] = s.wint[l][q]; }
+                for (int q = 0; q < 3; ++q) wi[p][l][q] = s.wint[l][q];
                 ws[p][l] = s.wsq[l];
             }
         }
@@ -1148,15 +1200,6 @@ struct TetFemSim : Sim {
         int q = 0;
         for (int r = 0; r < 7; ++r)
             for (int c = r; c < 7; ++c) pk[r][c] = pk[c][r] = (unsigned char)q++;
-        vec4<float> c4f[36];
-        vec4<double> c4d[36];
-        for (int p = 0; p < 6; ++p)
-            for (int l = 0; l < 6; ++l) {
-                c4f[6 * p + l] = vec4<float>{cf[p][l][0], cf[p][l][1], cf[p][l][2], 0.f};
-                c4d[6 * p + l] = vec4<double>{cd[p][l][0], cd[p][l][1], cd[p][l][2], 0.0};
-            }
-        EMS_CUDA(cudaMemcpyToSymbol(c_curl4_f, c4f, sizeof(c4f)));
-        EMS_CUDA(cudaMemcpyToSymbol(c_curl4_d, c4d, sizeof(c4d)));
         EMS_CUDA(cudaMemcpyToSymbol(c_wint, wi, sizeof(wi)));
         EMS_CUDA(cudaMemcpyToSymbol(c_wsq, ws, sizeof(ws)));
         EMS_CUDA(cudaMemcpyToSymbol(c_dir, kDir, sizeof(kDir)));
@@ -1174,14 +1217,12 @@ struct TetFemSim : Sim {
         up(d_tet_edge, tet_edge_h);
         up(d_inc_ptr, inc_ptr_h);
         up(d_inc, inc_h);
-        up(d_inc6, inc6_h);
-        up(d_ntet, ntet_h);
+        up(d_nrec, nrec_h);
         up(d_pec, pec_h);
         size_t w = fp64 ? 8 : 4;
         d_U.alloc(nslot * w); d_U.zero(stream);
         d_P.alloc(nslot * w); d_P.zero(stream);
         d_Uold.alloc(nslot * w); d_Uold.zero(stream);
-        d_B.alloc(4 * ntet * w);
         d_minv.alloc(28 * nnode * w);
         EMS_CUDA(cudaStreamSynchronize(stream));
     }
@@ -1191,9 +1232,15 @@ struct TetFemSim : Sim {
         EMS_CHECK_ARG(eps_r != nullptr, "eps_r required");
         for (size_t t = 0; t < ntet; ++t) EMS_CHECK_ARG(std::isfinite(eps_r[t]) && eps_r[t] > 0, "eps_r must be positive");
         if (sigma)
-            for (size_t t = 0; t < ntet; ++t)
-                if (sigma[t] != 0.0) throw Error{EMS_ERR_UNSUPPORTED, "conductivity in the tetrahedral solver is not supported"};
+            for (size_t t = 0; t < ntet; ++t) EMS_CHECK_ARG(std::isfinite(sigma[t]) && sigma[t] >= 0, "sigma must be >= 0");
         eps_h.assign(eps_r, eps_r + ntet);
+        sig_h.assign(ntet, 0.0);
+        has_loss = false;
+        if (sigma)
+            for (size_t t = 0; t < ntet; ++t) {
+                sig_h[t] = sigma[t] * tscale / kEps0;
+                has_loss = has_loss || sigma[t] > 0;
+            }
         ready = false;
         rec_nsteps = -1;   // the recorded run used the old mass blocks
     }
@@ -1243,7 +1290,90 @@ struct TetFemSim : Sim {
         }
         if (dtn >= dt_lim_n) throw Error{EMS_ERR_INVALID_ARGUMENT, "time step exceeds the stability limit of the integrator"};
         d_minv64.release();
+        loss_setup();
+        tune_step_block();
         ready = true;
+    }
+
+    // Block size of the fused step: the candidates are timed on this mesh
+    // (one warm-up and five timed launches each, a = c = 0 so P keeps its
+    // values and U is copied into the spare buffer; both are rewritten
+    // before they are read again) and the fastest is kept.  The environment
+    // variable EMS_TET_STEP_BLOCK forces one of the candidates.
+    void tune_step_block()
+    {
+        if (const char *env = std::getenv("EMS_TET_STEP_BLOCK")) {
+            const int b = std::atoi(env);
+            for (int c : kStepBlocks)
+                if (c == b) { step_block = b; return; }
+            throw Error{EMS_ERR_INVALID_ARGUMENT, "EMS_TET_STEP_BLOCK must be 32, 64, 128 or 256"};
+        }
+        float best = 0.0f;
+        int pick = step_block;
+        for (int c : kStepBlocks) {
+            step_block = c;
+            const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
+            auto body = [&](auto tag) {
+                using T = decltype(tag);
+                for (int r = 0; r < 6; ++r) {
+                    if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
+                    tet_step_kernel<T, 0, 0><<<nbv, step_block, 0, stream>>>(
+                        nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(),
+                        d_Uold.as<T>(), nullptr, T(0), T(0), SrcArgs{}, nullptr, nullptr, nullptr, nullptr);
+                }
+            };
+            if (fp64) body(double()); else body(float());
+            EMS_CUDA(cudaGetLastError());
+            EMS_CUDA(cudaEventRecord(ev1, stream));
+            EMS_CUDA(cudaEventSynchronize(ev1));
+            float ms = 0.0f;
+            EMS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+            if (c == kStepBlocks[0] || ms < best) { best = ms; pick = c; }
+        }
+        step_block = pick;
+    }
+
+    // Conductivity as a per-node loss rate: rho_v = sum sigma_T w / sum
+    // eps_T w over the incidences (T, l) of the node's live slots, w =
+    // |w_l|^2 integral (the weights of the mass block's alpha term), so
+    // M_sigma,v = rho_v M_eps,v and the loss term of the momentum equation
+    // is rho_v P.  The symplectic loop applies its flow exp(-rho dt/2) on
+    // each side of the middle kick (a time-symmetric composition, second
+    // order when sigma != 0); leapfrog takes the centred loss term.  Host
+    // FP64, O(ntet).
+    void loss_setup()
+    {
+        rho_h.assign(nnode, 0.0);
+        lden_h.assign(nnode, 0.0);
+        if (!has_loss) { d_damp.release(); return; }
+        double wsq[6][6];
+        for (int p = 0; p < 6; ++p) {
+            const Shape sh = make_shape(p);
+            for (int l = 0; l < 6; ++l) wsq[p][l] = sh.wsq[l];
+        }
+        const bool symp = schedule().symp;
+        std::vector<double> dmp(nnode);
+        for (size_t v = 0; v < nnode; ++v) {
+            double num = 0.0, den = 0.0;
+            for (int d = 0; d < 7; ++d) {
+                const size_t e = 7 * v + d;
+                if (pec_h[e] & kPecBit) continue;
+                for (int q = inc_ptr_h[e]; q < inc_ptr_h[e + 1]; ++q) {
+                    const int t = inc_h[q] >> 3, l = inc_h[q] & 7, p = t % 6;
+                    num += sig_h[t] * wsq[p][l];
+                    den += eps_h[t] * wsq[p][l];
+                }
+            }
+            rho_h[v] = den > 0.0 ? num / den : 0.0;
+            lden_h[v] = den;
+            dmp[v] = symp ? std::exp(-0.5 * dtn * rho_h[v]) : 0.5 * dtn * rho_h[v];
+        }
+        if (fp64) {
+            up(d_damp, dmp);
+        } else {
+            std::vector<float> f(dmp.begin(), dmp.end());
+            up(d_damp, f);
+        }
     }
 
     // *out = x.y on the device (deterministic: block partials, then their
@@ -1255,16 +1385,14 @@ struct TetFemSim : Sim {
         dot_finish_kernel<<<1, 512, 0, stream>>>(nb, part.as<double>(), out);
     }
 
-    // y = K x in FP64 through the curl kernel and the force-only kick (P = 0, a = -1)
-    void applyK64(const DevBuf &x, DevBuf &z, DevBuf &B)
+    // z = K x in FP64 through the force-only fused step (P = z = 0, a = -1)
+    void applyK64(const DevBuf &x, DevBuf &z)
     {
-        unsigned nbt = (unsigned)((ntet + 255) / 256);
-        tet_curl_kernel<double><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), x.as<double>(), nullptr, B.as<vec4<double>>());
         z.zero(stream);
-        unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
-        tet_kick_kernel<double><<<nbn, 256, 0, stream>>>(nnode, d_inc6.as<int>(), d_pec.as<unsigned char>(),
-                                                         B.as<vec4<double>>(), nullptr, z.as<double>(), nullptr, nullptr, -1.0, 0.0,
-                                                         SrcArgs{}, nullptr);
+        const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
+        tet_step_kernel<double, 0, 0><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), nullptr,
+                                                               z.as<double>(), x.as<double>(), nullptr, nullptr, -1.0, 0.0,
+                                                               SrcArgs{}, nullptr, nullptr, nullptr, nullptr);
     }
 
     // Largest eigenvalue of Minv K by Lanczos in the M inner product.  Minv K
@@ -1278,9 +1406,8 @@ struct TetFemSim : Sim {
     // not move the largest one.
     double lambda_max_lanczos(const DevBuf &minv_d, int max_iters)
     {
-        DevBuf vb[3], mb[3], B, part, coef;
+        DevBuf vb[3], mb[3], part, coef;
         for (int q = 0; q < 3; ++q) { vb[q].alloc(nslot * 8); mb[q].alloc(nslot * 8); }
-        B.alloc(4 * ntet * 8);
         part.alloc(512 * 8);
         coef.alloc(2 * (max_iters + 2) * 8);   // alpha_j at [2j], beta_{j+1}^2 at [2j+1]
         std::vector<double> x0(nslot);
@@ -1293,7 +1420,7 @@ struct TetFemSim : Sim {
         double *cf = coef.as<double>();
         // start pair (v1, Mv1) = (Minv K x0, K x0) / |.|_M, in buffers 1
         EMS_CUDA(cudaMemcpyAsync(vb[0].p, x0.data(), nslot * 8, cudaMemcpyHostToDevice, stream));
-        applyK64(vb[0], mb[1], B);
+        applyK64(vb[0], mb[1]);
         vb[1].zero(stream);
         tet_drift_kernel<double><<<nbn, 256, 0, stream>>>(nnode, minv_d.as<double>(), mb[1].as<double>(), vb[1].as<double>(), 1.0);
         dot(vb[1], mb[1], part, cf + 2 * max_iters + 2);
@@ -1304,7 +1431,7 @@ struct TetFemSim : Sim {
         int j = 0;
         for (; j < max_iters; ++j) {
             // w = Minv K v (mass image K v), alpha = v.K v
-            applyK64(vb[cur], mb[nxt], B);
+            applyK64(vb[cur], mb[nxt]);
             dot(vb[cur], mb[nxt], part, cf + 2 * j);
             vb[nxt].zero(stream);
             tet_drift_kernel<double><<<nbn, 256, 0, stream>>>(nnode, minv_d.as<double>(), mb[nxt].as<double>(),
@@ -1411,31 +1538,35 @@ struct TetFemSim : Sim {
         return s;
     }
 
-    // One substep: B = curl of Uin (tet_curl_kernel), then MODE 0
-    // (symplectic, tet_kick_kernel): P -= a (K Uin - f); Uout = Uin + c Minv P
-    // (zout = Minv P), or MODE 1 (leapfrog, tet_leapfrog_kernel):
-    // Uout = 2 Uin - Uold - c Minv (K Uin - f).  Returns the number of launches.
-    template <class T, int MODE>
-    int substep(const T *Uin, T *Uout, T *Pio, const T *Uold, T a, T c, const SrcArgs &sa, T *zout)
+    // One substep (tet_step_kernel): MODE 0 (symplectic) P -= a (K Uin - f);
+    // Uout = Uin + c Minv P (zout = Minv P), or MODE 1 (leapfrog) Uout =
+    // 2 Uin - Uold - c Minv (K Uin - f); DAMP selects the lossy forms (the
+    // middle kick, its adjoint, the lossy leapfrog).  Uout is a different
+    // buffer from Uin.  Returns the number of launches.
+    template <class T, int MODE, int DAMP = 0>
+    int substep(const T *Uin, T *Uout, T *Pio, const T *Uold, T a, T c, const SrcArgs &sa, T *zout, T *ppre = nullptr,
+                T *pmid = nullptr)
     {
-        const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
-        vec4<T> *B = d_B.as<vec4<T>>();
-        const unsigned nbv = (unsigned)((nnode + 127) / 128);
-        (void)nbn;
-        tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), Uin, nullptr, B);
-        tet_node_kernel<T, MODE><<<nbv, 128, 0, stream>>>(nnode, d_ntet.as<int>(), d_pec.as<unsigned char>(), B, d_minv.as<T>(),
-                                                          Pio, Uin, Uout, Uold, a, c, sa, zout);
-        return 2;
+        if (Uin == Uout) throw Error{EMS_ERR_STATE, "fused step needs separate input and output fields"};
+        const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
+        tet_step_kernel<T, MODE, DAMP><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(),
+                                                                        d_minv.as<T>(), Pio, Uin, Uout, Uold, a, c, sa, zout,
+                                                                        DAMP ? d_damp.as<T>() : nullptr, ppre, pmid);
+        return 1;
     }
 
     // One time step: receivers (and the step counter), then for the
-    // symplectic steps curl + kick per substep with the drifts merged (the
-    // last one also carries the first half drift of the next step), U and P
-    // updated in place; for leapfrog curl + update into Uo and the ring
-    // rotation (Uc, Pc, Uo) <- (Uo, Uc, Pc).  zout (symplectic only): Minv P
-    // of substep q goes to zout + q * nslot.  Returns the number of launches.
+    // symplectic steps one fused kick + drift per substep with the drifts
+    // merged (the last one also carries the first half drift of the next
+    // step), P in place and U from Uc into Uo with (Uc, Uo) swapped after
+    // every substep; for leapfrog one update into Uo and the ring rotation
+    // (Uc, Pc, Uo) <- (Uo, Uc, Pc).  zout (symplectic only): Minv P of
+    // substep q goes to zout + q * nslot.  Returns the number of launches.
+    // With losses the middle kick of a symplectic step is the lossy one;
+    // prec (recorded runs) receives P before its first loss factor and
+    // after the kick, at prec and prec + nslot.
     template <class T>
-    int enqueue_step(T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa0, T *zout)
+    int enqueue_step(T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa0, T *zout, T *prec = nullptr)
     {
         tet_receiver_kernel<T><<<1, 512, 0, stream>>>(nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), Uc, Pc, d_minv.as<T>(),
                                                       sc.symp ? (T)sc.hfirst : T(0), d_tr.as<double>(), nsamp,
@@ -1445,11 +1576,19 @@ struct TetFemSim : Sim {
             for (int q = 0; q < sc.nsub; ++q) {
                 SrcArgs sa = sa0;
                 sa.q = q;
-                nl += substep<T, 0>(Uc, Uc, Pc, nullptr, (T)sc.sub[q], (T)sc.c[q], sa,
-                                    zout ? zout + (size_t)q * nslot : nullptr);
+                T *z = zout ? zout + (size_t)q * nslot : nullptr;
+                if (has_loss && q == sc.nsub / 2)
+                    nl += substep<T, 0, 1>(Uc, Uo, Pc, nullptr, (T)sc.sub[q], (T)sc.c[q], sa, z, prec,
+                                           prec ? prec + nslot : nullptr);
+                else
+                    nl += substep<T, 0>(Uc, Uo, Pc, nullptr, (T)sc.sub[q], (T)sc.c[q], sa, z);
+                std::swap(Uc, Uo);
             }
         } else {
-            nl += substep<T, 1>(Uc, Uo, nullptr, Pc, T(0), (T)(dtn * dtn), sa0, nullptr);
+            if (has_loss)
+                nl += substep<T, 1, 1>(Uc, Uo, nullptr, Pc, T(0), (T)(dtn * dtn), sa0, nullptr);
+            else
+                nl += substep<T, 1>(Uc, Uo, nullptr, Pc, T(0), (T)(dtn * dtn), sa0, nullptr);
             T *tmp = Pc; Pc = Uc; Uc = Uo; Uo = tmp;
         }
         return nl;
@@ -1521,35 +1660,43 @@ struct TetFemSim : Sim {
         double t_end = 0.0;
         const SrcArgs sa = prepare_run(nsteps, sc, times, t_end);
         const unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
-        // symplectic: U and P updated in place; leapfrog ring: Uc = E^n,
-        // Pc = E^{n-1}, Uo = scratch for E^{n+1}
+        // symplectic: P in place, U alternating between Uc and Uo; leapfrog
+        // ring: Uc = E^n, Pc = E^{n-1}, Uo = scratch for E^{n+1}
         T *Uc = d_U.as<T>(), *Pc = d_P.as<T>(), *Uo = d_Uold.as<T>();
-        // one CUDA graph of kGraphSteps steps (a multiple of 3, so the
-        // leapfrog ring returns to the captured assignment), replayed
+        // CUDA graphs of kGraphSteps steps, replayed.  kGraphSteps is a
+        // multiple of 3 and even, so the leapfrog ring and the symplectic U
+        // pair return to the assignment a graph was captured with; a single
+        // symp4 step (three substeps) swaps the U pair, so a recorded run
+        // keeps one graph per assignment.
         constexpr int kGraphSteps = 12;
         struct StepGraph {   // destroyed on every exit path
             cudaGraph_t g = nullptr;
             cudaGraphExec_t exec = nullptr;
+            const void *start = nullptr;
             ~StepGraph()
             {
                 if (exec) cudaGraphExecDestroy(exec);
                 if (g) cudaGraphDestroy(g);
             }
-        } graph;
+        } graph[2];
         int per_graph = 0;
-        auto capture = [&] {
-            T *u = Uc, *p = Pc, *o = Uo;
+        auto capture = [&](StepGraph &G, T *u, T *p, T *o) {
+            G.start = u;
+            int nl = 0;
             EMS_CUDA(cudaStreamSynchronize(stream));
             EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-            for (int st = 0; st < kGraphSteps; ++st) per_graph += enqueue_step<T>(u, p, o, sc, sa, nullptr);
-            cudaError_t ce = cudaStreamEndCapture(stream, &graph.g);
+            for (int st = 0; st < kGraphSteps; ++st) nl += enqueue_step<T>(u, p, o, sc, sa, nullptr);
+            cudaError_t ce = cudaStreamEndCapture(stream, &G.g);
             if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
-            ce = cudaGraphInstantiate(&graph.exec, graph.g, 0);
+            ce = cudaGraphInstantiate(&G.exec, G.g, 0);
             if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+            per_graph = nl;
         };
         long long launches = 0;
         auto advance = [&](int k) {
-            cudaGraphExec_t exec = graph.exec;
+            cudaGraphExec_t exec = nullptr;
+            for (auto &G : graph)
+                if (G.exec && G.start == Uc) exec = G.exec;
             const int nrep = exec ? k / kGraphSteps : 0;
             for (int r = 0; r < nrep; ++r) EMS_CUDA(cudaGraphLaunch(exec, stream));
             launches += (long long)nrep * per_graph;
@@ -1561,7 +1708,10 @@ struct TetFemSim : Sim {
             nseg = (nsteps + seg_len - 1) / seg_len;
             d_snap.alloc((size_t)nseg * 2 * nslot * sizeof(T));
         }
-        if ((record ? seg_len : nsteps) >= kGraphSteps) capture();
+        if ((record ? seg_len : nsteps) >= kGraphSteps) {
+            capture(graph[0], Uc, Pc, Uo);
+            if (record && symp && sc.nsub % 2 == 1) capture(graph[1], Uo, Pc, Uc);
+        }
         EMS_CUDA(cudaEventRecord(ev0, stream));
         if (symp) {
             tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)sc.hfirst);
@@ -1659,31 +1809,37 @@ struct TetFemSim : Sim {
     // dJ/deps per tetrahedron (FP64) for dJ/dtraces tg (nobs x nsamp x 4,
     // column 0 ignored) of the recorded run.  Segments are recomputed from
     // their snapshots (keeping Minv P of every substep), then swept backward.
-    template <class T> void backward_t(const double *tg, double *grad)
+    template <class T> void backward_t(const double *tg, double *grad, double *grad_sigma)
     {
         const Schedule sc = schedule();
         const int N = rec_nsteps, L = rec_seg, nseg = (N + L - 1) / L, tf = P.time_frequency, nsub = sc.nsub;
         const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
-        const unsigned nbv = (unsigned)((nnode + 127) / 128);
+        const unsigned nbv = (unsigned)((nnode + 127) / 128), nbv2 = nbv;
         // adjoint sources per sample: r[s][rec][c]
         std::vector<double> rs((size_t)std::max(nsamp, 1) * std::max(nobs, 1) * 3, 0.0);
         for (int r = 0; r < nobs; ++r)
             for (int s = 0; s < nsamp; ++s)
                 for (int c = 0; c < 3; ++c) rs[((size_t)s * nobs + r) * 3 + c] = tg[((size_t)r * nsamp + s) * 4 + 1 + c];
-        DevBuf d_rs, Wb, Pb, Q, zbuf, ybuf, Uw, Pw, contrib, d_grad;
+        DevBuf d_rs, Wb, Pb, Pb2, Q, zbuf, ybuf, Uw, Uw2, Pw, contrib, d_grad, pstore, zr;
         up(d_rs, rs);
         RecAdj ra;
         build_receiver_adjoint(ra);
         const size_t w = sizeof(T);
         Wb.alloc(nslot * w); Wb.zero(stream);
         Pb.alloc(nslot * w); Pb.zero(stream);
+        Pb2.alloc(nslot * w);
         Q.alloc(28 * nnode * 8); Q.zero(stream);
         zbuf.alloc(((size_t)L * nsub + 1) * nslot * w);
         ybuf.alloc((size_t)L * nsub * nslot * w);
-        Uw.alloc(nslot * w); Pw.alloc(nslot * w);
+        Uw.alloc(nslot * w); Uw2.alloc(nslot * w); Pw.alloc(nslot * w);
+        if (has_loss) {   // P around every lossy middle kick of a segment, and the loss sensitivities
+            pstore.alloc((size_t)L * 2 * nslot * w);
+            zr.alloc(nnode * 8);
+            zr.zero(stream);
+        }
         const SrcArgs sa = rec_sa;   // the recorded run's source tables are still on the device
         T *zb = zbuf.as<T>(), *yb = ybuf.as<T>();
-        T *pb = Pb.as<T>();
+        T *pb = Pb.as<T>(), *pb2 = Pb2.as<T>();   // Pbar alternates between the two
         for (int s = nseg - 1; s >= 0; --s) {
             const int n0 = s * L, n1 = std::min(N, n0 + L);
             const T *snap = d_snap.as<T>() + (size_t)s * 2 * nslot;
@@ -1693,9 +1849,10 @@ struct TetFemSim : Sim {
             // z[0] = Minv P at the start of step n0
             EMS_CUDA(cudaMemsetAsync(zb, 0, nslot * w, stream));
             tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pw.as<T>(), zb, T(1));
-            T *uc = Uw.as<T>(), *pc = Pw.as<T>(), *unused = nullptr;
+            T *uc = Uw.as<T>(), *pc = Pw.as<T>(), *uo = Uw2.as<T>();
             for (int n = n0; n < n1; ++n)
-                enqueue_step<T>(uc, pc, unused, sc, sa, zb + ((size_t)(n - n0) * nsub + 1) * nslot);
+                enqueue_step<T>(uc, pc, uo, sc, sa, zb + ((size_t)(n - n0) * nsub + 1) * nslot,
+                                has_loss ? pstore.as<T>() + (size_t)(n - n0) * 2 * nslot : nullptr);
             for (int n = n1 - 1; n >= n0; --n) {
                 for (int q = nsub - 1; q >= 0; --q) {
                     // the drift before kick (n, q): same step (q > 0), the
@@ -1703,7 +1860,17 @@ struct TetFemSim : Sim {
                     const double c = q > 0 ? sc.c[q - 1] : (n > 0 ? sc.c[nsub - 1] : sc.hfirst);
                     T *y = yb + ((size_t)(n - n0) * nsub + q) * nslot;
                     // Wbar -= a K Pbar; Pbar += c Minv Wbar (y = Minv Wbar kept)
-                    substep<T, 0>(pb, pb, Wb.as<T>(), nullptr, (T)sc.sub[q], (T)c, SrcArgs{}, y);
+                    if (has_loss && q == nsub / 2) {
+                        // the lossy middle kick: Pbar = g Pbar before the
+                        // adjoint kick, Pbar = g Pbar + c Minv Wbar after it
+                        const T *pp = pstore.as<T>() + (size_t)(n - n0) * 2 * nslot;
+                        tet_loss_adjoint_kernel<T><<<nbv2, 128, 0, stream>>>(nnode, d_damp.as<T>(), pb, pp + nslot, pp,
+                                                                            zr.as<double>());
+                        substep<T, 0, 2>(pb, pb2, Wb.as<T>(), nullptr, (T)sc.sub[q], (T)c, SrcArgs{}, y);
+                    } else {
+                        substep<T, 0>(pb, pb2, Wb.as<T>(), nullptr, (T)sc.sub[q], (T)c, SrcArgs{}, y);
+                    }
+                    std::swap(pb, pb2);
                 }
                 if (n % tf == 0 && n > 0 && nobs > 0) {
                     const T *z = zb + (size_t)(n - n0) * nsub * nslot;
@@ -1731,16 +1898,88 @@ struct TetFemSim : Sim {
         EMS_CUDA(cudaGetLastError());
         EMS_CUDA(cudaMemcpyAsync(grad, d_grad.p, ntet * 8, cudaMemcpyDeviceToHost, stream));
         EMS_CUDA(cudaStreamSynchronize(stream));
+        loss_gradient(zr, grad, grad_sigma);
     }
 
-    void backward(const double *tg, size_t ntg, double *grad, size_t ngrad)
+    // Loss-rate terms of the gradient (host, FP64): each loss factor g_v =
+    // exp(-rho_v dt/2) gives dJ/drho_v = -(dt/2) g_v zr_v, and rho_v =
+    // sum sigma_T c_Tv / den_v (c_Tv the loss weights of T at v) gives
+    // dJ/dsigma_T = sum_v dJ/drho_v c_Tv / den_v and dJ/deps_T -= sum_v
+    // dJ/drho_v rho_v c_Tv / den_v.  grad_sigma is per S/m.
+    void loss_gradient(const DevBuf &zr, double *grad, double *grad_sigma)
+    {
+        if (grad_sigma)
+            for (size_t t = 0; t < ntet; ++t) grad_sigma[t] = 0.0;
+        if (!has_loss) return;
+        std::vector<double> z(nnode);
+        EMS_CUDA(cudaMemcpy(z.data(), zr.p, nnode * 8, cudaMemcpyDeviceToHost));
+        double wsq[6][6];
+        for (int p = 0; p < 6; ++p) {
+            const Shape sh = make_shape(p);
+            for (int l = 0; l < 6; ++l) wsq[p][l] = sh.wsq[l];
+        }
+        const double sig_unit = tscale / kEps0;   // d sigma_normalised / d sigma
+        for (size_t v = 0; v < nnode; ++v) {
+            if (lden_h[v] <= 0.0) continue;
+            const double gr = -0.5 * dtn * std::exp(-0.5 * dtn * rho_h[v]) * z[v];
+            for (int d = 0; d < 7; ++d) {
+                const size_t e = 7 * v + d;
+                if (pec_h[e] & kPecBit) continue;
+                for (int q = inc_ptr_h[e]; q < inc_ptr_h[e + 1]; ++q) {
+                    const int t = inc_h[q] >> 3, l = inc_h[q] & 7, p = t % 6;
+                    const double wv = wsq[p][l] / lden_h[v];
+                    if (grad_sigma) grad_sigma[t] += gr * wv * sig_unit;
+                    grad[t] -= gr * rho_h[v] * wv;
+                }
+            }
+        }
+    }
+
+    // Discrete energy H = 1/2 P.Minv P + 1/2 U.K U of the current
+    // symplectic state, per shot, in FP64 on the GPU.
+    void energy(double *out, int n)
+    {
+        if (!schedule().symp) throw Error{EMS_ERR_UNSUPPORTED, "the discrete energy is defined for the symplectic integrators"};
+        EMS_CHECK_ARG(out && n == (int)shots.size(), "energy needs one value per shot");
+        if (!ready) setup();
+        DevBuf u64, f64, e, part, res;
+        f64.alloc(nslot * 8);
+        e.alloc(nnode * 8);
+        part.alloc(512 * 8);
+        res.alloc(shots.size() * 8);
+        const DevBuf *u = &d_U;
+        if (!fp64) {
+            u64.alloc(nslot * 8);
+            widen_kernel<float><<<(unsigned)((nslot + 255) / 256), 256, 0, stream>>>(nslot, d_U.as<float>(), u64.as<double>());
+            u = &u64;
+        }
+        applyK64(*u, f64);
+        const unsigned nb = (unsigned)((nnode + 127) / 128);
+        if (fp64)
+            tet_energy_node_kernel<double><<<nb, 128, 0, stream>>>(nnode, d_minv.as<double>(), d_P.as<double>(),
+                                                                    d_U.as<double>(), f64.as<double>(), e.as<double>());
+        else
+            tet_energy_node_kernel<float><<<nb, 128, 0, stream>>>(nnode, d_minv.as<float>(), d_P.as<float>(), d_U.as<float>(),
+                                                                   f64.as<double>(), e.as<double>());
+        for (size_t k = 0; k < shots.size(); ++k) {
+            const Shot &S = shots[k];
+            const size_t nv = (size_t)(S.nx + 1) * (S.ny + 1) * (S.nz + 1);
+            dot_partial_kernel<<<512, 256, 0, stream>>>(nv, e.as<double>() + S.node0, nullptr, part.as<double>());
+            dot_finish_kernel<<<1, 512, 0, stream>>>(512, part.as<double>(), res.as<double>() + k);
+        }
+        EMS_CUDA(cudaGetLastError());
+        EMS_CUDA(cudaMemcpyAsync(out, res.p, shots.size() * 8, cudaMemcpyDeviceToHost, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    void backward(const double *tg, size_t ntg, double *grad, size_t ngrad, double *grad_sigma)
     {
         if (rec_nsteps < 0)
             throw Error{EMS_ERR_STATE, "no recorded run: call ems_tetfem_set_checkpoints, ems_reset, then ems_run"};
         EMS_CHECK_ARG(tg && grad, "trace gradient and output required");
         EMS_CHECK_ARG(ntg == (size_t)nobs * nsamp * 4, "trace gradient must have nrec * nsamp * 4 values");
         EMS_CHECK_ARG(ngrad == ntet, "gradient must have one value per tetrahedron");
-        if (fp64) backward_t<double>(tg, grad); else backward_t<float>(tg, grad);
+        if (fp64) backward_t<double>(tg, grad, grad_sigma); else backward_t<float>(tg, grad, grad_sigma);
     }
 
     void run(int nsteps) override
@@ -1805,16 +2044,14 @@ struct TetFemSim : Sim {
         in.alloc(nslot * w);
         out.alloc(nslot * w);
         out.zero(stream);
-        const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
+        const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
         auto body = [&](auto tag) {
             using T = decltype(tag);
             std::vector<T> h(u, u + nslot);
             EMS_CUDA(cudaMemcpyAsync(in.p, h.data(), nslot * w, cudaMemcpyHostToDevice, stream));
-            vec4<T> *B = d_B.as<vec4<T>>();
-            tet_curl_kernel<T><<<nbt, 256, 0, stream>>>(ntet, d_tet_edge.as<int>(), in.as<T>(), nullptr, B);
-            tet_kick_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_inc6.as<int>(), d_pec.as<unsigned char>(),
-                                                        B, nullptr, out.as<T>(), nullptr, nullptr, T(-1), T(0), SrcArgs{},
-                                                        nullptr);
+            tet_step_kernel<T, 0, 0><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), nullptr,
+                                                              out.as<T>(), in.as<T>(), nullptr, nullptr, T(-1), T(0), SrcArgs{},
+                                                              nullptr, nullptr, nullptr, nullptr);
             EMS_CUDA(cudaGetLastError());
             EMS_CUDA(cudaMemcpyAsync(h.data(), out.p, nslot * w, cudaMemcpyDeviceToHost, stream));
             EMS_CUDA(cudaStreamSynchronize(stream));
@@ -1831,20 +2068,30 @@ struct TetFemSim : Sim {
         EMS_CUDA(cudaStreamSynchronize(stream));
     }
 
+    void launch_shape(int b[3]) override
+    {
+        if (!ready) setup();
+        b[0] = step_block; b[1] = b[2] = 1;
+    }
+
     void time_dominant(int launches, double *ms, double *bytes, std::string *name) override
     {
         if (!ready) setup();
         const size_t w = fp64 ? 8 : 4;
-        const unsigned nbv = (unsigned)((nnode + 127) / 128);
-        // the node-centric kick of a substep; a = c = 0 leaves P unchanged
-        // and copies U into the spare buffer
+        const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
+        // the fused step of a substep as the time loop runs it: a = c = 0
+        // leaves P unchanged and copies U between the two buffers the loop
+        // alternates, so the fields keep their values and the caches see the
+        // loop's access pattern
         auto body = [&](auto tag) {
             using T = decltype(tag);
             for (int r = 0; r <= launches; ++r) {
                 if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
-                tet_node_kernel<T, 0><<<nbv, 128, 0, stream>>>(nnode, d_ntet.as<int>(), d_pec.as<unsigned char>(),
-                                                               d_B.as<vec4<T>>(), d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(),
-                                                               d_Uold.as<T>(), nullptr, T(0), T(0), SrcArgs{}, nullptr);
+                T *a = d_U.as<T>(), *b = d_Uold.as<T>();
+                if (r % 2) std::swap(a, b);
+                tet_step_kernel<T, 0, 0><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(),
+                                                                         d_minv.as<T>(), d_P.as<T>(), a, b, nullptr, T(0), T(0),
+                                                                         SrcArgs{}, nullptr, nullptr, nullptr, nullptr);
             }
         };
         if (fp64) body(double()); else body(float());
@@ -1854,12 +2101,11 @@ struct TetFemSim : Sim {
         float t = 0;
         EMS_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
         *ms = t / launches;
-        // unique bytes of one kick: node tetrahedron lists (18 ints per node)
-        // + B (3 values per tetrahedron, stored as 4) + P read and written +
-        // U read + U written + packed mass blocks + slot flags
-        *bytes = (double)nnode * 72 + (double)(4 * ntet) * w + (double)nslot * 4 * w + (double)(28 * nnode) * w +
-                 (double)nslot;
-        *name = fp64 ? "tet_node_kernel<double>" : "tet_node_kernel<float>";
+        // unique bytes of one substep: node records (8 B per node) + U read
+        // once (the neighbours' reads hit L1/L2) + P read and written + U
+        // written + packed mass blocks + slot flags
+        *bytes = (double)nnode * 8 + (double)nslot * 4 * w + (double)(28 * nnode) * w + (double)nslot;
+        *name = fp64 ? "tet_step_kernel<double>" : "tet_step_kernel<float>";
     }
 };
 
@@ -1941,14 +2187,15 @@ void tetfem_apply_stiffness(Sim *s, const double *u, double *f, size_t n)
 }
 
 void tetfem_set_checkpoints(Sim *s, int nsnap) { static_cast<TetFemSim *>(s)->set_checkpoints(nsnap); }
+void tetfem_energy(Sim *s, double *out, int n) { static_cast<TetFemSim *>(s)->energy(out, n); }
 
-void tetfem_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, size_t ngrad)
+void tetfem_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, double *grad_sigma, size_t ngrad)
 {
-    static_cast<TetFemSim *>(s)->backward(trace_grad, ntg, grad_eps, ngrad);
+    static_cast<TetFemSim *>(s)->backward(trace_grad, ntg, grad_eps, ngrad, grad_sigma);
 }
 
 void tetfem_gradient(Sim *s, int nsteps, int nsnap, int kind, const double *obs, const double *band, double *misfit,
-                     double *grad, size_t ngrad)
+                     double *grad, double *grad_sigma, size_t ngrad)
 {
     auto *f = static_cast<TetFemSim *>(s);
     EMS_CHECK_ARG(nsteps > 0 && nsnap > 0, "nsteps and nsnap must be positive");
@@ -1959,7 +2206,7 @@ void tetfem_gradient(Sim *s, int nsteps, int nsnap, int kind, const double *obs,
     f->run(nsteps);
     std::vector<double> tg(f->traces.size());
     trace_misfit(kind, f->nobs, f->nsamp, f->traces.data(), obs, misfit, tg.data(), band);
-    f->backward(tg.data(), tg.size(), grad, ngrad);
+    f->backward(tg.data(), tg.size(), grad, ngrad, grad_sigma);
 }
 
 void tetfem_time_step(const Sim *s, double *dt, double *lim)

@@ -60,6 +60,13 @@ class _Sim:
         TF_MISFIT_GOF_master/main.py."""
         self._check(lib().ems_save_trace_component(self._h, int(receiver), int(component), str(path).encode()))
 
+    def launch_shape(self):
+        """Threads per block (x, y, z) of the main kernels as the handle's
+        autotuner chose them (zeros for fixed shapes)."""
+        b = (C.c_int * 3)()
+        self._check(lib().ems_launch_shape(self._h, b))
+        return tuple(b)
+
     def run_stats(self):
         ms, n = C.c_double(), C.c_longlong()
         self._check(lib().ems_last_run_stats(self._h, C.byref(ms), C.byref(n)))
@@ -247,25 +254,39 @@ class TetFemSimulation(_Sim):
         keeping nsnap snapshots on the device (0 stops recording)."""
         self._check(lib().ems_tetfem_set_checkpoints(self._h, int(nsnap)))
 
-    def backward(self, trace_grad):
+    def energy(self):
+        """Discrete energy 1/2 P.Minv P + 1/2 U.K U of the current symplectic
+        state, per shot (FP64, computed on the GPU); a float for a single
+        shot, an array for a batch."""
+        n = len(self._cells())
+        out = np.zeros(n)
+        self._check(lib().ems_tetfem_energy(self._h, _dptr(out), n))
+        return out if isinstance(self, TetFemBatch) else float(out[0])
+
+    def backward(self, trace_grad, sigma=False):
         """dJ/deps_r per tetrahedron (FP64) of the recorded run, given
-        dJ/dtraces shaped like :meth:`traces` (column 0 ignored)."""
+        dJ/dtraces shaped like :meth:`traces` (column 0 ignored); with
+        sigma=True the pair (dJ/deps_r, dJ/dsigma per S/m)."""
         g = np.ascontiguousarray(trace_grad, dtype=np.float64).reshape(-1)
         out = np.zeros(self.ntet)
-        self._check(lib().ems_tetfem_backward(self._h, _dptr(g), g.size, _dptr(out), out.size))
-        return out
+        gs = np.zeros(self.ntet) if sigma else None
+        self._check(lib().ems_tetfem_backward(self._h, _dptr(g), g.size, _dptr(out),
+                                              _dptr(gs) if sigma else None, out.size))
+        return (out, gs) if sigma else out
 
-    def gradient(self, nsteps, observed, kind=0, nsnap=64, tf_band=None):
+    def gradient(self, nsteps, observed, kind=0, nsnap=64, tf_band=None, sigma=False):
         """Misfit J of an nsteps run from the reset state against `observed`
-        traces and dJ/deps_r per tetrahedron (one call of ems_tetfem_gradient)."""
+        traces and dJ/deps_r per tetrahedron (one call of ems_tetfem_gradient);
+        with sigma=True, (J, dJ/deps_r, dJ/dsigma)."""
         ob = np.ascontiguousarray(observed, dtype=np.float64)
         band = None if tf_band is None else np.ascontiguousarray(tf_band, dtype=np.float64)
         J = C.c_double()
         out = np.zeros(self.ntet)
+        gs = np.zeros(self.ntet) if sigma else None
         self._check(lib().ems_tetfem_gradient(self._h, int(nsteps), int(nsnap), int(kind), _dptr(ob),
                                               _dptr(band) if band is not None else None, C.byref(J), _dptr(out),
-                                              out.size))
-        return J.value, out
+                                              _dptr(gs) if sigma else None, out.size))
+        return (J.value, out, gs) if sigma else (J.value, out)
 
     @property
     def ntet(self):

@@ -193,21 +193,33 @@ int ems_tetbatch_add_receiver(ems_sim *sim, int shot, const double pos[3]);
  * segment from its snapshot and runs the reversed steps over it.  Fields are
  * in the handle's precision, the gradient is accumulated in FP64.  Works on
  * batch handles too (one gradient value per tetrahedron of every shot). */
+/* Discrete energy H = 1/2 P.Minv P + 1/2 U.K U of the current state of a
+ * symplectic run (EMS_SYMP2, EMS_SYMP4), the quantity those integrators
+ * keep bounded without drift; computed in FP64 on the GPU from the run's
+ * fields and mass blocks.  One value per shot (nshots = 1 for
+ * ems_create_tetfem handles).  New: the reference has no energy check.
+ * EMS_ERR_UNSUPPORTED for EMS_LEAPFROG. */
+int ems_tetfem_energy(ems_sim *sim, double *energy, int nshots);
+
+
 /* Record the next ems_run that starts from the reset state (nsnap > 0), or
  * stop recording (nsnap = 0).  EMS_ERR_UNSUPPORTED for EMS_LEAPFROG. */
 int ems_tetfem_set_checkpoints(ems_sim *sim, int nsnap);
-/* dJ/deps_r per tetrahedron (ntet values) of the recorded run, given
- * dJ/dtraces in the layout of ems_get_traces (nobs x nsamp x 4, column 0,
- * the time, ignored; n = nobs * nsamp * 4).  EMS_ERR_STATE when there is no
- * recorded run (or the material, dipoles or receivers changed since). */
-int ems_tetfem_backward(ems_sim *sim, const double *trace_grad, size_t n, double *grad_eps, size_t ntet);
+/* dJ/deps_r and, when grad_sigma is not NULL, dJ/dsigma (per S/m) per
+ * tetrahedron (ntet values each) of the recorded run, given dJ/dtraces in
+ * the layout of ems_get_traces (nobs x nsamp x 4, column 0, the time,
+ * ignored; n = nobs * nsamp * 4).  EMS_ERR_STATE when there is no recorded
+ * run (or the material, dipoles or receivers changed since). */
+int ems_tetfem_backward(ems_sim *sim, const double *trace_grad, size_t n, double *grad_eps, double *grad_sigma,
+                        size_t ntet);
 
 /* The whole gradient in one call (the pipeline above with ems_trace_misfit):
  * reset, record nsteps steps with nsnap snapshots, misfit of the traces
- * against `observed` (nobs x nsamp x 4), dJ/deps_r into grad_eps (ntet).
- * The fields end in the state after the forward run. */
+ * against `observed` (nobs x nsamp x 4), dJ/deps_r into grad_eps and, when
+ * not NULL, dJ/dsigma into grad_sigma (ntet each).  The fields end in the
+ * state after the forward run. */
 int ems_tetfem_gradient(ems_sim *sim, int nsteps, int nsnap, int misfit_kind, const double *observed,
-                        const double *tf_band, double *misfit, double *grad_eps, size_t ntet);
+                        const double *tf_band, double *misfit, double *grad_eps, double *grad_sigma, size_t ntet);
 
 enum {
     EMS_MISFIT_L2 = 0,          /* J = 1/2 sum (E - E_obs)^2 over receivers, samples, components */
@@ -256,6 +268,15 @@ int ems_set_field(ems_sim *sim, int which, const double *in, size_t n);
 int ems_last_run_stats(const ems_sim *sim, double *device_ms, long long *launches);
 int ems_time_dominant_kernel(ems_sim *sim, int launches, double *ms_per_launch, double *bytes_per_launch,
                              char *name, size_t name_cap);
+/* Threads per block (x, y, z) of the main time-step kernels as the handle's
+ * autotuner chose them by timing candidates on its own grid: tetrahedral
+ * handles time 32, 64, 128, 256 threads when the material is set up
+ * (EMS_TET_STEP_BLOCK forces one); FDTD handles time the shapes 32x8, 32x4,
+ * 64x4, 128x2, 256x1, 64x2 on the first steps of their first run of at
+ * least 40 steps (EMS_FDTD_BLOCK="XxY" forces one; 32x8 before tuning).
+ * Launch shapes change no result.  Zeros for solvers with fixed shapes.
+ * New: the reference has fixed OpenACC launch shapes. */
+int ems_launch_shape(ems_sim *sim, int block[3]);
 /* Zero every field level and rewind the simulation clock to t = 0, keeping
  * mesh, materials, sources and receivers: the state a freshly constructed
  * reference FemSimulation starts from. */

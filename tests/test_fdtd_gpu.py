@@ -141,3 +141,42 @@ def test_runs_are_deterministic():
     assert np.array_equal(a, b)
     for k in fa:
         assert np.array_equal(fa[k], fb[k])
+
+
+def test_launch_shape_autotuner_picks_a_candidate_and_changes_no_result():
+    # the first run of >= 24 steps times six launch shapes and keeps the
+    # fastest; forced shapes (EMS_FDTD_BLOCK, child processes) must give the
+    # same fields and traces bit for bit
+    import os
+    import subprocess
+    import sys
+    code = (
+        "import numpy as np, emsolvers_gb300 as ems\n"
+        "g = (37, 29, 23)\n"
+        "rng = np.random.default_rng(5)\n"
+        "s = ems.FdtdSimulation(g, 1e-3, 1.5e-12, 8.854187817e-12, 1.25663706212e-6, 2, precision=ems.FP32,\n"
+        "                       pml_cells=4)\n"
+        "s.set_material(rng.uniform(1, 4, g[::-1]) * 8.854187817e-12, rng.uniform(0, 0.05, g[::-1]))\n"
+        "s.setSource_z((18, 14, 11))\n"
+        "s.setObservationPoint(([(20, 15, 12)], [(20, 15, 12)], [(20, 15, 12)]))\n"
+        "s.run(40)\n"
+        "print('%%d %%d' %% s.launch_shape()[:2])\n"
+        "f = s.fields()\n"
+        "np.save('%s', np.concatenate([s.traces().ravel()] + [np.ravel(f[k]) for k in sorted(f)]))\n")
+    out = {}
+    for shape in ("", "32x8", "256x1", "64x2"):
+        env = dict(os.environ)
+        env.pop("EMS_FDTD_BLOCK", None)
+        if shape:
+            env["EMS_FDTD_BLOCK"] = shape
+        path = f"/tmp/ems_fdtd_shape_{shape or 'auto'}_{os.getpid()}.npy"
+        r = subprocess.run([sys.executable, "-c", code % path], env=env, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        x, y = map(int, r.stdout.strip().splitlines()[-1].split())
+        assert (x, y) in [(32, 8), (32, 4), (64, 4), (128, 2), (256, 1), (64, 2)]
+        if shape:
+            assert f"{x}x{y}" == shape
+        out[shape] = np.load(path)
+        os.remove(path)
+    for shape in ("32x8", "256x1", "64x2"):
+        assert np.array_equal(out[""], out[shape])

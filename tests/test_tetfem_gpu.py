@@ -106,13 +106,75 @@ def test_gpu_symplectic_state_conserves_discrete_energy():
     assert max(errs[5:]) < 1.3 * max(errs[:5]) + 1e-12
 
 
-def test_conductivity_is_rejected_as_unsupported():
-    n = (4, 4, 4)
-    _, _, ntet = oracle.tet_sizes(n)
-    s = ems.TetFemSimulation(n, H, 1, ems.SYMP2, ems.FP32, dt=1e-13)
-    with pytest.raises(ems.EmsError) as e:
-        s.set_material(np.ones(ntet), np.full(ntet, 0.01))
-    assert e.value.status == -8
+@pytest.mark.parametrize("precision,tol", [(ems.FP64, 1e-12), (ems.FP32, 2e-6)], ids=["fp64", "fp32"])
+def test_gpu_energy_matches_oracle_energy_of_the_same_state(precision, tol):
+    # the GPU's FP64 energy of the run's state against the oracle's energy
+    # of the same (widened) fields; FP32 runs keep FP32 mass blocks, which
+    # differ from the oracle's by ~1e-7 relative
+    n = (5, 6, 4)
+    _, nslot, ntet = oracle.tet_sizes(n)
+    rng = np.random.default_rng(21)
+    eps = rng.uniform(1, 4, ntet)
+    pec = oracle.tet_pec_mask(n)
+    U0 = np.where(pec, 0.0, rng.standard_normal(nslot))
+    dtn = 0.5 * oracle.stability_constant(oracle.SYMP4) / np.sqrt(oracle.tet_lambda_max(n, eps, 300))
+    s = ems.TetFemSimulation(n, H, 1, ems.SYMP4, precision, dt=dtn * TS)
+    s.set_material(eps)
+    s.set_field(0, U0)
+    s.run(40)
+    e_gpu = s.energy()
+    e_orc = oracle.tet_energy(n, eps, s.get_field(0), s.get_field(1))
+    assert abs(e_gpu - e_orc) < tol * e_orc
+
+
+@pytest.mark.parametrize("precision,bound", [(ems.FP64, 5e-3), (ems.FP32, 5e-3)], ids=["fp64", "fp32"])
+def test_gpu_energy_stays_bounded_without_drift(precision, bound):
+    # symplectic: the energy error oscillates at O(dt^4) and does not grow
+    n = (6, 6, 6)
+    _, nslot, ntet = oracle.tet_sizes(n)
+    rng = np.random.default_rng(9)
+    eps = rng.uniform(1, 4, ntet)
+    pec = oracle.tet_pec_mask(n)
+    U0 = np.where(pec, 0.0, rng.standard_normal(nslot))
+    dtn = 0.4 * oracle.stability_constant(oracle.SYMP4) / np.sqrt(oracle.tet_lambda_max(n, eps, 300))
+    s = ems.TetFemSimulation(n, H, 1, ems.SYMP4, precision, dt=dtn * TS)
+    s.set_material(eps)
+    s.set_field(0, U0)
+    e0 = s.energy()
+    errs = []
+    for _ in range(10):
+        s.run(30)
+        errs.append(abs(s.energy() - e0) / e0)
+    assert max(errs) < bound
+    assert max(errs[5:]) < 1.3 * max(errs[:5]) + 1e-6
+
+
+def test_gpu_energy_per_shot_of_a_batch_and_leapfrog_rejected():
+    cells = [(4, 5, 3), (3, 3, 6)]
+    rng = np.random.default_rng(13)
+    eps = [rng.uniform(1, 4, 6 * c[0] * c[1] * c[2]) for c in cells]
+    dt = 0.5 * 2.0 * TS / np.sqrt(max(oracle.tet_lambda_max(c, e, 100) for c, e in zip(cells, eps)))
+    b = ems.TetFemBatch(cells, H, integrator=ems.SYMP4, precision=ems.FP64, dt=dt)
+    b.set_material(np.concatenate(eps))
+    U = []
+    for c in cells:
+        _, ns, _ = oracle.tet_sizes(c)
+        U.append(np.where(oracle.tet_pec_mask(c), 0.0, rng.standard_normal(ns)))
+    b.set_field(0, np.concatenate(U))
+    b.run(25)
+    e = b.energy()
+    u, p = b.get_field(0), b.get_field(1)
+    off = 0
+    for k, c in enumerate(cells):
+        _, ns, _ = oracle.tet_sizes(c)
+        ref = oracle.tet_energy(c, eps[k], u[off:off + ns], p[off:off + ns])
+        assert abs(e[k] - ref) < 1e-12 * ref
+        off += ns
+    lf = ems.TetFemSimulation((3, 3, 3), H, 1, ems.LEAPFROG, ems.FP64, dt=1e-13)
+    lf.set_material(np.full(162, 2.0))
+    with pytest.raises(ems.EmsError) as err:
+        lf.energy()
+    assert err.value.status == -8
 
 
 def test_save_results_writes_reference_trace_format(tmp_path):
@@ -152,3 +214,38 @@ def test_apply_stiffness_matches_oracle(precision, tol):
     assert np.all(f[pec] == 0.0)
     # the solver state is untouched
     assert np.all(s.get_field(0) == 0.0)
+
+
+def test_step_block_autotuner_picks_a_candidate_and_changes_no_result():
+    # forced block sizes (EMS_TET_STEP_BLOCK) in child processes: the block
+    # size is a launch shape only, so traces and fields are bit-identical
+    import os
+    import subprocess
+    import sys
+    code = (
+        "import numpy as np, emsolvers_gb300 as ems\n"
+        "n = (9, 7, 8)\n"
+        "eps = np.random.default_rng(3).uniform(1, 4, 6 * 9 * 7 * 8)\n"
+        "s = ems.TetFemSimulation(n, 1e-3, 1, ems.SYMP4, ems.FP32, dt=0.0, cfl_fraction=0.8)\n"
+        "s.set_material(eps)\n"
+        "s.add_dipole(np.array([4.1, 3.3, 4.2]) * 1e-3, (0.2, 0.3, 1.0), ems.WAVE_RICKER, 4e10, 1.0)\n"
+        "s.add_receiver(np.array([6.2, 2.1, 3.3]) * 1e-3)\n"
+        "s.run(80)\n"
+        "print(s.launch_shape()[0])\n"
+        "np.save('%s', np.concatenate([s.traces().ravel(), s.get_field(0), s.get_field(1)]))\n")
+    out = {}
+    for b in ("", "32", "256"):
+        env = dict(os.environ)
+        env.pop("EMS_TET_STEP_BLOCK", None)
+        if b:
+            env["EMS_TET_STEP_BLOCK"] = b
+        path = f"/tmp/ems_step_block_{b or 'auto'}_{os.getpid()}.npy"
+        r = subprocess.run([sys.executable, "-c", code % path], env=env, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        chosen = int(r.stdout.strip().splitlines()[-1])
+        assert chosen in (32, 64, 128, 256)
+        if b:
+            assert chosen == int(b)
+        out[b] = np.load(path)
+        os.remove(path)
+    assert np.array_equal(out[""], out["32"]) and np.array_equal(out["32"], out["256"])
