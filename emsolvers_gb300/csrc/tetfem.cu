@@ -224,13 +224,24 @@ __global__ void tet_minv_setup_kernel(size_t nnode, const unsigned char *__restr
         }
 }
 
+// Plane layout of the time loop's arrays: slot d of node v (edge slot
+// e = 7 v + d of the mesh tables, the flags and the API) at d * nnode + v,
+// so a warp of consecutive nodes reads and writes contiguous memory for
+// every slot; the packed symmetric mass block of node v (28 entries) as
+// seven planes of four, entry p at ((p / 4) * nnode + v) * 4 + p % 4.
+__host__ __device__ __forceinline__ size_t fslot(size_t e, size_t nnode) { return (e % 7) * nnode + e / 7; }
+__host__ __device__ __forceinline__ size_t fpk(size_t v, int p, size_t nnode)
+{
+    return ((size_t)(p >> 2) * nnode + v) * 4 + (p & 3);
+}
+
 template <class T>
 __global__ void tet_pack_minv_kernel(size_t nnode, const double *__restrict__ full, T *__restrict__ packed)
 {
     size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nnode) return;
     for (int r = 0; r < 7; ++r)
-        for (int c = r; c < 7; ++c) packed[28 * v + c_pack[r][c]] = (T)full[49 * v + 7 * r + c];
+        for (int c = r; c < 7; ++c) packed[fpk(v, c_pack[r][c], nnode)] = (T)full[49 * v + 7 * r + c];
 }
 
 // ---------------------------------------------------------------- time step
@@ -245,27 +256,41 @@ __device__ __forceinline__ int pk7(int r, int c)
     return a * (13 - a) / 2 + b;
 }
 
-// (Minv_v x)_d with x_j held by lane j of the node's 8-lane group.
-template <class T>
-__device__ __forceinline__ T block_apply(const T *__restrict__ mv, int d, T x)
+// The packed mass block of node v (plane layout) into registers.
+template <class T> __device__ __forceinline__ void load_block(const T *__restrict__ minv, size_t nnode, size_t v, T (&mv)[28])
+{
+    const vec4<T> *m4 = reinterpret_cast<const vec4<T> *>(minv);
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        const vec4<T> w = m4[(size_t)q * nnode + v];
+        mv[4 * q] = w.x; mv[4 * q + 1] = w.y; mv[4 * q + 2] = w.z; mv[4 * q + 3] = w.w;
+    }
+}
+
+// (Minv_v x)_d from the packed block, terms in j order.
+template <class T> __device__ __forceinline__ T block_row(const T (&mv)[28], const T (&x)[7], int d)
 {
     T y = 0;
 #pragma unroll
     for (int j = 0; j < 7; ++j) {
-        T xj = __shfl_sync(0xffffffffu, x, j, 8);
-        if (d < 7) y = fma(mv[pk7(d, j)], xj, y);
+        const int r7 = d < j ? d : j, s7 = d < j ? j : d;
+        y = fma(mv[r7 * (13 - r7) / 2 + s7], x[j], y);
     }
     return y;
 }
 
 // Point-dipole loads fused into the step kernels: entry k adds
-// coef[k] * g[dipole(k)] to slot[k]; g for this (step, substep) is read at
+// coef[k] * g[dip[k]] to slot[k]; g for this (step, substep) is read at
 // g + ((ctl[0]-1)*nsub + q)*nd (the step counter was advanced at the start of
-// the step by the receiver kernel).
+// the step by the receiver kernel).  The entries are sorted by slot (entries
+// of one slot in dipole order), so a flagged slot finds its entries by
+// binary search: a linear scan of a batch's list (six entries per shot) kept
+// the few warps that hold dipole slots busy long after the rest of the grid.
 struct SrcArgs {
     int n;
     const int *slot;
     const double *coef;
+    const int *dip;
     const double *g;
     const int *ctl;
     int nd, nsub, q;
@@ -275,9 +300,13 @@ __device__ __forceinline__ double source_load(const SrcArgs &s, size_t e)
 {
     double f = 0.0;
     if (s.n == 0) return f;
+    int lo = 0, hi = s.n;   // first entry with slot >= e
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if ((size_t)s.slot[mid] < e) lo = mid + 1; else hi = mid;
+    }
     const double *g = s.g + ((size_t)(s.ctl[0] - 1) * s.nsub + s.q) * s.nd;
-    for (int k = 0; k < s.n; ++k)
-        if ((size_t)s.slot[k] == e) f += s.coef[k] * g[k / 6];
+    for (int k = lo; k < s.n && (size_t)s.slot[k] == e; ++k) f += s.coef[k] * g[s.dip[k]];
     return f;
 }
 
@@ -526,19 +555,19 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
     if (v >= nnode) return;
     const int2 r = __ldg(nrec + v);
     const int have = (int)((unsigned)r.x >> 26), sy = r.x & 0x3ffffff, sz = r.y;
-    const T *u0 = Uin + 7 * v;
+    const T *u0 = Uin + v;
     // a missing tail node only feeds missing tetrahedra: read the node's own
     // slots instead (in bounds) and let the cell test drop them
     int off[13];
 #pragma unroll
     for (int t = 0; t < 13; ++t)
-        off[t] = (tab.treq[t] & ~have) == 0 ? 7 * (tab.tail[t][0] + tab.tail[t][1] * sy + tab.tail[t][2] * sz) : 0;
+        off[t] = (tab.treq[t] & ~have) == 0 ? tab.tail[t][0] + tab.tail[t][1] * sy + tab.tail[t][2] * sz : 0;
     T ue[43];
 #pragma unroll
-    for (int k = 0; k < 43; ++k) ue[k] = u0[off[tab.etail[k]] + tab.edir[k]];
+    for (int k = 0; k < 43; ++k) ue[k] = u0[(size_t)tab.edir[k] * nnode + off[tab.etail[k]]];
     T f[7] = {0, 0, 0, 0, 0, 0, 0};
     step_tets<T>(ue, f, have, std::make_integer_sequence<int, 18>{});
-    const size_t e0 = 7 * v;
+    const size_t e0 = 7 * v;   // the node's slots in the flag table and the source list
     unsigned char m[7];
     T x[7], u[7];
     const T g = DAMP ? damp[v] : T(1);
@@ -546,13 +575,14 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
     for (int d = 0; d < 7; ++d) {
         m[d] = pec[e0 + d];
         u[d] = ue[tab.own[d]];
-        if (MODE == 0) x[d] = P[e0 + d];
+        if (MODE == 0) x[d] = P[(size_t)d * nnode + v];
     }
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
+        const size_t f0 = (size_t)d * nnode + v;
         if (MODE == 0) {
             if (DAMP == 1) {
-                if (ppre) ppre[e0 + d] = x[d];
+                if (ppre) ppre[f0] = x[d];
                 x[d] *= g;
             }
             if (!(m[d] & kPecBit)) {
@@ -560,10 +590,10 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
                 if (m[d] & kSrcBit) x[d] = fma(a, (T)source_load(src, e0 + d), x[d]);
             }
             if (DAMP == 1) {
-                if (pmid) pmid[e0 + d] = x[d];
+                if (pmid) pmid[f0] = x[d];
                 x[d] *= g;
             }
-            P[e0 + d] = x[d];
+            P[f0] = x[d];
         } else {
             x[d] = T(0);
             if (!(m[d] & kPecBit)) {
@@ -574,27 +604,18 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
     }
     if (minv == nullptr) return;   // force-only use (uniform across the grid)
     T mv[28];
-    const vec4<T> *m4 = reinterpret_cast<const vec4<T> *>(minv + 28 * v);
-#pragma unroll
-    for (int q = 0; q < 7; ++q) {
-        const vec4<T> w = m4[q];
-        mv[4 * q] = w.x; mv[4 * q + 1] = w.y; mv[4 * q + 2] = w.z; mv[4 * q + 3] = w.w;
-    }
+    load_block<T>(minv, nnode, v, mv);
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
-        T y = 0;
-#pragma unroll
-        for (int j = 0; j < 7; ++j) {
-            const int r7 = d < j ? d : j, s7 = d < j ? j : d;
-            y = fma(mv[r7 * (13 - r7) / 2 + s7], x[j], y);
-        }
+        const size_t f0 = (size_t)d * nnode + v;
+        const T y = block_row<T>(mv, x, d);
         if (MODE == 0) {
-            Uout[e0 + d] = fma(c, y, DAMP == 2 ? g * u[d] : u[d]);
-            if (zout) zout[e0 + d] = y;
+            Uout[f0] = fma(c, y, DAMP == 2 ? g * u[d] : u[d]);
+            if (zout) zout[f0] = y;
         } else if (DAMP) {
-            Uout[e0 + d] = (m[d] & kPecBit) ? T(0) : (fma(-c, y, T(2) * u[d]) - (T(1) - g) * Uold[e0 + d]) / (T(1) + g);
+            Uout[f0] = (m[d] & kPecBit) ? T(0) : (fma(-c, y, T(2) * u[d]) - (T(1) - g) * Uold[f0]) / (T(1) + g);
         } else {
-            Uout[e0 + d] = (m[d] & kPecBit) ? T(0) : fma(-c, y, T(2) * u[d] - Uold[e0 + d]);
+            Uout[f0] = (m[d] & kPecBit) ? T(0) : fma(-c, y, T(2) * u[d] - Uold[f0]);
         }
     }
 }
@@ -615,7 +636,7 @@ __global__ void __launch_bounds__(128) tet_loss_adjoint_kernel(size_t nnode, con
     double s = 0.0;
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
-        const size_t e = 7 * v + d;
+        const size_t e = (size_t)d * nnode + v;
         const T pb = Pb[e], pg = g * pb;
         s = fma((double)pb, (double)pmid[e], s);
         s = fma((double)pg, (double)ppre[e], s);
@@ -624,20 +645,22 @@ __global__ void __launch_bounds__(128) tet_loss_adjoint_kernel(size_t nnode, con
     zr[v] += s;
 }
 
-// U += c * Minv P (drift alone).
+// U += c * Minv P (drift alone), one thread per node.
 template <class T>
-__global__ void __launch_bounds__(256) tet_drift_kernel(size_t nnode, const T *__restrict__ minv, const T *__restrict__ P,
+__global__ void __launch_bounds__(128) tet_drift_kernel(size_t nnode, const T *__restrict__ minv, const T *__restrict__ P,
                                                         T *__restrict__ U, T c)
 {
-    size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t v = g >> 3;
-    int d = (int)(g & 7);
-    bool live = v < nnode && d < 7;
-    size_t e = 7 * v + d;
-    T p = live ? P[e] : T(0);
-    if (v >= nnode) v = nnode - 1;
-    T y = block_apply<T>(minv + 28 * v, d, p);
-    if (live) U[e] = fma(c, y, U[e]);
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nnode) return;
+    T x[7], mv[28];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) x[d] = P[(size_t)d * nnode + v];
+    load_block<T>(minv, nnode, v, mv);
+#pragma unroll
+    for (int d = 0; d < 7; ++d) {
+        const size_t f0 = (size_t)d * nnode + v;
+        U[f0] = fma(c, block_row<T>(mv, x, d), U[f0]);
+    }
 }
 
 // Receivers and step counter, one block: at the start of step n = ctl[0],
@@ -647,10 +670,10 @@ __global__ void __launch_bounds__(256) tet_drift_kernel(size_t nnode, const T *_
 // Eight lanes per receiver: lane l < 6 forms its slot's terms, lane 0 sums
 // them in slot order.
 template <class T>
-__global__ void __launch_bounds__(1024) tet_receiver_kernel(int nrec, const int *__restrict__ edges, const double *__restrict__ w,
-                                                            const T *__restrict__ U, const T *__restrict__ P,
-                                                            const T *__restrict__ minv, T unmerge, double *__restrict__ tr,
-                                                            int nsamp, int tf, int *ctl)
+__global__ void __launch_bounds__(1024) tet_receiver_kernel(size_t nnode, int nrec, const int *__restrict__ edges,
+                                                            const double *__restrict__ w, const T *__restrict__ U,
+                                                            const T *__restrict__ P, const T *__restrict__ minv, T unmerge,
+                                                            double *__restrict__ tr, int nsamp, int tf, int *ctl)
 {
     const int step = ctl[0];
     const int l = threadIdx.x & 7;
@@ -658,12 +681,13 @@ __global__ void __launch_bounds__(1024) tet_receiver_kernel(int nrec, const int 
         const int r = r0 + (threadIdx.x >> 3);
         double c[3] = {0, 0, 0};
         if (r < nrec && l < 6) {
-            const int e = edges[6 * r + l];
-            T u = U[e];
+            const size_t e = (size_t)edges[6 * r + l];
+            T u = U[fslot(e, nnode)];
             if (unmerge != T(0)) {
-                const int v = e / 7, dd = e % 7;
+                const size_t v = e / 7;
+                const int dd = (int)(e % 7);
                 T mp = 0;
-                for (int j = 0; j < 7; ++j) mp = fma(minv[28 * (size_t)v + pk7(dd, j)], P[7 * (size_t)v + j], mp);
+                for (int j = 0; j < 7; ++j) mp = fma(minv[fpk(v, pk7(dd, j), nnode)], P[(size_t)j * nnode + v], mp);
                 u = fma(-unmerge, mp, u);
             }
             for (int q = 0; q < 3; ++q) c[q] = (double)u * w[18 * r + 3 * l + q];
@@ -692,44 +716,47 @@ __global__ void __launch_bounds__(1024) tet_receiver_kernel(int nrec, const int 
 // streaming pass per segment, and tet_grad_node_kernel contracts Q with
 // dM_v/deps once at the end.
 
-// Q_v += sum_k c_k sym(y_k z_k^T) over the nk drifts of one segment (eight
-// lanes per node; lane d owns the entries (d, j >= d)).  Drift k = nsub * i
-// + q of the segment starting at step n0 has the coefficient cq[q - 1]
-// (q > 0), cq[nsub - 1] (q = 0, step > 0) or hfirst (the initial half
-// drift).  The products of a time step are summed in T, the steps in FP64.
+// Q_v += sum_k c_k sym(y_k z_k^T) over the nk drifts of one segment, one
+// thread per node (28 packed entries).  Drift k = nsub * i + q of the
+// segment starting at step n0 has the coefficient cq[q - 1] (q > 0),
+// cq[nsub - 1] (q = 0, step > 0) or hfirst (the initial half drift).  The
+// products of a time step are summed in T, the steps in FP64.
 template <class T>
-__global__ void __launch_bounds__(256) tet_grad_accumulate_kernel(size_t nnode, size_t nslot, int nk, int nsub, int n0,
+__global__ void __launch_bounds__(128) tet_grad_accumulate_kernel(size_t nnode, size_t nslot, int nk, int nsub, int n0,
                                                                   T c0, T c1, T c2, T hfirst, const T *__restrict__ ybuf,
                                                                   const T *__restrict__ zbuf, double *__restrict__ Q)
 {
-    size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    size_t v = g >> 3;
-    int d = (int)(g & 7);
-    bool live = v < nnode && d < 7;
-    if (v >= nnode) v = nnode - 1;
-    const size_t e = 7 * v + (d < 7 ? d : 6);
-    const T cq[3] = {c0, c1, c2};
-    double acc[7] = {0, 0, 0, 0, 0, 0, 0};
-    T part[7] = {0, 0, 0, 0, 0, 0, 0};
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nnode) return;
+    double acc[28];
+    T part[28];
+#pragma unroll
+    for (int p = 0; p < 28; ++p) { acc[p] = 0.0; part[p] = T(0); }
+    const T clast = nsub == 3 ? c2 : (nsub == 2 ? c1 : c0);   // cq[nsub - 1]
     for (int k = 0; k < nk; ++k) {
         const int q = k % nsub;
-        const T c = q > 0 ? cq[q - 1] : (n0 + k / nsub > 0 ? cq[nsub - 1] : hfirst);
-        const T y = live ? ybuf[(size_t)k * nslot + e] : T(0), z = live ? zbuf[(size_t)k * nslot + e] : T(0);
+        const T c = q > 0 ? (q == 1 ? c0 : c1) : (n0 + k / nsub > 0 ? clast : hfirst);
+        T y[7], z[7];
 #pragma unroll
-        for (int j = 0; j < 7; ++j) {
-            T yj = __shfl_sync(0xffffffffu, y, j, 8), zj = __shfl_sync(0xffffffffu, z, j, 8);
-            part[j] = fma(c, fma(y, zj, yj * z), part[j]);
+        for (int d = 0; d < 7; ++d) {
+            y[d] = ybuf[(size_t)k * nslot + (size_t)d * nnode + v];
+            z[d] = zbuf[(size_t)k * nslot + (size_t)d * nnode + v];
         }
+#pragma unroll
+        for (int d = 0; d < 7; ++d)
+#pragma unroll
+            for (int j = d; j < 7; ++j) {
+                const int p = d * (13 - d) / 2 + j;
+                part[p] = fma(c, fma(y[d], z[j], y[j] * z[d]), part[p]);
+            }
         if (q == nsub - 1 || k == nk - 1) {
 #pragma unroll
-            for (int j = 0; j < 7; ++j) { acc[j] += (double)part[j]; part[j] = T(0); }
+            for (int p = 0; p < 28; ++p) { acc[p] += (double)part[p]; part[p] = T(0); }
         }
     }
-    if (!live) return;
     double *qv = Q + 28 * v;
 #pragma unroll
-    for (int j = 0; j < 7; ++j)
-        if (j >= d) qv[pk7(d, j)] += 0.5 * acc[j];
+    for (int p = 0; p < 28; ++p) qv[p] += 0.5 * acc[p];
 }
 
 // Receiver adjoint of one sample, one block.  The receivers' edge slots are
@@ -744,13 +771,13 @@ __global__ void __launch_bounds__(1024) tet_receiver_adjoint_kernel(int nsl, con
                                                                     const int *__restrict__ nd_map, double *__restrict__ a_scr,
                                                                     T *__restrict__ Wb, T *__restrict__ Pb,
                                                                     const T *__restrict__ minv, const T *__restrict__ z,
-                                                                    double *__restrict__ Q, double cc)
+                                                                    double *__restrict__ Q, double cc, size_t nnode)
 {
     for (int k = threadIdx.x; k < nsl; k += blockDim.x) {
         double acc = 0.0;
         for (int s = sl_ptr[k]; s < sl_ptr[k + 1]; ++s) acc += term_w[s] * r[term_rc[s]];
         a_scr[k] = acc;
-        Wb[sl_slot[k]] += (T)acc;
+        Wb[fslot((size_t)sl_slot[k], nnode)] += (T)acc;
     }
     if (cc == 0.0) return;
     __syncthreads();
@@ -760,13 +787,13 @@ __global__ void __launch_bounds__(1024) tet_receiver_adjoint_kernel(int nsl, con
         for (int d = 0; d < 7; ++d) {
             int k = nd_map[7 * i + d];
             x[d] = k >= 0 ? (T)a_scr[k] : T(0);
-            zz[d] = z[7 * v + d];
+            zz[d] = z[(size_t)d * nnode + v];
         }
         for (int d = 0; d < 7; ++d) {
             T s = 0;
-            for (int j = 0; j < 7; ++j) s = fma(minv[28 * v + pk7(d, j)], x[j], s);
+            for (int j = 0; j < 7; ++j) s = fma(minv[fpk(v, pk7(d, j), nnode)], x[j], s);
             y[d] = s;
-            Pb[7 * v + d] = fma((T)cc, s, Pb[7 * v + d]);
+            Pb[(size_t)d * nnode + v] = fma((T)cc, s, Pb[(size_t)d * nnode + v]);
         }
         for (int d = 0; d < 7; ++d)
             for (int j = d; j < 7; ++j)
@@ -934,9 +961,9 @@ __global__ void __launch_bounds__(128) tet_energy_node_kernel(size_t nnode, cons
     if (v >= nnode) return;
     double p[7], mv[28];
 #pragma unroll
-    for (int d = 0; d < 7; ++d) p[d] = (double)P[7 * v + d];
+    for (int d = 0; d < 7; ++d) p[d] = (double)P[(size_t)d * nnode + v];
 #pragma unroll
-    for (int q = 0; q < 28; ++q) mv[q] = (double)minv[28 * v + q];
+    for (int q = 0; q < 28; ++q) mv[q] = (double)minv[fpk(v, q, nnode)];
     double s = 0.0;
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
@@ -947,7 +974,7 @@ __global__ void __launch_bounds__(128) tet_energy_node_kernel(size_t nnode, cons
             y = fma(mv[r7 * (13 - r7) / 2 + s7], p[j], y);
         }
         s = fma(0.5 * p[d], y, s);
-        s = fma(0.5 * (double)U[7 * v + d], F[7 * v + d], s);
+        s = fma(0.5 * (double)U[(size_t)d * nnode + v], F[(size_t)d * nnode + v], s);
     }
     e[v] = s;
 }
@@ -1072,7 +1099,7 @@ struct TetFemSim : Sim {
     std::vector<Dipole> dips;
     std::vector<std::array<int, 6>> rec_edges;
     std::vector<std::array<double, 18>> rec_w;
-    DevBuf d_src_slot, d_src_coef, d_src_g, d_rec_e, d_rec_w, d_tr, d_ctl;
+    DevBuf d_src_slot, d_src_coef, d_src_dip, d_src_g, d_rec_e, d_rec_w, d_tr, d_ctl;
     bool ready = false;
     bool flags_dirty = false;       // pec_h gained source bits not yet on the device
     // recording for the adjoint: snapshots of the merged state (U, P) at the
@@ -1414,15 +1441,15 @@ struct TetFemSim : Sim {
         unsigned long long st = 0x9E3779B97F4A7C15ull;
         for (size_t e = 0; e < nslot; ++e) {
             st ^= st << 13; st ^= st >> 7; st ^= st << 17;
-            x0[e] = (pec_h[e] & kPecBit) ? 0.0 : ((double)(st >> 11) / 9007199254740992.0 - 0.5);
+            x0[fslot(e, nnode)] = (pec_h[e] & kPecBit) ? 0.0 : ((double)(st >> 11) / 9007199254740992.0 - 0.5);
         }
-        const unsigned nbn = (unsigned)((8 * nnode + 255) / 256), nbs = (unsigned)((nslot + 255) / 256);
+        const unsigned nb128 = (unsigned)((nnode + 127) / 128), nbs = (unsigned)((nslot + 255) / 256);
         double *cf = coef.as<double>();
         // start pair (v1, Mv1) = (Minv K x0, K x0) / |.|_M, in buffers 1
         EMS_CUDA(cudaMemcpyAsync(vb[0].p, x0.data(), nslot * 8, cudaMemcpyHostToDevice, stream));
         applyK64(vb[0], mb[1]);
         vb[1].zero(stream);
-        tet_drift_kernel<double><<<nbn, 256, 0, stream>>>(nnode, minv_d.as<double>(), mb[1].as<double>(), vb[1].as<double>(), 1.0);
+        tet_drift_kernel<double><<<nb128, 128, 0, stream>>>(nnode, minv_d.as<double>(), mb[1].as<double>(), vb[1].as<double>(), 1.0);
         dot(vb[1], mb[1], part, cf + 2 * max_iters + 2);
         scale_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), cf + 2 * max_iters + 2);
         int prev = -1, cur = 1, nxt = 2;
@@ -1434,7 +1461,7 @@ struct TetFemSim : Sim {
             applyK64(vb[cur], mb[nxt]);
             dot(vb[cur], mb[nxt], part, cf + 2 * j);
             vb[nxt].zero(stream);
-            tet_drift_kernel<double><<<nbn, 256, 0, stream>>>(nnode, minv_d.as<double>(), mb[nxt].as<double>(),
+            tet_drift_kernel<double><<<nb128, 128, 0, stream>>>(nnode, minv_d.as<double>(), mb[nxt].as<double>(),
                                                               vb[nxt].as<double>(), 1.0);
             lanczos_step_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(), vb[cur].as<double>(),
                                                          mb[cur].as<double>(), prev >= 0 ? vb[prev].as<double>() : nullptr,
@@ -1568,7 +1595,7 @@ struct TetFemSim : Sim {
     template <class T>
     int enqueue_step(T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa0, T *zout, T *prec = nullptr)
     {
-        tet_receiver_kernel<T><<<1, 512, 0, stream>>>(nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), Uc, Pc, d_minv.as<T>(),
+        tet_receiver_kernel<T><<<1, 512, 0, stream>>>(nnode, nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), Uc, Pc, d_minv.as<T>(),
                                                       sc.symp ? (T)sc.hfirst : T(0), d_tr.as<double>(), nsamp,
                                                       P.time_frequency, d_ctl.as<int>());
         int nl = 1;
@@ -1615,14 +1642,23 @@ struct TetFemSim : Sim {
         size_t ntr = (size_t)std::max(nobs, 1) * std::max(nsamp, 1) * 4;
         d_tr.alloc(ntr * 8);
         d_tr.zero(stream);
-        std::vector<int> sslot;
+        // source entries sorted by slot, entries of one slot in dipole order
+        std::vector<std::array<int, 2>> ent;   // (slot, dipole * 6 + l)
+        for (size_t k = 0; k < dips.size(); ++k)
+            for (int l = 0; l < 6; ++l) ent.push_back({dips[k].slot[l], (int)(6 * k + l)});
+        std::stable_sort(ent.begin(), ent.end(), [](const std::array<int, 2> &x, const std::array<int, 2> &y) { return x[0] < y[0]; });
+        std::vector<int> sslot, sdip;
         std::vector<double> scoef;
-        for (auto &d : dips)
-            for (int l = 0; l < 6; ++l) { sslot.push_back(d.slot[l]); scoef.push_back(d.coef[l]); }
+        for (auto &en : ent) {
+            sslot.push_back(en[0]);
+            sdip.push_back(en[1] / 6);
+            scoef.push_back(dips[en[1] / 6].coef[en[1] % 6]);
+        }
         int nsrc = (int)sslot.size();
-        if (sslot.empty()) { sslot.push_back(0); scoef.push_back(0.0); }
+        if (sslot.empty()) { sslot.push_back(0); sdip.push_back(0); scoef.push_back(0.0); }
         up(d_src_slot, sslot);
         up(d_src_coef, scoef);
+        up(d_src_dip, sdip);
         if (flags_dirty) {
             EMS_CUDA(cudaMemcpyAsync(d_pec.p, pec_h.data(), nslot, cudaMemcpyHostToDevice, stream));
             flags_dirty = false;
@@ -1644,8 +1680,8 @@ struct TetFemSim : Sim {
         up(d_src_g, gv);
         d_ctl.alloc(16);
         d_ctl.zero(stream);
-        return SrcArgs{nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(), d_src_g.as<double>(), d_ctl.as<int>(), (int)nd,
-                       sc.nsub, 0};
+        return SrcArgs{nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(), d_src_dip.as<int>(), d_src_g.as<double>(),
+                       d_ctl.as<int>(), (int)nd, sc.nsub, 0};
     }
 
     template <class T> void run_t(int nsteps)
@@ -1659,7 +1695,7 @@ struct TetFemSim : Sim {
         std::vector<double> times;
         double t_end = 0.0;
         const SrcArgs sa = prepare_run(nsteps, sc, times, t_end);
-        const unsigned nbn = (unsigned)((8 * nnode + 255) / 256);
+        const unsigned nb128 = (unsigned)((nnode + 127) / 128);
         // symplectic: P in place, U alternating between Uc and Uo; leapfrog
         // ring: Uc = E^n, Pc = E^{n-1}, Uo = scratch for E^{n+1}
         T *Uc = d_U.as<T>(), *Pc = d_P.as<T>(), *Uo = d_Uold.as<T>();
@@ -1714,7 +1750,7 @@ struct TetFemSim : Sim {
         }
         EMS_CUDA(cudaEventRecord(ev0, stream));
         if (symp) {
-            tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)sc.hfirst);
+            tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)sc.hfirst);
             ++launches;
         }
         if (record) {
@@ -1729,7 +1765,7 @@ struct TetFemSim : Sim {
             advance(nsteps);
         }
         if (symp) {
-            tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)(-sc.hfirst));
+            tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)(-sc.hfirst));
             ++launches;
         }
         EMS_CUDA(cudaGetLastError());
@@ -1813,7 +1849,7 @@ struct TetFemSim : Sim {
     {
         const Schedule sc = schedule();
         const int N = rec_nsteps, L = rec_seg, nseg = (N + L - 1) / L, tf = P.time_frequency, nsub = sc.nsub;
-        const unsigned nbt = (unsigned)((ntet + 255) / 256), nbn = (unsigned)((8 * nnode + 255) / 256);
+        const unsigned nbt = (unsigned)((ntet + 255) / 256), nb128 = (unsigned)((nnode + 127) / 128);
         const unsigned nbv = (unsigned)((nnode + 127) / 128), nbv2 = nbv;
         // adjoint sources per sample: r[s][rec][c]
         std::vector<double> rs((size_t)std::max(nsamp, 1) * std::max(nobs, 1) * 3, 0.0);
@@ -1848,7 +1884,7 @@ struct TetFemSim : Sim {
             EMS_CUDA(cudaMemcpyAsync(d_ctl.p, &n0, sizeof(int), cudaMemcpyHostToDevice, stream));
             // z[0] = Minv P at the start of step n0
             EMS_CUDA(cudaMemsetAsync(zb, 0, nslot * w, stream));
-            tet_drift_kernel<T><<<nbn, 256, 0, stream>>>(nnode, d_minv.as<T>(), Pw.as<T>(), zb, T(1));
+            tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pw.as<T>(), zb, T(1));
             T *uc = Uw.as<T>(), *pc = Pw.as<T>(), *uo = Uw2.as<T>();
             for (int n = n0; n < n1; ++n)
                 enqueue_step<T>(uc, pc, uo, sc, sa, zb + ((size_t)(n - n0) * nsub + 1) * nslot,
@@ -1878,11 +1914,11 @@ struct TetFemSim : Sim {
                         ra.nsl, ra.sl_slot.as<int>(), ra.sl_ptr.as<int>(), ra.term_rc.as<int>(), ra.term_w.as<double>(),
                         d_rs.as<double>() + (size_t)(n / tf) * nobs * 3, ra.nnd, ra.nd_node.as<int>(), ra.nd_map.as<int>(),
                         ra.a_scr.as<double>(), Wb.as<T>(), pb, d_minv.as<T>(), z, Q.as<double>(),
-                        0.5 * sc.sub[nsub - 1]);
+                        0.5 * sc.sub[nsub - 1], nnode);
                 }
             }
             // the drifts of this segment: y at [k], z at [k] (k = nsub (n - n0) + q)
-            tet_grad_accumulate_kernel<T><<<nbn, 256, 0, stream>>>(nnode, nslot, (n1 - n0) * nsub, nsub, n0, (T)sc.c[0],
+            tet_grad_accumulate_kernel<T><<<nb128, 128, 0, stream>>>(nnode, nslot, (n1 - n0) * nsub, nsub, n0, (T)sc.c[0],
                                                                    (T)sc.c[1], (T)sc.c[2], (T)sc.hfirst, yb, zb,
                                                                    Q.as<double>());
             EMS_CUDA(cudaGetLastError());
@@ -1993,27 +2029,30 @@ struct TetFemSim : Sim {
         if (which < 0 || which > 1) throw Error{EMS_ERR_INVALID_ARGUMENT, "field index must be 0 (U) or 1 (P)"};
         return nslot;
     }
+    // Fields cross the API in slot order (e = 7 node + d) and live on the
+    // device in the plane layout (fslot).
+    template <class T> void download_slots(const DevBuf &b, double *out) const
+    {
+        std::vector<T> tmp(nslot);
+        EMS_CUDA(cudaMemcpy(tmp.data(), b.p, nslot * sizeof(T), cudaMemcpyDeviceToHost));
+        for (size_t e = 0; e < nslot; ++e) out[e] = (double)tmp[fslot(e, nnode)];
+    }
+    template <class T> void upload_slots(DevBuf &b, const double *in) const
+    {
+        std::vector<T> tmp(nslot);
+        for (size_t e = 0; e < nslot; ++e) tmp[fslot(e, nnode)] = (T)in[e];
+        EMS_CUDA(cudaMemcpy(b.p, tmp.data(), nslot * sizeof(T), cudaMemcpyHostToDevice));
+    }
     void get_field(int which, double *out) const override
     {
         const DevBuf &b = which == 0 ? d_U : d_P;
-        if (fp64) {
-            EMS_CUDA(cudaMemcpy(out, b.p, nslot * 8, cudaMemcpyDeviceToHost));
-        } else {
-            std::vector<float> tmp(nslot);
-            EMS_CUDA(cudaMemcpy(tmp.data(), b.p, nslot * 4, cudaMemcpyDeviceToHost));
-            for (size_t q = 0; q < nslot; ++q) out[q] = tmp[q];
-        }
+        if (fp64) download_slots<double>(b, out); else download_slots<float>(b, out);
     }
     void set_field(int which, const double *in) override
     {
         DevBuf &b = which == 0 ? d_U : d_P;
         fresh = false;
-        if (fp64) {
-            EMS_CUDA(cudaMemcpy(b.p, in, nslot * 8, cudaMemcpyHostToDevice));
-        } else {
-            std::vector<float> tmp(in, in + nslot);
-            EMS_CUDA(cudaMemcpy(b.p, tmp.data(), nslot * 4, cudaMemcpyHostToDevice));
-        }
+        if (fp64) upload_slots<double>(b, in); else upload_slots<float>(b, in);
     }
     void save(const char *path) const override
     {
@@ -2035,8 +2074,8 @@ struct TetFemSim : Sim {
         }
     }
 
-    // f = K u through the curl kernel (per-tet scratch B) and the gather of
-    // the kick kernel (with P = 0 and a = -1 the kick leaves P = F).
+    // f = K u through the force-only fused step (P = f = 0, a = -1 leaves
+    // P = K u), in slot order on both sides.
     void apply_stiffness(const double *u, double *f)
     {
         size_t w = fp64 ? 8 : 4;
@@ -2047,15 +2086,14 @@ struct TetFemSim : Sim {
         const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
         auto body = [&](auto tag) {
             using T = decltype(tag);
-            std::vector<T> h(u, u + nslot);
-            EMS_CUDA(cudaMemcpyAsync(in.p, h.data(), nslot * w, cudaMemcpyHostToDevice, stream));
+            EMS_CUDA(cudaStreamSynchronize(stream));
+            upload_slots<T>(in, u);
             tet_step_kernel<T, 0, 0><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), nullptr,
                                                               out.as<T>(), in.as<T>(), nullptr, nullptr, T(-1), T(0), SrcArgs{},
                                                               nullptr, nullptr, nullptr, nullptr);
             EMS_CUDA(cudaGetLastError());
-            EMS_CUDA(cudaMemcpyAsync(h.data(), out.p, nslot * w, cudaMemcpyDeviceToHost, stream));
             EMS_CUDA(cudaStreamSynchronize(stream));
-            for (size_t q = 0; q < nslot; ++q) f[q] = (double)h[q];
+            download_slots<T>(out, f);
         };
         if (fp64) body(double()); else body(float());
     }

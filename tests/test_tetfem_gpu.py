@@ -249,3 +249,26 @@ def test_step_block_autotuner_picks_a_candidate_and_changes_no_result():
         out[b] = np.load(path)
         os.remove(path)
     assert np.array_equal(out[""], out["32"]) and np.array_equal(out["32"], out["256"])
+
+
+@pytest.mark.parametrize("integ", [oracle.SYMP4, oracle.LEAPFROG], ids=["symp4", "leapfrog"])
+def test_dipoles_sharing_slots_match_oracle(integ):
+    # three dipoles, two of them in the same tetrahedron (their six slots
+    # coincide) and one in a neighbouring cell: the step kernels find a
+    # slot's entries in the sorted source list and sum them in dipole order
+    n = (6, 5, 5)
+    eps, _, recs = _case(n, 17)
+    p = (n[0] * 0.43, n[1] * 0.51, n[2] * 0.46)
+    dips = [(p, (0.2, 0.3, 1.0), 1, 0.08, 1.0), (p, (1.0, -0.5, 0.2), 1, 0.11, 0.7),
+            ((p[0] + 1.0, p[1], p[2]), (0.0, 1.0, 0.3), 1, 0.09, 1.3)]
+    dtn = 0.8 * oracle.stability_constant(integ) / np.sqrt(oracle.tet_lambda_max(n, eps, 300))
+    tr_o, U_o, _ = oracle.tet_run(n, eps, integ, dtn, 120, 1, dips, recs)
+    s = ems.TetFemSimulation(n, H, 1, INTEG[integ], ems.FP64, dt=dtn * TS)
+    s.set_material(eps)
+    for d in dips:
+        s.add_dipole(np.array(d[0]) * H, d[1], ems.WAVE_RICKER, d[3] / TS, d[4])
+    for r in recs:
+        s.add_receiver(np.array(r) * H)
+    s.run(120)
+    assert rel_l2(s.traces()[..., 1:], tr_o[..., 1:]) < FP64_TOL
+    assert rel_l2(s.get_field(0), U_o) < FP64_TOL
