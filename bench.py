@@ -456,10 +456,10 @@ def run_gpu(args):
                 "d2h_bytes_per_step": int(tr.nbytes)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     # DRAM bytes of one kick launch from the ncu capture in
-                     # profiles/tet_kick_tet32_symp4.md (cold fill: the 17 MB
+                     # DRAM bytes of one step launch from the ncu capture in
+                     # profiles/tet_step_tet32_symp4.md (cold fill: the 8.6 MB
                      # working set is L2-resident in the timed loop)
-                     "traffic": 15486208, "kernel": kname, "kernel_us": kms * 1e3, "bytes_per_launch": kbytes,
+                     "traffic": 6598656, "kernel": kname, "kernel_us": kms * 1e3, "bytes_per_launch": kbytes,
                      "threads_per_block": block, "peak_source": peak_kind},
         "clocks": clk,
         "wall_s": wall,
