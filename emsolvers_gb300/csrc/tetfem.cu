@@ -39,7 +39,7 @@ const int kLoc[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
 const int kDir[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
 // Per-slot flag byte: the slot is PEC or unused (no DOF), or it carries a
 // dipole load (only those slots search the source list).
-constexpr unsigned char kPecBit = 1, kSrcBit = 2;
+constexpr unsigned char kPecBit = 1, kSrcBit = 2, kRecBit = 4;   // kRecBit: a receiver reads the slot
 constexpr double kEps0 = 8.8541878128e-12;   // vacuum permittivity, F/m
 
 struct Shape {
@@ -280,9 +280,8 @@ template <class T> __device__ __forceinline__ T block_row(const T (&mv)[28], con
 }
 
 // Point-dipole loads fused into the step kernels: entry k adds
-// coef[k] * g[dip[k]] to slot[k]; g for this (step, substep) is read at
-// g + ((ctl[0]-1)*nsub + q)*nd (the step counter was advanced at the start of
-// the step by the receiver kernel).  The entries are sorted by slot (entries
+// coef[k] * g[dip[k]] to slot[k]; g for this (step n, substep q) is read at
+// g + (n*nsub + q)*nd with n = ctl[par].  The entries are sorted by slot (entries
 // of one slot in dipole order), so a flagged slot finds its entries by
 // binary search: a linear scan of a batch's list (six entries per shot) kept
 // the few warps that hold dipole slots busy long after the rest of the grid.
@@ -294,6 +293,7 @@ struct SrcArgs {
     const double *g;
     const int *ctl;
     int nd, nsub, q;
+    int par;   // the step counter of this step is ctl[par] (double-buffered by step parity)
 };
 
 __device__ __forceinline__ double source_load(const SrcArgs &s, size_t e)
@@ -305,9 +305,74 @@ __device__ __forceinline__ double source_load(const SrcArgs &s, size_t e)
         const int mid = (lo + hi) >> 1;
         if ((size_t)s.slot[mid] < e) lo = mid + 1; else hi = mid;
     }
-    const double *g = s.g + ((size_t)(s.ctl[0] - 1) * s.nsub + s.q) * s.nd;
+    const double *g = s.g + ((size_t)s.ctl[s.par] * s.nsub + s.q) * s.nd;
     for (int k = lo; k < s.n && (size_t)s.slot[k] == e; ++k) f += s.coef[k] * g[s.dip[k]];
     return f;
+}
+
+// Receivers sampled inside the step launches.  The first launch of step n
+// reads the step counter ctl[par] (n) and, from one block beyond the node
+// blocks, records E(x) = sum_l w_l(x) U_l of every receiver when n is a
+// sampling step; U is that launch's input, which no thread of the launch
+// writes.  With the symplectic drifts merged the stored U holds W = U +
+// h Minv P, so the sample subtracts h Minv P of the receiver slots, which
+// the last launch of step n-1 left in rz (double-buffered by parity like the
+// counter, so a one-launch step reads one copy and writes the other).  The
+// first launch also sets ctl[1 - par] = n + 1 for the next step; no launch
+// reads the copy it writes.
+template <class T> struct RecArgs {
+    int nrec;                  // receivers to sample at the start of this step (0: no sampling blocks)
+    int nsb;                   // sampling blocks, the first of the launch
+    const int *edges;          // six slot ids per receiver
+    const int *rk;             // their entries in the receiver-slot list
+    const double *w;           // 18 weights per receiver
+    const T *rz_in;            // Minv P at the receiver slots, start of this step
+    T unmerge;                 // the merged half drift (symplectic), else 0
+    double *tr;
+    int nsamp, tf;
+    int nk;                    // receiver slots (sorted ids in kslot)
+    const int *kslot;
+    const int *kidx;           // per slot, its entry in kslot (read for receiver slots only)
+    T *rz_out;                 // written by the step's last launch for the next step's sampling
+    int *ctl;
+    int par, adv;              // counter parity of this step; advance it in this launch
+};
+
+__device__ __forceinline__ int find_slot(const int *list, int n, size_t e)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if ((size_t)list[mid] < e) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// The sampling blocks (the first nsb blocks of the launch): eight lanes per
+// receiver, lane l < 6 forms its slot's terms (explicitly rounded FP64
+// products), lane 0 sums them in slot order.
+template <class T> __device__ __noinline__ void sample_receivers(const RecArgs<T> rec, const T *__restrict__ U, size_t nnode)
+{
+    const int step = rec.ctl[rec.par];
+    if (step % rec.tf != 0 || step / rec.tf >= rec.nsamp) return;
+    const int l = threadIdx.x & 7, per = blockDim.x >> 3;
+    for (int r0 = blockIdx.x * per; r0 < rec.nrec; r0 += rec.nsb * per) {
+        const int r = r0 + (int)(threadIdx.x >> 3);
+        double c[3] = {0.0, 0.0, 0.0};
+        if (r < rec.nrec && l < 6) {
+            const size_t e = (size_t)rec.edges[6 * r + l];
+            T u = U[fslot(e, nnode)];
+            if (rec.unmerge != T(0)) u = fma(-rec.unmerge, rec.rz_in[rec.rk[6 * r + l]], u);
+            for (int q = 0; q < 3; ++q) c[q] = __dmul_rn((double)u, rec.w[18 * r + 3 * l + q]);
+        }
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int jl = 0; jl < 6; ++jl)
+            for (int q = 0; q < 3; ++q) acc[q] = __dadd_rn(acc[q], __shfl_sync(0xffffffffu, c[q], jl, 8));
+        if (r < rec.nrec && l == 0) {
+            double *o = rec.tr + ((size_t)r * rec.nsamp + step / rec.tf) * 4;
+            o[1] = acc[0]; o[2] = acc[1]; o[3] = acc[2];
+        }
+    }
 }
 
 // ------------------------------------------------------ node-centric step
@@ -535,7 +600,8 @@ __host__ __device__ constexpr int step_record_x(int sy, int mask) { return sy | 
 // given, keep P before the first factor and after the kick); DAMP 2 with
 // MODE 0 is its adjoint, Uout = g Uin + c Minv P; DAMP 1 with MODE 1 is the
 // lossy leapfrog, Uout = (2 Uin - (1 - r) Uold - c Minv (F - f)) / (1 + r)
-// with r = rho dt / 2.
+// with r = rho dt / 2.  REC (the last launch of a symplectic step) also
+// keeps Minv P of the receiver slots in rec.rz_out.
 // Threads per block of the fused step: chosen per handle by timing these
 // candidates on the handle's own mesh (TetFemSim::tune_step_block); small
 // meshes (a 32^3 mesh has 36k nodes) spread better over the 152 SMs in
@@ -543,16 +609,26 @@ __host__ __device__ constexpr int step_record_x(int sy, int mask) { return sy | 
 constexpr int kStepBlocks[4] = {32, 64, 128, 256};
 constexpr int kStepBlockMax = 256;
 
-template <class T, int MODE, int DAMP>
+template <class T, int MODE, int DAMP, int REC = 0>
 __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, const int2 *__restrict__ nrec,
                                                        const unsigned char *__restrict__ pec, const T *__restrict__ minv,
                                                        T *__restrict__ P, const T *__restrict__ Uin, T *__restrict__ Uout,
                                                        const T *__restrict__ Uold, T a, T c, SrcArgs src, T *__restrict__ zout,
-                                                       const T *__restrict__ damp, T *__restrict__ ppre, T *__restrict__ pmid)
+                                                       const T *__restrict__ damp, T *__restrict__ ppre, T *__restrict__ pmid,
+                                                       RecArgs<T> rec)
 {
     constexpr StepTab tab = make_step_tab();
-    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // the first rec.nsb blocks sample the receivers when this launch does
+    // (they run in the first wave, beside the node blocks); the node blocks
+    // follow them
+    const int nb = (int)blockIdx.x - rec.nsb;
+    if (nb < 0) {
+        sample_receivers<T>(rec, Uin, nnode);
+        return;
+    }
+    const size_t v = (size_t)nb * blockDim.x + threadIdx.x;
     if (v >= nnode) return;
+    if (rec.adv && v == 0) rec.ctl[1 - rec.par] = rec.ctl[rec.par] + 1;
     const int2 r = __ldg(nrec + v);
     const int have = (int)((unsigned)r.x >> 26), sy = r.x & 0x3ffffff, sz = r.y;
     const T *u0 = Uin + v;
@@ -571,9 +647,11 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
     unsigned char m[7];
     T x[7], u[7];
     const T g = DAMP ? damp[v] : T(1);
+    int recmask = 0;   // the node's receiver slots (REC)
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
         m[d] = pec[e0 + d];
+        if (REC && (m[d] & kRecBit)) recmask |= 1 << d;
         u[d] = ue[tab.own[d]];
         if (MODE == 0) x[d] = P[(size_t)d * nnode + v];
     }
@@ -612,6 +690,7 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
         if (MODE == 0) {
             Uout[f0] = fma(c, y, DAMP == 2 ? g * u[d] : u[d]);
             if (zout) zout[f0] = y;
+            if (REC && ((recmask >> d) & 1)) rec.rz_out[rec.kidx[e0 + d]] = y;
         } else if (DAMP) {
             Uout[f0] = (m[d] & kPecBit) ? T(0) : (fma(-c, y, T(2) * u[d]) - (T(1) - g) * Uold[f0]) / (T(1) + g);
         } else {
@@ -645,6 +724,22 @@ __global__ void __launch_bounds__(128) tet_loss_adjoint_kernel(size_t nnode, con
     zr[v] += s;
 }
 
+// Minv P at the receiver slots (rz for the sampling at the start of a run
+// or of a recomputed segment), the arithmetic of the step kernel's drift.
+template <class T>
+__global__ void tet_rz_init_kernel(int nk, const int *__restrict__ kslot, size_t nnode, const T *__restrict__ minv,
+                                   const T *__restrict__ P, T *__restrict__ rz)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nk) return;
+    const size_t e = (size_t)kslot[k], v = e / 7;
+    T x[7], mv[28];
+#pragma unroll
+    for (int j = 0; j < 7; ++j) x[j] = P[(size_t)j * nnode + v];
+    load_block<T>(minv, nnode, v, mv);
+    rz[k] = block_row<T>(mv, x, (int)(e % 7));
+}
+
 // U += c * Minv P (drift alone), one thread per node.
 template <class T>
 __global__ void __launch_bounds__(128) tet_drift_kernel(size_t nnode, const T *__restrict__ minv, const T *__restrict__ P,
@@ -661,47 +756,6 @@ __global__ void __launch_bounds__(128) tet_drift_kernel(size_t nnode, const T *_
         const size_t f0 = (size_t)d * nnode + v;
         U[f0] = fma(c, block_row<T>(mv, x, d), U[f0]);
     }
-}
-
-// Receivers and step counter, one block: at the start of step n = ctl[0],
-// record E(x) = sum_l w_l(x) U_l if n is a sampling step, then advance ctl.
-// With the symplectic drifts merged across steps the state holds
-// W = U + h Minv P; the receivers undo that half drift on their six slots.
-// Eight lanes per receiver: lane l < 6 forms its slot's terms, lane 0 sums
-// them in slot order.
-template <class T>
-__global__ void __launch_bounds__(1024) tet_receiver_kernel(size_t nnode, int nrec, const int *__restrict__ edges,
-                                                            const double *__restrict__ w, const T *__restrict__ U,
-                                                            const T *__restrict__ P, const T *__restrict__ minv, T unmerge,
-                                                            double *__restrict__ tr, int nsamp, int tf, int *ctl)
-{
-    const int step = ctl[0];
-    const int l = threadIdx.x & 7;
-    for (int r0 = 0; r0 < nrec && step % tf == 0; r0 += blockDim.x >> 3) {
-        const int r = r0 + (threadIdx.x >> 3);
-        double c[3] = {0, 0, 0};
-        if (r < nrec && l < 6) {
-            const size_t e = (size_t)edges[6 * r + l];
-            T u = U[fslot(e, nnode)];
-            if (unmerge != T(0)) {
-                const size_t v = e / 7;
-                const int dd = (int)(e % 7);
-                T mp = 0;
-                for (int j = 0; j < 7; ++j) mp = fma(minv[fpk(v, pk7(dd, j), nnode)], P[(size_t)j * nnode + v], mp);
-                u = fma(-unmerge, mp, u);
-            }
-            for (int q = 0; q < 3; ++q) c[q] = (double)u * w[18 * r + 3 * l + q];
-        }
-        double acc[3] = {0, 0, 0};
-        for (int j = 0; j < 6; ++j)
-            for (int q = 0; q < 3; ++q) acc[q] += __shfl_sync(0xffffffffu, c[q], j, 8);
-        if (r < nrec && l == 0) {
-            double *o = tr + ((size_t)r * nsamp + step / tf) * 4;
-            o[1] = acc[0]; o[2] = acc[1]; o[3] = acc[2];
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) ctl[0] = step + 1;
 }
 
 // ---------------------------------------------------------------- adjoint
@@ -1099,7 +1153,8 @@ struct TetFemSim : Sim {
     std::vector<Dipole> dips;
     std::vector<std::array<int, 6>> rec_edges;
     std::vector<std::array<double, 18>> rec_w;
-    DevBuf d_src_slot, d_src_coef, d_src_dip, d_src_g, d_rec_e, d_rec_w, d_tr, d_ctl;
+    DevBuf d_src_slot, d_src_coef, d_src_dip, d_src_g, d_rec_e, d_rec_w, d_rec_k, d_kslot, d_kidx, d_rz, d_tr, d_ctl;
+    int nk = 0;   // distinct receiver slots
     bool ready = false;
     bool flags_dirty = false;       // pec_h gained source bits not yet on the device
     // recording for the adjoint: snapshots of the merged state (U, P) at the
@@ -1346,7 +1401,7 @@ struct TetFemSim : Sim {
                     if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
                     tet_step_kernel<T, 0, 0><<<nbv, step_block, 0, stream>>>(
                         nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(),
-                        d_Uold.as<T>(), nullptr, T(0), T(0), SrcArgs{}, nullptr, nullptr, nullptr, nullptr);
+                        d_Uold.as<T>(), nullptr, T(0), T(0), SrcArgs{}, nullptr, nullptr, nullptr, nullptr, RecArgs<T>{});
                 }
             };
             if (fp64) body(double()); else body(float());
@@ -1419,7 +1474,7 @@ struct TetFemSim : Sim {
         const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
         tet_step_kernel<double, 0, 0><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), nullptr,
                                                                z.as<double>(), x.as<double>(), nullptr, nullptr, -1.0, 0.0,
-                                                               SrcArgs{}, nullptr, nullptr, nullptr, nullptr);
+                                                               SrcArgs{}, nullptr, nullptr, nullptr, nullptr, RecArgs<double>{});
     }
 
     // Largest eigenvalue of Minv K by Lanczos in the M inner product.  Minv K
@@ -1572,13 +1627,23 @@ struct TetFemSim : Sim {
     // buffer from Uin.  Returns the number of launches.
     template <class T, int MODE, int DAMP = 0>
     int substep(const T *Uin, T *Uout, T *Pio, const T *Uold, T a, T c, const SrcArgs &sa, T *zout, T *ppre = nullptr,
-                T *pmid = nullptr)
+                T *pmid = nullptr, const RecArgs<T> &rec = RecArgs<T>{})
     {
         if (Uin == Uout) throw Error{EMS_ERR_STATE, "fused step needs separate input and output fields"};
-        const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
+        // rec.nsb leading blocks sample the receivers when this launch does
+        const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block) + (unsigned)rec.nsb;
+        const T *dm = DAMP ? d_damp.as<T>() : nullptr;
+        if constexpr (MODE == 0 && DAMP != 2) {
+            if (rec.rz_out) {
+                tet_step_kernel<T, MODE, DAMP, 1><<<nbv, step_block, 0, stream>>>(
+                    nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), d_minv.as<T>(), Pio, Uin, Uout, Uold, a, c, sa, zout, dm,
+                    ppre, pmid, rec);
+                return 1;
+            }
+        }
         tet_step_kernel<T, MODE, DAMP><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(),
-                                                                        d_minv.as<T>(), Pio, Uin, Uout, Uold, a, c, sa, zout,
-                                                                        DAMP ? d_damp.as<T>() : nullptr, ppre, pmid);
+                                                                        d_minv.as<T>(), Pio, Uin, Uout, Uold, a, c, sa, zout, dm,
+                                                                        ppre, pmid, rec);
         return 1;
     }
 
@@ -1592,33 +1657,76 @@ struct TetFemSim : Sim {
     // With losses the middle kick of a symplectic step is the lossy one;
     // prec (recorded runs) receives P before its first loss factor and
     // after the kick, at prec and prec + nslot.
-    template <class T>
-    int enqueue_step(T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa0, T *zout, T *prec = nullptr)
+    // Receiver arguments of substep q of a step with counter parity par:
+    // the first launch samples (and advances the counter), the last one of
+    // a symplectic step keeps Minv P of the receiver slots for the next.
+    template <class T> RecArgs<T> rec_args(const Schedule &sc, int q, int par)
     {
-        tet_receiver_kernel<T><<<1, 512, 0, stream>>>(nnode, nobs, d_rec_e.as<int>(), d_rec_w.as<double>(), Uc, Pc, d_minv.as<T>(),
-                                                      sc.symp ? (T)sc.hfirst : T(0), d_tr.as<double>(), nsamp,
-                                                      P.time_frequency, d_ctl.as<int>());
-        int nl = 1;
+        RecArgs<T> r{};
+        const int nrz = std::max(nk, 1);
+        if (q == 0) {
+            r.nrec = nobs;
+            r.nsb = nobs > 0 ? (nobs + step_block / 8 - 1) / (step_block / 8) : 0;   // eight lanes per receiver
+            r.adv = 1;
+        }
+        r.edges = d_rec_e.as<int>();
+        r.rk = d_rec_k.as<int>();
+        r.w = d_rec_w.as<double>();
+        r.rz_in = d_rz.as<T>() + (size_t)par * nrz;
+        r.unmerge = sc.symp ? (T)sc.hfirst : T(0);
+        r.tr = d_tr.as<double>();
+        r.nsamp = nsamp;
+        r.tf = P.time_frequency;
+        r.nk = nk;
+        r.kslot = d_kslot.as<int>();
+        r.kidx = d_kidx.as<int>();
+        if (sc.symp && q == sc.nsub - 1 && nk > 0) r.rz_out = d_rz.as<T>() + (size_t)(1 - par) * nrz;
+        r.ctl = d_ctl.as<int>();
+        r.par = par;
+        return r;
+    }
+
+    // One time step n (counter parity par = n % 2).  Returns the number of
+    // launches.
+    template <class T>
+    int enqueue_step(T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa0, T *zout, int par, T *prec = nullptr)
+    {
+        int nl = 0;
         if (sc.symp) {
             for (int q = 0; q < sc.nsub; ++q) {
                 SrcArgs sa = sa0;
                 sa.q = q;
+                sa.par = par;
+                const RecArgs<T> ra = rec_args<T>(sc, q, par);
                 T *z = zout ? zout + (size_t)q * nslot : nullptr;
                 if (has_loss && q == sc.nsub / 2)
                     nl += substep<T, 0, 1>(Uc, Uo, Pc, nullptr, (T)sc.sub[q], (T)sc.c[q], sa, z, prec,
-                                           prec ? prec + nslot : nullptr);
+                                           prec ? prec + nslot : nullptr, ra);
                 else
-                    nl += substep<T, 0>(Uc, Uo, Pc, nullptr, (T)sc.sub[q], (T)sc.c[q], sa, z);
+                    nl += substep<T, 0>(Uc, Uo, Pc, nullptr, (T)sc.sub[q], (T)sc.c[q], sa, z, nullptr, nullptr, ra);
                 std::swap(Uc, Uo);
             }
         } else {
+            SrcArgs sa = sa0;
+            sa.par = par;
+            const RecArgs<T> ra = rec_args<T>(sc, 0, par);
             if (has_loss)
-                nl += substep<T, 1, 1>(Uc, Uo, nullptr, Pc, T(0), (T)(dtn * dtn), sa0, nullptr);
+                nl += substep<T, 1, 1>(Uc, Uo, nullptr, Pc, T(0), (T)(dtn * dtn), sa, nullptr, nullptr, nullptr, ra);
             else
-                nl += substep<T, 1>(Uc, Uo, nullptr, Pc, T(0), (T)(dtn * dtn), sa0, nullptr);
+                nl += substep<T, 1>(Uc, Uo, nullptr, Pc, T(0), (T)(dtn * dtn), sa, nullptr, nullptr, nullptr, ra);
             T *tmp = Pc; Pc = Uc; Uc = Uo; Uo = tmp;
         }
         return nl;
+    }
+
+    // Minv P of the receiver slots into rz[par] (symplectic runs, before the
+    // first step of a run or of a recomputed segment).
+    template <class T> void rz_init(const T *Pc, int par)
+    {
+        if (nk == 0) return;
+        const int nrz = std::max(nk, 1);
+        tet_rz_init_kernel<T><<<(nk + 127) / 128, 128, 0, stream>>>(nk, d_kslot.as<int>(), nnode, d_minv.as<T>(), Pc,
+                                                                     d_rz.as<T>() + (size_t)par * nrz);
     }
 
     // Uploads the receivers, the dipole table and the per-substep source
@@ -1636,9 +1744,31 @@ struct TetFemSim : Sim {
             re.insert(re.end(), rec_edges[r].begin(), rec_edges[r].end());
             rw.insert(rw.end(), rec_w[r].begin(), rec_w[r].end());
         }
-        if (re.empty()) { re.assign(6, 0); rw.assign(18, 0.0); }
+        // the receivers' distinct slots (sorted), each receiver slot's entry
+        // among them, and the flag bit that makes the step kernel keep
+        // Minv P of those slots
+        std::vector<int> ks(re.begin(), re.end());
+        std::sort(ks.begin(), ks.end());
+        ks.erase(std::unique(ks.begin(), ks.end()), ks.end());
+        std::vector<int> rk(re.size());
+        for (size_t q = 0; q < re.size(); ++q) rk[q] = (int)(std::lower_bound(ks.begin(), ks.end(), re[q]) - ks.begin());
+        for (size_t e = 0; e < nslot; ++e)
+            if (pec_h[e] & kRecBit) { pec_h[e] &= (unsigned char)~kRecBit; flags_dirty = true; }
+        for (int e : ks) { pec_h[e] |= kRecBit; flags_dirty = true; }
+        nk = (int)ks.size();
+        if (re.empty()) { re.assign(6, 0); rw.assign(18, 0.0); rk.assign(6, 0); }
+        if (ks.empty()) ks.push_back(0);
         up(d_rec_e, re);
         up(d_rec_w, rw);
+        up(d_rec_k, rk);
+        up(d_kslot, ks);
+        {
+            std::vector<int> kidx(nslot, -1);
+            for (int k = 0; k < nk; ++k) kidx[ks[k]] = k;
+            up(d_kidx, kidx);
+        }
+        d_rz.alloc(2 * ks.size() * (fp64 ? 8 : 4));
+        d_rz.zero(stream);
         size_t ntr = (size_t)std::max(nobs, 1) * std::max(nsamp, 1) * 4;
         d_tr.alloc(ntr * 8);
         d_tr.zero(stream);
@@ -1681,7 +1811,7 @@ struct TetFemSim : Sim {
         d_ctl.alloc(16);
         d_ctl.zero(stream);
         return SrcArgs{nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(), d_src_dip.as<int>(), d_src_g.as<double>(),
-                       d_ctl.as<int>(), (int)nd, sc.nsub, 0};
+                       d_ctl.as<int>(), (int)nd, sc.nsub, 0, 0};
     }
 
     template <class T> void run_t(int nsteps)
@@ -1700,28 +1830,31 @@ struct TetFemSim : Sim {
         // ring: Uc = E^n, Pc = E^{n-1}, Uo = scratch for E^{n+1}
         T *Uc = d_U.as<T>(), *Pc = d_P.as<T>(), *Uo = d_Uold.as<T>();
         // CUDA graphs of kGraphSteps steps, replayed.  kGraphSteps is a
-        // multiple of 3 and even, so the leapfrog ring and the symplectic U
-        // pair return to the assignment a graph was captured with; a single
-        // symp4 step (three substeps) swaps the U pair, so a recorded run
-        // keeps one graph per assignment.
+        // multiple of 3 and even, so the leapfrog ring, the symplectic U
+        // pair and the counter parity return to the assignment a graph was
+        // captured with; a single symp4 or symp2 step swaps the U pair and
+        // the parity together, so a recorded run keeps one graph per
+        // assignment.
         constexpr int kGraphSteps = 12;
         struct StepGraph {   // destroyed on every exit path
             cudaGraph_t g = nullptr;
             cudaGraphExec_t exec = nullptr;
             const void *start = nullptr;
+            int par = 0;
             ~StepGraph()
             {
                 if (exec) cudaGraphExecDestroy(exec);
                 if (g) cudaGraphDestroy(g);
             }
         } graph[2];
-        int per_graph = 0;
-        auto capture = [&](StepGraph &G, T *u, T *p, T *o) {
+        int per_graph = 0, par = 0;   // par: parity of the next step's counter copy
+        auto capture = [&](StepGraph &G, T *u, T *p, T *o, int par0) {
             G.start = u;
+            G.par = par0;
             int nl = 0;
             EMS_CUDA(cudaStreamSynchronize(stream));
             EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-            for (int st = 0; st < kGraphSteps; ++st) nl += enqueue_step<T>(u, p, o, sc, sa, nullptr);
+            for (int st = 0; st < kGraphSteps; ++st) nl += enqueue_step<T>(u, p, o, sc, sa, nullptr, (par0 + st) & 1);
             cudaError_t ce = cudaStreamEndCapture(stream, &G.g);
             if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
             ce = cudaGraphInstantiate(&G.exec, G.g, 0);
@@ -1732,11 +1865,14 @@ struct TetFemSim : Sim {
         auto advance = [&](int k) {
             cudaGraphExec_t exec = nullptr;
             for (auto &G : graph)
-                if (G.exec && G.start == Uc) exec = G.exec;
+                if (G.exec && G.start == Uc && G.par == par) exec = G.exec;
             const int nrep = exec ? k / kGraphSteps : 0;
             for (int r = 0; r < nrep; ++r) EMS_CUDA(cudaGraphLaunch(exec, stream));
             launches += (long long)nrep * per_graph;
-            for (int st = nrep * kGraphSteps; st < k; ++st) launches += enqueue_step<T>(Uc, Pc, Uo, sc, sa, nullptr);
+            for (int st = nrep * kGraphSteps; st < k; ++st) {
+                launches += enqueue_step<T>(Uc, Pc, Uo, sc, sa, nullptr, par);
+                par ^= 1;
+            }
         };
         int seg_len = 0, nseg = 0;
         if (record) {
@@ -1745,13 +1881,14 @@ struct TetFemSim : Sim {
             d_snap.alloc((size_t)nseg * 2 * nslot * sizeof(T));
         }
         if ((record ? seg_len : nsteps) >= kGraphSteps) {
-            capture(graph[0], Uc, Pc, Uo);
-            if (record && symp && sc.nsub % 2 == 1) capture(graph[1], Uo, Pc, Uc);
+            capture(graph[0], Uc, Pc, Uo, 0);
+            if (record && symp && sc.nsub % 2 == 1) capture(graph[1], Uo, Pc, Uc, 1);
         }
         EMS_CUDA(cudaEventRecord(ev0, stream));
         if (symp) {
             tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)sc.hfirst);
-            ++launches;
+            rz_init<T>(Pc, 0);
+            launches += nk > 0 ? 2 : 1;
         }
         if (record) {
             // snapshot of the merged state at the start of every segment
@@ -1881,13 +2018,14 @@ struct TetFemSim : Sim {
             const T *snap = d_snap.as<T>() + (size_t)s * 2 * nslot;
             EMS_CUDA(cudaMemcpyAsync(Uw.p, snap, nslot * w, cudaMemcpyDeviceToDevice, stream));
             EMS_CUDA(cudaMemcpyAsync(Pw.p, snap + nslot, nslot * w, cudaMemcpyDeviceToDevice, stream));
-            EMS_CUDA(cudaMemcpyAsync(d_ctl.p, &n0, sizeof(int), cudaMemcpyHostToDevice, stream));
+            EMS_CUDA(cudaMemcpyAsync(d_ctl.as<int>() + (n0 & 1), &n0, sizeof(int), cudaMemcpyHostToDevice, stream));
+            rz_init<T>(Pw.as<T>(), n0 & 1);
             // z[0] = Minv P at the start of step n0
             EMS_CUDA(cudaMemsetAsync(zb, 0, nslot * w, stream));
             tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pw.as<T>(), zb, T(1));
             T *uc = Uw.as<T>(), *pc = Pw.as<T>(), *uo = Uw2.as<T>();
             for (int n = n0; n < n1; ++n)
-                enqueue_step<T>(uc, pc, uo, sc, sa, zb + ((size_t)(n - n0) * nsub + 1) * nslot,
+                enqueue_step<T>(uc, pc, uo, sc, sa, zb + ((size_t)(n - n0) * nsub + 1) * nslot, n & 1,
                                 has_loss ? pstore.as<T>() + (size_t)(n - n0) * 2 * nslot : nullptr);
             for (int n = n1 - 1; n >= n0; --n) {
                 for (int q = nsub - 1; q >= 0; --q) {
@@ -2090,7 +2228,7 @@ struct TetFemSim : Sim {
             upload_slots<T>(in, u);
             tet_step_kernel<T, 0, 0><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), nullptr,
                                                               out.as<T>(), in.as<T>(), nullptr, nullptr, T(-1), T(0), SrcArgs{},
-                                                              nullptr, nullptr, nullptr, nullptr);
+                                                              nullptr, nullptr, nullptr, nullptr, RecArgs<T>{});
             EMS_CUDA(cudaGetLastError());
             EMS_CUDA(cudaStreamSynchronize(stream));
             download_slots<T>(out, f);
@@ -2129,7 +2267,7 @@ struct TetFemSim : Sim {
                 if (r % 2) std::swap(a, b);
                 tet_step_kernel<T, 0, 0><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(),
                                                                          d_minv.as<T>(), d_P.as<T>(), a, b, nullptr, T(0), T(0),
-                                                                         SrcArgs{}, nullptr, nullptr, nullptr, nullptr);
+                                                                         SrcArgs{}, nullptr, nullptr, nullptr, nullptr, RecArgs<T>{});
             }
         };
         if (fp64) body(double()); else body(float());
