@@ -338,16 +338,6 @@ template <class T> struct RecArgs {
     int par, adv;              // counter parity of this step; advance it in this launch
 };
 
-__device__ __forceinline__ int find_slot(const int *list, int n, size_t e)
-{
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if ((size_t)list[mid] < e) lo = mid + 1; else hi = mid;
-    }
-    return lo;
-}
-
 // The sampling blocks (the first nsb blocks of the launch): eight lanes per
 // receiver, lane l < 6 forms its slot's terms (explicitly rounded FP64
 // products), lane 0 sums them in slot order.
@@ -1481,9 +1471,11 @@ struct TetFemSim : Sim {
     // is self-adjoint there, and every Lanczos vector v travels with its mass
     // image Mv: K v is the mass image of w = Minv K v, so <v, w>_M = v.K v and
     // <w, w>_M = w.(M w) need no M.  The start pair is x = Minv K x0, Mx =
-    // K x0.  The tridiagonal coefficients stay on the device; every 20 steps
+    // K x0.  The tridiagonal coefficients stay on the device; every 10 steps
     // the largest eigenvalue of the tridiagonal matrix (Sturm bisection) is
-    // checked and the iteration stops once it changes by less than 1e-10.
+    // checked and the iteration stops once it changes by less than 1e-9
+    // relative (the time step is a fraction of the limit; 1e-9 is far below
+    // any effect on it).
     // Without reorthogonalisation converged Ritz values repeat, which does
     // not move the largest one.
     double lambda_max_lanczos(const DevBuf &minv_d, int max_iters)
@@ -1526,13 +1518,13 @@ struct TetFemSim : Sim {
             scale_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(), cf + 2 * j + 1);
             const int t = prev < 0 ? 0 : prev;
             prev = cur; cur = nxt; nxt = t;
-            if ((j + 1) % 20 == 0 || j + 1 == max_iters) {
+            if ((j + 1) % 10 == 0 || j + 1 == max_iters) {
                 h.resize(2 * (j + 1));
                 EMS_CUDA(cudaMemcpyAsync(h.data(), cf, h.size() * 8, cudaMemcpyDeviceToHost, stream));
                 EMS_CUDA(cudaStreamSynchronize(stream));
                 lam = tridiag_max_eig(h, j + 1);
                 const bool breakdown = !(h[2 * j + 1] > 1e-300);
-                if (breakdown || std::fabs(lam - lam_old) <= 1e-10 * lam) break;
+                if (breakdown || std::fabs(lam - lam_old) <= 1e-9 * lam) break;
                 lam_old = lam;
             }
         }
