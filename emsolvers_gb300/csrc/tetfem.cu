@@ -1032,7 +1032,11 @@ template <class T> __global__ void widen_kernel(size_t n, const T *__restrict__ 
 
 // *out = sum of the nb <= 512 partial sums, by a fixed-shape tree (one
 // block of 512 threads; deterministic).
-__global__ void __launch_bounds__(512) dot_finish_kernel(int nb, const double *__restrict__ part, double *__restrict__ out)
+// With jp given, the coefficient pointers of the Lanczos kernels below are
+// offset by 2 * (*jp): the iteration index lives on the device so that a
+// captured graph of iterations can be replayed.
+__global__ void __launch_bounds__(512) dot_finish_kernel(int nb, const double *__restrict__ part, double *__restrict__ out,
+                                                         const int *__restrict__ jp = nullptr)
 {
     __shared__ double sh[512];
     const int t = threadIdx.x;
@@ -1042,15 +1046,21 @@ __global__ void __launch_bounds__(512) dot_finish_kernel(int nb, const double *_
         if (t < w) sh[t] += sh[t + w];
         __syncthreads();
     }
-    if (t == 0) *out = sh[0];
+    if (t == 0) out[jp ? 2 * *jp : 0] = sh[0];
 }
 
 // x, y *= 1 / sqrt(*nrm)
-__global__ void scale_kernel(size_t n, double *x, double *y, const double *__restrict__ nrm)
+__global__ void scale_kernel(size_t n, double *x, double *y, const double *__restrict__ nrm, const int *__restrict__ jp = nullptr)
 {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const double s = 1.0 / sqrt(*nrm);
+    const double s = 1.0 / sqrt(nrm[jp ? 2 * *jp : 0]);
     if (i < n) { x[i] *= s; y[i] *= s; }
+}
+
+// The device iteration index of a captured Lanczos graph, advanced once per iteration.
+__global__ void inc_kernel(int *jp)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) *jp += 1;
 }
 
 // Lanczos three-term step on a vector and its mass image:
@@ -1058,11 +1068,13 @@ __global__ void scale_kernel(size_t n, double *x, double *y, const double *__res
 __global__ void lanczos_step_kernel(size_t n, double *__restrict__ w, double *__restrict__ Mw, const double *__restrict__ v,
                                     const double *__restrict__ Mv, const double *__restrict__ vp,
                                     const double *__restrict__ Mvp, const double *__restrict__ a,
-                                    const double *__restrict__ b2)
+                                    const double *__restrict__ b2, const int *__restrict__ jp = nullptr)
 {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double al = *a, be = b2 ? sqrt(*b2) : 0.0;
+    // with jp: a = alpha_0's slot, b2 = beta_1^2's slot (iteration j reads beta_j^2)
+    const int o = jp ? 2 * *jp : 0;
+    const double al = a[o], be = b2 ? sqrt(b2[jp ? o - 2 : 0]) : 0.0;
     w[i] = w[i] - al * v[i] - be * (vp ? vp[i] : 0.0);
     Mw[i] = Mw[i] - al * Mv[i] - be * (Mvp ? Mvp[i] : 0.0);
 }
@@ -1450,11 +1462,11 @@ struct TetFemSim : Sim {
 
     // *out = x.y on the device (deterministic: block partials, then their
     // sum in order)
-    void dot(const DevBuf &x, const DevBuf &y, DevBuf &part, double *out)
+    void dot(const DevBuf &x, const DevBuf &y, DevBuf &part, double *out, const int *jp = nullptr)
     {
         const int nb = 512;
         dot_partial_kernel<<<nb, 256, 0, stream>>>(nslot, x.as<double>(), y.as<double>(), part.as<double>());
-        dot_finish_kernel<<<1, 512, 0, stream>>>(nb, part.as<double>(), out);
+        dot_finish_kernel<<<1, 512, 0, stream>>>(nb, part.as<double>(), out, jp);
     }
 
     // z = K x in FP64 through the force-only fused step (P = z = 0, a = -1)
@@ -1471,7 +1483,7 @@ struct TetFemSim : Sim {
     // is self-adjoint there, and every Lanczos vector v travels with its mass
     // image Mv: K v is the mass image of w = Minv K v, so <v, w>_M = v.K v and
     // <w, w>_M = w.(M w) need no M.  The start pair is x = Minv K x0, Mx =
-    // K x0.  The tridiagonal coefficients stay on the device; every 10 steps
+    // K x0.  The tridiagonal coefficients stay on the device; every 9 steps
     // the largest eigenvalue of the tridiagonal matrix (Sturm bisection) is
     // checked and the iteration stops once it changes by less than 1e-9
     // relative (the time step is a fraction of the limit; 1e-9 is far below
@@ -1483,7 +1495,7 @@ struct TetFemSim : Sim {
         DevBuf vb[3], mb[3], part, coef;
         for (int q = 0; q < 3; ++q) { vb[q].alloc(nslot * 8); mb[q].alloc(nslot * 8); }
         part.alloc(512 * 8);
-        coef.alloc(2 * (max_iters + 2) * 8);   // alpha_j at [2j], beta_{j+1}^2 at [2j+1]
+        coef.alloc(2 * (max_iters + 6) * 8);   // alpha_j at [2j], beta_{j+1}^2 at [2j+1]; scratch at the end
         std::vector<double> x0(nslot);
         unsigned long long st = 0x9E3779B97F4A7C15ull;
         for (size_t e = 0; e < nslot; ++e) {
@@ -1497,33 +1509,64 @@ struct TetFemSim : Sim {
         applyK64(vb[0], mb[1]);
         vb[1].zero(stream);
         tet_drift_kernel<double><<<nb128, 128, 0, stream>>>(nnode, minv_d.as<double>(), mb[1].as<double>(), vb[1].as<double>(), 1.0);
-        dot(vb[1], mb[1], part, cf + 2 * max_iters + 2);
-        scale_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), cf + 2 * max_iters + 2);
+        dot(vb[1], mb[1], part, cf + 2 * max_iters + 10);
+        scale_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), cf + 2 * max_iters + 10);
         int prev = -1, cur = 1, nxt = 2;
-        std::vector<double> h;
-        double lam = 0.0, lam_old = -1.0;
-        int j = 0;
-        for (; j < max_iters; ++j) {
+        // one iteration; jp == nullptr: host index jj, else the device index
+        auto iteration = [&](int jj, const int *jp) {
             // w = Minv K v (mass image K v), alpha = v.K v
             applyK64(vb[cur], mb[nxt]);
-            dot(vb[cur], mb[nxt], part, cf + 2 * j);
+            dot(vb[cur], mb[nxt], part, jp ? cf : cf + 2 * jj, jp);
             vb[nxt].zero(stream);
             tet_drift_kernel<double><<<nb128, 128, 0, stream>>>(nnode, minv_d.as<double>(), mb[nxt].as<double>(),
                                                               vb[nxt].as<double>(), 1.0);
             lanczos_step_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(), vb[cur].as<double>(),
                                                          mb[cur].as<double>(), prev >= 0 ? vb[prev].as<double>() : nullptr,
-                                                         prev >= 0 ? mb[prev].as<double>() : nullptr, cf + 2 * j,
-                                                         j > 0 ? cf + 2 * j - 1 : nullptr);
-            dot(vb[nxt], mb[nxt], part, cf + 2 * j + 1);   // beta_{j+1}^2
-            scale_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(), cf + 2 * j + 1);
+                                                         prev >= 0 ? mb[prev].as<double>() : nullptr, jp ? cf : cf + 2 * jj,
+                                                         jp ? cf + 1 : (jj > 0 ? cf + 2 * jj - 1 : nullptr), jp);
+            dot(vb[nxt], mb[nxt], part, jp ? cf + 1 : cf + 2 * jj + 1, jp);   // beta_{j+1}^2
+            scale_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(),
+                                                  jp ? cf + 1 : cf + 2 * jj + 1, jp);
+            if (jp) inc_kernel<<<1, 32, 0, stream>>>(const_cast<int *>(jp));
             const int t = prev < 0 ? 0 : prev;
             prev = cur; cur = nxt; nxt = t;
-            if ((j + 1) % 10 == 0 || j + 1 == max_iters) {
-                h.resize(2 * (j + 1));
+        };
+        iteration(0, nullptr);
+        // iterations 1, 2, 3, ...: after the first, the three buffers rotate
+        // with period 3, so one captured graph of three iterations (the
+        // coefficient index on the device) is replayed; the largest Ritz
+        // value is checked every nine iterations
+        struct Graph {   // destroyed on every exit path
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t exec = nullptr;
+            ~Graph()
+            {
+                if (exec) cudaGraphExecDestroy(exec);
+                if (g) cudaGraphDestroy(g);
+            }
+        } graph;
+        DevBuf jbuf;
+        jbuf.alloc(sizeof(int));
+        const int one = 1;
+        EMS_CUDA(cudaMemcpyAsync(jbuf.p, &one, sizeof(int), cudaMemcpyHostToDevice, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        for (int q = 0; q < 3; ++q) iteration(0, jbuf.as<int>());
+        cudaError_t ce = cudaStreamEndCapture(stream, &graph.g);
+        if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
+        ce = cudaGraphInstantiate(&graph.exec, graph.g, 0);
+        if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+        std::vector<double> h;
+        double lam = 0.0, lam_old = -1.0;
+        for (int done = 1, rep = 1; done < max_iters; ++rep) {
+            EMS_CUDA(cudaGraphLaunch(graph.exec, stream));
+            done += 3;
+            if (rep % 3 == 0 || done >= max_iters) {
+                h.resize(2 * done);
                 EMS_CUDA(cudaMemcpyAsync(h.data(), cf, h.size() * 8, cudaMemcpyDeviceToHost, stream));
                 EMS_CUDA(cudaStreamSynchronize(stream));
-                lam = tridiag_max_eig(h, j + 1);
-                const bool breakdown = !(h[2 * j + 1] > 1e-300);
+                lam = tridiag_max_eig(h, done);
+                const bool breakdown = !(h[2 * done - 1] > 1e-300);
                 if (breakdown || std::fabs(lam - lam_old) <= 1e-9 * lam) break;
                 lam_old = lam;
             }
