@@ -5,17 +5,22 @@
 // symplectic_4/fem_simulation.cpp:1347-1350, fem_v2/fem_simulation.cpp:
 // 627-654) to a mesh of cubes split into six Kuhn tetrahedra:
 //
-//   DOF layout   edge slot 7*node + d, d over the 7 edge directions leaving a
-//                node; node-major, so the 7 edges of a node are contiguous.
-//   K apply      tet_curl_kernel: per tetrahedron, B_T = |T|/mu_T curl(E|_T)
-//                (3 values); tet_node_kernel: one thread per node gathers
-//                the curl-transpose of its 7 slots from the node's 18
-//                incident tetrahedra (each B read once per node, in
-//                ascending tetrahedron order: deterministic, no atomics).
+//   DOF names    edge slot e = 7*node + d, d over the 7 edge directions
+//                leaving a node (mesh tables, flags, the API).
+//   layout       the time loop's arrays in planes: slot d of node v at
+//                d*nnode + v (fslot); packed mass blocks in seven vec4 planes.
+//   time step    tet_step_kernel, one thread per node and one launch per
+//                substep: the curls of the node's 18 tetrahedra recomputed
+//                from the 43 edge values around it (no per-tetrahedron array
+//                in the loop), the curl-transpose summed over them in
+//                ascending tetrahedron order (deterministic, no atomics), the
+//                kick, the mass-block drift; U alternates between two
+//                buffers.  The receivers are sampled by leading blocks of a
+//                step's first launch.
 //   mass inverse per-node 7x7 blocks, built and inverted in FP64 on the GPU
 //                (tet_minv_setup_kernel), stored packed symmetric in the run
-//                precision; applied inside tet_node_kernel from registers.
-//   adjoint      the same kernels run the reversed steps (see "adjoint").
+//                precision; applied inside tet_step_kernel from registers.
+//   adjoint      the same kernel runs the reversed steps (see "adjoint").
 // Units are normalised (cube edge 1, c0 = 1); the API converts.
 #include <cuda_runtime.h>
 
@@ -749,13 +754,14 @@ __global__ void __launch_bounds__(128) tet_drift_kernel(size_t nnode, const T *_
 }
 
 // ---------------------------------------------------------------- adjoint
-// The discrete adjoint of the merged symplectic loop runs the same two
-// launches per substep backward in time.  Only the mass blocks depend on
+// The discrete adjoint of the merged symplectic loop runs the same step
+// launch per substep backward in time.  Only the mass blocks depend on
 // eps, so each drift U += c Minv P adds
 // -c (Minv Ubar)^T dM (Minv P) to dJ/deps.  The adjoint substep is the
 // forward one with the roles swapped (curl of Pbar, kick on Ubar, drift on
-// Pbar), storing y = Minv Ubar of every drift of a segment next to the
-// forward z = Minv P; tet_grad_accumulate_kernel then sums the outer products per node
+// Pbar; Pbar alternates between two buffers like U), storing y = Minv Ubar
+// of every drift of a segment next to the forward z = Minv P;
+// tet_grad_accumulate_kernel then sums the outer products per node
 // (Q_v += c sym(y z^T), FP64, packed symmetric like the mass blocks) in one
 // streaming pass per segment, and tet_grad_node_kernel contracts Q with
 // dM_v/deps once at the end.

@@ -272,3 +272,24 @@ def test_dipoles_sharing_slots_match_oracle(integ):
     s.run(120)
     assert rel_l2(s.traces()[..., 1:], tr_o[..., 1:]) < FP64_TOL
     assert rel_l2(s.get_field(0), U_o) < FP64_TOL
+
+
+@pytest.mark.parametrize("integ", [oracle.SYMP2, oracle.SYMP4, oracle.LEAPFROG], ids=["symp2", "symp4", "leapfrog"])
+def test_a_continued_run_matches_one_long_run(integ):
+    # the second run restarts the step counter and the receivers' Minv P
+    # buffer; its traces are the tail of one run over both intervals (FP64;
+    # the symplectic runs close and reopen the merged half drift in between,
+    # which changes the last bits only)
+    n = (6, 5, 5)
+    eps, dip, recs = _case(n, 21)
+    dtn = 0.8 * oracle.stability_constant(integ) / np.sqrt(oracle.tet_lambda_max(n, eps, 300))
+    one = _gpu(n, eps, dip, recs, integ, dtn, 75, ems.FP64)
+    two = _gpu(n, eps, dip, recs, integ, dtn, 40, ems.FP64)
+    first = two.traces()
+    two.run(35)
+    second = two.traces()
+    full = one.traces()
+    np.testing.assert_allclose(first[..., 0], full[:, :40, 0], rtol=1e-12)
+    np.testing.assert_allclose(second[..., 0], full[:, 40:, 0], rtol=1e-12)
+    assert rel_l2(first[..., 1:], full[:, :40, 1:]) < 1e-13
+    assert rel_l2(second[..., 1:], full[:, 40:, 1:]) < 1e-11
