@@ -1157,6 +1157,7 @@ struct TetFemSim : Sim {
     bool has_loss = false;
     DevBuf d_damp;
     int step_block = 64;            // threads per block of tet_step_kernel (tune_step_block)
+    bool step_tuned = false;        // the block size depends on the mesh only: tuned once per handle
     DevBuf d_tet_edge, d_inc_ptr, d_inc, d_nrec, d_pec, d_eps, d_minv64, d_minv, d_U, d_P, d_Uold, d_status;
     std::vector<Dipole> dips;
     std::vector<std::array<int, 6>> rec_edges;
@@ -1385,41 +1386,51 @@ struct TetFemSim : Sim {
         ready = true;
     }
 
-    // Block size of the fused step: the candidates are timed on this mesh
-    // (one warm-up and five timed launches each, a = c = 0 so P keeps its
-    // values and U is copied into the spare buffer; both are rewritten
-    // before they are read again) and the fastest is kept.  The environment
-    // variable EMS_TET_STEP_BLOCK forces one of the candidates.
+    // Block size of the fused step, chosen once per handle (it depends on
+    // the mesh, not the material): the candidates are timed on this mesh in
+    // two sweeps (three warm-up and ten timed launches each, a = c = 0 so P
+    // keeps its values and U is copied into the spare buffer; both are
+    // rewritten before they are read again) and the one with the shortest
+    // sweep time is kept.  The environment variable EMS_TET_STEP_BLOCK
+    // forces one of the candidates.
     void tune_step_block()
     {
+        if (step_tuned) return;
+        step_tuned = true;
         if (const char *env = std::getenv("EMS_TET_STEP_BLOCK")) {
             const int b = std::atoi(env);
             for (int c : kStepBlocks)
                 if (c == b) { step_block = b; return; }
             throw Error{EMS_ERR_INVALID_ARGUMENT, "EMS_TET_STEP_BLOCK must be 32, 64, 128 or 256"};
         }
-        float best = 0.0f;
-        int pick = step_block;
-        for (int c : kStepBlocks) {
-            step_block = c;
-            const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
-            auto body = [&](auto tag) {
-                using T = decltype(tag);
-                for (int r = 0; r < 6; ++r) {
-                    if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
-                    tet_step_kernel<T, 0, 0><<<nbv, step_block, 0, stream>>>(
-                        nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), d_minv.as<T>(), d_P.as<T>(), d_U.as<T>(),
-                        d_Uold.as<T>(), nullptr, T(0), T(0), SrcArgs{}, nullptr, nullptr, nullptr, nullptr, RecArgs<T>{});
-                }
-            };
-            if (fp64) body(double()); else body(float());
-            EMS_CUDA(cudaGetLastError());
-            EMS_CUDA(cudaEventRecord(ev1, stream));
-            EMS_CUDA(cudaEventSynchronize(ev1));
-            float ms = 0.0f;
-            EMS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-            if (c == kStepBlocks[0] || ms < best) { best = ms; pick = c; }
-        }
+        float best[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int sweep = 0; sweep < 2; ++sweep)
+            for (int ci = 0; ci < 4; ++ci) {
+                step_block = kStepBlocks[ci];
+                const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
+                auto body = [&](auto tag) {
+                    using T = decltype(tag);
+                    for (int r = 0; r < 13; ++r) {
+                        if (r == 3) EMS_CUDA(cudaEventRecord(ev0, stream));
+                        T *a = d_U.as<T>(), *b = d_Uold.as<T>();
+                        if (r % 2) std::swap(a, b);
+                        tet_step_kernel<T, 0, 0><<<nbv, step_block, 0, stream>>>(
+                            nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), d_minv.as<T>(), d_P.as<T>(), a, b, nullptr, T(0),
+                            T(0), SrcArgs{}, nullptr, nullptr, nullptr, nullptr, RecArgs<T>{});
+                    }
+                };
+                if (fp64) body(double()); else body(float());
+                EMS_CUDA(cudaGetLastError());
+                EMS_CUDA(cudaEventRecord(ev1, stream));
+                EMS_CUDA(cudaEventSynchronize(ev1));
+                float ms = 0.0f;
+                EMS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+                if (sweep == 0 || ms < best[ci]) best[ci] = ms;
+            }
+        int pick = kStepBlocks[0];
+        float bmin = best[0];
+        for (int ci = 1; ci < 4; ++ci)
+            if (best[ci] < bmin) { bmin = best[ci]; pick = kStepBlocks[ci]; }
         step_block = pick;
     }
 
