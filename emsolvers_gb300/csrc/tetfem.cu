@@ -1063,6 +1063,20 @@ __global__ void scale_kernel(size_t n, double *x, double *y, const double *__res
     if (i < n) { x[i] *= s; y[i] *= s; }
 }
 
+// Start vector of the Lanczos iteration: per slot a value in [-0.5, 0.5)
+// from the splitmix64 hash of its slot id (PEC and unused slots zero), in the
+// plane layout.
+__global__ void lanczos_start_kernel(size_t nslot, size_t nnode, const unsigned char *__restrict__ pec, double *__restrict__ x)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nslot) return;
+    unsigned long long z = (unsigned long long)e + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    x[fslot(e, nnode)] = (pec[e] & kPecBit) ? 0.0 : (double)(z >> 11) / 9007199254740992.0 - 0.5;
+}
+
 // The device iteration index of a captured Lanczos graph, advanced once per iteration.
 __global__ void inc_kernel(int *jp)
 {
@@ -1500,11 +1514,11 @@ struct TetFemSim : Sim {
     // is self-adjoint there, and every Lanczos vector v travels with its mass
     // image Mv: K v is the mass image of w = Minv K v, so <v, w>_M = v.K v and
     // <w, w>_M = w.(M w) need no M.  The start pair is x = Minv K x0, Mx =
-    // K x0.  The tridiagonal coefficients stay on the device; every 9 steps
+    // K x0.  The tridiagonal coefficients stay on the device; every 6 steps
     // the largest eigenvalue of the tridiagonal matrix (Sturm bisection) is
-    // checked and the iteration stops once it changes by less than 1e-9
-    // relative (the time step is a fraction of the limit; 1e-9 is far below
-    // any effect on it).
+    // checked and the iteration stops once it changes by less than 1e-8
+    // relative (Ritz values approach it from below, and the time step is a
+    // fraction of the limit: 1e-8 is far below any effect on it).
     // Without reorthogonalisation converged Ritz values repeat, which does
     // not move the largest one.
     double lambda_max_lanczos(const DevBuf &minv_d, int max_iters)
@@ -1513,16 +1527,10 @@ struct TetFemSim : Sim {
         for (int q = 0; q < 3; ++q) { vb[q].alloc(nslot * 8); mb[q].alloc(nslot * 8); }
         part.alloc(512 * 8);
         coef.alloc(2 * (max_iters + 6) * 8);   // alpha_j at [2j], beta_{j+1}^2 at [2j+1]; scratch at the end
-        std::vector<double> x0(nslot);
-        unsigned long long st = 0x9E3779B97F4A7C15ull;
-        for (size_t e = 0; e < nslot; ++e) {
-            st ^= st << 13; st ^= st >> 7; st ^= st << 17;
-            x0[fslot(e, nnode)] = (pec_h[e] & kPecBit) ? 0.0 : ((double)(st >> 11) / 9007199254740992.0 - 0.5);
-        }
         const unsigned nb128 = (unsigned)((nnode + 127) / 128), nbs = (unsigned)((nslot + 255) / 256);
         double *cf = coef.as<double>();
         // start pair (v1, Mv1) = (Minv K x0, K x0) / |.|_M, in buffers 1
-        EMS_CUDA(cudaMemcpyAsync(vb[0].p, x0.data(), nslot * 8, cudaMemcpyHostToDevice, stream));
+        lanczos_start_kernel<<<nbs, 256, 0, stream>>>(nslot, nnode, d_pec.as<unsigned char>(), vb[0].as<double>());
         applyK64(vb[0], mb[1]);
         vb[1].zero(stream);
         tet_drift_kernel<double><<<nb128, 128, 0, stream>>>(nnode, minv_d.as<double>(), mb[1].as<double>(), vb[1].as<double>(), 1.0);
@@ -1552,7 +1560,7 @@ struct TetFemSim : Sim {
         // iterations 1, 2, 3, ...: after the first, the three buffers rotate
         // with period 3, so one captured graph of three iterations (the
         // coefficient index on the device) is replayed; the largest Ritz
-        // value is checked every nine iterations
+        // value is checked every six iterations
         struct Graph {   // destroyed on every exit path
             cudaGraph_t g = nullptr;
             cudaGraphExec_t exec = nullptr;
@@ -1578,13 +1586,13 @@ struct TetFemSim : Sim {
         for (int done = 1, rep = 1; done < max_iters; ++rep) {
             EMS_CUDA(cudaGraphLaunch(graph.exec, stream));
             done += 3;
-            if (rep % 3 == 0 || done >= max_iters) {
+            if (rep % 2 == 0 || done >= max_iters) {
                 h.resize(2 * done);
                 EMS_CUDA(cudaMemcpyAsync(h.data(), cf, h.size() * 8, cudaMemcpyDeviceToHost, stream));
                 EMS_CUDA(cudaStreamSynchronize(stream));
                 lam = tridiag_max_eig(h, done);
                 const bool breakdown = !(h[2 * done - 1] > 1e-300);
-                if (breakdown || std::fabs(lam - lam_old) <= 1e-9 * lam) break;
+                if (breakdown || std::fabs(lam - lam_old) <= 1e-8 * lam) break;
                 lam_old = lam;
             }
         }
