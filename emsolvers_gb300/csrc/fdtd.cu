@@ -98,49 +98,61 @@ __device__ __forceinline__ T pml_curl(T d1, T d2, const Prof<T> &p1, int s1, con
 
 // H from curl E at cell (i,j,k): fdtd_simulation.cpp:119-169.  Offsets are
 // 32-bit, formed once per array and moved by the strides; E values shared
-// by two components are loaded once.
+// by two components are loaded once.  Every load of the cell is issued
+// before its first store (the three read-modify-writes touch distinct
+// arrays and no other thread writes them), so a thread waits for one round
+// of memory latency instead of one per component.
 template <class T, bool PML>
 __device__ __forceinline__ void fdtd_h_cell(const FdtdArgs<T> &a, int i, int j, int k, bool slab)
 {
     const FdtdStrides &st = a.st;
     const unsigned oEx = i + j * st.ex_y + k * st.ex_z, oEy = i + j * st.ey_y + k * st.ey_z;
     const unsigned oEz = i + j * st.ez_y + k * st.ez_z;
+    const unsigned px = i + j * st.hx_y + k * st.hx_z, py = i + j * st.hy_y + k * st.hy_z;
+    const unsigned pz = i + j * st.hz_y + k * st.hz_z;
     const bool hx = i < a.nx, hy = j < a.ny, hz = k < a.nz;
     T ez11 = 0, ey1k = 0, ex1k = 0;   // Ez(i+1,j+1,k), Ey(i+1,j,k+1), Ex(i,j+1,k+1)
+    T ez1 = 0, ey1 = 0, ex1 = 0, ez0 = 0, ey0 = 0, ex0 = 0, hx0 = 0, hy0 = 0, hz0 = 0;
     if (hx || hy) ez11 = __ldg(a.Ez + oEz + 1 + st.ez_y);
     if (hx || hz) ey1k = __ldg(a.Ey + oEy + 1 + st.ey_z);
     if (hy || hz) ex1k = __ldg(a.Ex + oEx + st.ex_y + st.ex_z);
     if (hx) {
-        const unsigned p = i + j * st.hx_y + k * st.hx_z;
-        const T e1 = ez11, e2 = __ldg(a.Ez + oEz + 1);
-        const T e3 = ey1k, e4 = __ldg(a.Ey + oEy + 1);
+        hx0 = a.Hx[px];
+        ez1 = __ldg(a.Ez + oEz + 1);
+        ey1 = __ldg(a.Ey + oEy + 1);
+    }
+    if (hy) {
+        hy0 = a.Hy[py];
+        ex1 = __ldg(a.Ex + oEx + st.ex_y);
+        ez0 = __ldg(a.Ez + oEz + st.ez_y);
+    }
+    if (hz) {
+        hz0 = a.Hz[pz];
+        ey0 = __ldg(a.Ey + oEy + st.ey_z);
+        ex0 = __ldg(a.Ex + oEx + st.ex_z);
+    }
+    if (hx) {
         if (slab && (a.ph[1].on[j] | a.ph[2].on[k])) {
-            T c = pml_curl(rsub(e1, e2), rsub(e3, e4), a.ph[1], j, a.ph[2], k, &a.psiH[0][0][p], &a.psiH[0][1][p]);
-            a.Hx[p] = rsub(a.Hx[p], rmul(a.ch, c));
+            T c = pml_curl(rsub(ez11, ez1), rsub(ey1k, ey1), a.ph[1], j, a.ph[2], k, &a.psiH[0][0][px], &a.psiH[0][1][px]);
+            a.Hx[px] = rsub(hx0, rmul(a.ch, c));
         } else {
-            a.Hx[p] = rsub(a.Hx[p], rmul(a.ch, curl4(e1, e2, e3, e4)));
+            a.Hx[px] = rsub(hx0, rmul(a.ch, curl4(ez11, ez1, ey1k, ey1)));
         }
     }
     if (hy) {
-        const unsigned p = i + j * st.hy_y + k * st.hy_z;
-        const T e1 = ex1k, e2 = __ldg(a.Ex + oEx + st.ex_y);
-        const T e3 = ez11, e4 = __ldg(a.Ez + oEz + st.ez_y);
         if (slab && (a.ph[2].on[k] | a.ph[0].on[i])) {
-            T c = pml_curl(rsub(e1, e2), rsub(e3, e4), a.ph[2], k, a.ph[0], i, &a.psiH[1][0][p], &a.psiH[1][1][p]);
-            a.Hy[p] = rsub(a.Hy[p], rmul(a.ch, c));
+            T c = pml_curl(rsub(ex1k, ex1), rsub(ez11, ez0), a.ph[2], k, a.ph[0], i, &a.psiH[1][0][py], &a.psiH[1][1][py]);
+            a.Hy[py] = rsub(hy0, rmul(a.ch, c));
         } else {
-            a.Hy[p] = rsub(a.Hy[p], rmul(a.ch, curl4(e1, e2, e3, e4)));
+            a.Hy[py] = rsub(hy0, rmul(a.ch, curl4(ex1k, ex1, ez11, ez0)));
         }
     }
     if (hz) {
-        const unsigned p = i + j * st.hz_y + k * st.hz_z;
-        const T e1 = ey1k, e2 = __ldg(a.Ey + oEy + st.ey_z);
-        const T e3 = ex1k, e4 = __ldg(a.Ex + oEx + st.ex_z);
         if (slab && (a.ph[0].on[i] | a.ph[1].on[j])) {
-            T c = pml_curl(rsub(e1, e2), rsub(e3, e4), a.ph[0], i, a.ph[1], j, &a.psiH[2][0][p], &a.psiH[2][1][p]);
-            a.Hz[p] = rsub(a.Hz[p], rmul(a.ch, c));
+            T c = pml_curl(rsub(ey1k, ey0), rsub(ex1k, ex0), a.ph[0], i, a.ph[1], j, &a.psiH[2][0][pz], &a.psiH[2][1][pz]);
+            a.Hz[pz] = rsub(hz0, rmul(a.ch, c));
         } else {
-            a.Hz[p] = rsub(a.Hz[p], rmul(a.ch, curl4(e1, e2, e3, e4)));
+            a.Hz[pz] = rsub(hz0, rmul(a.ch, curl4(ey1k, ey0, ex1k, ex0)));
         }
     }
 }
@@ -159,8 +171,22 @@ __global__ void __launch_bounds__(256) fdtd_h_kernel(FdtdArgs<T> a)
     }
 }
 
+// (ca, cb) of one material through the read-only path.
+__device__ __forceinline__ CaCb<float> load_cab(const CaCb<float> *p)
+{
+    const float2 v = __ldg(reinterpret_cast<const float2 *>(p));
+    return {v.x, v.y};
+}
+__device__ __forceinline__ CaCb<double> load_cab(const CaCb<double> *p)
+{
+    const double2 v = __ldg(reinterpret_cast<const double2 *>(p));
+    return {v.x, v.y};
+}
+
 // E from curl H at (i,j,k): fdtd_simulation.cpp:170-220, E = ca E + cb curl
-// (ca, cb of the cell's material; uniform: E += ce curl).
+// (ca, cb of the cell's material; uniform: E += ce curl).  As in the H
+// update, all loads of the cell (fields, material ids, then their (ca, cb))
+// are issued before the first store.
 template <class T, bool MAT, bool PML>
 __device__ __forceinline__ void fdtd_e_cell(const FdtdArgs<T> &a, int i, int j, int k, bool slab)
 {
@@ -168,64 +194,63 @@ __device__ __forceinline__ void fdtd_e_cell(const FdtdArgs<T> &a, int i, int j, 
     const FdtdStrides &st = a.st;
     const unsigned oHx = i + j * st.hx_y + k * st.hx_z, oHy = i + j * st.hy_y + k * st.hy_z;
     const unsigned oHz = i + j * st.hz_y + k * st.hz_z;
+    const unsigned px = i + j * st.ex_y + k * st.ex_z, py = i + j * st.ey_y + k * st.ey_z;
+    const unsigned pz = i + j * st.ez_y + k * st.ez_z;
     const bool ex = j >= 1 && k >= 1, ey = i >= 1 && k >= 1, ez = i >= 1 && j >= 1;
     T hz_k = 0, hy_j = 0, hx_i = 0;   // Hz(i,j,k-1), Hy(i,j-1,k), Hx(i-1,j,k)
+    T hz_jk = 0, hy_jk = 0, hx_ik = 0, hz_ik = 0, hy_ij = 0, hx_ij = 0, ex0 = 0, ey0 = 0, ez0 = 0;
+    unsigned m0 = 0, m1 = 0, m2 = 0;
     if (ex || ey) hz_k = __ldg(a.Hz + oHz - st.hz_z);
     if (ex || ez) hy_j = __ldg(a.Hy + oHy - st.hy_y);
     if (ey || ez) hx_i = __ldg(a.Hx + oHx - 1);
-    auto upd = [&](T *f, unsigned p, T ca, T cb, T c) {
-        if (MAT) f[p] = radd(rmul(ca, f[p]), rmul(cb, c));
-        else f[p] = radd(f[p], rmul(a.ce, c));
-    };
-    auto coef = [&](int ci, int cj, int ck, T &ca, T &cb) {
-        const int m = __ldg(a.mat + (unsigned)ci + (unsigned)cj * st.m_y + (unsigned)ck * st.m_z);
-        const CaCb<T> c = a.cab[m];
-        ca = c.ca;
-        cb = c.cb;
-    };
     if (ex) {  // Ex, i in [0,nx]
-        const unsigned p = i + j * st.ex_y + k * st.ex_z;
-        T ca = 1, cb = 0;
-        if (MAT) coef(i < nx ? i : nx - 1, j - 1, k - 1, ca, cb);
-        const T h1 = hz_k, h2 = __ldg(a.Hz + oHz - st.hz_y - st.hz_z);
-        const T h3 = hy_j, h4 = __ldg(a.Hy + oHy - st.hy_y - st.hy_z);
-        if (slab && (a.pe[1].on[j] | a.pe[2].on[k])) {
-            T c = pml_curl(rsub(h1, h2), rsub(h3, h4), a.pe[1], j, a.pe[2], k, &a.psiE[0][0][p], &a.psiE[0][1][p]);
-            T cbb = MAT ? cb : a.ce;
-            T caa = MAT ? ca : T(1);
-            a.Ex[p] = radd(rmul(caa, a.Ex[p]), rmul(cbb, c));
-        } else {
-            upd(a.Ex, p, ca, cb, curl4(h1, h2, h3, h4));
-        }
+        ex0 = a.Ex[px];
+        hz_jk = __ldg(a.Hz + oHz - st.hz_y - st.hz_z);
+        hy_jk = __ldg(a.Hy + oHy - st.hy_y - st.hy_z);
+        if (MAT) m0 = __ldg(a.mat + (unsigned)(i < nx ? i : nx - 1) + (unsigned)(j - 1) * st.m_y + (unsigned)(k - 1) * st.m_z);
     }
     if (ey) {  // Ey, j in [0,ny]
-        const unsigned p = i + j * st.ey_y + k * st.ey_z;
-        T ca = 1, cb = 0;
-        if (MAT) coef(i - 1, j < ny ? j : ny - 1, k - 1, ca, cb);
-        const T h1 = hx_i, h2 = __ldg(a.Hx + oHx - 1 - st.hx_z);
-        const T h3 = hz_k, h4 = __ldg(a.Hz + oHz - 1 - st.hz_z);
-        if (slab && (a.pe[2].on[k] | a.pe[0].on[i])) {
-            T c = pml_curl(rsub(h1, h2), rsub(h3, h4), a.pe[2], k, a.pe[0], i, &a.psiE[1][0][p], &a.psiE[1][1][p]);
-            T cbb = MAT ? cb : a.ce;
-            T caa = MAT ? ca : T(1);
-            a.Ey[p] = radd(rmul(caa, a.Ey[p]), rmul(cbb, c));
-        } else {
-            upd(a.Ey, p, ca, cb, curl4(h1, h2, h3, h4));
-        }
+        ey0 = a.Ey[py];
+        hx_ik = __ldg(a.Hx + oHx - 1 - st.hx_z);
+        hz_ik = __ldg(a.Hz + oHz - 1 - st.hz_z);
+        if (MAT) m1 = __ldg(a.mat + (unsigned)(i - 1) + (unsigned)(j < ny ? j : ny - 1) * st.m_y + (unsigned)(k - 1) * st.m_z);
     }
     if (ez) {  // Ez, k in [0,nz]
-        const unsigned p = i + j * st.ez_y + k * st.ez_z;
-        T ca = 1, cb = 0;
-        if (MAT) coef(i - 1, j - 1, k < nz ? k : nz - 1, ca, cb);
-        const T h1 = hy_j, h2 = __ldg(a.Hy + oHy - 1 - st.hy_y);
-        const T h3 = hx_i, h4 = __ldg(a.Hx + oHx - 1 - st.hx_y);
-        if (slab && (a.pe[0].on[i] | a.pe[1].on[j])) {
-            T c = pml_curl(rsub(h1, h2), rsub(h3, h4), a.pe[0], i, a.pe[1], j, &a.psiE[2][0][p], &a.psiE[2][1][p]);
-            T cbb = MAT ? cb : a.ce;
-            T caa = MAT ? ca : T(1);
-            a.Ez[p] = radd(rmul(caa, a.Ez[p]), rmul(cbb, c));
+        ez0 = a.Ez[pz];
+        hy_ij = __ldg(a.Hy + oHy - 1 - st.hy_y);
+        hx_ij = __ldg(a.Hx + oHx - 1 - st.hx_y);
+        if (MAT) m2 = __ldg(a.mat + (unsigned)(i - 1) + (unsigned)(j - 1) * st.m_y + (unsigned)(k < nz ? k : nz - 1) * st.m_z);
+    }
+    CaCb<T> c0{1, 0}, c1{1, 0}, c2{1, 0};
+    if (MAT) {
+        if (ex) c0 = load_cab(a.cab + m0);
+        if (ey) c1 = load_cab(a.cab + m1);
+        if (ez) c2 = load_cab(a.cab + m2);
+    }
+    // ca E + cb c, or E + ce c without materials (ca = 1 multiplies exactly)
+    auto upd = [&](T e, const CaCb<T> &m, T c) { return MAT ? radd(rmul(m.ca, e), rmul(m.cb, c)) : radd(e, rmul(a.ce, c)); };
+    if (ex) {
+        if (slab && (a.pe[1].on[j] | a.pe[2].on[k])) {
+            T c = pml_curl(rsub(hz_k, hz_jk), rsub(hy_j, hy_jk), a.pe[1], j, a.pe[2], k, &a.psiE[0][0][px], &a.psiE[0][1][px]);
+            a.Ex[px] = upd(ex0, c0, c);
         } else {
-            upd(a.Ez, p, ca, cb, curl4(h1, h2, h3, h4));
+            a.Ex[px] = upd(ex0, c0, curl4(hz_k, hz_jk, hy_j, hy_jk));
+        }
+    }
+    if (ey) {
+        if (slab && (a.pe[2].on[k] | a.pe[0].on[i])) {
+            T c = pml_curl(rsub(hx_i, hx_ik), rsub(hz_k, hz_ik), a.pe[2], k, a.pe[0], i, &a.psiE[1][0][py], &a.psiE[1][1][py]);
+            a.Ey[py] = upd(ey0, c1, c);
+        } else {
+            a.Ey[py] = upd(ey0, c1, curl4(hx_i, hx_ik, hz_k, hz_ik));
+        }
+    }
+    if (ez) {
+        if (slab && (a.pe[0].on[i] | a.pe[1].on[j])) {
+            T c = pml_curl(rsub(hy_j, hy_ij), rsub(hx_i, hx_ij), a.pe[0], i, a.pe[1], j, &a.psiE[2][0][pz], &a.psiE[2][1][pz]);
+            a.Ez[pz] = upd(ez0, c2, c);
+        } else {
+            a.Ez[pz] = upd(ez0, c2, curl4(hy_j, hy_ij, hx_i, hx_ij));
         }
     }
 }
