@@ -103,7 +103,9 @@ __device__ void sym3_eig(double A[3][3], double w[3], double V[3][3])
         for (int j = 0; j < 3; ++j) V[i][j] = i == j ? 1.0 : 0.0;
     for (int sweep = 0; sweep < 50; ++sweep) {
         double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
-        if (off == 0.0) break;
+        // converged: the off-diagonal sum at the rounding floor (exact zero
+        // is rarely reached, and each further sweep only rounds again)
+        if (off <= 1e-14 * (fabs(A[0][0]) + fabs(A[1][1]) + fabs(A[2][2]))) break;
         for (int p = 0; p < 2; ++p)
             for (int q = p + 1; q < 3; ++q) {
                 if (A[p][q] == 0.0) continue;
@@ -151,81 +153,128 @@ __device__ void sym3_pinv(const double Ain[3][3], double P[3][3])
 // vector, S = sym(D^T W), G = D^T D, alpha = mean consistent diagonal), then
 // inverted by Cholesky.  Writes 49 doubles per node; status[v] = 1 if the
 // block is not positive definite.
-__global__ void tet_minv_setup_kernel(size_t nnode, const unsigned char *__restrict__ pec, const int *__restrict__ inc_ptr,
-                                      const int *__restrict__ inc, const double *__restrict__ eps, double *__restrict__ minv,
-                                      int *__restrict__ status)
+__global__ void __launch_bounds__(128) tet_minv_setup_kernel(size_t nnode, const unsigned char *__restrict__ pec,
+                                                             const int *__restrict__ inc_ptr, const int *__restrict__ inc,
+                                                             const double *__restrict__ eps, double *__restrict__ minv,
+                                                             int *__restrict__ status)
 {
-    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nnode) return;
     double *B = minv + 49 * v;
-    for (int q = 0; q < 49; ++q) B[q] = 0.0;
-    int slot[7], k = 0;
-    for (int d = 0; d < 7; ++d)
-        if (!(pec[7 * v + d] & kPecBit)) slot[k++] = d;
-    if (k == 0) return;
-    double W[7][3], D[7][3], diag[7];
-    for (int r = 0; r < k; ++r) {
-        size_t e = 7 * v + slot[r];
-        W[r][0] = W[r][1] = W[r][2] = 0.0;
-        diag[r] = 0.0;
-        for (int q = 0; q < 3; ++q) D[r][q] = c_dir[slot[r]][q];
-        for (int s = inc_ptr[e]; s < inc_ptr[e + 1]; ++s) {
-            int t = inc[s] >> 3, l = inc[s] & 7, p = t % 6;
-            double ep = eps[t];
-            for (int q = 0; q < 3; ++q) W[r][q] += ep * c_wint[p][l][q];
-            diag[r] += ep * c_wsq[p][l];
-        }
+    // Slots are indexed by their direction d, a compile-time index once the
+    // loops are unrolled, so every array below stays in registers.  A PEC or
+    // unused slot enters the block as an identity row and column: the
+    // factors of the active slots gain only exact-zero terms, and its row
+    // and column of the inverse are written as zeros.
+    bool live[7];
+    int k = 0;
+    double W[7][3], diag[7];
+#pragma unroll
+    for (int d = 0; d < 7; ++d) {
+        const size_t e = 7 * v + d;
+        live[d] = !(pec[e] & kPecBit);
+        k += live[d] ? 1 : 0;
+        W[d][0] = W[d][1] = W[d][2] = 0.0;
+        diag[d] = 0.0;
+        if (live[d])
+            for (int s = inc_ptr[e]; s < inc_ptr[e + 1]; ++s) {
+                const int t = inc[s] >> 3, l = inc[s] & 7, p = t % 6;
+                const double ep = eps[t];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) W[d][q] += ep * c_wint[p][l][q];
+                diag[d] += ep * c_wsq[p][l];
+            }
+    }
+    if (k == 0) {
+        for (int q = 0; q < 49; ++q) B[q] = 0.0;
+        return;
     }
     double S[3][3], G[3][3], Sp[3][3], Gp[3][3];
+#pragma unroll
     for (int a = 0; a < 3; ++a)
+#pragma unroll
         for (int b = 0; b < 3; ++b) {
             double s1 = 0.0, s2 = 0.0, g = 0.0;
-            for (int r = 0; r < k; ++r) { s1 += D[r][a] * W[r][b]; s2 += W[r][a] * D[r][b]; g += D[r][a] * D[r][b]; }
+#pragma unroll
+            for (int d = 0; d < 7; ++d)
+                if (live[d]) {
+                    s1 += c_dir[d][a] * W[d][b];
+                    s2 += W[d][a] * c_dir[d][b];
+                    g += c_dir[d][a] * c_dir[d][b];
+                }
             S[a][b] = 0.5 * (s1 + s2);
             G[a][b] = g;
         }
     sym3_pinv(S, Sp);
     sym3_pinv(G, Gp);
     double alpha = 0.0;
-    for (int r = 0; r < k; ++r) alpha += diag[r];
+#pragma unroll
+    for (int d = 0; d < 7; ++d)
+        if (live[d]) alpha += diag[d];
     alpha /= k;
-    double M[7][7], L[7][7], Li[7][7];
-    for (int r = 0; r < k; ++r)
-        for (int c = 0; c < k; ++c) {
-            double ws = 0.0, dq = 0.0;
-            for (int a = 0; a < 3; ++a)
-                for (int b = 0; b < 3; ++b) {
-                    ws += W[r][a] * Sp[a][b] * W[c][b];
-                    dq += D[r][a] * Gp[a][b] * D[c][b];
-                }
-            M[r][c] = ws + alpha * ((r == c ? 1.0 : 0.0) - dq);
-        }
-    for (int i = 0; i < k; ++i)
-        for (int j = 0; j < k; ++j) { L[i][j] = 0.0; Li[i][j] = 0.0; }
-    for (int i = 0; i < k; ++i)
+    // lower triangle, packed by rows: entry (i, j), j <= i, at i (i + 1) / 2 + j
+    double A[28];
+#pragma unroll
+    for (int i = 0; i < 7; ++i)
+#pragma unroll
         for (int j = 0; j <= i; ++j) {
-            double s = M[i][j];
-            for (int q = 0; q < j; ++q) s -= L[i][q] * L[j][q];
+            double m = i == j ? 1.0 : 0.0;
+            if (live[i] && live[j]) {
+                double ws = 0.0, dq = 0.0;
+#pragma unroll
+                for (int a = 0; a < 3; ++a)
+#pragma unroll
+                    for (int b = 0; b < 3; ++b) {
+                        ws += W[i][a] * Sp[a][b] * W[j][b];
+                        dq += c_dir[i][a] * Gp[a][b] * c_dir[j][b];
+                    }
+                m = ws + alpha * ((i == j ? 1.0 : 0.0) - dq);
+            }
+            A[i * (i + 1) / 2 + j] = m;
+        }
+    // Cholesky factor L in place
+#pragma unroll
+    for (int i = 0; i < 7; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j) {
+            double s = A[i * (i + 1) / 2 + j];
+#pragma unroll
+            for (int q = 0; q < j; ++q) s -= A[i * (i + 1) / 2 + q] * A[j * (j + 1) / 2 + q];
             if (i == j) {
-                if (!(s > 0.0)) { status[v] = 1; return; }
-                L[i][i] = sqrt(s);
+                if (!(s > 0.0)) {
+                    status[v] = 1;
+                    return;
+                }
+                A[i * (i + 1) / 2 + i] = sqrt(s);
             } else {
-                L[i][j] = s / L[j][j];
+                A[i * (i + 1) / 2 + j] = s / A[j * (j + 1) / 2 + j];
             }
         }
-    for (int i = 0; i < k; ++i) {
-        Li[i][i] = 1.0 / L[i][i];
+    // L^-1 in place, row by row (row i reads its own L entries at q >= j,
+    // not yet overwritten, and the inverted rows above it)
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        const double lii = A[i * (i + 1) / 2 + i];
+#pragma unroll
         for (int j = 0; j < i; ++j) {
             double s = 0.0;
-            for (int q = j; q < i; ++q) s += L[i][q] * Li[q][j];
-            Li[i][j] = -s / L[i][i];
+#pragma unroll
+            for (int q = j; q < i; ++q) s += A[i * (i + 1) / 2 + q] * A[q * (q + 1) / 2 + j];
+            A[i * (i + 1) / 2 + j] = -s / lii;
         }
+        A[i * (i + 1) / 2 + i] = 1.0 / lii;
     }
-    for (int i = 0; i < k; ++i)
-        for (int j = 0; j < k; ++j) {
+    // Minv = L^-T L^-1
+#pragma unroll
+    for (int i = 0; i < 7; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j) {
             double s = 0.0;
-            for (int q = (i > j ? i : j); q < k; ++q) s += Li[q][i] * Li[q][j];
-            B[slot[i] * 7 + slot[j]] = s;
+#pragma unroll
+            for (int q = i; q < 7; ++q) s += A[q * (q + 1) / 2 + i] * A[q * (q + 1) / 2 + j];
+            const double r = live[i] && live[j] ? s : 0.0;
+            B[i * 7 + j] = r;
+            B[j * 7 + i] = r;
         }
 }
 
@@ -1055,12 +1104,102 @@ __global__ void __launch_bounds__(512) dot_finish_kernel(int nb, const double *_
     if (t == 0) out[jp ? 2 * *jp : 0] = sh[0];
 }
 
-// x, y *= 1 / sqrt(*nrm)
-__global__ void scale_kernel(size_t n, double *x, double *y, const double *__restrict__ nrm, const int *__restrict__ jp = nullptr)
+// Lanczos reductions without a finishing launch: every block writes its
+// FP64 partial sum, and the block that finishes last (the one whose atomic
+// ticket is gridDim.x - 1, after every block fenced its partial) adds all
+// partials in block order, so the result has the same bits whichever block
+// is last.  Grids are capped at kLzBlocks blocks (grid-stride loops).
+constexpr int kLzBlocks = 1024;
+
+// Block sum of s (warp butterflies, then the warps in order); every thread
+// of the block must call it; the result is valid in thread 0.
+__device__ __forceinline__ double block_sum(double s)
 {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const double s = 1.0 / sqrt(nrm[jp ? 2 * *jp : 0]);
-    if (i < n) { x[i] *= s; y[i] *= s; }
+    __shared__ double ws[32];
+#pragma unroll
+    for (int m = 16; m > 0; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+    __syncthreads();   // ws may still be read from an earlier call
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) t += ws[w];
+    return t;
+}
+
+// *out = sum over the grid of s (see above); ticket must be zero before the
+// launch and is zero again after it.
+__device__ __forceinline__ void grid_sum(double s, double *__restrict__ part, unsigned *__restrict__ ticket,
+                                         double *__restrict__ out)
+{
+    __shared__ bool last;
+    const double b = block_sum(s);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    double r = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) r += __ldcg(part + i);
+    r = block_sum(r);
+    if (threadIdx.x == 0) {
+        *out = r;
+        *ticket = 0u;
+    }
+}
+
+// x, y *= 1 / sqrt(nrm), nrm = nrm_base[2 * *jp] with jp, else nrm_base[0];
+// x32 = (float) x afterwards and kz = 0 (the FP32 buffer the next apply
+// accumulates K x32 into).
+__global__ void __launch_bounds__(256) scale_kernel(size_t n, double *__restrict__ x, double *__restrict__ y,
+                                                    const double *__restrict__ nrm_base, const int *__restrict__ jp,
+                                                    float *__restrict__ x32, float *__restrict__ kz)
+{
+    const double s = 1.0 / sqrt(nrm_base[jp ? 2 * *jp : 0]);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double xs = x[i] * s;
+        x[i] = xs;
+        y[i] *= s;
+        x32[i] = (float)xs;
+        kz[i] = 0.0f;
+    }
+}
+
+// y = (float)x
+__global__ void narrow_kernel(size_t n, const double *__restrict__ x, float *__restrict__ y)
+{
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = (float)x[i];
+}
+
+// One Lanczos apply after K v was formed in FP32: per node Mw = (double)
+// Kv32, w = Minv Mw (FP64 mass blocks), and *alpha = v . Mw.  With jp
+// given, the device iteration index is advanced here (no kernel of this
+// iteration has read it yet).
+__global__ void __launch_bounds__(128) lanczos_minv_kernel(size_t nnode, const double *__restrict__ minv,
+                                                           const float *__restrict__ kv32, const double *__restrict__ vcur,
+                                                           double *__restrict__ Mw, double *__restrict__ w,
+                                                           double *__restrict__ part, unsigned *__restrict__ ticket,
+                                                           double *__restrict__ alpha, int *__restrict__ jp)
+{
+    if (jp && blockIdx.x == 0 && threadIdx.x == 0) *jp += 1;
+    double acc = 0.0;
+    for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nnode; v += (size_t)gridDim.x * blockDim.x) {
+        double x[7], mv[28];
+#pragma unroll
+        for (int d = 0; d < 7; ++d) {
+            const size_t f = (size_t)d * nnode + v;
+            x[d] = (double)kv32[f];
+            Mw[f] = x[d];
+            acc += vcur[f] * x[d];
+        }
+        load_block<double>(minv, nnode, v, mv);
+#pragma unroll
+        for (int d = 0; d < 7; ++d) w[(size_t)d * nnode + v] = block_row<double>(mv, x, d);
+    }
+    grid_sum(acc, part, ticket, alpha);
 }
 
 // Start vector of the Lanczos iteration: per slot a value in [-0.5, 0.5)
@@ -1077,26 +1216,29 @@ __global__ void lanczos_start_kernel(size_t nslot, size_t nnode, const unsigned 
     x[fslot(e, nnode)] = (pec[e] & kPecBit) ? 0.0 : (double)(z >> 11) / 9007199254740992.0 - 0.5;
 }
 
-// The device iteration index of a captured Lanczos graph, advanced once per iteration.
-__global__ void inc_kernel(int *jp)
+// Lanczos three-term step on a vector and its mass image: alpha_j = *alpha
+// (kept at cf[2j]), beta_j^2 at cf[2j - 1]; w -= alpha v + beta vp, Mw -=
+// alpha Mv + beta Mvp (vp == nullptr: no beta term), then beta_{j+1}^2 =
+// w . Mw at cf[2j + 1].  j = *jp when jp is given, else j0.
+__global__ void __launch_bounds__(256) lanczos_step_kernel(size_t n, double *__restrict__ w, double *__restrict__ Mw,
+                                                           const double *__restrict__ v, const double *__restrict__ Mv,
+                                                           const double *__restrict__ vp, const double *__restrict__ Mvp,
+                                                           const double *__restrict__ alpha, double *__restrict__ part,
+                                                           unsigned *__restrict__ ticket, double *__restrict__ cf, int j0,
+                                                           const int *__restrict__ jp)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *jp += 1;
-}
-
-// Lanczos three-term step on a vector and its mass image:
-// w -= alpha v + beta vp,  Mw -= alpha Mv + beta Mvp  (alpha = *a, beta = sqrt(*b2)).
-__global__ void lanczos_step_kernel(size_t n, double *__restrict__ w, double *__restrict__ Mw, const double *__restrict__ v,
-                                    const double *__restrict__ Mv, const double *__restrict__ vp,
-                                    const double *__restrict__ Mvp, const double *__restrict__ a,
-                                    const double *__restrict__ b2, const int *__restrict__ jp = nullptr)
-{
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    // with jp: a = alpha_0's slot, b2 = beta_1^2's slot (iteration j reads beta_j^2)
-    const int o = jp ? 2 * *jp : 0;
-    const double al = a[o], be = b2 ? sqrt(b2[jp ? o - 2 : 0]) : 0.0;
-    w[i] = w[i] - al * v[i] - be * (vp ? vp[i] : 0.0);
-    Mw[i] = Mw[i] - al * Mv[i] - be * (Mvp ? Mvp[i] : 0.0);
+    const int j = jp ? *jp : j0;
+    const double al = *alpha, be = vp ? sqrt(cf[2 * j - 1]) : 0.0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) cf[2 * j] = al;
+    double acc = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double wi = w[i] - al * v[i] - be * (vp ? vp[i] : 0.0);
+        const double mi = Mw[i] - al * Mv[i] - be * (Mvp ? Mvp[i] : 0.0);
+        w[i] = wi;
+        Mw[i] = mi;
+        acc += wi * mi;
+    }
+    grid_sum(acc, part, ticket, cf + 2 * j + 1);
 }
 
 // -------------------------------------------------------------- host side
@@ -1510,11 +1652,31 @@ struct TetFemSim : Sim {
                                                                SrcArgs{}, nullptr, nullptr, nullptr, nullptr, RecArgs<double>{});
     }
 
+    // Mz = K x formed in FP32 from x32 (accumulated into kv32, which must be
+    // zero) and z = Minv Mz in FP64, with *alpha = vcur . Mz: one Lanczos
+    // apply.  K x in FP64 is the same fused step, but GB300
+    // issues FP64 at a small fraction of its FP32 rate and the FP64 step took
+    // about 50 us per apply on a 32^3 mesh.
+    void applyMinvK32(const DevBuf &x32, DevBuf &kv32, const DevBuf &minv_d, const DevBuf &vcur, DevBuf &Mz, DevBuf &z,
+                      DevBuf &part, unsigned *ticket, double *alpha, int *jp)
+    {
+        const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
+        tet_step_kernel<float, 0, 0><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), nullptr,
+                                                              kv32.as<float>(), x32.as<float>(), nullptr, nullptr, -1.0f, 0.0f,
+                                                              SrcArgs{}, nullptr, nullptr, nullptr, nullptr, RecArgs<float>{});
+        const int nb = (int)std::min<size_t>((nnode + 127) / 128, kLzBlocks);
+        lanczos_minv_kernel<<<nb, 128, 0, stream>>>(nnode, minv_d.as<double>(), kv32.as<float>(), vcur.as<double>(),
+                                                    Mz.as<double>(), z.as<double>(), part.as<double>(), ticket, alpha, jp);
+    }
+
     // Largest eigenvalue of Minv K by Lanczos in the M inner product.  Minv K
     // is self-adjoint there, and every Lanczos vector v travels with its mass
     // image Mv: K v is the mass image of w = Minv K v, so <v, w>_M = v.K v and
     // <w, w>_M = w.(M w) need no M.  The start pair is x = Minv K x0, Mx =
-    // K x0.  The tridiagonal coefficients stay on the device; every 6 steps
+    // K x0.  K v is formed in FP32 by the fused step (applyMinvK32), Minv
+    // K v, the dot products and the recurrence in FP64; the largest Ritz
+    // value then agrees with an all-FP64 iteration to about 1e-6 relative.
+    // The tridiagonal coefficients stay on the device; every 6 steps
     // the largest eigenvalue of the tridiagonal matrix (Sturm bisection) is
     // checked and the iteration stops once it changes by less than 1e-8
     // relative (Ritz values approach it from below, and the time step is a
@@ -1523,36 +1685,40 @@ struct TetFemSim : Sim {
     // not move the largest one.
     double lambda_max_lanczos(const DevBuf &minv_d, int max_iters)
     {
-        DevBuf vb[3], mb[3], part, coef;
+        DevBuf vb[3], mb[3], part, tickets, coef, v32, kv32;
         for (int q = 0; q < 3; ++q) { vb[q].alloc(nslot * 8); mb[q].alloc(nslot * 8); }
-        part.alloc(512 * 8);
-        coef.alloc(2 * (max_iters + 6) * 8);   // alpha_j at [2j], beta_{j+1}^2 at [2j+1]; scratch at the end
-        const unsigned nb128 = (unsigned)((nnode + 127) / 128), nbs = (unsigned)((nslot + 255) / 256);
-        double *cf = coef.as<double>();
+        v32.alloc(nslot * 4);    // FP32 copy of the vector K is applied to
+        kv32.alloc(nslot * 4);   // K v in FP32 (zeroed by each scale launch for the next apply)
+        part.alloc(kLzBlocks * 8);   // block partials of the reductions
+        tickets.alloc(2 * sizeof(unsigned));
+        tickets.zero(stream);
+        unsigned *tk = tickets.as<unsigned>();
+        // alpha_j at [2j], beta_{j+1}^2 at [2j+1]; scratch at 2 max_iters + 10 (start norm) and + 11 (alpha)
+        coef.alloc(2 * (max_iters + 6) * 8);
+        const unsigned nbs = (unsigned)((nslot + 255) / 256);
+        const int nbl = (int)std::min<size_t>(nbs, kLzBlocks);
+        double *cf = coef.as<double>(), *nrm0 = cf + 2 * max_iters + 10, *alpha = cf + 2 * max_iters + 11;
         // start pair (v1, Mv1) = (Minv K x0, K x0) / |.|_M, in buffers 1
         lanczos_start_kernel<<<nbs, 256, 0, stream>>>(nslot, nnode, d_pec.as<unsigned char>(), vb[0].as<double>());
-        applyK64(vb[0], mb[1]);
-        vb[1].zero(stream);
-        tet_drift_kernel<double><<<nb128, 128, 0, stream>>>(nnode, minv_d.as<double>(), mb[1].as<double>(), vb[1].as<double>(), 1.0);
-        dot(vb[1], mb[1], part, cf + 2 * max_iters + 10);
-        scale_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), cf + 2 * max_iters + 10);
+        narrow_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[0].as<double>(), v32.as<float>());
+        kv32.zero(stream);
+        applyMinvK32(v32, kv32, minv_d, vb[0], mb[1], vb[1], part, tk, alpha, nullptr);
+        dot_partial_kernel<<<512, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), part.as<double>());
+        dot_finish_kernel<<<1, 512, 0, stream>>>(512, part.as<double>(), nrm0);
+        scale_kernel<<<nbl, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), nrm0, nullptr, v32.as<float>(),
+                                              kv32.as<float>());
         int prev = -1, cur = 1, nxt = 2;
-        // one iteration; jp == nullptr: host index jj, else the device index
-        auto iteration = [&](int jj, const int *jp) {
-            // w = Minv K v (mass image K v), alpha = v.K v
-            applyK64(vb[cur], mb[nxt]);
-            dot(vb[cur], mb[nxt], part, jp ? cf : cf + 2 * jj, jp);
-            vb[nxt].zero(stream);
-            tet_drift_kernel<double><<<nb128, 128, 0, stream>>>(nnode, minv_d.as<double>(), mb[nxt].as<double>(),
-                                                              vb[nxt].as<double>(), 1.0);
-            lanczos_step_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(), vb[cur].as<double>(),
+        // one iteration: apply (+ alpha), three-term step (+ beta^2),
+        // normalisation; jp == nullptr: host index jj, else the device index
+        // (advanced by the apply)
+        auto iteration = [&](int jj, int *jp) {
+            applyMinvK32(v32, kv32, minv_d, vb[cur], mb[nxt], vb[nxt], part, tk, alpha, jp);
+            lanczos_step_kernel<<<nbl, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(), vb[cur].as<double>(),
                                                          mb[cur].as<double>(), prev >= 0 ? vb[prev].as<double>() : nullptr,
-                                                         prev >= 0 ? mb[prev].as<double>() : nullptr, jp ? cf : cf + 2 * jj,
-                                                         jp ? cf + 1 : (jj > 0 ? cf + 2 * jj - 1 : nullptr), jp);
-            dot(vb[nxt], mb[nxt], part, jp ? cf + 1 : cf + 2 * jj + 1, jp);   // beta_{j+1}^2
-            scale_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(),
-                                                  jp ? cf + 1 : cf + 2 * jj + 1, jp);
-            if (jp) inc_kernel<<<1, 32, 0, stream>>>(const_cast<int *>(jp));
+                                                         prev >= 0 ? mb[prev].as<double>() : nullptr, alpha, part.as<double>(),
+                                                         tk + 1, cf, jj, jp);
+            scale_kernel<<<nbl, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(),
+                                                  jp ? cf + 1 : cf + 2 * jj + 1, jp, v32.as<float>(), kv32.as<float>());
             const int t = prev < 0 ? 0 : prev;
             prev = cur; cur = nxt; nxt = t;
         };
@@ -1570,10 +1736,10 @@ struct TetFemSim : Sim {
                 if (g) cudaGraphDestroy(g);
             }
         } graph;
-        DevBuf jbuf;
+        DevBuf jbuf;   // iteration index, advanced to 1 by the first replayed apply
         jbuf.alloc(sizeof(int));
-        const int one = 1;
-        EMS_CUDA(cudaMemcpyAsync(jbuf.p, &one, sizeof(int), cudaMemcpyHostToDevice, stream));
+        const int zero = 0;
+        EMS_CUDA(cudaMemcpyAsync(jbuf.p, &zero, sizeof(int), cudaMemcpyHostToDevice, stream));
         EMS_CUDA(cudaStreamSynchronize(stream));
         EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         for (int q = 0; q < 3; ++q) iteration(0, jbuf.as<int>());

@@ -146,7 +146,9 @@ void orc_sym3_eig(const double A_in[3][3], double w[3], double V[3][3])
         for (int j = 0; j < 3; ++j) V[i][j] = i == j ? 1.0 : 0.0;
     for (int sweep = 0; sweep < 50; ++sweep) {
         double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
-        if (off == 0.0) break;
+        /* converged: the off-diagonal sum at the rounding floor (exact zero
+           is rarely reached, and each further sweep only rounds again) */
+        if (off <= 1e-14 * (fabs(A[0][0]) + fabs(A[1][1]) + fabs(A[2][2]))) break;
         for (int p = 0; p < 2; ++p)
             for (int q = p + 1; q < 3; ++q) {
                 if (A[p][q] == 0.0) continue;
