@@ -148,19 +148,37 @@ __device__ void sym3_pinv(const double Ain[3][3], double P[3][3])
         }
 }
 
+// Plane layout of the time loop's arrays: slot d of node v (edge slot
+// e = 7 v + d of the mesh tables, the flags and the API) at d * nnode + v,
+// so a warp of consecutive nodes reads and writes contiguous memory for
+// every slot; the packed symmetric mass block of node v (28 entries) as
+// seven planes of four, entry p at ((p / 4) * nnode + v) * 4 + p % 4.
+__host__ __device__ __forceinline__ size_t fslot(size_t e, size_t nnode) { return (e % 7) * nnode + e / 7; }
+__host__ __device__ __forceinline__ size_t fpk(size_t v, int p, size_t nnode)
+{
+    return ((size_t)(p >> 2) * nnode + v) * 4 + (p & 3);
+}
+
 // Per-node inverse mass block in FP64: M_v = W S^+ W^T + alpha (I - D G^+ D^T)
 // over the node's active slots (W_i = sum_T eps_T int_T w_i, D_i the edge
 // vector, S = sym(D^T W), G = D^T D, alpha = mean consistent diagonal), then
-// inverted by Cholesky.  Writes 49 doubles per node; status[v] = 1 if the
-// block is not positive definite.
+// inverted by Cholesky.  Writes the packed block (28 entries) in the plane
+// layout in FP64 and, when pk32 is given, in FP32; *status = 1 if a block
+// is not positive definite.
 __global__ void __launch_bounds__(128) tet_minv_setup_kernel(size_t nnode, const unsigned char *__restrict__ pec,
                                                              const int *__restrict__ inc_ptr, const int *__restrict__ inc,
-                                                             const double *__restrict__ eps, double *__restrict__ minv,
-                                                             int *__restrict__ status)
+                                                             const double *__restrict__ eps, double *__restrict__ pk64,
+                                                             float *__restrict__ pk32, int *__restrict__ status)
 {
     const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nnode) return;
-    double *B = minv + 49 * v;
+    // entry (i, j), j >= i, of the packed block in the plane layout, FP64
+    // and (for FP32 runs) FP32
+    auto put = [&](int i, int j, double x) {
+        const size_t f = fpk(v, i * (13 - i) / 2 + j, nnode);
+        pk64[f] = x;
+        if (pk32) pk32[f] = (float)x;
+    };
     // Slots are indexed by their direction d, a compile-time index once the
     // loops are unrolled, so every array below stays in registers.  A PEC or
     // unused slot enters the block as an identity row and column: the
@@ -186,7 +204,10 @@ __global__ void __launch_bounds__(128) tet_minv_setup_kernel(size_t nnode, const
             }
     }
     if (k == 0) {
-        for (int q = 0; q < 49; ++q) B[q] = 0.0;
+#pragma unroll
+        for (int i = 0; i < 7; ++i)
+#pragma unroll
+            for (int j = i; j < 7; ++j) put(i, j, 0.0);
         return;
     }
     double S[3][3], G[3][3], Sp[3][3], Gp[3][3];
@@ -242,7 +263,7 @@ __global__ void __launch_bounds__(128) tet_minv_setup_kernel(size_t nnode, const
             for (int q = 0; q < j; ++q) s -= A[i * (i + 1) / 2 + q] * A[j * (j + 1) / 2 + q];
             if (i == j) {
                 if (!(s > 0.0)) {
-                    status[v] = 1;
+                    *status = 1;
                     return;
                 }
                 A[i * (i + 1) / 2 + i] = sqrt(s);
@@ -272,31 +293,10 @@ __global__ void __launch_bounds__(128) tet_minv_setup_kernel(size_t nnode, const
             double s = 0.0;
 #pragma unroll
             for (int q = i; q < 7; ++q) s += A[q * (q + 1) / 2 + i] * A[q * (q + 1) / 2 + j];
-            const double r = live[i] && live[j] ? s : 0.0;
-            B[i * 7 + j] = r;
-            B[j * 7 + i] = r;
+            put(j, i, live[i] && live[j] ? s : 0.0);
         }
 }
 
-// Plane layout of the time loop's arrays: slot d of node v (edge slot
-// e = 7 v + d of the mesh tables, the flags and the API) at d * nnode + v,
-// so a warp of consecutive nodes reads and writes contiguous memory for
-// every slot; the packed symmetric mass block of node v (28 entries) as
-// seven planes of four, entry p at ((p / 4) * nnode + v) * 4 + p % 4.
-__host__ __device__ __forceinline__ size_t fslot(size_t e, size_t nnode) { return (e % 7) * nnode + e / 7; }
-__host__ __device__ __forceinline__ size_t fpk(size_t v, int p, size_t nnode)
-{
-    return ((size_t)(p >> 2) * nnode + v) * 4 + (p & 3);
-}
-
-template <class T>
-__global__ void tet_pack_minv_kernel(size_t nnode, const double *__restrict__ full, T *__restrict__ packed)
-{
-    size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nnode) return;
-    for (int r = 0; r < 7; ++r)
-        for (int c = r; c < 7; ++c) packed[fpk(v, c_pack[r][c], nnode)] = (T)full[49 * v + 7 * r + c];
-}
 
 // ---------------------------------------------------------------- time step
 template <class T> struct alignas(4 * sizeof(T)) vec4 {
@@ -1314,7 +1314,26 @@ struct TetFemSim : Sim {
     DevBuf d_damp;
     int step_block = 64;            // threads per block of tet_step_kernel (tune_step_block)
     bool step_tuned = false;        // the block size depends on the mesh only: tuned once per handle
-    DevBuf d_tet_edge, d_inc_ptr, d_inc, d_nrec, d_pec, d_eps, d_minv64, d_minv, d_U, d_P, d_Uold, d_status;
+    DevBuf d_tet_edge, d_inc_ptr, d_inc, d_nrec, d_pec, d_eps, d_minv, d_U, d_P, d_Uold, d_status;
+    // Workspace of the Lanczos stability limit and its captured graph of
+    // three iterations, kept across set_material calls (allocating, freeing
+    // and instantiating them anew cost about 0.7 ms per setup on a 32^3
+    // mesh); the graph is captured again when the step block size changes.
+    struct LanczosWork {
+        DevBuf vb[3], mb[3], part, tickets, coef, v32, kv32, jbuf, minv;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        int block = 0;
+        const void *reads[3] = {};   // mass blocks, slot flags and node records the graph reads
+        void drop_graph()
+        {
+            if (exec) cudaGraphExecDestroy(exec);
+            if (g) cudaGraphDestroy(g);
+            exec = nullptr;
+            g = nullptr;
+        }
+        ~LanczosWork() { drop_graph(); }
+    } lz;
     std::vector<Dipole> dips;
     std::vector<std::array<int, 6>> rec_edges;
     std::vector<std::array<double, 18>> rec_w;
@@ -1505,27 +1524,25 @@ struct TetFemSim : Sim {
     // iteration (Rayleigh quotient x.Kx / x.Mx) and the time step.
     void setup()
     {
-        up(d_eps, eps_h);
-        d_minv64.alloc(49 * nnode * 8);
-        d_status.alloc(nnode * 4);
+        if (d_eps.bytes == eps_h.size() * sizeof(double))   // same size: no reallocation
+            EMS_CUDA(cudaMemcpyAsync(d_eps.p, eps_h.data(), d_eps.bytes, cudaMemcpyHostToDevice, stream));
+        else
+            up(d_eps, eps_h);
+        if (!d_status.p) d_status.alloc(sizeof(int));
         d_status.zero(stream);
+        // FP64 packed blocks for the stability limit: the run's own array in
+        // FP64 runs, a copy kept with the Lanczos workspace in FP32 runs
+        if (!fp64 && !lz.minv.p) lz.minv.alloc(28 * nnode * 8);
+        const DevBuf &minv_d = fp64 ? d_minv : lz.minv;
         unsigned nb = (unsigned)((nnode + 127) / 128);
         tet_minv_setup_kernel<<<nb, 128, 0, stream>>>(nnode, d_pec.as<unsigned char>(), d_inc_ptr.as<int>(), d_inc.as<int>(),
-                                                      d_eps.as<double>(), d_minv64.as<double>(), d_status.as<int>());
+                                                      d_eps.as<double>(), minv_d.as<double>(),
+                                                      fp64 ? nullptr : d_minv.as<float>(), d_status.as<int>());
         EMS_CUDA(cudaGetLastError());
-        std::vector<int> st(nnode);
-        EMS_CUDA(cudaMemcpyAsync(st.data(), d_status.p, nnode * 4, cudaMemcpyDeviceToHost, stream));
+        int bad = 0;
+        EMS_CUDA(cudaMemcpyAsync(&bad, d_status.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
         EMS_CUDA(cudaStreamSynchronize(stream));
-        for (int s : st)
-            if (s) throw Error{EMS_ERR_NOT_FINITE, "mass block is not positive definite"};
-        DevBuf minv_d;   // FP64 packed copy for the setup iterations
-        minv_d.alloc(28 * nnode * 8);
-        tet_pack_minv_kernel<double><<<nb, 128, 0, stream>>>(nnode, d_minv64.as<double>(), minv_d.as<double>());
-        if (fp64)
-            EMS_CUDA(cudaMemcpyAsync(d_minv.p, minv_d.p, 28 * nnode * 8, cudaMemcpyDeviceToDevice, stream));
-        else
-            tet_pack_minv_kernel<float><<<nb, 128, 0, stream>>>(nnode, d_minv64.as<double>(), d_minv.as<float>());
-        EMS_CUDA(cudaGetLastError());
+        if (bad) throw Error{EMS_ERR_NOT_FINITE, "mass block is not positive definite"};
         if (P.dt > 0) {
             dtn = P.dt / tscale;
             lambda_max = lambda_max_lanczos(minv_d, 400);
@@ -1536,7 +1553,6 @@ struct TetFemSim : Sim {
             dtn = P.cfl_fraction * dt_lim_n;
         }
         if (dtn >= dt_lim_n) throw Error{EMS_ERR_INVALID_ARGUMENT, "time step exceeds the stability limit of the integrator"};
-        d_minv64.release();
         loss_setup();
         tune_step_block();
         ready = true;
@@ -1658,13 +1674,13 @@ struct TetFemSim : Sim {
     // issues FP64 at a small fraction of its FP32 rate and the FP64 step took
     // about 50 us per apply on a 32^3 mesh.
     void applyMinvK32(const DevBuf &x32, DevBuf &kv32, const DevBuf &minv_d, const DevBuf &vcur, DevBuf &Mz, DevBuf &z,
-                      DevBuf &part, unsigned *ticket, double *alpha, int *jp)
+                      DevBuf &part, unsigned *ticket, double *alpha, int *jp, int max_blocks)
     {
         const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
         tet_step_kernel<float, 0, 0><<<nbv, step_block, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), nullptr,
                                                               kv32.as<float>(), x32.as<float>(), nullptr, nullptr, -1.0f, 0.0f,
                                                               SrcArgs{}, nullptr, nullptr, nullptr, nullptr, RecArgs<float>{});
-        const int nb = (int)std::min<size_t>((nnode + 127) / 128, kLzBlocks);
+        const int nb = (int)std::min<size_t>((nnode + 127) / 128, max_blocks);
         lanczos_minv_kernel<<<nb, 128, 0, stream>>>(nnode, minv_d.as<double>(), kv32.as<float>(), vcur.as<double>(),
                                                     Mz.as<double>(), z.as<double>(), part.as<double>(), ticket, alpha, jp);
     }
@@ -1685,72 +1701,78 @@ struct TetFemSim : Sim {
     // not move the largest one.
     double lambda_max_lanczos(const DevBuf &minv_d, int max_iters)
     {
-        DevBuf vb[3], mb[3], part, tickets, coef, v32, kv32;
-        for (int q = 0; q < 3; ++q) { vb[q].alloc(nslot * 8); mb[q].alloc(nslot * 8); }
-        v32.alloc(nslot * 4);    // FP32 copy of the vector K is applied to
-        kv32.alloc(nslot * 4);   // K v in FP32 (zeroed by each scale launch for the next apply)
-        part.alloc(kLzBlocks * 8);   // block partials of the reductions
-        tickets.alloc(2 * sizeof(unsigned));
-        tickets.zero(stream);
-        unsigned *tk = tickets.as<unsigned>();
-        // alpha_j at [2j], beta_{j+1}^2 at [2j+1]; scratch at 2 max_iters + 10 (start norm) and + 11 (alpha)
-        coef.alloc(2 * (max_iters + 6) * 8);
+        LanczosWork &w = lz;
+        if (!w.v32.p) {
+            for (int q = 0; q < 3; ++q) { w.vb[q].alloc(nslot * 8); w.mb[q].alloc(nslot * 8); }
+            w.v32.alloc(nslot * 4);    // FP32 copy of the vector K is applied to
+            w.kv32.alloc(nslot * 4);   // K v in FP32 (zeroed by each scale launch for the next apply)
+            w.part.alloc(kLzBlocks * 8);   // block partials of the reductions
+            w.tickets.alloc(2 * sizeof(unsigned));
+            w.tickets.zero(stream);
+            // alpha_j at [2j], beta_{j+1}^2 at [2j+1]; scratch at 2 max_iters + 10 (start norm) and + 11 (alpha)
+            w.coef.alloc(2 * (max_iters + 6) * 8);
+            w.jbuf.alloc(sizeof(int));
+        }
+        int nsm = 0;
+        EMS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, 0));
+        unsigned *tk = w.tickets.as<unsigned>();
         const unsigned nbs = (unsigned)((nslot + 255) / 256);
-        const int nbl = (int)std::min<size_t>(nbs, kLzBlocks);
-        double *cf = coef.as<double>(), *nrm0 = cf + 2 * max_iters + 10, *alpha = cf + 2 * max_iters + 11;
+        // the reducing launches: at most two blocks per SM (grid-stride), so
+        // that few blocks queue on the atomic ticket of the last-block sum
+        const int nbl = (int)std::min<size_t>(nbs, std::min(kLzBlocks, 2 * std::max(nsm, 1)));
+        double *cf = w.coef.as<double>(), *nrm0 = cf + 2 * max_iters + 10, *alpha = cf + 2 * max_iters + 11;
+        DevBuf *vb = w.vb, *mb = w.mb;
         // start pair (v1, Mv1) = (Minv K x0, K x0) / |.|_M, in buffers 1
         lanczos_start_kernel<<<nbs, 256, 0, stream>>>(nslot, nnode, d_pec.as<unsigned char>(), vb[0].as<double>());
-        narrow_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[0].as<double>(), v32.as<float>());
-        kv32.zero(stream);
-        applyMinvK32(v32, kv32, minv_d, vb[0], mb[1], vb[1], part, tk, alpha, nullptr);
-        dot_partial_kernel<<<512, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), part.as<double>());
-        dot_finish_kernel<<<1, 512, 0, stream>>>(512, part.as<double>(), nrm0);
-        scale_kernel<<<nbl, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), nrm0, nullptr, v32.as<float>(),
-                                              kv32.as<float>());
+        narrow_kernel<<<nbs, 256, 0, stream>>>(nslot, vb[0].as<double>(), w.v32.as<float>());
+        w.kv32.zero(stream);
+        applyMinvK32(w.v32, w.kv32, minv_d, vb[0], mb[1], vb[1], w.part, tk, alpha, nullptr, nbl);
+        dot_partial_kernel<<<512, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), w.part.as<double>());
+        dot_finish_kernel<<<1, 512, 0, stream>>>(512, w.part.as<double>(), nrm0);
+        scale_kernel<<<nbl, 256, 0, stream>>>(nslot, vb[1].as<double>(), mb[1].as<double>(), nrm0, nullptr, w.v32.as<float>(),
+                                              w.kv32.as<float>());
         int prev = -1, cur = 1, nxt = 2;
         // one iteration: apply (+ alpha), three-term step (+ beta^2),
         // normalisation; jp == nullptr: host index jj, else the device index
         // (advanced by the apply)
         auto iteration = [&](int jj, int *jp) {
-            applyMinvK32(v32, kv32, minv_d, vb[cur], mb[nxt], vb[nxt], part, tk, alpha, jp);
+            applyMinvK32(w.v32, w.kv32, minv_d, vb[cur], mb[nxt], vb[nxt], w.part, tk, alpha, jp, nbl);
             lanczos_step_kernel<<<nbl, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(), vb[cur].as<double>(),
                                                          mb[cur].as<double>(), prev >= 0 ? vb[prev].as<double>() : nullptr,
-                                                         prev >= 0 ? mb[prev].as<double>() : nullptr, alpha, part.as<double>(),
-                                                         tk + 1, cf, jj, jp);
+                                                         prev >= 0 ? mb[prev].as<double>() : nullptr, alpha,
+                                                         w.part.as<double>(), tk + 1, cf, jj, jp);
             scale_kernel<<<nbl, 256, 0, stream>>>(nslot, vb[nxt].as<double>(), mb[nxt].as<double>(),
-                                                  jp ? cf + 1 : cf + 2 * jj + 1, jp, v32.as<float>(), kv32.as<float>());
+                                                  jp ? cf + 1 : cf + 2 * jj + 1, jp, w.v32.as<float>(), w.kv32.as<float>());
             const int t = prev < 0 ? 0 : prev;
             prev = cur; cur = nxt; nxt = t;
         };
         iteration(0, nullptr);
         // iterations 1, 2, 3, ...: after the first, the three buffers rotate
         // with period 3, so one captured graph of three iterations (the
-        // coefficient index on the device) is replayed; the largest Ritz
-        // value is checked every six iterations
-        struct Graph {   // destroyed on every exit path
-            cudaGraph_t g = nullptr;
-            cudaGraphExec_t exec = nullptr;
-            ~Graph()
-            {
-                if (exec) cudaGraphExecDestroy(exec);
-                if (g) cudaGraphDestroy(g);
+        // coefficient index on the device, advanced to 1 by the first
+        // replayed apply) is replayed; the largest Ritz value is checked
+        // every six iterations
+        EMS_CUDA(cudaMemsetAsync(w.jbuf.p, 0, sizeof(int), stream));
+        const void *reads[3] = {minv_d.p, d_pec.p, d_nrec.p};
+        if (!w.exec || w.block != step_block || !std::equal(reads, reads + 3, w.reads)) {
+            w.drop_graph();
+            EMS_CUDA(cudaStreamSynchronize(stream));
+            EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            for (int q = 0; q < 3; ++q) iteration(0, w.jbuf.as<int>());
+            cudaError_t ce = cudaStreamEndCapture(stream, &w.g);
+            if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
+            ce = cudaGraphInstantiate(&w.exec, w.g, 0);
+            if (ce != cudaSuccess) {
+                w.exec = nullptr;
+                throw Error{EMS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
             }
-        } graph;
-        DevBuf jbuf;   // iteration index, advanced to 1 by the first replayed apply
-        jbuf.alloc(sizeof(int));
-        const int zero = 0;
-        EMS_CUDA(cudaMemcpyAsync(jbuf.p, &zero, sizeof(int), cudaMemcpyHostToDevice, stream));
-        EMS_CUDA(cudaStreamSynchronize(stream));
-        EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        for (int q = 0; q < 3; ++q) iteration(0, jbuf.as<int>());
-        cudaError_t ce = cudaStreamEndCapture(stream, &graph.g);
-        if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
-        ce = cudaGraphInstantiate(&graph.exec, graph.g, 0);
-        if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+            w.block = step_block;
+            std::copy(reads, reads + 3, w.reads);
+        }
         std::vector<double> h;
         double lam = 0.0, lam_old = -1.0;
         for (int done = 1, rep = 1; done < max_iters; ++rep) {
-            EMS_CUDA(cudaGraphLaunch(graph.exec, stream));
+            EMS_CUDA(cudaGraphLaunch(w.exec, stream));
             done += 3;
             if (rep % 2 == 0 || done >= max_iters) {
                 h.resize(2 * done);
