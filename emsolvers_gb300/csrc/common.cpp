@@ -26,6 +26,12 @@ void DevBuf::alloc(size_t b)
     bytes = b;
 }
 
+void DevBuf::ensure(size_t b)
+{
+    if (p && bytes == (b == 0 ? 16 : b)) return;
+    alloc(b);
+}
+
 void DevBuf::zero(cudaStream_t s) { EMS_CUDA(cudaMemsetAsync(p, 0, bytes, s)); }
 
 void DevBuf::release()

@@ -42,6 +42,7 @@ struct DevBuf {
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
     void alloc(size_t b);
+    void ensure(size_t b);   // alloc(b) unless the buffer already holds exactly b bytes
     void zero(cudaStream_t s);
     void release();
     template <class T> T *as() const { return static_cast<T *>(p); }

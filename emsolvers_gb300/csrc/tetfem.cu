@@ -1341,6 +1341,8 @@ struct TetFemSim : Sim {
     int nk = 0;   // distinct receiver slots
     bool ready = false;
     bool flags_dirty = false;       // pec_h gained source bits not yet on the device
+    std::vector<int> rec_ks;        // receiver slots flagged in pec_h and indexed by d_kidx
+    bool kidx_valid = false;        // d_kidx holds the table of rec_ks
     // recording for the adjoint: snapshots of the merged state (U, P) at the
     // start of every segment of rec_seg steps of the last run, if that run
     // started from the reset state with ckpt_nsnap > 0
@@ -1474,7 +1476,7 @@ struct TetFemSim : Sim {
 
     template <class V> void up(DevBuf &d, const std::vector<V> &v)
     {
-        d.alloc(v.size() * sizeof(V));
+        d.ensure(v.size() * sizeof(V));
         EMS_CUDA(cudaMemcpyAsync(d.p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, stream));
     }
 
@@ -2000,25 +2002,26 @@ struct TetFemSim : Sim {
         ks.erase(std::unique(ks.begin(), ks.end()), ks.end());
         std::vector<int> rk(re.size());
         for (size_t q = 0; q < re.size(); ++q) rk[q] = (int)(std::lower_bound(ks.begin(), ks.end(), re[q]) - ks.begin());
-        for (size_t e = 0; e < nslot; ++e)
-            if (pec_h[e] & kRecBit) { pec_h[e] &= (unsigned char)~kRecBit; flags_dirty = true; }
-        for (int e : ks) { pec_h[e] |= kRecBit; flags_dirty = true; }
         nk = (int)ks.size();
+        if (!kidx_valid || ks != rec_ks) {   // the receiver slots changed: flag bits and slot -> entry table
+            for (int e : rec_ks) { pec_h[e] &= (unsigned char)~kRecBit; flags_dirty = true; }
+            for (int e : ks) { pec_h[e] |= kRecBit; flags_dirty = true; }
+            std::vector<int> kidx(nslot, -1);
+            for (int k = 0; k < nk; ++k) kidx[ks[k]] = k;
+            up(d_kidx, kidx);
+            rec_ks = ks;
+            kidx_valid = true;
+        }
         if (re.empty()) { re.assign(6, 0); rw.assign(18, 0.0); rk.assign(6, 0); }
         if (ks.empty()) ks.push_back(0);
         up(d_rec_e, re);
         up(d_rec_w, rw);
         up(d_rec_k, rk);
         up(d_kslot, ks);
-        {
-            std::vector<int> kidx(nslot, -1);
-            for (int k = 0; k < nk; ++k) kidx[ks[k]] = k;
-            up(d_kidx, kidx);
-        }
-        d_rz.alloc(2 * ks.size() * (fp64 ? 8 : 4));
+        d_rz.ensure(2 * ks.size() * (fp64 ? 8 : 4));
         d_rz.zero(stream);
         size_t ntr = (size_t)std::max(nobs, 1) * std::max(nsamp, 1) * 4;
-        d_tr.alloc(ntr * 8);
+        d_tr.ensure(ntr * 8);
         d_tr.zero(stream);
         // source entries sorted by slot, entries of one slot in dipole order
         std::vector<std::array<int, 2>> ent;   // (slot, dipole * 6 + l)
@@ -2056,7 +2059,7 @@ struct TetFemSim : Sim {
         }
         t_end = t;
         up(d_src_g, gv);
-        d_ctl.alloc(16);
+        d_ctl.ensure(16);
         d_ctl.zero(stream);
         return SrcArgs{nsrc, d_src_slot.as<int>(), d_src_coef.as<double>(), d_src_dip.as<int>(), d_src_g.as<double>(),
                        d_ctl.as<int>(), (int)nd, sc.nsub, 0, 0};
