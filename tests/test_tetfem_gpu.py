@@ -293,3 +293,57 @@ def test_a_continued_run_matches_one_long_run(integ):
     np.testing.assert_allclose(second[..., 0], full[:, 40:, 0], rtol=1e-12)
     assert rel_l2(first[..., 1:], full[:, :40, 1:]) < 1e-13
     assert rel_l2(second[..., 1:], full[:, 40:, 1:]) < 1e-11
+
+
+@pytest.mark.parametrize("precision", [ems.FP32, ems.FP64], ids=["fp32", "fp64"])
+def test_material_change_on_one_handle_equals_fresh_handles(precision):
+    # the handle keeps its stability-limit workspace, the captured graph of
+    # its iterations and its run tables between set_material calls: a second
+    # material on the same handle must give what a fresh handle gives
+    n = (9, 8, 7)
+    _, _, ntet = oracle.tet_sizes(n)
+    rng = np.random.default_rng(21)
+    eps = [rng.uniform(1.0, 4.0, ntet), rng.uniform(2.0, 9.0, ntet)]
+    _, dip, recs = _case(n, 21)
+
+    def fresh(e):
+        s = ems.TetFemSimulation(n, H, 1, ems.SYMP4, precision, dt=0.0, cfl_fraction=0.9)
+        s.set_material(e)
+        s.add_dipole(np.array(dip[0]) * H, dip[1], ems.WAVE_RICKER, dip[3] / TS, dip[4])
+        for r in recs:
+            s.add_receiver(np.array(r) * H)
+        s.run(60)
+        return s.time_step(), s.traces()
+
+    s = ems.TetFemSimulation(n, H, 1, ems.SYMP4, precision, dt=0.0, cfl_fraction=0.9)
+    s.add_dipole(np.array(dip[0]) * H, dip[1], ems.WAVE_RICKER, dip[3] / TS, dip[4])
+    for r in recs:
+        s.add_receiver(np.array(r) * H)
+    for e in eps + eps[:1]:
+        s.set_material(e)
+        s.reset()
+        s.run(60)
+        ts, tr = fresh(e)
+        assert s.time_step() == ts
+        assert np.array_equal(s.traces(), tr)
+        # the oracle's power iteration converges linearly: 600 iterations leave
+        # about 3e-5 of lambda on this mesh, 4000 converge it
+        lim_o = oracle.stability_constant(oracle.SYMP4) / np.sqrt(oracle.tet_lambda_max(n, e, 4000)) * TS
+        assert abs(ts[1] - lim_o) / lim_o < 1e-5
+
+
+def test_receivers_added_between_runs_equal_a_fresh_handle():
+    # the receiver slot table is rebuilt only when the receiver set changes
+    n = (8, 8, 8)
+    eps, dip, recs = _case(n, 22)
+    more = [(n[0] * 0.33, n[1] * 0.61, n[2] * 0.52), recs[0]]
+    dtn = 0.8 * oracle.stability_constant(oracle.SYMP4) / np.sqrt(oracle.tet_lambda_max(n, eps, 300))
+    s = _gpu(n, eps, dip, recs, oracle.SYMP4, dtn, 50, ems.FP32)
+    s.run(50)   # unchanged receivers
+    for r in more:
+        s.add_receiver(np.array(r) * H)
+    s.reset()
+    s.run(70)
+    f = _gpu(n, eps, dip, recs + more, oracle.SYMP4, dtn, 70, ems.FP32)
+    assert np.array_equal(s.traces(), f.traces())
+    assert np.array_equal(s.get_field(0), f.get_field(0))
