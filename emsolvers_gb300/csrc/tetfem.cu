@@ -864,46 +864,53 @@ __global__ void __launch_bounds__(128) tet_grad_accumulate_kernel(size_t nnode, 
     for (int p = 0; p < 28; ++p) qv[p] += 0.5 * acc[p];
 }
 
-// Receiver adjoint of one sample, one block.  The receivers' edge slots are
-// listed once each (slot k gathers w * r over its receiver terms), then
-// every node holding such a slot gets the half drift that the merged loop
-// folded into the sampling: Pbar += cc Minv a, Q += cc sym((Minv a) z^T).
+// Receiver adjoint of one sample, in two launches.  The receivers' edge
+// slots are listed once each: tet_receiver_gather_kernel gathers w * r over
+// each slot's receiver terms (a, also added to Wbar); then every node
+// holding such a slot gets the half drift that the merged loop folded into
+// the sampling, Pbar += cc Minv a, Q += cc sym((Minv a) z^T), one thread per
+// node in tet_receiver_drift_kernel.  (On one block the node part was
+// bound by a single SM's FP64 rate: about 37 us per sample for 512
+// receivers.)
 template <class T>
-__global__ void __launch_bounds__(1024) tet_receiver_adjoint_kernel(int nsl, const int *__restrict__ sl_slot,
-                                                                    const int *__restrict__ sl_ptr, const int *__restrict__ term_rc,
-                                                                    const double *__restrict__ term_w, const double *__restrict__ r,
-                                                                    int nnd, const int *__restrict__ nd_node,
-                                                                    const int *__restrict__ nd_map, double *__restrict__ a_scr,
-                                                                    T *__restrict__ Wb, T *__restrict__ Pb,
-                                                                    const T *__restrict__ minv, const T *__restrict__ z,
-                                                                    double *__restrict__ Q, double cc, size_t nnode)
+__global__ void __launch_bounds__(256) tet_receiver_gather_kernel(int nsl, const int *__restrict__ sl_slot,
+                                                                  const int *__restrict__ sl_ptr, const int *__restrict__ term_rc,
+                                                                  const double *__restrict__ term_w, const double *__restrict__ r,
+                                                                  double *__restrict__ a_scr, T *__restrict__ Wb, size_t nnode)
 {
-    for (int k = threadIdx.x; k < nsl; k += blockDim.x) {
-        double acc = 0.0;
-        for (int s = sl_ptr[k]; s < sl_ptr[k + 1]; ++s) acc += term_w[s] * r[term_rc[s]];
-        a_scr[k] = acc;
-        Wb[fslot((size_t)sl_slot[k], nnode)] += (T)acc;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nsl) return;
+    double acc = 0.0;
+    for (int s = sl_ptr[k]; s < sl_ptr[k + 1]; ++s) acc += term_w[s] * r[term_rc[s]];
+    a_scr[k] = acc;
+    Wb[fslot((size_t)sl_slot[k], nnode)] += (T)acc;
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) tet_receiver_drift_kernel(int nnd, const int *__restrict__ nd_node,
+                                                                 const int *__restrict__ nd_map, const double *__restrict__ a_scr,
+                                                                 T *__restrict__ Pb, const T *__restrict__ minv,
+                                                                 const T *__restrict__ z, double *__restrict__ Q, double cc,
+                                                                 size_t nnode)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nnd) return;
+    const size_t v = (size_t)nd_node[i];
+    T x[7], y[7], zz[7];
+    for (int d = 0; d < 7; ++d) {
+        int k = nd_map[7 * i + d];
+        x[d] = k >= 0 ? (T)a_scr[k] : T(0);
+        zz[d] = z[(size_t)d * nnode + v];
     }
-    if (cc == 0.0) return;
-    __syncthreads();
-    for (int i = threadIdx.x; i < nnd; i += blockDim.x) {
-        const size_t v = (size_t)nd_node[i];
-        T x[7], y[7], zz[7];
-        for (int d = 0; d < 7; ++d) {
-            int k = nd_map[7 * i + d];
-            x[d] = k >= 0 ? (T)a_scr[k] : T(0);
-            zz[d] = z[(size_t)d * nnode + v];
-        }
-        for (int d = 0; d < 7; ++d) {
-            T s = 0;
-            for (int j = 0; j < 7; ++j) s = fma(minv[fpk(v, pk7(d, j), nnode)], x[j], s);
-            y[d] = s;
-            Pb[(size_t)d * nnode + v] = fma((T)cc, s, Pb[(size_t)d * nnode + v]);
-        }
-        for (int d = 0; d < 7; ++d)
-            for (int j = d; j < 7; ++j)
-                Q[28 * v + pk7(d, j)] += 0.5 * cc * ((double)y[d] * (double)zz[j] + (double)y[j] * (double)zz[d]);
+    for (int d = 0; d < 7; ++d) {
+        T s = 0;
+        for (int j = 0; j < 7; ++j) s = fma(minv[fpk(v, pk7(d, j), nnode)], x[j], s);
+        y[d] = s;
+        Pb[(size_t)d * nnode + v] = fma((T)cc, s, Pb[(size_t)d * nnode + v]);
     }
+    for (int d = 0; d < 7; ++d)
+        for (int j = d; j < 7; ++j)
+            Q[28 * v + pk7(d, j)] += 0.5 * cc * ((double)y[d] * (double)zz[j] + (double)y[j] * (double)zz[d]);
 }
 
 // dJ/deps contributions of node v, FP64.  With M_v = W S^+ W^T +
@@ -2186,7 +2193,7 @@ struct TetFemSim : Sim {
 
     // ---- discrete adjoint of the recorded run
     // Receiver terms grouped by edge slot and by node for
-    // tet_receiver_adjoint_kernel.
+    // tet_receiver_gather_kernel and tet_receiver_drift_kernel.
     struct RecAdj {
         DevBuf sl_slot, sl_ptr, term_rc, term_w, nd_node, nd_map, a_scr;
         int nsl = 0, nnd = 0;
@@ -2303,13 +2310,15 @@ struct TetFemSim : Sim {
                     }
                     std::swap(pb, pb2);
                 }
-                if (n % tf == 0 && n > 0 && nobs > 0) {
+                if (n % tf == 0 && n > 0 && nobs > 0 && ra.nsl > 0) {
                     const T *z = zb + (size_t)(n - n0) * nsub * nslot;
-                    tet_receiver_adjoint_kernel<T><<<1, 1024, 0, stream>>>(
+                    tet_receiver_gather_kernel<T><<<(ra.nsl + 255) / 256, 256, 0, stream>>>(
                         ra.nsl, ra.sl_slot.as<int>(), ra.sl_ptr.as<int>(), ra.term_rc.as<int>(), ra.term_w.as<double>(),
-                        d_rs.as<double>() + (size_t)(n / tf) * nobs * 3, ra.nnd, ra.nd_node.as<int>(), ra.nd_map.as<int>(),
-                        ra.a_scr.as<double>(), Wb.as<T>(), pb, d_minv.as<T>(), z, Q.as<double>(),
-                        0.5 * sc.sub[nsub - 1], nnode);
+                        d_rs.as<double>() + (size_t)(n / tf) * nobs * 3, ra.a_scr.as<double>(), Wb.as<T>(), nnode);
+                    if (sc.sub[nsub - 1] != 0.0 && ra.nnd > 0)
+                        tet_receiver_drift_kernel<T><<<(ra.nnd + 127) / 128, 128, 0, stream>>>(
+                            ra.nnd, ra.nd_node.as<int>(), ra.nd_map.as<int>(), ra.a_scr.as<double>(), pb, d_minv.as<T>(),
+                            z, Q.as<double>(), 0.5 * sc.sub[nsub - 1], nnode);
                 }
             }
             // the drifts of this segment: y at [k], z at [k] (k = nsub (n - n0) + q)
