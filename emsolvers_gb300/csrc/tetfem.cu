@@ -1535,8 +1535,8 @@ struct TetFemSim : Sim {
         if (nsnap == 0) { rec_nsteps = -1; d_snap.release(); }
     }
 
-    // FP64 mass-inverse setup on the GPU, then the stability limit by power
-    // iteration (Rayleigh quotient x.Kx / x.Mx) and the time step.
+    // FP64 mass-inverse setup on the GPU, then the stability limit (Lanczos,
+    // lambda_max_lanczos) and the time step.
     void setup()
     {
         if (d_eps.bytes == eps_h.size() * sizeof(double))   // same size: no reallocation

@@ -191,8 +191,10 @@ int ems_tetbatch_add_receiver(ems_sim *sim, int shot, const double pos[3]);
  * The recorded run keeps nsnap snapshots of the state on the device (one per
  * segment of ceil(n / nsnap) steps); the backward sweep recomputes each
  * segment from its snapshot and runs the reversed steps over it.  Fields are
- * in the handle's precision, the gradient is accumulated in FP64.  Works on
- * batch handles too (one gradient value per tetrahedron of every shot). */
+ * in the handle's precision; the gradient is accumulated in FP64 (the
+ * products of four time steps are summed in the field precision first).
+ * Works on batch handles too (one gradient value per tetrahedron of every
+ * shot). */
 /* Discrete energy H = 1/2 P.Minv P + 1/2 U.K U of the current state of a
  * symplectic run (EMS_SYMP2, EMS_SYMP4), the quantity those integrators
  * keep bounded without drift; computed in FP64 on the GPU from the run's
