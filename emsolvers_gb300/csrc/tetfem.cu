@@ -1923,13 +1923,16 @@ struct TetFemSim : Sim {
     // Receiver arguments of substep q of a step with counter parity par:
     // the first launch samples (and advances the counter), the last one of
     // a symplectic step keeps Minv P of the receiver slots for the next.
-    template <class T> RecArgs<T> rec_args(const Schedule &sc, int q, int par)
+    // sample == false (segment recomputes of the adjoint, whose traces were
+    // recorded): no sampling blocks and no Minv P kept at the receiver slots,
+    // only the step counter advance the source terms read.
+    template <class T> RecArgs<T> rec_args(const Schedule &sc, int q, int par, bool sample = true)
     {
         RecArgs<T> r{};
         const int nrz = std::max(nk, 1);
         if (q == 0) {
-            r.nrec = nobs;
-            r.nsb = nobs > 0 ? (nobs + step_block / 8 - 1) / (step_block / 8) : 0;   // eight lanes per receiver
+            r.nrec = sample ? nobs : 0;
+            r.nsb = sample && nobs > 0 ? (nobs + step_block / 8 - 1) / (step_block / 8) : 0;   // eight lanes per receiver
             r.adv = 1;
         }
         r.edges = d_rec_e.as<int>();
@@ -1943,7 +1946,7 @@ struct TetFemSim : Sim {
         r.nk = nk;
         r.kslot = d_kslot.as<int>();
         r.kidx = d_kidx.as<int>();
-        if (sc.symp && q == sc.nsub - 1 && nk > 0) r.rz_out = d_rz.as<T>() + (size_t)(1 - par) * nrz;
+        if (sample && sc.symp && q == sc.nsub - 1 && nk > 0) r.rz_out = d_rz.as<T>() + (size_t)(1 - par) * nrz;
         r.ctl = d_ctl.as<int>();
         r.par = par;
         return r;
@@ -1952,7 +1955,8 @@ struct TetFemSim : Sim {
     // One time step n (counter parity par = n % 2).  Returns the number of
     // launches.
     template <class T>
-    int enqueue_step(T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa0, T *zout, int par, T *prec = nullptr)
+    int enqueue_step(T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa0, T *zout, int par, T *prec = nullptr,
+                     bool sample = true)
     {
         int nl = 0;
         if (sc.symp) {
@@ -1960,7 +1964,7 @@ struct TetFemSim : Sim {
                 SrcArgs sa = sa0;
                 sa.q = q;
                 sa.par = par;
-                const RecArgs<T> ra = rec_args<T>(sc, q, par);
+                const RecArgs<T> ra = rec_args<T>(sc, q, par, sample);
                 T *z = zout ? zout + (size_t)q * nslot : nullptr;
                 if (has_loss && q == sc.nsub / 2)
                     nl += substep<T, 0, 1>(Uc, Uo, Pc, nullptr, (T)sc.sub[q], (T)sc.c[q], sa, z, prec,
@@ -2283,14 +2287,13 @@ struct TetFemSim : Sim {
             EMS_CUDA(cudaMemcpyAsync(Uw.p, snap, nslot * w, cudaMemcpyDeviceToDevice, stream));
             EMS_CUDA(cudaMemcpyAsync(Pw.p, snap + nslot, nslot * w, cudaMemcpyDeviceToDevice, stream));
             EMS_CUDA(cudaMemcpyAsync(d_ctl.as<int>() + (n0 & 1), &n0, sizeof(int), cudaMemcpyHostToDevice, stream));
-            rz_init<T>(Pw.as<T>(), n0 & 1);
             // z[0] = Minv P at the start of step n0
             EMS_CUDA(cudaMemsetAsync(zb, 0, nslot * w, stream));
             tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pw.as<T>(), zb, T(1));
             T *uc = Uw.as<T>(), *pc = Pw.as<T>(), *uo = Uw2.as<T>();
             for (int n = n0; n < n1; ++n)
                 enqueue_step<T>(uc, pc, uo, sc, sa, zb + ((size_t)(n - n0) * nsub + 1) * nslot, n & 1,
-                                has_loss ? pstore.as<T>() + (size_t)(n - n0) * 2 * nslot : nullptr);
+                                has_loss ? pstore.as<T>() + (size_t)(n - n0) * 2 * nslot : nullptr, false);
             for (int n = n1 - 1; n >= n0; --n) {
                 for (int q = nsub - 1; q >= 0; --q) {
                     // the drift before kick (n, q): same step (q > 0), the
