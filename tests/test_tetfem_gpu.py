@@ -347,3 +347,35 @@ def test_receivers_added_between_runs_equal_a_fresh_handle():
     f = _gpu(n, eps, dip, recs + more, oracle.SYMP4, dtn, 70, ems.FP32)
     assert np.array_equal(s.traces(), f.traces())
     assert np.array_equal(s.get_field(0), f.get_field(0))
+
+
+def test_headline_workload_at_full_size_against_the_oracle():
+    # the headline configuration at its full size: 32^3 cubes x 6 tets,
+    # eps_r U[1,4], symp4, dt = 0.9 x the stability limit chosen by the GPU,
+    # 2000 steps, one Ricker dipole (10 elements per wavelength), 8
+    # receivers on a ring.  FP64 within 1e-9 of the FP64 oracle (rounding
+    # differences over 2000 steps).  FP32 measured at 1.08e-4 here: the
+    # FP32 rounding of K U (whose curl terms cancel strongly at 10 elements
+    # per wavelength) random-walks over the 6000 substeps; below 1e-4 for
+    # 400 steps (test above) and at 1.2e-5 on the forward+adjoint workload,
+    # so the bound at this length is 2e-4
+    n = (32, 32, 32)
+    eps = np.random.default_rng(1234).uniform(1.0, 4.0, 6 * 32 ** 3)
+    f0 = C0 / (10 * H * np.sqrt(2.0))
+    src = (16.3, 15.7, 16.1)
+    recs = [(16 + 10 * np.cos(k), 16 + 10 * np.sin(k), 16.2) for k in range(8)]
+    out = {}
+    for precision in (ems.FP32, ems.FP64):
+        s = ems.TetFemSimulation(n, H, 1, ems.SYMP4, precision, dt=0.0, cfl_fraction=0.9)
+        s.set_material(eps)
+        s.add_dipole(np.array(src) * H, (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0, 1.0)
+        for r in recs:
+            s.add_receiver(np.array(r) * H)
+        s.run(2000)
+        out[precision] = (s.time_step()[0], s.traces())
+    dt = out[ems.FP32][0]
+    assert out[ems.FP64][0] == dt
+    tr_o, _, _ = oracle.tet_run(n, eps, oracle.SYMP4, dt / TS, 2000, 1, [(src, (0.0, 0.0, 1.0), 1, f0 * TS, 1.0)], recs)
+    assert np.abs(tr_o[..., 1:]).max() > 0
+    assert rel_l2(out[ems.FP64][1][..., 1:], tr_o[..., 1:]) < 1e-9
+    assert rel_l2(out[ems.FP32][1][..., 1:], tr_o[..., 1:]) < 2e-4
