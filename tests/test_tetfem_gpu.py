@@ -354,11 +354,13 @@ def test_headline_workload_at_full_size_against_the_oracle():
     # eps_r U[1,4], symp4, dt = 0.9 x the stability limit chosen by the GPU,
     # 2000 steps, one Ricker dipole (10 elements per wavelength), 8
     # receivers on a ring.  FP64 within 1e-9 of the FP64 oracle (rounding
-    # differences over 2000 steps).  FP32 measured at 1.08e-4 here: the
-    # FP32 rounding of K U (whose curl terms cancel strongly at 10 elements
-    # per wavelength) random-walks over the 6000 substeps; below 1e-4 for
-    # 400 steps (test above) and at 1.2e-5 on the forward+adjoint workload,
-    # so the bound at this length is 2e-4
+    # differences over 2000 steps).  FP32 measured at 1.08e-4 here: a phase
+    # error that grows faster than linearly with the run length (3.0e-6 at
+    # 250 steps, 4.0e-5 at 1000, 3.3e-4 at 4000), as from a fixed relative
+    # perturbation of about 1e-7 of the operator (the FP32 evaluation of
+    # K U, whose curl terms cancel at 10 elements per wavelength); the
+    # rounding of the step coefficients moves their sums by only 2e-8.  The
+    # bound at this length is therefore 2e-4
     n = (32, 32, 32)
     eps = np.random.default_rng(1234).uniform(1.0, 4.0, 6 * 32 ** 3)
     f0 = C0 / (10 * H * np.sqrt(2.0))
