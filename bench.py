@@ -374,6 +374,7 @@ def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, sample_steps=400):
             "fp64_sample": f"1 shot x {sample_steps} steps (time loop scaled to {steps}, setup once)",
             "fp64_setup_s": t1 - t0,
             "fp32_vs_fp64_trace_rel_l2": tr_err, "fp32_vs_fp64_grad_rel_l2": g_err,
+            "fp32_vs_fp64_over": f"shot 0, its first {sample_steps} of {steps} steps (forward and gradient)",
             "timing": "wall clock: material upload + FP64 mass setup + recorded forward + misfit + backward"}
 
 
