@@ -357,10 +357,8 @@ def test_headline_workload_at_full_size_against_the_oracle():
     # differences over 2000 steps).  FP32 measured at 1.08e-4 here: a phase
     # error that grows faster than linearly with the run length (3.0e-6 at
     # 250 steps, 4.0e-5 at 1000, 3.3e-4 at 4000), as from a fixed relative
-    # perturbation of about 1e-7 of the operator (the FP32 evaluation of
-    # K U, whose curl terms cancel at 10 elements per wavelength); the
-    # rounding of the step coefficients moves their sums by only 2e-8.  The
-    # bound at this length is therefore 2e-4
+    # perturbation of about 1e-7 of the FP32 operator.  The bound at this
+    # length is therefore 2e-4
     n = (32, 32, 32)
     eps = np.random.default_rng(1234).uniform(1.0, 4.0, 6 * 32 ** 3)
     f0 = C0 / (10 * H * np.sqrt(2.0))
