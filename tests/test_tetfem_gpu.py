@@ -356,9 +356,9 @@ def test_headline_workload_at_full_size_against_the_oracle():
     # receivers on a ring.  FP64 within 1e-9 of the FP64 oracle (rounding
     # differences over 2000 steps).  FP32 measured at 1.08e-4 here: a phase
     # error that grows faster than linearly with the run length (3.0e-6 at
-    # 250 steps, 4.0e-5 at 1000, 3.3e-4 at 4000), as from a fixed relative
-    # perturbation of about 1e-7 of the FP32 operator.  The bound at this
-    # length is therefore 2e-4
+    # 250 steps, 4.0e-5 at 1000, 3.3e-4 at 4000) from the FP32 rounding of
+    # the U and P updates (an FP64 loop that rounds only U and P to FP32
+    # grows the same way).  The bound at this length is therefore 2e-4
     n = (32, 32, 32)
     eps = np.random.default_rng(1234).uniform(1.0, 4.0, 6 * 32 ** 3)
     f0 = C0 / (10 * H * np.sqrt(2.0))
