@@ -164,14 +164,22 @@ extern "C" int ems_tet_stiffness_apply_static(const int cells[3], const float *u
     }
     int dev = 0;
     cudaError_t rc = cudaGetDevice(&dev);
-    if (rc != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    if (rc != cudaSuccess) {
         ems::record_error(std::string("cudaGetDevice: ") + cudaGetErrorString(rc));
         return EMS_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= kMaxDevices) {
+        ems::record_error("device index " + std::to_string(dev) + " beyond the " + std::to_string(kMaxDevices) +
+                          " devices ems_tet_stiffness_apply_static keeps scratch addresses for");
+        return EMS_ERR_INVALID_ARGUMENT;
     }
     float *scratch = nullptr;
     {
         // once per device, with that device current: the host-side name of the
-        // array is not a device address, so look the address up
+        // array is not a device address, so look the address up.  The address
+        // is kept for the life of the process; a cudaDeviceReset of the device
+        // unloads the module that holds the array, so the library must not be
+        // used on a device after the process reset it.
         std::lock_guard<std::mutex> lock(g_mu);
         if (!g_scratch[dev]) {
             rc = cudaGetSymbolAddress((void **)&scratch, g_tet_curl_scratch);

@@ -163,7 +163,8 @@ int ems_tetfem_apply_stiffness(ems_sim *sim, const double *u, double *f, size_t 
  * (12 MiB, held on every device that loads the library until exit); larger
  * meshes are rejected with EMS_ERR_INVALID_ARGUMENT.  The first call on a
  * device looks up the scratch address for that device (make that first call
- * before any stream capture).  Every call shares the one scratch array, so
+ * before any stream capture); the address is kept until the process exits,
+ * so do not call this entry point on a device after a cudaDeviceReset of it.  Every call shares the one scratch array, so
  * calls that overlap on the GPU race; the scratch is fully overwritten before
  * it is read, so nothing needs clearing between calls.  Errors are reported
  * through ems_last_error(NULL). */
