@@ -180,6 +180,22 @@ def fdtd_512(steps=60, n=512):
             "kernel": kname, "kernel_ms": kms, "kernel_bytes": kbytes, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
 
 
+def head_solve(steps=STEPS_PER_SOLVE):
+    """One headline solve (setup, then `steps` time steps) for profiling."""
+    import emsolvers_gb300 as ems
+    eps, f0, src, recs = workload()
+    sim = ems.TetFemSimulation((N, N, N), H, 1, ems.SYMP4, ems.FP32, dt=0.0, cfl_fraction=0.9, time_frequency=1)
+    sim.set_material(eps)
+    sim.add_dipole(src, (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0, 1.0)
+    for r in recs:
+        sim.add_receiver(r)
+    sim.run(steps)
+    ms, launches = sim.run_stats()
+    sim.close()
+    return {"workload": "tet32_symp4", "steps": steps, "device_ms": ms, "launches": launches,
+            "dof_updates_per_s": n_edges(N) * steps / (ms * 1e-3)}
+
+
 def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
     """Batched forward shots: nshots cubes of side n ~ U[12,40] (6 n^3
     tetrahedra each), eps_r ~ U[1,6] per tet, one Ricker dipole each, 4th-order
@@ -509,9 +525,12 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-hex", action="store_true")
-    ap.add_argument("--only", choices=["batch", "fdtd", "adjoint", "hex"],
+    ap.add_argument("--only", choices=["head", "batch", "fdtd", "adjoint", "hex"],
                     help="run one secondary workload alone and print its JSON (for profiling)")
     ap.add_argument("--fdtd-n", type=int, default=512, help="FDTD cube side for --only fdtd")
+    ap.add_argument("--head-steps", type=int, default=STEPS_PER_SOLVE, help="time steps for --only head")
+    ap.add_argument("--batch-steps", type=int, default=3000, help="time steps for --only batch")
+    ap.add_argument("--batch-sample", type=int, default=8, help="per-shot FP64 sample size for --only batch")
     ap.add_argument("--adj-n", type=int, default=48, help="cube side for --only adjoint")
     ap.add_argument("--adj-steps", type=int, default=4000, help="time steps for --only adjoint")
     ap.add_argument("--adj-shots", type=int, default=16, help="shots for --only adjoint")
@@ -521,8 +540,12 @@ def main():
     if args.only:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        fn = {"batch": batch64, "fdtd": lambda: fdtd_512(n=args.fdtd_n), "hex": hex72, "adjoint": lambda: adjoint16(n=args.adj_n, nshots=args.adj_shots, steps=args.adj_steps,
-                                             sample_steps=min(400, args.adj_steps))}[args.only]
+        fn = {"head": lambda: head_solve(args.head_steps),
+              "batch": lambda: batch64(steps=args.batch_steps, sample=args.batch_sample,
+                                       sample_steps=min(300, args.batch_steps)),
+              "fdtd": lambda: fdtd_512(n=args.fdtd_n), "hex": hex72,
+              "adjoint": lambda: adjoint16(n=args.adj_n, nshots=args.adj_shots, steps=args.adj_steps,
+                                           sample_steps=min(400, args.adj_steps))}[args.only]
         print(json.dumps(fn()))
     elif args.impl == "reference":
         run_reference(args)

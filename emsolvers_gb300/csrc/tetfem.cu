@@ -21,10 +21,10 @@
 //                (tet_minv_setup_kernel), stored packed symmetric in the run
 //                precision; applied inside tet_step_kernel from registers.
 //   adjoint      the same kernel runs the reversed steps (see "adjoint").
-//   FP32 runs    U and P carry a bfloat16 compensation plane each: every
-//                symplectic kick and drift adds its increment by an exact
-//                two-sum and keeps the rounding error for the next update
-//                (see "compensated updates").
+//   FP32 runs    the symplectic kick in double-float arithmetic: the
+//                gathered force as hi + lo, the increment split exactly, P
+//                with a bfloat16 compensation plane (see "compensated
+//                updates").
 // Units are normalised (cube edge 1, c0 = 1); the API converts.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -349,13 +349,15 @@ template <class T> __device__ __forceinline__ T block_row(const T (&mv)[28], con
 // kick in double-float arithmetic: the gathered force is kept as hi + lo
 // (each curl term is an exact product, added by an error-free two-sum,
 // Knuth), the increment a (f_hi + f_lo) is split exactly with one fused
-// multiply-add, and P and U each carry their own rounding error in a
-// bfloat16 plane (true value ~ hi + lo, |lo| <= ulp(hi)/2) that enters the
-// next update of that slot.  Only hi enters the curls, Minv P and the
-// receivers; lo is node-local and updated in place.  Curl rounding needs no
-// care: it perturbs B, and K's image of any B stays outside the null space.
+// multiply-add, and P carries its own rounding error in a bfloat16 plane
+// (true value ~ hi + lo, |lo| <= ulp(hi)/2) that enters the next kick of
+// that slot.  Only hi enters Minv P; lo is node-local and updated in place.
+// Curl rounding needs no care: it perturbs B, and K's image of any B stays
+// outside the null space.  The drift's rounding needs none either: an
+// emulation of the 32^3 headline run (2000 steps, FP64 reference) gave
+// 5.9e-6 with U compensated as well and 5.7e-6 without, against 1.3e-4
+// for plain FP32 and 2.9e-5 when the gathered force is rounded once.
 struct Comp {
-    __nv_bfloat16 *u = nullptr;   // compensation of U (the field the drift updates)
     __nv_bfloat16 *p = nullptr;   // compensation of P (the field the kick updates)
 };
 
@@ -562,6 +564,7 @@ struct StepTab {
     int eidx[18][6];   // distinct-edge index of local edge l of entry q
     int qreq[18];      // mask bits the cell of entry q needs
     int own[7];        // distinct-edge index of the node's own slot d
+    int first[7];      // entry q * 3 + component of slot d's first gather term
 };
 
 constexpr int offset_bits(int x, int y, int z)
@@ -620,6 +623,11 @@ constexpr StepTab make_step_tab()
             if (s.tail[t][0] == 0 && s.tail[t][1] == 0 && s.tail[t][2] == 0) s.own[c] = s.nedge;
             ++s.nedge;
         }
+    for (int d = 0; d < 7; ++d) s.first[d] = -1;
+    for (int q = 0; q < 18; ++q)
+        for (int k = 0; k < s.n.ne[q]; ++k)
+            for (int c = 0; c < 3; ++c)
+                if (s.n.curl[s.n.p[q]][s.n.l[q][k]][c] != 0 && s.first[s.n.d[q][k]] < 0) s.first[s.n.d[q][k]] = q * 3 + c;
     for (int q = 0; q < 18; ++q) {
         s.qreq[q] = (s.n.o[q][0] < 0 ? 1 : 2) | (s.n.o[q][1] < 0 ? 4 : 8) | (s.n.o[q][2] < 0 ? 16 : 32);
         for (int l = 0; l < 6; ++l)
@@ -639,42 +647,55 @@ static_assert(make_step_tab().ntail == 13 && make_step_tab().nedge == 43, "Kuhn 
 
 // Contribution of entry Q of the node table (a template parameter, so every
 // table index below is a compile-time constant and ue, f stay in
-// registers): the curl of the tetrahedron from the edge values ue, B =
-// curl / 6, and B . curl(w_l) added to the node's slots it feeds.  Zero curl
-// entries are left out.
-// COMP: f is kept as hi + lo (fl): every term B . curl(w_l) is exact (the
-// curl factors are +-2 or +-4), and each is added to hi by a two-sum whose
-// error goes to lo, so the gathered force carries no rounding of its own.
+// registers): the curl of the tetrahedron from the edge values ue and its
+// B = curl / 6 gathered into the node's slots it feeds, B . curl(w_l).
+// Every curl factor of the Kuhn split is +-2, so the curl is 2 S with S a
+// signed sum of edge values, B = 2 B' with B' = S / 6 rounded, and each
+// gather term B . curl(w_l) component is +-4 B'; the kernel sums +-B' and
+// scales the sum by 4 at the end (scaling by a power of two commutes with
+// rounding, so these are the bits of the straightforward evaluation).  A
+// tetrahedron outside the mesh contributes B' = 0, so every slot's first
+// term is known at compile time and starts its sum without an addition.
+// COMP: f is kept as hi + lo (fl): each term is added to hi by a two-sum
+// whose exact error goes to lo, so the gathered force carries no rounding
+// of its own.
 template <class T, int Q, int COMP>
 __device__ __forceinline__ void step_tet(const T (&ue)[43], T (&f)[7], T (&fl)[7], int have)
 {
     constexpr StepTab tab = make_step_tab();
     constexpr int p = tab.n.p[Q];
-    if ((tab.qreq[Q] & ~have) != 0) return;   // cell outside the mesh
-    T c0 = 0, c1 = 0, c2 = 0;
+    const bool inside = (tab.qreq[Q] & ~have) == 0;   // cell inside the mesh
+    T b[3];
 #pragma unroll
-    for (int l = 0; l < 6; ++l) {
-        const T u = ue[tab.eidx[Q][l]];
-        if (tab.n.curl[p][l][0] != 0) c0 = fma(u, (T)tab.n.curl[p][l][0], c0);
-        if (tab.n.curl[p][l][1] != 0) c1 = fma(u, (T)tab.n.curl[p][l][1], c1);
-        if (tab.n.curl[p][l][2] != 0) c2 = fma(u, (T)tab.n.curl[p][l][2], c2);
+    for (int c = 0; c < 3; ++c) {
+        T sum = 0;
+        bool started = false;
+#pragma unroll
+        for (int l = 0; l < 6; ++l) {
+            if (tab.n.curl[p][l][c] == 0) continue;
+            const T u = ue[tab.eidx[Q][l]];
+            if (!started) sum = tab.n.curl[p][l][c] > 0 ? u : -u;
+            else sum = tab.n.curl[p][l][c] > 0 ? sum + u : sum - u;
+            started = true;
+        }
+        b[c] = inside ? T(1.0 / 6.0) * sum : T(0);
     }
-    const T s6 = T(1.0 / 6.0);
-    const T bx = s6 * c0, by = s6 * c1, bz = s6 * c2;
 #pragma unroll
     for (int k = 0; k < 3; ++k)
         if (k < tab.n.ne[Q]) {
             const int d = tab.n.d[Q][k], l = tab.n.l[Q][k];
-            const T b3[3] = {bx, by, bz};
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                if (tab.n.curl[p][l][q] == 0) continue;
-                if constexpr (COMP) {
+            for (int c = 0; c < 3; ++c) {
+                if (tab.n.curl[p][l][c] == 0) continue;
+                const T t = tab.n.curl[p][l][c] > 0 ? b[c] : -b[c];
+                if (tab.first[d] == Q * 3 + c) {
+                    f[d] = t;
+                } else if constexpr (COMP) {
                     T e;
-                    f[d] = two_sum(f[d], b3[q] * (T)tab.n.curl[p][l][q], e);
+                    f[d] = two_sum(f[d], t, e);
                     fl[d] += e;
                 } else {
-                    f[d] = fma(b3[q], (T)tab.n.curl[p][l][q], f[d]);
+                    f[d] += t;
                 }
             }
         }
@@ -706,7 +727,7 @@ __host__ __device__ constexpr int step_record_x(int sy, int mask) { return sy | 
 // with r = rho dt / 2.  REC (the last launch of a symplectic step) also
 // keeps Minv P of the receiver slots in rec.rz_out.  COMP (FP32, MODE 0)
 // adds the kick and drift increments by compensated sums with the bfloat16
-// planes cmp.p and cmp.u (see "compensated updates"); the loss factors
+// plane cmp.p (see "compensated updates"); the loss factors
 // scale lo with hi.
 // Threads per block of the fused step: chosen per handle by timing these
 // candidates on the handle's own mesh (TetFemSim::tune_step_block); small
@@ -750,6 +771,8 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
     for (int k = 0; k < 43; ++k) ue[k] = u0[(size_t)tab.edir[k] * nnode + off[tab.etail[k]]];
     T f[7] = {0, 0, 0, 0, 0, 0, 0}, fl[7] = {0, 0, 0, 0, 0, 0, 0};
     step_tets<T, COMP>(ue, f, fl, have, std::make_integer_sequence<int, 18>{});
+#pragma unroll
+    for (int d = 0; d < 7; ++d) { f[d] *= T(4); fl[d] *= T(4); }
     const size_t e0 = 7 * v;   // the node's slots in the flag table and the source list
     unsigned char m[7];
     T x[7], u[7];
@@ -818,14 +841,7 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
     for (int d = 0; d < 7; ++d) {
         const size_t f0 = (size_t)d * nnode + v;
         const T y = block_row<T>(mv, x, d);
-        if constexpr (COMP) {
-            T uu = u[d], lu = comp_load(cmp.u, f0);
-            if (DAMP == 2) comp_scale(uu, lu, g);
-            Uout[f0] = two_sum(uu, fma(c, y, lu), lu);
-            comp_store(cmp.u, f0, lu);
-            if (zout) zout[f0] = y;
-            if (REC && ((recmask >> d) & 1)) rec.rz_out[rec.kidx[e0 + d]] = y;
-        } else if (MODE == 0) {
+        if (MODE == 0) {
             Uout[f0] = fma(c, y, DAMP == 2 ? g * u[d] : u[d]);
             if (zout) zout[f0] = y;
             if (REC && ((recmask >> d) & 1)) rec.rz_out[rec.kidx[e0 + d]] = y;
@@ -878,11 +894,10 @@ __global__ void tet_rz_init_kernel(int nk, const int *__restrict__ kslot, size_t
     rz[k] = block_row<T>(mv, x, (int)(e % 7));
 }
 
-// U += c * Minv P (drift alone), one thread per node; with cu (FP32 runs)
-// the compensated sum of the step kernel.
+// U += c * Minv P (drift alone), one thread per node.
 template <class T>
 __global__ void __launch_bounds__(128) tet_drift_kernel(size_t nnode, const T *__restrict__ minv, const T *__restrict__ P,
-                                                        T *__restrict__ U, T c, __nv_bfloat16 *__restrict__ cu = nullptr)
+                                                        T *__restrict__ U, T c)
 {
     const size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nnode) return;
@@ -893,13 +908,7 @@ __global__ void __launch_bounds__(128) tet_drift_kernel(size_t nnode, const T *_
 #pragma unroll
     for (int d = 0; d < 7; ++d) {
         const size_t f0 = (size_t)d * nnode + v;
-        if (cu) {
-            T lo = (T)comp_load(cu, f0);
-            U[f0] = two_sum(U[f0], fma(c, block_row<T>(mv, x, d), lo), lo);
-            comp_store(cu, f0, (float)lo);
-        } else {
-            U[f0] = fma(c, block_row<T>(mv, x, d), U[f0]);
-        }
+        U[f0] = fma(c, block_row<T>(mv, x, d), U[f0]);
     }
 }
 
@@ -1432,10 +1441,7 @@ struct TetFemSim : Sim {
     // FP32 runs: bfloat16 compensation planes of U and then P, one
     // allocation (plane layout, updated in place; zero after a reset)
     DevBuf d_comp;
-    Comp comp() const
-    {
-        return fp64 ? Comp{} : Comp{d_comp.as<__nv_bfloat16>(), d_comp.as<__nv_bfloat16>() + nslot};
-    }
+    Comp comp() const { return fp64 ? Comp{} : Comp{d_comp.as<__nv_bfloat16>()}; }
     // Workspace of the Lanczos stability limit and its captured graph of
     // three iterations, kept across set_material calls (allocating, freeing
     // and instantiating them anew cost about 0.7 ms per setup on a 32^3
@@ -1613,7 +1619,7 @@ struct TetFemSim : Sim {
         d_P.alloc(nslot * w); d_P.zero(stream);
         d_Uold.alloc(nslot * w); d_Uold.zero(stream);
         if (!fp64) {
-            d_comp.alloc(2 * nslot * 2);
+            d_comp.alloc(nslot * 2);
             d_comp.zero(stream);
         }
         d_minv.alloc(28 * nnode * w);
@@ -2008,7 +2014,7 @@ struct TetFemSim : Sim {
             return 1;
         };
         if constexpr (MODE == 0 && std::is_same<T, float>::value) {
-            if (cm.u) {
+            if (cm.p) {
                 if constexpr (DAMP != 2)
                     if (rec.rz_out) return go(tet_step_kernel<T, MODE, DAMP, 1, 1>);
                 return go(tet_step_kernel<T, MODE, DAMP, 0, 1>);
@@ -2029,7 +2035,7 @@ struct TetFemSim : Sim {
             T *a = d_U.as<T>(), *b = d_Uold.as<T>();
             if (odd) std::swap(a, b);
             const Comp cm = comp();
-            if (cm.u)
+            if (cm.p)
                 tet_step_kernel<T, 0, 0, 0, std::is_same<T, float>::value><<<nbv, step_block, 0, stream>>>(
                     nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), d_minv.as<T>(), d_P.as<T>(), a, b, nullptr, T(0), T(0),
                     SrcArgs{}, nullptr, nullptr, nullptr, nullptr, RecArgs<T>{}, cm);
@@ -2215,25 +2221,24 @@ struct TetFemSim : Sim {
     }
 
     // Snapshot s of the merged state of a recorded run: U and P in the run
-    // precision, then (FP32) their compensation planes.
-    size_t snap_bytes() const { return 2 * nslot * (fp64 ? 8 : 4) + (fp64 ? 0 : 2 * nslot * 2); }
+    // precision, then (FP32) the compensation plane of P.
+    size_t snap_bytes() const { return 2 * nslot * (fp64 ? 8 : 4) + (fp64 ? 0 : nslot * 2); }
     template <class T> void save_snapshot(int s, const T *U, const T *Pv)
     {
         char *b = d_snap.as<char>() + (size_t)s * snap_bytes();
         const size_t w = nslot * sizeof(T);
         EMS_CUDA(cudaMemcpyAsync(b, U, w, cudaMemcpyDeviceToDevice, stream));
         EMS_CUDA(cudaMemcpyAsync(b + w, Pv, w, cudaMemcpyDeviceToDevice, stream));
-        if (!fp64) EMS_CUDA(cudaMemcpyAsync(b + 2 * w, d_comp.p, 2 * nslot * 2, cudaMemcpyDeviceToDevice, stream));
+        if (!fp64) EMS_CUDA(cudaMemcpyAsync(b + 2 * w, d_comp.p, nslot * 2, cudaMemcpyDeviceToDevice, stream));
     }
-    // Restores snapshot s into U, P and the 2 nslot compensation values at
-    // cu (U's plane, then P's).
-    template <class T> void load_snapshot(int s, T *U, T *Pv, __nv_bfloat16 *cu)
+    // Restores snapshot s into U, P and (FP32) P's compensation plane cp.
+    template <class T> void load_snapshot(int s, T *U, T *Pv, __nv_bfloat16 *cp)
     {
         const char *b = d_snap.as<char>() + (size_t)s * snap_bytes();
         const size_t w = nslot * sizeof(T);
         EMS_CUDA(cudaMemcpyAsync(U, b, w, cudaMemcpyDeviceToDevice, stream));
         EMS_CUDA(cudaMemcpyAsync(Pv, b + w, w, cudaMemcpyDeviceToDevice, stream));
-        if (cu) EMS_CUDA(cudaMemcpyAsync(cu, b + 2 * w, 2 * nslot * 2, cudaMemcpyDeviceToDevice, stream));
+        if (cp) EMS_CUDA(cudaMemcpyAsync(cp, b + 2 * w, nslot * 2, cudaMemcpyDeviceToDevice, stream));
     }
 
     template <class T> void run_t(int nsteps)
@@ -2310,7 +2315,7 @@ struct TetFemSim : Sim {
         }
         EMS_CUDA(cudaEventRecord(ev0, stream));
         if (symp) {
-            tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)sc.hfirst, cm.u);
+            tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)sc.hfirst);
             rz_init<T>(Pc, 0);
             launches += nk > 0 ? 2 : 1;
         }
@@ -2324,7 +2329,7 @@ struct TetFemSim : Sim {
             advance(nsteps);
         }
         if (symp) {
-            tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)(-sc.hfirst), cm.u);
+            tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)(-sc.hfirst));
             ++launches;
         }
         EMS_CUDA(cudaGetLastError());
@@ -2432,11 +2437,11 @@ struct TetFemSim : Sim {
         // U, Wbar in the role of P), the latter carried across segments
         Comp cfw, cadj;
         if (!fp64) {
-            cw.alloc(2 * nslot * 2);
-            cb.alloc(2 * nslot * 2);
+            cw.alloc(nslot * 2);
+            cb.alloc(nslot * 2);
             cb.zero(stream);
-            cfw = Comp{cw.as<__nv_bfloat16>(), cw.as<__nv_bfloat16>() + nslot};
-            cadj = Comp{cb.as<__nv_bfloat16>(), cb.as<__nv_bfloat16>() + nslot};
+            cfw = Comp{cw.as<__nv_bfloat16>()};
+            cadj = Comp{cb.as<__nv_bfloat16>()};
         }
         if (has_loss) {   // P around every lossy middle kick of a segment, and the loss sensitivities
             pstore.alloc((size_t)L * 2 * nslot * w);
@@ -2448,7 +2453,7 @@ struct TetFemSim : Sim {
         T *pb = Pb.as<T>(), *pb2 = Pb2.as<T>();   // Pbar alternates between the two
         for (int s = nseg - 1; s >= 0; --s) {
             const int n0 = s * L, n1 = std::min(N, n0 + L);
-            load_snapshot<T>(s, Uw.as<T>(), Pw.as<T>(), cfw.u);
+            load_snapshot<T>(s, Uw.as<T>(), Pw.as<T>(), cfw.p);
             EMS_CUDA(cudaMemcpyAsync(d_ctl.as<int>() + (n0 & 1), &n0, sizeof(int), cudaMemcpyHostToDevice, stream));
             // z[0] = Minv P at the start of step n0
             EMS_CUDA(cudaMemsetAsync(zb, 0, nslot * w, stream));
@@ -2644,13 +2649,13 @@ struct TetFemSim : Sim {
         u += 0x7fffu + ((u >> 16) & 1u);
         return (uint16_t)(u >> 16);
     }
-    // The compensation plane of field `which` (0 = U, 1 = P) of an FP32
-    // symplectic handle, else nullptr.
+    // The compensation plane of P (which == 1) of an FP32 symplectic
+    // handle, else nullptr.
     __nv_bfloat16 *comp_plane(int which) const
     {
         const Comp c = comp();
-        if (!c.u || !schedule().symp) return nullptr;
-        return which == 0 ? c.u : c.p;
+        if (!c.p || !schedule().symp || which != 1) return nullptr;
+        return c.p;
     }
     void get_field(int which, double *out) const override
     {
@@ -2743,10 +2748,10 @@ struct TetFemSim : Sim {
         *ms = t / launches;
         // unique bytes of one substep: node records (8 B per node) + U read
         // once (the neighbours' reads hit L1/L2) + P read and written + U
-        // written + packed mass blocks + slot flags (+ FP32: the two
-        // bfloat16 compensation planes read and written)
+        // written + packed mass blocks + slot flags (+ FP32: P's bfloat16
+        // compensation plane read and written)
         *bytes = (double)nnode * 8 + (double)nslot * 4 * w + (double)(28 * nnode) * w + (double)nslot +
-                 (fp64 ? 0.0 : (double)nslot * 4 * 2);
+                 (fp64 ? 0.0 : (double)nslot * 2 * 2);
         *name = fp64 ? "tet_step_kernel<double>" : "tet_step_kernel<float>";
     }
 };

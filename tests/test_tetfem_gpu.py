@@ -429,26 +429,32 @@ def test_fp32_long_runs_within_1e4_of_fp64(side, steps, model):
 
 
 def test_fp32_field_access_carries_the_compensation():
-    # an FP32 symplectic handle keeps U and P as hi + lo (FP32 value plus a
+    # an FP32 symplectic handle keeps P as hi + lo (FP32 value plus a
     # bfloat16 compensation); get_field returns the sum, set_field splits a
-    # double again, so a round trip keeps about 24 + 8 significant bits
+    # double again, so a round trip of P keeps about 24 + 8 significant bits
+    # and one of U (plain FP32) 24
     n = (5, 4, 6)
     _, nslot, ntet = oracle.tet_sizes(n)
     rng = np.random.default_rng(31)
     eps = rng.uniform(1, 4, ntet)
     pec = oracle.tet_pec_mask(n)
     U0 = np.where(pec, 0.0, rng.standard_normal(nslot))
+    P0 = np.where(pec, 0.0, rng.standard_normal(nslot))
     s = ems.TetFemSimulation(n, H, 1, ems.SYMP4, ems.FP32, dt=0.0, cfl_fraction=0.5)
     s.set_material(eps)
     s.set_field(0, U0)
-    back = s.get_field(0)
-    assert np.max(np.abs(back - U0) / np.maximum(np.abs(U0), 1e-30)) < 2.0 ** -30
-    assert np.array_equal(back[pec], np.zeros(pec.sum()))
+    s.set_field(1, P0)
+    rel = lambda a, b: np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30))
+    assert rel(s.get_field(1), P0) < 2.0 ** -30
+    assert rel(s.get_field(0), U0) < 2.0 ** -23
+    assert np.array_equal(s.get_field(1)[pec], np.zeros(pec.sum()))
     # a continued run equals one run of the same total length
     a = ems.TetFemSimulation(n, H, 1, ems.SYMP4, ems.FP32, dt=0.0, cfl_fraction=0.5)
     a.set_material(eps)
     a.set_field(0, U0)
+    a.set_field(1, P0)
     a.run(40)
     s.run(25)
     s.run(15)
     assert rel_l2(s.get_field(0), a.get_field(0)) < 1e-6
+    assert rel_l2(s.get_field(1), a.get_field(1)) < 1e-6
