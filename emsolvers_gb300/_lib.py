@@ -38,6 +38,12 @@ class HexFemParams(C.Structure):
                 ("use_ofem", C.c_int), ("integrator", C.c_int), ("precision", C.c_int), ("kmat_dir", C.c_char_p)]
 
 
+class FemStabParams(C.Structure):
+    _fields_ = [("grid", C.c_int * 3), ("h", C.c_double), ("dt", C.c_double), ("permittivity", C.c_double),
+                ("permeability", C.c_double), ("time_frequency", C.c_int), ("stabilization_factor", C.c_double),
+                ("use_ofem", C.c_int), ("precision", C.c_int)]
+
+
 class TetFemParams(C.Structure):
     _fields_ = [("cells", C.c_int * 3), ("h", C.c_double), ("order", C.c_int), ("integrator", C.c_int),
                 ("precision", C.c_int), ("dt", C.c_double), ("cfl_fraction", C.c_double),
@@ -78,6 +84,8 @@ def lib():
         "ems_hexfem_add_observation": (C.c_int, [vp, ip]),
         "ems_hexfem_add_dipole": (C.c_int, [vp, ip]),
         "ems_hexfem_add_observation_edges": (C.c_int, [vp, ip, C.c_int, ip, C.c_int, ip, C.c_int]),
+        "ems_femstab_create": (C.c_int, [C.POINTER(FemStabParams), C.POINTER(vp)]),
+        "ems_femstab_element_matrix": (C.c_int, [vp, dp, C.c_size_t]),
         "ems_tetfem_create": (C.c_int, [C.POINTER(TetFemParams), C.POINTER(vp)]),
         "ems_tetbatch_create": (C.c_int, [C.POINTER(TetFemParams), C.c_int, ip, C.POINTER(vp)]),
         "ems_tetbatch_add_dipole": (C.c_int, [vp, C.c_int, dp, dp, C.c_int, C.c_double, C.c_double]),

@@ -16,50 +16,19 @@
 #include <iomanip>
 
 #include "ems_internal.hpp"
+#include "hexedge.cuh"
 
 namespace ems {
 
 namespace {
 
-__device__ __forceinline__ double ad(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double sb(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double ml(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double dv(double a, double b) { return __ddiv_rn(a, b); }
-__device__ __forceinline__ float ad(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ float sb(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ float ml(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ float dv(float a, float b) { return __fdiv_rn(a, b); }
-
-struct AbmGeom {
-    int gx, gy, gz;
-    size_t n[3];
-};
+using AbmGeom = HexGeom;
 
 // the four field levels of E and H for one step (ring slots 0..2, scratch 3)
 template <class T> struct Lev {
     T *E[4];
     T *H[4];
 };
-
-__device__ __forceinline__ void abm_coords(const AbmGeom &g, int c, size_t t, int &i, int &j, int &k)
-{
-    int nxc = c == 0 ? g.gx : g.gx + 1;
-    int nyc = c == 1 ? g.gy : g.gy + 1;
-    i = (int)(t % nxc);
-    size_t r = t / nxc;
-    j = (int)(r % nyc);
-    k = (int)(r / nyc);
-}
-
-// edge index of local edge q (cyclic order) of component c in cell (i,j,k)
-__device__ __forceinline__ size_t abm_edge(const AbmGeom &g, int c, int i, int j, int k, int q)
-{
-    int a0 = q & 1, a1 = q >> 1;
-    const int gx = g.gx, gy = g.gy;
-    if (c == 0) return (size_t)i + (size_t)(j + a0) * gx + (size_t)(k + a1) * gx * (gy + 1);
-    if (c == 1) return (size_t)(i + a1) + (size_t)j * (gx + 1) + (size_t)(k + a0) * (gx + 1) * gy;
-    return (size_t)(i + a0) + (size_t)(j + a1) * (gx + 1) + (size_t)k * (gx + 1) * (gy + 1);
-}
 
 // predictor / corrector right-hand sides (fem_abm 295-319, 484-508, 573-615):
 //  AB: Es = (3 H1 - H0) dt/8/eps/h,            Hs = -(3 E1 - E0) dt/8/mu/h
@@ -85,12 +54,6 @@ __global__ void abm_rhs_kernel(AbmGeom g, Lev<T> L, int am, T dt, T eps, T mu, T
     H[3][o + t] = hs;
 }
 
-__device__ __forceinline__ bool abm_e_pec(const AbmGeom &g, int c, int i, int j, int k)
-{
-    if (c == 0) return j == 0 || j == g.gy || k == 0 || k == g.gz;
-    if (c == 1) return i == 0 || i == g.gx || k == 0 || k == g.gz;
-    return i == 0 || i == g.gx || j == 0 || j == g.gy;
-}
 __device__ __forceinline__ bool abm_h_pec(const AbmGeom &g, int c, int i, int j, int k)
 {
     if (c == 0) return i == 0 || i == g.gx - 1;
@@ -110,7 +73,7 @@ __global__ void __launch_bounds__(128) abm_sweep_kernel(AbmGeom g, const T *__re
     if (t >= g.n[c]) return;
     const size_t off[3] = {0, g.n[0], g.n[0] + g.n[1]};
     int i, j, k;
-    abm_coords(g, c, t, i, j, k);
+    hex_coords(g, c, t, i, j, k);
     // candidate cells: offsets (a0, a1) on the two transverse axes of the
     // cyclic order, local q = a0 + 2 a1, visited in increasing element index
     T acc_e = 0, acc_h = 0;
@@ -127,7 +90,7 @@ __global__ void __launch_bounds__(128) abm_sweep_kernel(AbmGeom g, const T *__re
         T te = 0, th = 0;
         for (int m = 0; m < 12; ++m) {
             int mc = m >> 2, mq = m & 3;
-            size_t idx = off[mc] + abm_edge(g, mc, ci, cj, ck, mq);
+            size_t idx = off[mc] + hex_edge(g, mc, ci, cj, ck, mq);
             T es = E[3][idx], hs = H[3][idx];
             if (EXACT) {
                 te = ad(te, ml(K[m * 12 + r], es));
@@ -143,49 +106,11 @@ __global__ void __launch_bounds__(128) abm_sweep_kernel(AbmGeom g, const T *__re
     T e2 = EXACT ? ad(acc_e, E[1][off[c] + t]) : acc_e + E[1][off[c] + t];
     T h2 = EXACT ? ad(acc_h, H[1][off[c] + t]) : acc_h + H[1][off[c] + t];
     if (bc) {
-        if (abm_e_pec(g, c, i, j, k)) e2 = 0;
+        if (hex_e_pec(g, c, i, j, k)) e2 = 0;
         if (abm_h_pec(g, c, i, j, k)) h2 = 0;
     }
     E[2][off[c] + t] = e2;
     H[2][off[c] + t] = h2;
-}
-
-// Point sources and dipole weights in the reference's statement order.
-// op: 0 = subtract, 1 = add.  Entries on PEC-zeroed DOFs are skipped when
-// `bc` is set (the reference zeroes them right after).
-template <class T>
-__global__ void abm_source_kernel(AbmGeom g, T *E2, int n, const long long *idx, const double *val, const int *op, int bc)
-{
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int s = 0; s < n; ++s) {
-        size_t q = (size_t)idx[s];
-        if (bc) {
-            int c = q < g.n[0] ? 0 : (q < g.n[0] + g.n[1] ? 1 : 2);
-            size_t t = q - (c == 0 ? 0 : (c == 1 ? g.n[0] : g.n[0] + g.n[1]));
-            int i, j, k;
-            abm_coords(g, c, t, i, j, k);
-            if (abm_e_pec(g, c, i, j, k)) continue;
-        }
-        T v = (T)val[s];
-        E2[q] = op[s] ? ad(E2[q], v) : sb(E2[q], v);
-    }
-}
-
-// Receivers: sums over listed edges of E2, divided by the count (972-1013).
-template <class T>
-__global__ void abm_sample_kernel(int nobs, const int *cnt, const int *start, const long long *idx, const T *E2, double *tr,
-                                  int nsamp, int s)
-{
-    int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= nobs) return;
-    double *out = tr + ((size_t)o * nsamp + s) * 3;
-    int q = start[o];
-    for (int c = 0; c < 3; ++c) {
-        int n = cnt[3 * o + c];
-        double acc = out[c];
-        for (int r = 0; r < n; ++r, ++q) acc = __dadd_rn(acc, (double)E2[idx[q]]);
-        out[c] = acc / (double)n;
-    }
 }
 
 double abm_source(double t, double h)
@@ -223,10 +148,7 @@ struct AbmSim : Sim {
         EMS_CHECK_ARG(P.grid[0] >= 2 && P.grid[1] >= 2 && P.grid[2] >= 2, "need at least two cells per direction");
         double c = 1.0 / std::sqrt(P.permittivity * P.permeability);
         EMS_CHECK_ARG(c * P.dt < P.h, "time step violates c*dt < h (reference check_params)");
-        g.gx = P.grid[0]; g.gy = P.grid[1]; g.gz = P.grid[2];
-        g.n[0] = (size_t)g.gx * (g.gy + 1) * (g.gz + 1);
-        g.n[1] = (size_t)(g.gx + 1) * g.gy * (g.gz + 1);
-        g.n[2] = (size_t)(g.gx + 1) * (g.gy + 1) * g.gz;
+        g = hex_geom(P.grid[0], P.grid[1], P.grid[2]);
         ntot = g.n[0] + g.n[1] + g.n[2];
         fp64 = P.precision == EMS_FP64;
         // K = A + 0.05 Abar (fem_abm/fem_simulation.cpp:143-246)
@@ -261,14 +183,7 @@ struct AbmSim : Sim {
     }
 
     size_t comp_off(int c) const { return c == 0 ? 0 : (c == 1 ? g.n[0] : g.n[0] + g.n[1]); }
-    long long flat(int c, int i, int j, int k) const
-    {
-        const int gx = g.gx, gy = g.gy;
-        size_t t = c == 0 ? (size_t)i + (size_t)j * gx + (size_t)k * gx * (gy + 1)
-                 : c == 1 ? (size_t)i + (size_t)j * (gx + 1) + (size_t)k * (gx + 1) * gy
-                          : (size_t)i + (size_t)j * (gx + 1) + (size_t)k * (gx + 1) * (gy + 1);
-        return (long long)(comp_off(c) + t);
-    }
+    long long flat(int c, int i, int j, int k) const { return hex_flat(g, c, i, j, k); }
     // device layout: [level][component], 4 levels of ntot values; the ring
     // maps the logical levels n-1, n, n+1 to storage slots
     template <class T> Lev<T> levels(int ring[3]) const
@@ -278,35 +193,6 @@ struct AbmSim : Sim {
         L.E[3] = dE.as<T>() + 3 * ntot;
         L.H[3] = dH.as<T>() + 3 * ntot;
         return L;
-    }
-
-    // The reference's dipole statement list for one cell (fem_abm 407-481):
-    // (edge index, weight, +1 add / -1 subtract)
-    void dipole_terms(const std::array<int, 3> &p, std::vector<long long> &idx, std::vector<double> &wt, std::vector<int> &op) const
-    {
-        int i = p[0], j = p[1], k = p[2];
-        auto X = [&](int ci, int cj, int ck, int q) { return flat(0, ci, cj + (q & 1), ck + (q >> 1)); };
-        auto Y = [&](int ci, int cj, int ck, int q) { return flat(1, ci + (q >> 1), cj, ck + (q & 1)); };
-        auto Z = [&](int ci, int cj, int ck, int q) { return flat(2, ci + (q & 1), cj + (q >> 1), ck); };
-        // cells c0 = (i,j,k), c1 = (i,j+1,k), c2 = (i,j,k+1), c3 = (i,j+1,k+1)
-        const int C[4][3] = {{i, j, k}, {i, j + 1, k}, {i, j, k + 1}, {i, j + 1, k + 1}};
-        struct T { int comp, cell, q; double w; int add; };
-        const double s2 = kSF / 2.0;
-        const T terms[] = {
-            {0, 0, 0, 1.0 / 8.0, 1}, {0, 0, 1, 3.0 / 4.0, 1}, {0, 0, 2, 3.0 / 4.0, 1}, {0, 0, 3, 9.0 / 2.0, 1},
-            {0, 1, 1, 1.0 / 8.0, 1}, {0, 1, 3, 3.0 / 4.0, 1}, {0, 2, 2, 1.0 / 8.0, 1}, {0, 2, 3, 3.0 / 4.0, 1},
-            {0, 3, 3, 1.0 / 8.0, 1},
-            {1, 0, 0, s2, 1}, {1, 0, 2, s2, 1}, {1, 1, 0, s2, 1}, {1, 1, 2, s2, 1},
-            {1, 2, 1, s2, 0}, {1, 2, 3, s2, 0}, {1, 3, 1, s2, 0}, {1, 3, 3, s2, 0},
-            {2, 0, 0, s2, 0}, {2, 0, 1, s2, 0}, {2, 1, 2, s2, 1}, {2, 1, 3, s2, 1},
-            {2, 2, 0, s2, 0}, {2, 2, 1, s2, 0}, {2, 3, 2, s2, 1}, {2, 3, 3, s2, 1}};
-        for (const T &t : terms) {
-            const int *cc = C[t.cell];
-            long long e = t.comp == 0 ? X(cc[0], cc[1], cc[2], t.q) : t.comp == 1 ? Y(cc[0], cc[1], cc[2], t.q) : Z(cc[0], cc[1], cc[2], t.q);
-            idx.push_back(e);
-            wt.push_back(t.w);
-            op.push_back(t.add);
-        }
     }
 
     template <class T> void run_t(int nsteps)
@@ -344,7 +230,7 @@ struct AbmSim : Sim {
                 if (s[0] == c) { sidx.push_back(flat(c, s[1], s[2], s[3])); swt.push_back(1.0); sop.push_back(0); skind.push_back(0); }
         for (auto &d : dips) {
             size_t b = sidx.size();
-            dipole_terms(d, sidx, swt, sop);
+            hex_dipole_terms(g, d, kSF, sidx, swt, sop);
             for (size_t q = b; q < sidx.size(); ++q) skind.push_back(1);
         }
         const int ns = (int)sidx.size();
@@ -387,7 +273,7 @@ struct AbmSim : Sim {
             else abm_sweep_kernel<T, false><<<grid, 128, 0, stream>>>(g, dK.as<T>(), L, 0);
             launches += 2;
             if (ns) {
-                abm_source_kernel<T><<<1, 32, 0, stream>>>(g, Ep[2], ns, d_src_idx.as<long long>(),
+                hex_source_kernel<T><<<1, 32, 0, stream>>>(g, Ep[2], ns, d_src_idx.as<long long>(),
                                                            d_src_val.as<double>() + ((size_t)(step - 1) * 2 + 0) * ns, d_src_op.as<int>(), 0);
                 ++launches;
             }
@@ -396,12 +282,12 @@ struct AbmSim : Sim {
             else abm_sweep_kernel<T, false><<<grid, 128, 0, stream>>>(g, dK.as<T>(), L, 1);
             launches += 2;
             if (ns) {
-                abm_source_kernel<T><<<1, 32, 0, stream>>>(g, Ep[2], ns, d_src_idx.as<long long>(),
+                hex_source_kernel<T><<<1, 32, 0, stream>>>(g, Ep[2], ns, d_src_idx.as<long long>(),
                                                            d_src_val.as<double>() + ((size_t)(step - 1) * 2 + 1) * ns, d_src_op.as<int>(), 1);
                 ++launches;
             }
             if (nobs > 0 && step % tf == 0) {
-                abm_sample_kernel<T><<<(nobs + 63) / 64, 64, 0, stream>>>(nobs, d_obs_cnt.as<int>(), d_obs_start.as<int>(),
+                hex_sample_kernel<T><<<(nobs + 63) / 64, 64, 0, stream>>>(nobs, d_obs_cnt.as<int>(), d_obs_start.as<int>(),
                                                                          d_obs_idx.as<long long>(), Ep[2], d_tr.as<double>(), nsamp, step / tf);
                 ++launches;
             }
@@ -424,6 +310,7 @@ struct AbmSim : Sim {
     {
         EMS_CHECK_ARG(nsteps >= 0, "num_steps must be >= 0");
         if (fp64) run_t<double>(nsteps); else run_t<float>(nsteps);
+        check_finite({{dE.p, 3 * ntot}, {dH.p, 3 * ntot}}, fp64);   // the three ring levels (the scratch level is not state)
     }
 
     // which 0..2: E components (4 levels each, the reference's layout per

@@ -22,21 +22,10 @@
 
 #include "ems.h"
 
-namespace {
-std::string compress(double value)
-{
-    char buf[64];
-    std::snprintf(buf, sizeof buf, "%.6e", value);
-    std::string s = buf;
-    size_t e = s.find_first_of("eE");
-    if (e == std::string::npos) return s;
-    std::string mant = s.substr(0, e), ex = s.substr(e);
-    if (ex == "e+00" || ex == "E+00") ex = "";
-    mant.erase(mant.find_last_not_of('0') + 1, std::string::npos);
-    if (!mant.empty() && mant.back() == '.') mant.pop_back();
-    return mant + ex;
+namespace ems {
+// the reference's number format in result file names (libems, common.cpp)
+std::string compress_number(double v);
 }
-}  // namespace
 
 int main(int argc, char *argv[])
 {
@@ -74,9 +63,9 @@ int main(int argc, char *argv[])
     else if (integ == "leapfrog") { p.integrator = EMS_LEAPFROG; prefix = ""; }
     else { std::cerr << "EMS_INTEGRATOR must be leapfrog, symp2 or symp4" << std::endl; return 1; }
     std::string filename = prefix + (use_ofem ? "ofem" : "fem") + std::to_string(order) + "_" + std::to_string(scale) + "_" +
-                           compress(dsx) + "_" + compress(dsy) + "_" + compress(dsz) + "_" + compress(duration) + "_" +
-                           compress(sp[0]) + "_" + compress(sp[1]) + "_" + compress(sp[2]) + "_" + compress(op[0]) + "_" +
-                           compress(op[1]) + "_" + compress(op[2]) + ".csv";
+                           ems::compress_number(dsx) + "_" + ems::compress_number(dsy) + "_" + ems::compress_number(dsz) + "_" + ems::compress_number(duration) + "_" +
+                           ems::compress_number(sp[0]) + "_" + ems::compress_number(sp[1]) + "_" + ems::compress_number(sp[2]) + "_" + ems::compress_number(op[0]) + "_" +
+                           ems::compress_number(op[1]) + "_" + ems::compress_number(op[2]) + ".csv";
     // check_params (fem_v2/fem_simulation.cpp:1355-1388)
     if (dsx <= 0 || dsy <= 0 || dsz <= 0 || grid <= 0 || duration <= 0 || dt <= 0 ||
         std::round(dsx / grid) != std::round(dsy / grid) || std::round(dsx / grid) != std::round(dsz / grid) || c * dt >= h) {

@@ -121,6 +121,7 @@ int ems_hexfem_set_source(ems_sim *s, int comp, const int ijk[3])
     return guard(s, [&] {
         if (comp < 0 || comp > 2 || !ijk) throw Error{EMS_ERR_INVALID_ARGUMENT, "component must be 0, 1 or 2"};
         if (ems::is_abm(s->impl)) ems::abm_set_source(s->impl, comp, ijk);
+        else if (ems::is_femstab(s->impl)) ems::femstab_set_source(s->impl, comp, ijk);
         else ems::hexfem_set_source(s->impl, comp, ijk);
     });
 }
@@ -128,8 +129,8 @@ int ems_hexfem_add_observation(ems_sim *s, const int ijk[3])
 {
     NEED(s, ems::Kind::HEXFEM);
     return guard(s, [&] {
-        if (ems::is_abm(s->impl))
-            throw Error{EMS_ERR_STATE, "Adams-Bashforth-Moulton receivers take edge lists (ems_hexfem_add_observation_edges)"};
+        if (ems::is_abm(s->impl) || ems::is_femstab(s->impl))
+            throw Error{EMS_ERR_STATE, "this solver's receivers take edge lists (ems_hexfem_add_observation_edges)"};
         ems::hexfem_add_observation(s->impl, ijk);
     });
 }
@@ -137,16 +138,34 @@ int ems_hexfem_add_dipole(ems_sim *s, const int ijk[3])
 {
     NEED(s, ems::Kind::HEXFEM);
     return guard(s, [&] {
-        if (!ems::is_abm(s->impl)) throw Error{EMS_ERR_STATE, "Hertz dipoles belong to the Adams-Bashforth-Moulton solver"};
-        ems::abm_add_dipole(s->impl, ijk);
+        if (ems::is_femstab(s->impl)) ems::femstab_add_dipole(s->impl, ijk);
+        else if (ems::is_abm(s->impl)) ems::abm_add_dipole(s->impl, ijk);
+        else throw Error{EMS_ERR_STATE, "Hertz dipoles belong to the Adams-Bashforth-Moulton and fem/ solvers"};
     });
 }
 int ems_hexfem_add_observation_edges(ems_sim *s, const int *x, int nx, const int *y, int ny, const int *z, int nz)
 {
     NEED(s, ems::Kind::HEXFEM);
     return guard(s, [&] {
-        if (!ems::is_abm(s->impl)) throw Error{EMS_ERR_STATE, "edge-list receivers belong to the Adams-Bashforth-Moulton solver"};
-        ems::abm_add_observation(s->impl, x, nx, y, ny, z, nz);
+        if (ems::is_femstab(s->impl)) ems::femstab_add_observation(s->impl, x, nx, y, ny, z, nz);
+        else if (ems::is_abm(s->impl)) ems::abm_add_observation(s->impl, x, nx, y, ny, z, nz);
+        else throw Error{EMS_ERR_STATE, "edge-list receivers belong to the Adams-Bashforth-Moulton and fem/ solvers"};
+    });
+}
+
+int ems_femstab_create(const ems_femstab_params *p, ems_sim **out)
+{
+    if (!p) return EMS_ERR_INVALID_ARGUMENT;
+    return create(out, [&] { return ems::make_femstab(p); });
+}
+int ems_femstab_element_matrix(const ems_sim *s, double *K, size_t n)
+{
+    if (!s) return EMS_ERR_INVALID_ARGUMENT;
+    auto *m = const_cast<ems_sim *>(s);
+    return guard(m, [&] {
+        if (!ems::is_femstab(s->impl)) throw Error{EMS_ERR_STATE, "handle is not a fem/ (ems_femstab_create) solver"};
+        EMS_CHECK_ARG(K != nullptr && n == 144, "K must hold 144 values");
+        ems::femstab_element_matrix(s->impl, K);
     });
 }
 

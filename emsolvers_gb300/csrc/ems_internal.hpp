@@ -4,6 +4,8 @@
 
 #include <array>
 #include <cstdio>
+#include <initializer_list>
+#include <utility>
 #include <type_traits>
 #include <string>
 #include <vector>
@@ -78,6 +80,10 @@ struct Sim {
     // One receiver component as the `t,u` CSV that
     // TF_MISFIT_GOF_master/main.py:6-40 reads.
     void save_component(int receiver, int component, const char *path) const;
+    // Throws EMS_ERR_NOT_FINITE when one of the device arrays (pointer,
+    // element count; FP64 or FP32) holds a NaN or an Inf.
+    void check_finite(std::initializer_list<std::pair<const void *, size_t>> arrays, bool fp64);
+    DevBuf d_finite;
 };
 
 // CSV element matrices in the reference format (fem_v2/fem_simulation.cpp:1477-1524).
@@ -94,6 +100,12 @@ Sim *make_tetbatch(const ems_tetfem_params *p, int nshots, const int *cells);
 void tetbatch_add_dipole(Sim *s, int shot, const double pos[3], const double dir[3], int waveform, double f0, double amp);
 void tetbatch_add_receiver(Sim *s, int shot, const double pos[3]);
 bool is_abm(const Sim *s);
+Sim *make_femstab(const ems_femstab_params *p);
+bool is_femstab(const Sim *s);
+void femstab_set_source(Sim *s, int comp, const int ijk[3]);
+void femstab_add_dipole(Sim *s, const int ijk[3]);
+void femstab_add_observation(Sim *s, const int *x, int nx, const int *y, int ny, const int *z, int nz);
+void femstab_element_matrix(const Sim *s, double *K);
 void abm_set_source(Sim *s, int comp, const int ijk[3]);
 void abm_add_dipole(Sim *s, const int ijk[3]);
 void abm_add_observation(Sim *s, const int *x, int nx, const int *y, int ny, const int *z, int nz);

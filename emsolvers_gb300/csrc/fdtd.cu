@@ -675,6 +675,7 @@ struct FdtdSim : Sim {
     {
         EMS_CHECK_ARG(nsteps >= 0, "num_steps must be >= 0");
         if (fp64) run_t<double>(nsteps); else run_t<float>(nsteps);
+        check_finite({{F[0].p, n[0]}, {F[1].p, n[1]}, {F[2].p, n[2]}, {F[3].p, n[3]}, {F[4].p, n[4]}, {F[5].p, n[5]}}, fp64);
     }
 
     size_t field_size(int which) const override

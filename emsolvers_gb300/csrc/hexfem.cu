@@ -442,6 +442,8 @@ struct HexFemSim : Sim {
         EMS_CHECK_ARG(nsteps >= 0, "num_steps must be >= 0");
         EMS_CHECK_ARG(srcs.size() <= (size_t)kMaxSrc, "at most 8 point sources");
         if (fp64) run_t<double>(nsteps); else run_t<float>(nsteps);
+        const size_t w = fp64 ? 8 : 4;
+        check_finite({{lev[0].p, lev[0].bytes / w}, {lev[1].p, lev[1].bytes / w}, {lev[2].p, lev[2].bytes / w}}, fp64);
     }
 
     size_t field_size(int which) const override

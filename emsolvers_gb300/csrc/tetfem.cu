@@ -2599,6 +2599,7 @@ struct TetFemSim : Sim {
     {
         EMS_CHECK_ARG(nsteps >= 0, "num_steps must be >= 0");
         if (fp64) run_t<double>(nsteps); else run_t<float>(nsteps);
+        check_finite({{d_U.p, nslot}, {d_P.p, nslot}}, fp64);
     }
 
     size_t field_size(int which) const override

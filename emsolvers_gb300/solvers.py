@@ -5,6 +5,8 @@ C ABI.  Method names and argument meanings follow the reference's
 * :class:`FdtdSimulation`  — fdtd/fdtd_simulation.hpp:9-30
 * :class:`HexFemSimulation` — fem_v2/fem_simulation.hpp:10-42 (with the
   integrator of symplectic_2 / symplectic_4 selectable)
+* :class:`FemStabSimulation` — fem/fem_simulation.hpp:9-36 (stabilised
+  order-1 hexahedra)
 * :class:`TetFemSimulation` — tetrahedral Nedelec elements (new)
 """
 import ctypes as C
@@ -205,6 +207,56 @@ class HexFemSimulation(_Sim):
 
     def levels(self):
         return [self.get_field(q) for q in range(3)]
+
+    def saveResults(self, num_steps, filename):
+        self._check(lib().ems_save_results(self._h, filename.encode()))
+
+
+class FemStabSimulation(_Sim):
+    """fem/fem_simulation.hpp:12-14 constructor: the stabilised order-1
+    hexahedral solver (conventional or OFEM basis, stabilisation factor s)."""
+
+    def __init__(self, grid_size, domain_size, time_step, permittivity, permeability, time_frequency,
+                 stabilization_factor, use_ofem, precision=FP64):
+        super().__init__()
+        p = _lib.FemStabParams()
+        p.grid[:] = list(grid_size)
+        p.h, p.dt, p.permittivity, p.permeability = domain_size, time_step, permittivity, permeability
+        p.time_frequency, p.stabilization_factor = time_frequency, stabilization_factor
+        p.use_ofem, p.precision = use_ofem, precision
+        self.params = p
+        check(lib().ems_femstab_create(C.byref(p), C.byref(self._h)))
+
+    def _src(self, comp, position):
+        ijk = (C.c_int * 3)(*[int(v) for v in position])
+        self._check(lib().ems_hexfem_set_source(self._h, comp, ijk))
+
+    def setSource_x(self, position):
+        self._src(0, position)
+
+    def setSource_y(self, position):
+        self._src(1, position)
+
+    def setSource_z(self, position):
+        self._src(2, position)
+
+    def setSourceDipole_x(self, position):
+        """x-directed Hertz dipole over cells (i, j..j+1, k..k+1)."""
+        ijk = (C.c_int * 3)(*[int(v) for v in position])
+        self._check(lib().ems_hexfem_add_dipole(self._h, ijk))
+
+    def setObservationPoint(self, position):
+        """Three lists of (i, j, k) edges of Ex, Ey and Ez, averaged."""
+        arrs = [np.ascontiguousarray(np.array(l, np.int32).reshape(-1)) for l in position]
+        ptrs = [a.ctypes.data_as(_ip) for a in arrs]
+        self._check(lib().ems_hexfem_add_observation_edges(self._h, ptrs[0], len(position[0]), ptrs[1], len(position[1]),
+                                                           ptrs[2], len(position[2])))
+
+    def element_matrix(self):
+        """The element matrix K (12 x 12) of the handle."""
+        K = np.zeros(144)
+        self._check(lib().ems_femstab_element_matrix(self._h, _dptr(K), K.size))
+        return K.reshape(12, 12)
 
     def saveResults(self, num_steps, filename):
         self._check(lib().ems_save_results(self._h, filename.encode()))

@@ -4,6 +4,7 @@
  *   fdtd/          Yee FDTD                 -> ems_fdtd_*
  *   fem_v2/, symplectic_2/, symplectic_4/   -> ems_hexfem_* (leapfrog, symp2, symp4)
  *   fem_abm/       Adams-Bashforth-Moulton  -> ems_hexfem_* with EMS_ABM
+ *   fem/           stabilised order 1       -> ems_femstab_*
  *   (new)          tetrahedral Nedelec FEM  -> ems_tetfem_*
  * The reference exposes C++ classes named FemSimulation; each entry point
  * below names the member it replaces.  Conventions:
@@ -36,7 +37,8 @@ enum ems_status {
     EMS_ERR_IO = -4,                /* file missing / unreadable / malformed */
     EMS_ERR_STATE = -5,             /* call not valid in the handle's state */
     EMS_ERR_DEVICE_TIMEOUT = -6,    /* a bounded device-side wait gave up */
-    EMS_ERR_NOT_FINITE = -7,        /* NaN/Inf detected in the fields */
+    EMS_ERR_NOT_FINITE = -7,        /* NaN/Inf in the fields after ems_run (the run's traces stay readable),
+                                       or a tetrahedral mass block that is not positive definite */
     EMS_ERR_UNSUPPORTED = -8        /* combination not implemented */
 };
 
@@ -122,6 +124,31 @@ int ems_hexfem_add_dipole(ems_sim *sim, const int ijk[3]);
  * averaging n_x x-edges, n_y y-edges and n_z z-edges of E. */
 int ems_hexfem_add_observation_edges(ems_sim *sim, const int *x_ijk, int n_x, const int *y_ijk, int n_y, const int *z_ijk,
                                      int n_z);
+
+/* ------------------------------- stabilised order-1 hexahedral FEM (fem/) */
+typedef struct {
+    int grid[3];                /* cells per direction (order 1: one edge per cell side) */
+    double h;                   /* cell size [m] (reference: domain_size) */
+    double dt;                  /* time step [s] */
+    double permittivity, permeability;
+    int time_frequency;
+    double stabilization_factor;/* s of At = A + s Abar, Bt = B + s Bbar, Ct = C + s Cbar (reference default 0.3) */
+    int use_ofem;               /* 0: conventional basis, 1: orthogonal (OFEM) basis */
+    int precision;              /* EMS_FP64 (bit-identical to the reference) or EMS_FP32 */
+} ems_femstab_params;
+
+/* Replaces FemSimulation::FemSimulation + calculateElementStiffnessMatrix of
+ * fem/fem_simulation.cpp:40-57,125-434: the three-level update
+ * E^{n+1} = -K E^n + 2 E^n - E^{n-1} with K = dt^2 / (2 mu eps h^2) Ct Bt^-1 At.
+ * The handle takes point sources (ems_hexfem_set_source, fem/:436-454),
+ * x-directed Hertz dipoles (ems_hexfem_add_dipole, fem/:456-459, injection
+ * 636-740) and edge-list receivers (ems_hexfem_add_observation_edges,
+ * fem/:461-466, sampling 856-903).  Fields: which 0..2 = Ex, Ey, Ez, the
+ * reference's three levels per component (fem/:67-72). */
+int ems_femstab_create(const ems_femstab_params *params, ems_sim **out);
+/* The handle's element matrix K (12 x 12 row-major, the dt^2 / (2 mu eps h^2)
+ * factor included; the reference's element_stiffness_matrix_), n = 144. */
+int ems_femstab_element_matrix(const ems_sim *sim, double *K, size_t n);
 
 /* -------------------------------------------------------- tetrahedral FEM */
 typedef struct {

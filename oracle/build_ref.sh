@@ -18,6 +18,11 @@ for v in fem_v2 symplectic_2 symplectic_4; do
   $CXX -I"$REF/$v" "$HERE/ref_drivers/femv2_ref_main.cpp" "$REF/$v/fem_simulation.cpp" -o "$OUT/${v}_ref" & pids+=($!)
 done
 $CXX -I"$REF/fem_abm" "$HERE/ref_drivers/abm_ref_main.cpp" "$REF/fem_abm/fem_simulation.cpp" -o "$OUT/fem_abm_ref" & pids+=($!)
+$CXX -I"$REF/fem" "$HERE/ref_drivers/femstab_ref_main.cpp" "$REF/fem/fem_simulation.cpp" -o "$OUT/fem_ref" & pids+=($!)
+# the reference's own fem_v2 program (argv interface, output file name and format)
+for v in fem_v2 symplectic_2 symplectic_4; do
+  $CXX -fopenmp -I"$REF/$v" "$REF/$v/main.cpp" "$REF/$v/fem_simulation.cpp" -o "$OUT/${v}_main" & pids+=($!)
+done
 rc=0
 for p in "${pids[@]}"; do wait "$p" || rc=1; done
 exit $rc

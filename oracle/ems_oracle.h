@@ -119,6 +119,25 @@ typedef struct {
 int orc_abm_run(const orc_abm_case *c, int nsteps, double *E[3], double *H[3], double *traces);
 void orc_abm_kmat(const double *lamped1, double *K);
 
+/* ------------------------------ stabilised order-1 hexahedral FEM (fem/) --- */
+typedef struct {
+    int gx, gy, gz;
+    double h, dt, eps, mu;
+    int time_frequency;
+    double stabilization;
+    int use_ofem;
+    int nsrc; const int *src_comp; const int *src_ijk;
+    int ndip; const int *dip_ijk;   /* x-directed Hertz dipoles */
+    int nobs; const int *obs_n; const int *obs_ijk;
+} orc_femstab_case;
+
+/* E[c]: 3 levels per component (the reference's ring).  traces: nobs*(nsteps/tf+1)*3. */
+int orc_femstab_run(const orc_femstab_case *c, int nsteps, double *E[3], double *traces);
+/* K of the reference (12 x 12, row-major, the dt^2 / (2 mu eps h^2) factor included) */
+int orc_femstab_kmat(double dt, double mu, double eps, double h, double stabilization, int use_ofem, double *K);
+/* A, Abar, B, Bbar, C, Cbar of the conventional (0) or OFEM (1) basis */
+void orc_femstab_parts(int use_ofem, double *A, double *Abar, double *B, double *Bbar, double *C, double *Cbar);
+
 #ifdef __cplusplus
 }
 #endif

@@ -384,3 +384,55 @@ def abm_kmat(lamped1):
     K = np.zeros(144)
     lib().orc_abm_kmat(_ptr(np.ascontiguousarray(lamped1, np.float64)), _ptr(K))
     return K.reshape(12, 12)
+
+
+# -------------------------------------------- stabilised hexahedral FEM (fem/)
+class _FemStabCase(C.Structure):
+    _fields_ = [("gx", C.c_int), ("gy", C.c_int), ("gz", C.c_int),
+                ("h", C.c_double), ("dt", C.c_double), ("eps", C.c_double), ("mu", C.c_double),
+                ("time_frequency", C.c_int), ("stabilization", C.c_double), ("use_ofem", C.c_int),
+                ("nsrc", C.c_int), ("src_comp", _ip), ("src_ijk", _ip),
+                ("ndip", C.c_int), ("dip_ijk", _ip),
+                ("nobs", C.c_int), ("obs_n", _ip), ("obs_ijk", _ip)]
+
+
+def femstab_run(grid, h, dt, eps, mu, tf, stabilization, use_ofem, nsteps, sources=(), dipoles=(), observations=(), E=None):
+    """FP64 oracle of the reference's fem/ solver.  sources: [(comp, (i,j,k))];
+    dipoles: [(i,j,k)] (x-directed Hertz); observations: [(xs, ys, zs)].
+    Returns (traces, E) with E the 3-level array of each component."""
+    gx, gy, gz = grid
+    sz = hexfem_sizes(gx, gy, gz)
+    E = [np.zeros(3 * n) for n in sz] if E is None else [np.ascontiguousarray(a, np.float64).copy() for a in E]
+    c = _FemStabCase()
+    c.gx, c.gy, c.gz, c.h, c.dt, c.eps, c.mu, c.time_frequency = gx, gy, gz, h, dt, eps, mu, tf
+    c.stabilization, c.use_ofem = stabilization, use_ofem
+    comp = np.array([s[0] for s in sources] or [0], np.int32)
+    sijk = np.array([s[1] for s in sources] or [(0, 0, 0)], np.int32).reshape(-1)
+    dijk = np.array(list(dipoles) or [(0, 0, 0)], np.int32).reshape(-1)
+    on = np.array([len(l) for o in observations for l in o] or [0], np.int32)
+    oi = np.array([p for o in observations for l in o for p in l] or [(0, 0, 0)], np.int32).reshape(-1)
+    c.nsrc, c.src_comp, c.src_ijk = len(sources), _ptr(comp, _ip), _ptr(sijk, _ip)
+    c.ndip, c.dip_ijk = len(dipoles), _ptr(dijk, _ip)
+    c.nobs, c.obs_n, c.obs_ijk = len(observations), _ptr(on, _ip), _ptr(oi, _ip)
+    nsamp = nsteps // tf + 1
+    tr = np.zeros((max(len(observations), 1), nsamp, 3))
+    Ea = (_dp * 3)(*[_ptr(a) for a in E])
+    if lib().orc_femstab_run(C.byref(c), C.c_int(nsteps), Ea, _ptr(tr)) != 0:
+        raise RuntimeError("orc_femstab_run failed")
+    return tr[:len(observations)], E
+
+
+def femstab_kmat(dt, mu, eps, h, stabilization, use_ofem):
+    """The fem/ element matrix K (12 x 12)."""
+    K = np.zeros(144)
+    if lib().orc_femstab_kmat(C.c_double(dt), C.c_double(mu), C.c_double(eps), C.c_double(h),
+                              C.c_double(stabilization), C.c_int(use_ofem), _ptr(K)) != 0:
+        raise RuntimeError("element mass matrix is singular")
+    return K.reshape(12, 12)
+
+
+def femstab_parts(use_ofem):
+    """(A, Abar, B, Bbar, C, Cbar) of the conventional (0) or OFEM (1) basis."""
+    m = [np.zeros(144) for _ in range(6)]
+    lib().orc_femstab_parts(C.c_int(use_ofem), *[_ptr(a) for a in m])
+    return [a.reshape(12, 12) for a in m]

@@ -14,6 +14,13 @@ Outputs (committed, small):
   fdtd_cases.npz             reference FDTD traces and final fields
   femv2_cases.npz            reference fem_v2 / symplectic_2 / symplectic_4
                               traces and final fields, orders 1-3
+  abm_cases.npz              reference fem_abm traces and E, H levels
+  femstab_cases.npz          reference fem/ (stabilised order 1, conventional
+                              and OFEM bases) traces, E levels and the
+                              element matrix
+  cli_cases.json             argv of the reference's fem_v2 / symplectic_2 /
+                              symplectic_4 programs, the file name each wrote
+                              and its contents
 Each case records its inputs beside the outputs so the tests can replay it.
 """
 import json
@@ -46,6 +53,27 @@ ABM_CASES = [
      [([(4, 4, 4)], [(3, 3, 4), (3, 4, 4), (4, 3, 4), (4, 4, 4)], [(3, 4, 3), (3, 4, 4), (4, 4, 3), (4, 4, 4)])]),
     ("cube8_dipole", (8, 8, 8), 0.05, 0.6, 1, 30, [], [(3, 3, 3)],
      [([(4, 4, 4), (3, 4, 4)], [(4, 4, 4)], [(4, 4, 4)])]),
+]
+
+# fem/ (stabilised order-1 hexahedra): h and dt of the reference driver
+# (fem/main.cpp: h = 4 m / 200, dt = 0.8e-8 s / 400, c dt / h = 0.3)
+FEMSTAB_CASES = [
+    # name, grid, stabilization, use_ofem, tf, nsteps, sources, dipoles, observations
+    ("conv_s0.3_point_dipole", (9, 8, 7), 0.3, 0, 2, 60, [(0, (4, 3, 3)), (2, (5, 4, 3))], [(3, 3, 2)],
+     [([(5, 4, 4)], [(4, 3, 4), (4, 4, 4), (5, 3, 4), (5, 4, 4)], [(4, 4, 3), (4, 4, 4), (5, 4, 3), (5, 4, 4)])]),
+    ("ofem_s0.3_point_dipole", (9, 8, 7), 0.3, 1, 2, 60, [(1, (4, 3, 3))], [(3, 3, 2)],
+     [([(5, 4, 4)], [(4, 3, 4), (4, 4, 4), (5, 3, 4), (5, 4, 4)], [(4, 4, 3), (4, 4, 4), (5, 4, 3), (5, 4, 4)])]),
+    ("conv_s0_dipole", (8, 8, 8), 0.0, 0, 1, 50, [], [(3, 3, 3)], [([(4, 4, 4), (3, 4, 4)], [(4, 4, 4)], [(4, 4, 4)])]),
+    ("ofem_s0.1_dipole", (8, 8, 8), 0.1, 1, 1, 50, [], [(3, 3, 3)], [([(4, 4, 4), (3, 4, 4)], [(4, 4, 4)], [(4, 4, 4)])]),
+]
+
+# the reference's own programs (fem_v2, symplectic_2, symplectic_4 main.cpp):
+# argv, the file name they write and its bytes
+CLI_CASES = [
+    ("fem_v2", ["1", "1", "2", "0.8", "0.8", "0.8", "8", "2e-9", "0.4", "0.4", "0.4", "0.5", "0.4", "0.3", "1", "1", "1"]),
+    ("fem_v2", ["1", "0", "1", "0.6", "0.6", "0.6", "10", "1.5e-9", "0.3", "0.32", "0.28", "0.42", "0.3", "0.3", "1", "1", "1"]),
+    ("symplectic_2", ["1", "1", "1", "0.6", "0.6", "0.6", "9", "1.5e-9", "0.3", "0.3", "0.3", "0.4", "0.3", "0.3", "1", "1", "1"]),
+    ("symplectic_4", ["2", "1", "2", "0.8", "0.8", "0.8", "4", "1e-9", "0.4", "0.4", "0.4", "0.5", "0.4", "0.4", "1", "1", "1"]),
 ]
 
 FEM_CASES = []
@@ -106,6 +134,26 @@ def main():
                          observations=[[list(map(list, l)) for l in o] for o in obs]))
     out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
     np.savez_compressed(os.path.join(HERE, "abm_cases.npz"), **out)
+    out = {}
+    meta = []
+    for name, g, sf, ofem, tf, ns, src, dip, obs in FEMSTAB_CASES:
+        h, dt = 4.0 / 200, 0.8e-8 / 400
+        tr, E, K = refrun.femstab(g, h, dt, EPS0_FDTD, MU0, tf, sf, ofem, ns, src, dip, obs)
+        out[f"{name}/traces"] = tr
+        out[f"{name}/K"] = K
+        for q in range(3):
+            out[f"{name}/E{q}"] = E[q]
+        meta.append(dict(name=name, grid=list(g), h=h, dt=dt, eps=EPS0_FDTD, mu=MU0, tf=tf, stabilization=sf,
+                         use_ofem=ofem, nsteps=ns, sources=[[c, list(p)] for c, p in src], dipoles=[list(p) for p in dip],
+                         observations=[[list(map(list, l)) for l in o] for o in obs]))
+    out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "femstab_cases.npz"), **out)
+    cli = []
+    for variant, argv in CLI_CASES:
+        name, content = refrun.reference_program(variant, argv, kdir)
+        cli.append(dict(variant=variant, argv=argv, filename=name, content=content))
+    with open(os.path.join(HERE, "cli_cases.json"), "w") as f:
+        json.dump(cli, f, indent=1)
     print("golden fixtures written to", HERE)
 
 

@@ -36,3 +36,10 @@ def abm_cases():
     for m in meta:
         n = m["name"]
         yield m, z[f"{n}/traces"], [z[f"{n}/E{q}"] for q in range(3)], [z[f"{n}/H{q}"] for q in range(3)]
+
+
+def femstab_cases():
+    z, meta = load("femstab_cases.npz")
+    for m in meta:
+        n = m["name"]
+        yield m, z[f"{n}/traces"], [z[f"{n}/E{q}"] for q in range(3)], z[f"{n}/K"]

@@ -102,3 +102,51 @@ def abm(grid, h, dt, eps, mu, tf, nsteps, sources, dipoles, observations):
         fields.append(np.frombuffer(raw[off:off + 8 * n]).copy())
         off += 8 * n
     return tr, fields[:3], fields[3:]
+
+
+def femstab(grid, h, dt, eps, mu, tf, stabilization, use_ofem, nsteps, sources, dipoles, observations):
+    """Reference fem/ run: (traces, E levels per component, element matrix K)."""
+    gx, gy, gz = grid
+    lines = [f"{gx} {gy} {gz} {float(h)!r} {float(dt)!r} {float(eps)!r} {float(mu)!r} {tf} "
+             f"{float(stabilization)!r} {int(use_ofem)} {nsteps}", str(len(sources))]
+    lines += [f"{c} {i} {j} {k}" for c, (i, j, k) in sources]
+    lines.append(str(len(dipoles)))
+    lines += [f"{i} {j} {k}" for (i, j, k) in dipoles]
+    lines.append(str(len(observations)))
+    for o in observations:
+        toks = []
+        for lst in o:
+            toks.append(str(len(lst)))
+            toks += [f"{i} {j} {k}" for (i, j, k) in lst]
+        lines.append(" ".join(toks))
+    with tempfile.TemporaryDirectory() as td:
+        out = os.path.join(td, "o.bin")
+        subprocess.run([os.path.join(REF_BIN, "fem_ref"), out], input="\n".join(lines) + "\n",
+                       text=True, check=True, stderr=subprocess.DEVNULL, stdout=subprocess.DEVNULL)
+        raw = open(out, "rb").read()
+    nobs, ns = np.frombuffer(raw[:8], np.int32)
+    off = 8
+    tr = np.frombuffer(raw[off:off + 8 * nobs * ns * 3]).reshape(nobs, ns, 3).copy()
+    off += 8 * nobs * ns * 3
+    sz = [gx * (gy + 1) * (gz + 1), (gx + 1) * gy * (gz + 1), (gx + 1) * (gy + 1) * gz]
+    E = []
+    for q in range(3):
+        n = 3 * sz[q]
+        E.append(np.frombuffer(raw[off:off + 8 * n]).copy())
+        off += 8 * n
+    K = np.frombuffer(raw[off:off + 8 * 144]).reshape(12, 12).copy()
+    return tr, E, K
+
+
+def reference_program(variant, argv, kmat_dir):
+    """Runs the reference's own program of `variant` (its main.cpp) with argv
+    in a scratch directory holding kmat/; returns (file name, file text)."""
+    import shutil
+    with tempfile.TemporaryDirectory() as td:
+        shutil.copytree(kmat_dir, os.path.join(td, "kmat"))
+        subprocess.run([os.path.join(REF_BIN, f"{variant}_main"), *argv], cwd=td, check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        out = [f for f in os.listdir(td) if f.endswith(".csv")]
+        if len(out) != 1:
+            raise RuntimeError(f"expected one result file, found {out}")
+        return out[0], open(os.path.join(td, out[0])).read()
