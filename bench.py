@@ -43,6 +43,9 @@ N = 32
 STEPS_PER_SOLVE = 2000
 H = 1e-3
 SEED = 2024
+# DRAM bytes (read + write) of one fused-step launch on the headline mesh,
+# from the ncu capture summarised in profiles/tet_step_tet32_symp4.md
+TRAFFIC_PER_LAUNCH = 7125504
 
 
 def peaks():
@@ -118,6 +121,32 @@ def cpu_oracle_rate(steps, threads):
     return n_edges(N) * steps / dt, dt
 
 
+def _cpu_timed(code, threads=1, procs=1):
+    """Runs `code` (python, prints the seconds of its timed part) in `procs`
+    concurrent processes with OMP_NUM_THREADS=threads; returns the seconds of
+    each.  A fresh process per sample, so the thread count takes effect."""
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    pre = f"import sys, time; sys.path.insert(0, {ROOT!r}); import numpy as np; import oracle\n"
+    ps = [subprocess.Popen([sys.executable, "-c", pre + code], env=env, stdout=subprocess.PIPE, text=True) for _ in range(procs)]
+    out = []
+    for p in ps:
+        o, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError("CPU sample failed")
+        out.append(float(o.strip().splitlines()[-1]))
+    return out
+
+
+def cpu_rates(code, work, procs=None):
+    """`work` units per run of `code`: single-core units/s, and the
+    aggregate units/s of nproc concurrent single-threaded processes."""
+    procs = procs or (os.cpu_count() or 1)
+    one = _cpu_timed(code, 1, 1)[0]
+    many = _cpu_timed(code, 1, procs)
+    return {"single_core": work / one, "nproc_processes": procs * work / max(many), "processes": procs,
+            "sample_s": one}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -146,9 +175,85 @@ def run_reference(args):
     }))
 
 
-def fdtd_512(steps=60, n=512):
-    """n^3 (512^3 by default) FP32 Yee step with a 10-cell CPML: device rate
-    and roofline of the E kernel."""
+def fdtd64_sphere(steps=1000):
+    """The FDTD family's FP64 workload at full size: 64^3 cells of 1 mm,
+    vacuum with a centred sphere (radius 16 cells, eps_r 4), PEC, dt = 0.99
+    x CFL, a Jz Ricker point source (10 GHz) at the centre, `steps` steps, Ez
+    at 8 receivers on a 20-cell ring.  FP64 (bit-identical to the oracle and
+    so to the reference, tests/test_fdtd_gpu.py) and FP32 device rates, and
+    the FP64 oracle of the reference loop on the host cores."""
+    import emsolvers_gb300 as ems
+    n, h, eps0, mu0 = 64, 1e-3, 8.854187817e-12, 1.25663706212e-6
+    dt = 0.99 * h / (C0 * np.sqrt(3))
+    zz, yy, xx = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    r = np.sqrt((xx + 0.5 - n / 2) ** 2 + (yy + 0.5 - n / 2) ** 2 + (zz + 0.5 - n / 2) ** 2)
+    eps = np.where(r < 16, 4.0, 1.0) * eps0
+    c = n // 2
+    recs = [(c + int(round(20 * np.cos(a))), c + int(round(20 * np.sin(a))), c) for a in np.arange(8) * np.pi / 4]
+    out = {"workload": "fdtd64_sphere_1000", "cells": n ** 3, "steps": steps, "receivers": len(recs)}
+    for prec, name in ((ems.FP64, "fp64"), (ems.FP32, "fp32")):
+        s = ems.FdtdSimulation((n, n, n), h, dt, eps0, mu0, 1, precision=prec)
+        s.set_material(eps, np.zeros_like(eps))
+        s.setSource_z((c, c, c), waveform=ems.WAVE_RICKER, f0=10e9)
+        for q in recs:
+            s.setObservationPoint(([], [], [q]))
+        s.run(steps)
+        s.run(steps)
+        ms, _ = s.run_stats()
+        out[f"cell_updates_per_s_{name}"] = n ** 3 * steps / (ms * 1e-3)
+        out[f"ms_{name}"] = ms
+        s.close()
+    sample = 100
+    code = (f"n={n}; h={h!r}; dt={dt!r}; eps0={eps0!r}; mu0={mu0!r}\n"
+            "zz, yy, xx = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing='ij')\n"
+            "r = np.sqrt((xx + 0.5 - n / 2) ** 2 + (yy + 0.5 - n / 2) ** 2 + (zz + 0.5 - n / 2) ** 2)\n"
+            "ids = (r < 16).astype(np.uint16)\n"
+            "t0 = time.perf_counter()\n"
+            f"oracle.fdtd_run(n, n, n, h, dt, eps0, mu0, 1, {sample}, [(2, (32, 32, 32), 1, 10e9, 1.0)], [([], [], [(52, 32, 32)])],"
+            " material=(ids, np.array([eps0, 4 * eps0]), np.zeros(2)))\n"
+            "print(time.perf_counter() - t0)\n")
+    cpu = cpu_rates(code, n ** 3 * sample)
+    out["cpu_baseline"] = {"value": cpu["single_core"], "unit": "cell-updates/s", "cores": 1, "kind": "port",
+                           "nproc_processes_value": cpu["nproc_processes"], "processes": cpu["processes"],
+                           "sample": f"{sample} steps of the same case, FP64 oracle of the reference loop "
+                                     "(bit-identical to it); single core, and nproc concurrent single-threaded processes"}
+    out["speedup_fp64_vs_cpu_core"] = out["cell_updates_per_s_fp64"] / cpu["single_core"]
+    return out
+
+
+def tet32_symp2(steps=STEPS_PER_SOLVE):
+    """The headline mesh and material with the second-order symplectic
+    (leapfrog, symplectic_2) step instead of the fourth-order one: FP32
+    device rate and the FP32-vs-FP64 trace error over the whole run."""
+    import emsolvers_gb300 as ems
+    eps, f0, src, recs = workload()
+    out = {"workload": "tet32_symp2_2000", "steps": steps, "integrator": "symp2"}
+    tr = {}
+    for prec, name in ((ems.FP32, "fp32"), (ems.FP64, "fp64")):
+        sim = ems.TetFemSimulation((N, N, N), H, 1, ems.SYMP2, prec, dt=0.0, cfl_fraction=0.9)
+        sim.set_material(eps)
+        sim.add_dipole(src, (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0, 1.0)
+        for r in recs:
+            sim.add_receiver(r)
+        sim.run(steps)
+        sim.reset()
+        sim.run(steps)
+        ms, _ = sim.run_stats()
+        out[f"dof_updates_per_s_{name}"] = n_edges(N) * steps / (ms * 1e-3)
+        out["dt_s"] = sim.time_step()[0]
+        tr[name] = sim.traces()[..., 1:]
+        sim.close()
+    out["fp32_vs_fp64_trace_rel_l2"] = float(np.linalg.norm(tr["fp32"] - tr["fp64"]) / np.linalg.norm(tr["fp64"]))
+    return out
+
+
+def fdtd_512(steps=4000, n=512, nrec=64, compare_fp64=True):
+    """n^3 (512^3) Yee FDTD with a 10-cell CPML: eps_r log-uniform [1, 10] on
+    16^3-cell blocks, sigma U[0, 0.05] S/m, 4 Ricker point sources (f0 U[5,
+    15] GHz) at random interior cells, `steps` steps, `nrec` receivers (Ex,
+    Ey, Ez at one cell each).  FP32 device rate, the step's bytes against HBM
+    and the E kernel alone; with compare_fp64 the same run in FP64 and the
+    FP32-vs-FP64 trace error over all receivers and steps."""
     import emsolvers_gb300 as ems
     h = 1e-3
     eps0, mu0 = 8.854187817e-12, 1.25663706212e-6
@@ -159,25 +264,46 @@ def fdtd_512(steps=60, n=512):
     blk_sig = rng.uniform(0, 0.05, nb ** 3)
     idx = (np.arange(n) // 16)
     cell_blk = (idx[None, None, :] + nb * (idx[None, :, None] + nb * idx[:, None, None])).reshape(-1)
-    s = ems.FdtdSimulation((n, n, n), h, dt, eps0, mu0, 1, precision=ems.FP32, pml_cells=10, pml_order=3.0,
-                           pml_kappa_max=1.0, pml_alpha_max=0.0, pml_reflection=1e-6)
-    s.set_material(blk_eps[cell_blk], blk_sig[cell_blk])
-    del cell_blk
-    for q in range(4):
-        c = rng.integers(20, n - 20, 3)
-        s.setSource_z(tuple(int(v) for v in c), waveform=ems.WAVE_RICKER, f0=float(rng.uniform(5e9, 15e9)))
-    s.run(24)          # warm-up; the handle's first run of >= 24 steps picks the launch shape
-    s.run(steps)
-    ms, launches = s.run_stats()
+    srcs = [(tuple(int(v) for v in rng.integers(20, n - 20, 3)), float(rng.uniform(5e9, 15e9))) for _ in range(4)]
+    recs = [tuple(int(v) for v in rng.integers(12, n - 12, 3)) for _ in range(nrec)]
+
+    def one(precision):
+        s = ems.FdtdSimulation((n, n, n), h, dt, eps0, mu0, 1, precision=precision, pml_cells=10, pml_order=3.0,
+                               pml_kappa_max=1.0, pml_alpha_max=0.0, pml_reflection=1e-6)
+        s.set_material(blk_eps[cell_blk], blk_sig[cell_blk])
+        for c, f in srcs:
+            s.setSource_z(c, waveform=ems.WAVE_RICKER, f0=f)
+        for r in recs:
+            s.setObservationPoint(([r], [r], [r]))
+        s.run(40)          # warm-up; the handle's first run of >= 40 steps picks the launch shape
+        s.reset()
+        s.run(steps)
+        ms, launches = s.run_stats()
+        return s, ms, launches
+
+    s, ms, launches = one(ems.FP32)
     kms, kbytes, kname = s.time_dominant_kernel(10)
     shape = s.launch_shape()
-    cells = n ** 3
+    tr32 = s.traces()
     s.close()
-    return {"workload": f"fdtd{n}_fp32_cpml10", "steps": steps, "ms_per_step": ms / steps,
-            "launch_shape": list(shape[:2]),
-            "cell_updates_per_s": cells * steps / (ms * 1e-3),
-            "dof_updates_per_s": 6 * cells * steps / (ms * 1e-3),
-            "kernel": kname, "kernel_ms": kms, "kernel_bytes": kbytes, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
+    cells = n ** 3
+    npml = cells - (n - 20) ** 3
+    # one step's algorithmic bytes: E and H read and written (12 words per
+    # cell), the 2-byte material id per cell, 12 CPML psi values read and
+    # written per cell inside the slabs
+    step_bytes = 4.0 * 12 * cells + 2.0 * cells + 4.0 * 24 * npml
+    out = {"workload": f"fdtd{n}_fp32_cpml10_{steps}", "steps": steps, "receivers": nrec, "sources": len(srcs),
+           "ms_per_step": ms / steps, "launches": int(launches), "launch_shape": list(shape[:2]),
+           "cell_updates_per_s": cells * steps / (ms * 1e-3), "dof_updates_per_s": 6 * cells * steps / (ms * 1e-3),
+           "step_bytes": step_bytes, "step_gbs": step_bytes / (ms / steps * 1e-3) / 1e9,
+           "kernel": kname, "kernel_ms": kms, "kernel_bytes": kbytes, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9}
+    if compare_fp64:
+        s, ms64, _ = one(ems.FP64)
+        tr64 = s.traces()
+        s.close()
+        out["fp64_ms_per_step"] = ms64 / steps
+        out["fp32_vs_fp64_trace_rel_l2"] = float(np.linalg.norm(tr32 - tr64) / np.linalg.norm(tr64))
+    return out
 
 
 def head_solve(steps=STEPS_PER_SOLVE):
@@ -240,13 +366,27 @@ def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
     shots_batch = nshots / (ms_batch * 1e-3)
     shots_fp64 = 1.0 / (np.mean(per[ems.FP64]) * 1e-3)
     shots_fp32 = 1.0 / (np.mean(per[ems.FP32]) * 1e-3)
+    # CPU: one shot of the batch's mean size, FP64 oracle, sample steps scaled
+    nm = int(round(np.cbrt(np.mean(sides.astype(float) ** 3))))
+    cpu_steps = 100
+    code = (f"n = {nm}; eps = np.random.default_rng(0).uniform(1.0, 6.0, 6 * n ** 3)\n"
+            f"dip = ((0.5 * n, 0.47 * n, 0.52 * n), (0.0, 0.0, 1.0), 1, {f0 * H / C0!r}, 1.0)\n"
+            f"dtn = {dt * C0 / H!r}\n"
+            "t0 = time.perf_counter()\n"
+            f"oracle.tet_run((n, n, n), eps, oracle.SYMP4, dtn, {cpu_steps}, 1, [dip], [(0.3 * n, 0.6 * n, 0.4 * n)])\n"
+            "print(time.perf_counter() - t0)\n")
+    cpu = cpu_rates(code, cpu_steps / steps)
     return {"workload": "tet_batch64_symp4_3000", "shots": nshots, "steps": steps, "tets": int(sum(6 * sides ** 3)),
             "edges": int(edges), "order": 1, "dt_s": dt, "batch_ms": ms_batch, "launches": int(launches),
             "shots_per_s_fp32_batched": shots_batch, "shots_per_s_fp64_per_shot": shots_fp64,
             "shots_per_s_fp32_per_shot": shots_fp32, "speedup_vs_fp64_per_shot": shots_batch / shots_fp64,
             "dof_updates_per_s": edges * steps / (ms_batch * 1e-3),
             "per_shot_sample": f"{len(pick)} shots x {sample_steps} steps, scaled to {steps}",
-            "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9, "threads_per_block": block}
+            "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9, "threads_per_block": block,
+            "cpu_baseline": {"value": cpu["single_core"], "unit": "shots/s", "cores": 1, "kind": "port",
+                             "nproc_processes_value": cpu["nproc_processes"], "processes": cpu["processes"],
+                             "sample": f"one {nm}^3 x 6 tet shot (the batch's mean size), {cpu_steps} steps of the FP64 "
+                                       f"oracle scaled to {steps}; single core, and nproc concurrent single-threaded processes"}}
 
 
 def hex72(steps=200, order=2, sample_steps=10):
@@ -304,13 +444,15 @@ def blob_model(n, rng, background=2.0, nblob=3):
     return eps
 
 
-def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, sample_steps=400):
+def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, fd_elements=32, fd_h=1e-4, cpu_steps=20):
     """Forward + adjoint misfit gradient: nshots Ricker dipole shots on an
     n^3 x 6 tet cube (true eps_r = 2 + 3 Gaussian blobs, start model 2), nrec
-    receivers per shot, symp4, `steps` steps, L2 trace misfit, nsnap
-    snapshots.  FP32 batched (all shots in one handle) against the plain
-    per-shot FP64 GPU path, the latter timed on one shot over
-    `sample_steps` steps (same segment length) and scaled to `steps`."""
+    receivers per shot, symp4, `steps` steps, nsnap snapshots; L2 and TF
+    envelope misfits.  FP32 batched (all shots in one handle) against the
+    plain per-shot FP64 GPU path (shot 0, the whole run).  Checks: FP32 vs
+    FP64 traces and gradient over the whole run of shot 0, and central
+    differences (relative step fd_h, FP64, all perturbed models in one
+    batch) of the L2 misfit on fd_elements random tetrahedra."""
     import emsolvers_gb300 as ems
     rng = np.random.default_rng(SEED + 5)
     true = blob_model(n, rng)
@@ -325,9 +467,9 @@ def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, sample_steps=400):
 
     def handle(precision, shots, model):
         b = ems.TetFemBatch([(n, n, n)] * len(shots), H, integrator=ems.SYMP4, precision=precision, dt=dt)
-        b.set_material(np.tile(model, len(shots)))
-        for k, s in enumerate(shots):
-            b.add_dipole(k, src[s], (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
+        b.set_material(np.tile(model, len(shots)) if np.ndim(model) == 1 and len(model) == true.size else model)
+        for k, sh in enumerate(shots):
+            b.add_dipole(k, src[sh], (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
             for r in rec:
                 b.add_receiver(k, r)
         return b
@@ -336,8 +478,10 @@ def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, sample_steps=400):
     b = handle(ems.FP32, shots, true)
     b.run(steps)
     obs = b.traces()
+    b.close()
     import torch
     torch.cuda.synchronize()
+    b = handle(ems.FP32, shots, start)
     t0 = time.perf_counter()
     b.set_material(np.tile(start, nshots))
     b.set_checkpoints(nsnap)
@@ -349,48 +493,78 @@ def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, sample_steps=400):
     fwd_ms, _ = b.run_stats()
     J, tg = ems.trace_misfit(b.traces(), obs, ems.MISFIT_L2)
     ts.append(time.perf_counter())
-    g32 = b.backward(tg).reshape(nshots, -1).sum(0)
+    g32 = b.backward(tg).reshape(nshots, -1)
     ts.append(time.perf_counter())
     wall32 = ts[-1] - t0
     stages = {"setup_s": ts[0] - t0, "forward_s": ts[1] - ts[0], "misfit_s": ts[2] - ts[1], "backward_s": ts[3] - ts[2]}
+    # the TF envelope misfit on the same recorded run (a second backward sweep)
+    t1 = time.perf_counter()
+    Jtf, tgtf = ems.trace_misfit(b.traces(), obs, ems.MISFIT_TF_ENVELOPE)
+    gtf = b.backward(tgtf).reshape(nshots, -1).sum(0)
+    tf_s = time.perf_counter() - t1
+    tr32_0 = b.traces()[:nrec]
     b.close()
-    # per-shot FP64 sample with the same segment length
-    seg = -(-steps // nsnap)
+    # plain per-shot FP64 GPU path: shot 0, the whole run
     one = handle(ems.FP64, [0], start)
-    one.set_checkpoints(-(-sample_steps // seg))
-    obs0 = obs[:nrec, :sample_steps]
+    one.set_checkpoints(nsnap)
+    obs0 = obs[:nrec]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     one.set_material(start)
-    one.time_step()                    # FP64 mass setup and stability limit, once per gradient
-    t1 = time.perf_counter()
+    one.time_step()
     one.reset()
-    one.run(sample_steps)
-    _, tg0 = ems.trace_misfit(one.traces(), obs0, ems.MISFIT_L2)
+    one.run(steps)
+    J0, tg0 = ems.trace_misfit(one.traces(), obs0, ems.MISFIT_L2)
     g64_0 = one.backward(tg0)
-    t2 = time.perf_counter()
-    wall64 = (t1 - t0) + (t2 - t1) * steps / sample_steps
+    wall64 = time.perf_counter() - t0
     tr64 = one.traces()
     one.close()
-    # FP32 against FP64 on the same sampled shot
-    one32 = handle(ems.FP32, [0], start)
-    one32.set_checkpoints(-(-sample_steps // seg))
-    one32.reset()
-    one32.run(sample_steps)
-    g32_0 = one32.backward(tg0)
-    tr_err = float(np.linalg.norm(one32.traces()[..., 1:] - tr64[..., 1:]) / np.linalg.norm(tr64[..., 1:]))
-    one32.close()
-    g_err = float(np.linalg.norm(g32_0 - g64_0) / np.linalg.norm(g64_0))
+    tr_err = float(np.linalg.norm(tr32_0[..., 1:] - tr64[..., 1:]) / np.linalg.norm(tr64[..., 1:]))
+    g_err = float(np.linalg.norm(g32[0] - g64_0) / np.linalg.norm(g64_0))
+    # central differences of J0 on fd_elements tetrahedra, FP64, one batch of
+    # 2 fd_elements perturbed copies of the start model (shot 0 each)
+    pick = rng.choice(true.size, size=fd_elements, replace=False)
+    models = np.tile(start, 2 * fd_elements).reshape(2 * fd_elements, -1)
+    for q, t in enumerate(pick):
+        models[2 * q, t] += fd_h * start[t]
+        models[2 * q + 1, t] -= fd_h * start[t]
+    t1 = time.perf_counter()
+    fd = handle(ems.FP64, [0] * (2 * fd_elements), models.reshape(-1))
+    fd.run(steps)
+    trs = fd.traces().reshape(2 * fd_elements, nrec, -1, 4)
+    fd.close()
+    fd_s = time.perf_counter() - t1
+    Jp = np.array([ems.trace_misfit(trs[k], obs0, ems.MISFIT_L2)[0] for k in range(2 * fd_elements)])
+    g_fd = (Jp[0::2] - Jp[1::2]) / (2 * fd_h * start[pick])
+    fd_err = float(np.linalg.norm(g64_0[pick] - g_fd) / np.linalg.norm(g_fd))
+    # CPU: the FP64 oracle adjoint of one shot over cpu_steps steps, scaled
+    code = (f"n = {n}; rng = np.random.default_rng(0); eps = np.full(6 * n ** 3, 2.0)\n"
+            f"dip = ({tuple(src[0] / H)!r}, (0.0, 0.0, 1.0), 1, {f0 * H / C0!r}, 1.0)\n"
+            f"recs = {[tuple(r / H) for r in rec]!r}\n"
+            f"dtn = {dt * C0 / H!r}\n"
+            f"tr, _, _ = oracle.tet_run((n, n, n), eps, oracle.SYMP4, dtn, {cpu_steps}, 1, [dip], recs)\n"
+            "t0 = time.perf_counter()\n"
+            f"tr, _, _ = oracle.tet_run((n, n, n), eps, oracle.SYMP4, dtn, {cpu_steps}, 1, [dip], recs)\n"
+            "g = tr.copy(); g[..., 0] = 0.0\n"
+            f"oracle.tet_gradient((n, n, n), eps, oracle.SYMP4, dtn, {cpu_steps}, g, 1, [dip], recs)\n"
+            "print(time.perf_counter() - t0)\n")
+    cpu = cpu_rates(code, cpu_steps / steps)   # shots per run of the sample
     return {"workload": f"tet{n}_adjoint_{nshots}shots_symp4_{steps}", "tets_per_shot": int(true.size),
-            "shots": nshots, "receivers_per_shot": nrec, "steps": steps, "snapshots": nsnap, "misfit": "L2",
-            "order": 1, "dt_s": dt, "misfit_value": J, "grad_norm": float(np.linalg.norm(g32)),
-            "fp32_batched_s": wall32, "fp32_forward_ms": fwd_ms, "fp32_stages": stages,
+            "shots": nshots, "receivers_per_shot": nrec, "steps": steps, "snapshots": nsnap, "misfits": ["L2", "TF_envelope"],
+            "order": 1, "dt_s": dt, "misfit_l2": J, "misfit_tf_envelope": Jtf,
+            "grad_norm_l2": float(np.linalg.norm(g32.sum(0))), "grad_norm_tf": float(np.linalg.norm(gtf)),
+            "fp32_batched_s": wall32, "fp32_forward_ms": fwd_ms, "fp32_stages": stages, "tf_envelope_backward_s": tf_s,
             "shots_per_s_fp32_batched": nshots / wall32, "shots_per_s_fp64_per_shot": 1.0 / wall64,
             "speedup_vs_fp64_per_shot": (nshots / wall32) * wall64,
-            "fp64_sample": f"1 shot x {sample_steps} steps (time loop scaled to {steps}, setup once)",
-            "fp64_setup_s": t1 - t0,
+            "fp64_per_shot": "shot 0, the whole run: material upload, FP64 mass setup, recorded forward, misfit, backward",
             "fp32_vs_fp64_trace_rel_l2": tr_err, "fp32_vs_fp64_grad_rel_l2": g_err,
-            "fp32_vs_fp64_over": f"shot 0, its first {sample_steps} of {steps} steps (forward and gradient)",
+            "fp32_vs_fp64_over": f"shot 0, all {steps} steps (forward traces and gradient)",
+            "fd_check": {"elements": fd_elements, "h_rel": fd_h, "fp64_adjoint_vs_central_diff_rel_l2": fd_err,
+                         "seconds": fd_s},
+            "cpu_baseline": {"value": cpu["single_core"], "unit": "shots/s", "cores": 1, "kind": "port",
+                             "nproc_processes_value": cpu["nproc_processes"], "processes": cpu["processes"],
+                             "sample": f"one shot, {cpu_steps} steps forward + adjoint (FP64 oracle), scaled to {steps}; "
+                                       "single core, and nproc concurrent single-threaded processes"},
             "timing": "wall clock: material upload + FP64 mass setup + recorded forward + misfit + backward"}
 
 
@@ -456,11 +630,18 @@ def run_gpu(args):
         tr = sim.traces()              # device -> host
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
     e2e = world * dofs * STEPS_PER_SOLVE * args.steps / (np.sum(e2e_ms) * 1e-3)
-    # ---- dominant kernel roofline
+    # ---- dominant kernel roofline.  In the loop every substep is one launch
+    # of the fused step (3 per symp4 step, replayed from CUDA graphs); the
+    # solve's device time over those launches is the in-loop time per launch
+    # (an upper bound: it also holds the two half drifts and the graph launch
+    # gaps).  The same kernel timed alone by repeated launches outside a graph
+    # is reported beside it.
     kms, kbytes, kname = sim.time_dominant_kernel(200)
     block = sim.launch_shape()[0]
     peak, peak_kind = peaks()
-    achieved = kbytes / (kms * 1e-3) / 1e9
+    step_launches = 3 * STEPS_PER_SOLVE
+    inloop_ms = float(np.mean(dev_ms)) / step_launches
+    achieved = kbytes / (inloop_ms * 1e-3) / 1e9
     out = {
         "metric": "DOF-updates/s (32^3x6 tet Nedelec FEM, symp4, 2000 steps)", "value": value, "unit": "DOF-updates/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -476,7 +657,9 @@ def run_gpu(args):
                      # DRAM bytes of one step launch from the ncu capture in
                      # profiles/tet_step_tet32_symp4.md (cold fill: the 8.6 MB
                      # working set is L2-resident in the timed loop)
-                     "traffic": 6598656, "kernel": kname, "kernel_us": kms * 1e3, "bytes_per_launch": kbytes,
+                     "traffic": TRAFFIC_PER_LAUNCH, "kernel": kname, "kernel_us": inloop_ms * 1e3,
+                     "kernel_us_alone": kms * 1e3, "launches_per_solve": step_launches, "bytes_per_launch": kbytes,
+                     "timing": "in-loop: solve device time / fused-step launches (includes the half drifts and launch gaps)",
                      "threads_per_block": block, "peak_source": peak_kind},
         "clocks": clk,
         "wall_s": wall,
@@ -485,9 +668,32 @@ def run_gpu(args):
         if not args.no_cpu:
             secs = [cpu_oracle_rate(STEPS_PER_SOLVE, os.cpu_count() or 1)[1] for _ in range(3)]
             r = n_edges(N) * 3 * STEPS_PER_SOLVE / sum(secs)
+            sample = 200
+            code = ("import bench\n"
+                    "eps, f0, src, recs = bench.workload()\n"
+                    f"dtn = {dt * C0 / H!r}\n"
+                    "dip = (tuple(src / bench.H), (0.0, 0.0, 1.0), 1, f0 * bench.H / bench.C0, 1.0)\n"
+                    "t0 = time.perf_counter()\n"
+                    f"oracle.tet_run((bench.N,) * 3, eps, oracle.SYMP4, dtn, {sample}, 1, [dip], [tuple(q / bench.H) for q in recs])\n"
+                    "print(time.perf_counter() - t0)\n")
+            per = cpu_rates(code, n_edges(N) * sample)
             out["cpu_baseline"] = {"value": r, "unit": "DOF-updates/s", "cores": os.cpu_count() or 1, "kind": "port",
                                    "sample": f"three full solves ({STEPS_PER_SOLVE} time steps each), FP64 oracle, "
-                                             f"{sum(secs):.1f} s"}
+                                             f"{sum(secs):.1f} s",
+                                   "single_core_value": per["single_core"], "nproc_processes_value": per["nproc_processes"],
+                                   "processes": per["processes"],
+                                   "per_core_sample": f"{sample} steps in one thread, and in nproc concurrent single-threaded "
+                                                      "processes (one solve each)"}
+        if not args.no_fdtd:
+            try:
+                out["fdtd64_sphere"] = fdtd64_sphere()
+            except Exception as e:  # secondary measurement only
+                out["fdtd64_sphere"] = {"error": str(e)}
+        if not args.no_batch:
+            try:
+                out["tet32_symp2"] = tet32_symp2()
+            except Exception as e:  # secondary measurement only
+                out["tet32_symp2"] = {"error": str(e)}
         if not args.no_batch:
             try:
                 out["batch64"] = batch64()
@@ -507,6 +713,7 @@ def run_gpu(args):
             try:
                 out["fdtd_512"] = fdtd_512()
                 out["fdtd_512"]["hbm_frac"] = out["fdtd_512"]["kernel_gbs"] / peak
+                out["fdtd_512"]["step_hbm_frac"] = out["fdtd_512"]["step_gbs"] / peak
             except Exception as e:  # secondary measurement only
                 out["fdtd_512"] = {"error": str(e)}
         print(json.dumps(out))
@@ -525,7 +732,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-hex", action="store_true")
-    ap.add_argument("--only", choices=["head", "batch", "fdtd", "adjoint", "hex"],
+    ap.add_argument("--only", choices=["head", "batch", "fdtd", "adjoint", "hex", "sphere", "symp2"],
                     help="run one secondary workload alone and print its JSON (for profiling)")
     ap.add_argument("--fdtd-n", type=int, default=512, help="FDTD cube side for --only fdtd")
     ap.add_argument("--head-steps", type=int, default=STEPS_PER_SOLVE, help="time steps for --only head")
@@ -534,6 +741,8 @@ def main():
     ap.add_argument("--adj-n", type=int, default=48, help="cube side for --only adjoint")
     ap.add_argument("--adj-steps", type=int, default=4000, help="time steps for --only adjoint")
     ap.add_argument("--adj-shots", type=int, default=16, help="shots for --only adjoint")
+    ap.add_argument("--adj-fd", type=int, default=32, help="central-difference elements for --only adjoint")
+    ap.add_argument("--fdtd-steps", type=int, default=4000, help="time steps for --only fdtd")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -543,9 +752,10 @@ def main():
         fn = {"head": lambda: head_solve(args.head_steps),
               "batch": lambda: batch64(steps=args.batch_steps, sample=args.batch_sample,
                                        sample_steps=min(300, args.batch_steps)),
-              "fdtd": lambda: fdtd_512(n=args.fdtd_n), "hex": hex72,
+              "fdtd": lambda: fdtd_512(n=args.fdtd_n, steps=args.fdtd_steps, compare_fp64=args.fdtd_steps >= 1000),
+              "hex": hex72, "sphere": fdtd64_sphere, "symp2": tet32_symp2,
               "adjoint": lambda: adjoint16(n=args.adj_n, nshots=args.adj_shots, steps=args.adj_steps,
-                                           sample_steps=min(400, args.adj_steps))}[args.only]
+                                           fd_elements=args.adj_fd)}[args.only]
         print(json.dumps(fn()))
     elif args.impl == "reference":
         run_reference(args)

@@ -180,3 +180,76 @@ def test_launch_shape_autotuner_picks_a_candidate_and_changes_no_result():
         os.remove(path)
     for shape in ("32x8", "256x1", "64x2"):
         assert np.array_equal(out[""], out[shape])
+
+
+def _cpml_traces(n, src, recs, steps, precision, pml_cells, kmax=1.0, amax=0.0, f0=None):
+    h, c0 = 1e-3, 299792458.0
+    dt = 0.99 * h / (c0 * np.sqrt(3))
+    s = ems.FdtdSimulation((n, n, n), h, dt, 8.854187817e-12, 1.25663706212e-6, 1, precision=precision,
+                           pml_cells=pml_cells, pml_order=3.0, pml_kappa_max=kmax, pml_alpha_max=amax, pml_reflection=1e-6)
+    s.setSource_z(src, waveform=ems.WAVE_RICKER, f0=f0 or c0 / (15 * h))
+    for r in recs:
+        s.setObservationPoint(([], [], [r]))
+    s.run(steps)
+    tr = s.traces()[:, :, 2]
+    s.close()
+    return tr
+
+
+@pytest.mark.parametrize("precision", [ems.FP64, ems.FP32], ids=["fp64", "fp32"])
+def test_cpml_reflection_on_the_gpu(precision):
+    # the physical CPML pin of test_fdtd_cpml.py through the library: 8-cell
+    # CPML against a box too large for echoes within 160 steps
+    n, L, big = 40, 8, 104
+    c, off = n // 2, (big - n) // 2
+    recs = [(c, c, c + 9), (c + 8, c + 8, c), (c + 7, c + 7, c + 7)]
+    small = _cpml_traces(n, (c, c, c), recs, 160, precision, L)
+    ref = _cpml_traces(big, (c + off,) * 3, [tuple(v + off for v in r) for r in recs], 160, precision, 0)
+    for q in range(3):
+        assert np.linalg.norm(small[q] - ref[q]) / np.linalg.norm(ref[q]) < 1e-3
+
+
+def test_cfs_cpml_stays_stable_over_10000_steps():
+    # kappa_max > 1 and alpha_max > 0, FP32, 10,000 steps: the CPML absorbs
+    # the pulse and nothing grows back (late-time fields far below the early
+    # peak and still decaying)
+    n, c = 32, 16
+    recs = [(c, c, c + 5), (c + 5, c + 5, c), (c - 4, c + 3, c - 5)]
+    tr = np.abs(_cpml_traces(n, (c, c, c), recs, 10000, ems.FP32, 10, kmax=5.0, amax=0.05))
+    early = tr[:, :2000].max()
+    assert early > 0
+    assert tr[:, 6000:8000].max() < 1e-3 * early
+    assert tr[:, 8000:].max() <= tr[:, 6000:8000].max() + 1e-6 * early
+
+
+def test_sphere_workload_at_full_size_bitwise_equal_to_oracle():
+    # the FP64 workload of the reference's FDTD family at its full size:
+    # 64^3 cells of 1 mm, vacuum with a centred sphere of radius 16 cells,
+    # eps_r 4, PEC walls, dt = 0.99 x CFL, a Jz Ricker point source (10 GHz)
+    # at the centre, 1000 steps, Ez at 8 receivers on a 20-cell ring in the
+    # source's z plane: traces and all six fields bit-identical to the oracle
+    n, h = 64, 1e-3
+    dt = 0.99 * h / (299792458.0 * np.sqrt(3))
+    zz, yy, xx = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    r = np.sqrt((xx + 0.5 - n / 2) ** 2 + (yy + 0.5 - n / 2) ** 2 + (zz + 0.5 - n / 2) ** 2)
+    inside = r < 16
+    eps = np.where(inside, 4.0, 1.0) * EPS0
+    c = n // 2
+    recs = [(c + int(round(20 * np.cos(a))), c + int(round(20 * np.sin(a))), c) for a in np.arange(8) * np.pi / 4]
+    obs = [([], [], [q]) for q in recs]
+    first = 0 if not inside.ravel()[0] else 1          # library table: materials in first-occurrence order
+    ids = np.where(inside, 1 - first, first).astype(np.uint16)
+    table = np.array([EPS0, 4.0 * EPS0]) if first == 0 else np.array([4.0 * EPS0, EPS0])
+    tr_o, f_o = oracle.fdtd_run(n, n, n, h, dt, EPS0, MU0, 1, 1000, [(2, (c, c, c), ems.WAVE_RICKER, 10e9, 1.0)], obs,
+                                material=(ids, table, np.zeros(2)))
+    s = ems.FdtdSimulation((n, n, n), h, dt, EPS0, MU0, 1, precision=ems.FP64)
+    s.set_material(eps, np.zeros_like(eps))
+    s.setSource_z((c, c, c), waveform=ems.WAVE_RICKER, f0=10e9)
+    for o in obs:
+        s.setObservationPoint(o)
+    s.run(1000)
+    t = s.traces()
+    assert np.abs(tr_o[:, :, 2]).max() > 0
+    np.testing.assert_array_equal(t[:, :, 2], tr_o[:, :, 2])
+    for k, v in s.fields().items():
+        np.testing.assert_array_equal(v, f_o[k], err_msg=k)
