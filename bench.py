@@ -347,7 +347,7 @@ def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
     b.run(steps)
     ms_batch, launches = b.run_stats()
     kms, kbytes, kname = b.time_dominant_kernel(20)
-    block = b.launch_shape()[0]
+    block = list(b.launch_shape())
     edges = sum(n_edges(int(n)) for n in sides)
     b.close()
     per = {ems.FP64: [], ems.FP32: []}
@@ -382,7 +382,7 @@ def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
             "shots_per_s_fp32_per_shot": shots_fp32, "speedup_vs_fp64_per_shot": shots_batch / shots_fp64,
             "dof_updates_per_s": edges * steps / (ms_batch * 1e-3),
             "per_shot_sample": f"{len(pick)} shots x {sample_steps} steps, scaled to {steps}",
-            "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9, "threads_per_block": block,
+            "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9, "launch_shape": block,
             "cpu_baseline": {"value": cpu["single_core"], "unit": "shots/s", "cores": 1, "kind": "port",
                              "nproc_processes_value": cpu["nproc_processes"], "processes": cpu["processes"],
                              "sample": f"one {nm}^3 x 6 tet shot (the batch's mean size), {cpu_steps} steps of the FP64 "
@@ -637,7 +637,7 @@ def run_gpu(args):
     # gaps).  The same kernel timed alone by repeated launches outside a graph
     # is reported beside it.
     kms, kbytes, kname = sim.time_dominant_kernel(200)
-    block = sim.launch_shape()[0]
+    block = list(sim.launch_shape())
     peak, peak_kind = peaks()
     step_launches = 3 * STEPS_PER_SOLVE
     inloop_ms = float(np.mean(dev_ms)) / step_launches
@@ -660,7 +660,7 @@ def run_gpu(args):
                      "traffic": TRAFFIC_PER_LAUNCH, "kernel": kname, "kernel_us": inloop_ms * 1e3,
                      "kernel_us_alone": kms * 1e3, "launches_per_solve": step_launches, "bytes_per_launch": kbytes,
                      "timing": "in-loop: solve device time / fused-step launches (includes the half drifts and launch gaps)",
-                     "threads_per_block": block, "peak_source": peak_kind},
+                     "launch_shape": block, "peak_source": peak_kind},
         "clocks": clk,
         "wall_s": wall,
     }

@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
@@ -371,13 +372,19 @@ template <class T> __device__ __forceinline__ T two_sum(T a, T b, T &err)
     return s;
 }
 
+// A rounded product that the compiler may not fuse into a following
+// addition: the two-sums below need the product's rounded value, and the
+// kernels must evaluate every sum the same way to give the same bits.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
 __device__ __forceinline__ float comp_load(const __nv_bfloat16 *c, size_t i) { return __bfloat162float(c[i]); }
 __device__ __forceinline__ void comp_store(__nv_bfloat16 *c, size_t i, float x) { c[i] = __float2bfloat16_rn(x); }
 
 // x *= g with the product's rounding error added to lo (lo scales too).
 __device__ __forceinline__ void comp_scale(float &x, float &lo, float g)
 {
-    const float p = x * g;
+    const float p = mul_rn(x, g);
     lo = fmaf(lo, g, fmaf(x, g, -p));
     x = p;
 }
@@ -444,13 +451,14 @@ template <class T> struct RecArgs {
 // The sampling blocks (the first nsb blocks of the launch): eight lanes per
 // receiver, lane l < 6 forms its slot's terms (explicitly rounded FP64
 // products), lane 0 sums them in slot order.
-template <class T> __device__ __noinline__ void sample_receivers(const RecArgs<T> rec, const T *__restrict__ U, size_t nnode)
+template <class T>
+__device__ __noinline__ void sample_receivers(const RecArgs<T> rec, const T *__restrict__ U, size_t nnode, int tid, int nthr)
 {
     const int step = rec.ctl[rec.par];
     if (step % rec.tf != 0 || step / rec.tf >= rec.nsamp) return;
-    const int l = threadIdx.x & 7, per = blockDim.x >> 3;
+    const int l = tid & 7, per = nthr >> 3;
     for (int r0 = blockIdx.x * per; r0 < rec.nrec; r0 += rec.nsb * per) {
-        const int r = r0 + (int)(threadIdx.x >> 3);
+        const int r = r0 + (tid >> 3);
         double c[3] = {0.0, 0.0, 0.0};
         if (r < rec.nrec && l < 6) {
             const size_t e = (size_t)rec.edges[6 * r + l];
@@ -678,7 +686,7 @@ __device__ __forceinline__ void step_tet(const T (&ue)[43], T (&f)[7], T (&fl)[7
             else sum = tab.n.curl[p][l][c] > 0 ? sum + u : sum - u;
             started = true;
         }
-        b[c] = inside ? T(1.0 / 6.0) * sum : T(0);
+        b[c] = inside ? mul_rn(T(1.0 / 6.0), sum) : T(0);
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -730,7 +738,7 @@ __host__ __device__ constexpr int step_record_x(int sy, int mask) { return sy | 
 // plane cmp.p (see "compensated updates"); the loss factors
 // scale lo with hi.
 // Threads per block of the fused step: chosen per handle by timing these
-// candidates on the handle's own mesh (TetFemSim::tune_step_block); small
+// candidates on the handle's own mesh (TetFemSim::force_launch_shape); small
 // meshes (a 32^3 mesh has 36k nodes) spread better over the 152 SMs in
 // small blocks.  The block size changes no arithmetic.
 constexpr int kStepBlocks[4] = {32, 64, 128, 256};
@@ -751,7 +759,7 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
     // follow them
     const int nb = (int)blockIdx.x - rec.nsb;
     if (nb < 0) {
-        sample_receivers<T>(rec, Uin, nnode);
+        sample_receivers<T>(rec, Uin, nnode, (int)threadIdx.x, (int)blockDim.x);
         return;
     }
     const size_t v = (size_t)nb * blockDim.x + threadIdx.x;
@@ -798,7 +806,7 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
                 // P + lo - a (f + fl) + a s as hi + lo: the product -a f
                 // split exactly into p1 and its error, the small terms summed
                 // into t, then two exact sums
-                const T p1 = -a * f[d];
+                const T p1 = mul_rn(-a, f[d]);
                 T t = fma(-a, f[d], -p1) + lp;
                 t = fma(-a, fl[d], t);
                 if (m[d] & kSrcBit) t = fma(a, (T)source_load(src, e0 + d), t);
@@ -851,6 +859,206 @@ __global__ void __launch_bounds__(kStepBlockMax) tet_step_kernel(size_t nnode, c
             Uout[f0] = (m[d] & kPecBit) ? T(0) : fma(-c, y, T(2) * u[d] - Uold[f0]);
         }
     }
+}
+
+// ------------------------------------------------------ slot-split step
+// One thread per node gives a mesh held in L2 (a 32^3 mesh has 36k nodes)
+// about seven warps per SM, too few to hide the latency of the neighbour
+// loads.  The slot-split step runs seven warps per 32 nodes: warp d takes
+// slot d of its 32 nodes.  It reads the edge values of the tetrahedra that
+// hold the slot's edge, forms only the curl components the slot's gather
+// needs, gathers the slot's force and kicks P_d; after a block barrier it
+// forms (Minv P)_d from the node's seven kicked P values in shared memory
+// and drifts U_d.  Every sum runs in the order of the node kernel (entries
+// ascending, components ascending, the mass row in column order), so both
+// kernels give the same bits.  MODE 0 without losses only.
+constexpr int kSlotNodes = 32;               // nodes per block (one per lane)
+constexpr int kSlotThreads = 7 * kSlotNodes; // the block: one warp per slot direction
+
+struct SlotTab {
+    int nt[7];          // node-table entries whose tetrahedron holds slot d's edge
+    int q[7][6];        // those entries, ascending
+    int l[7][6];        // the local edge of slot d in each
+    int nu[7];          // distinct edge values slot d reads
+    int ue[7][36];      // their indices in the 43-edge list of StepTab
+    int ui[7][6][6];    // local edge l' of feed k -> index into the slot's values (-1: not read)
+};
+
+constexpr SlotTab make_slot_tab()
+{
+    SlotTab s{};
+    const StepTab t = make_step_tab();
+    for (int d = 0; d < 7; ++d) {
+        for (int q = 0; q < 18; ++q)
+            for (int k = 0; k < t.n.ne[q]; ++k)
+                if (t.n.d[q][k] == d) {
+                    s.q[d][s.nt[d]] = q;
+                    s.l[d][s.nt[d]] = t.n.l[q][k];
+                    ++s.nt[d];
+                }
+        for (int k = 0; k < s.nt[d]; ++k) {
+            const int q = s.q[d][k], p = t.n.p[q], l = s.l[d][k];
+            for (int l2 = 0; l2 < 6; ++l2) {
+                s.ui[d][k][l2] = -1;
+                bool need = false;   // l2 enters a curl component that the gather of slot d uses
+                for (int c = 0; c < 3; ++c)
+                    if (t.n.curl[p][l][c] != 0 && t.n.curl[p][l2][c] != 0) need = true;
+                if (!need) continue;
+                const int e = t.eidx[q][l2];
+                int at = -1;
+                for (int u = 0; u < s.nu[d]; ++u)
+                    if (s.ue[d][u] == e) at = u;
+                if (at < 0) { at = s.nu[d]; s.ue[d][s.nu[d]++] = e; }
+                s.ui[d][k][l2] = at;
+            }
+        }
+    }
+    return s;
+}
+
+// Feed K of slot D: the curl components of that tetrahedron that the gather
+// of slot D needs, B' = S / 6 (zero outside the mesh), and their terms
+// +-B' added to f in component order (the first term of the slot starts the
+// sum).  Template parameters make every table index a constant.
+template <class T, int D, int K, int COMP, int NU>
+__device__ __forceinline__ void slot_feed(const T (&ue)[NU], int have, T &f, T &fl)
+{
+    constexpr StepTab tab = make_step_tab();
+    constexpr SlotTab st = make_slot_tab();
+    constexpr int q = st.q[D][K], p = tab.n.p[q], l = st.l[D][K];
+    const bool inside = (tab.qreq[q] & ~have) == 0;
+    bool first = K == 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (tab.n.curl[p][l][c] == 0) continue;
+        T sum = 0;
+        bool started = false;
+#pragma unroll
+        for (int l2 = 0; l2 < 6; ++l2) {
+            if (tab.n.curl[p][l2][c] == 0) continue;
+            const T u = ue[st.ui[D][K][l2]];
+            if (!started) sum = tab.n.curl[p][l2][c] > 0 ? u : -u;
+            else sum = tab.n.curl[p][l2][c] > 0 ? sum + u : sum - u;
+            started = true;
+        }
+        const T b = inside ? mul_rn(T(1.0 / 6.0), sum) : T(0);
+        const T t = tab.n.curl[p][l][c] > 0 ? b : -b;
+        if (first) {
+            f = t;
+            first = false;
+        } else if constexpr (COMP) {
+            T e;
+            f = two_sum(f, t, e);
+            fl += e;
+        } else {
+            f += t;
+        }
+    }
+}
+
+template <class T, int D, int COMP, int NU, int... K>
+__device__ __forceinline__ void slot_feeds(const T (&ue)[NU], int have, T &f, T &fl, std::integer_sequence<int, K...>)
+{
+    (slot_feed<T, D, K, COMP, NU>(ue, have, f, fl), ...);
+}
+
+template <class T, int D, int NU, int... K>
+__device__ __forceinline__ void slot_loads(T (&ue)[NU], const T *__restrict__ u0, size_t nnode, const int (&off)[13],
+                                           std::integer_sequence<int, K...>)
+{
+    constexpr StepTab tab = make_step_tab();
+    constexpr SlotTab st = make_slot_tab();
+    ((ue[K] = u0[(size_t)tab.edir[st.ue[D][K]] * nnode + off[tab.etail[st.ue[D][K]]]]), ...);
+}
+
+// Force of slot D of one node, f = K U restricted to the slot, as hi + lo
+// with COMP (see step_tet).
+template <class T, int D, int COMP>
+__device__ __forceinline__ void slot_force(const T *__restrict__ u0, size_t nnode, const int (&off)[13], int have, T &f, T &fl)
+{
+    constexpr SlotTab st = make_slot_tab();
+    constexpr int nu = st.nu[D], nt = st.nt[D];
+    T ue[nu];
+    slot_loads<T, D, nu>(ue, u0, nnode, off, std::make_integer_sequence<int, nu>{});
+    f = 0;
+    fl = 0;
+    slot_feeds<T, D, COMP, nu>(ue, have, f, fl, std::make_integer_sequence<int, nt>{});
+    f *= T(4);
+    fl *= T(4);
+}
+
+template <class T, int REC, int COMP>
+__global__ void __launch_bounds__(kSlotThreads) tet_slot_kernel(size_t nnode, const int2 *__restrict__ nrec,
+                                                                const unsigned char *__restrict__ pec,
+                                                                const T *__restrict__ minv, T *__restrict__ P,
+                                                                const T *__restrict__ Uin, T *__restrict__ Uout, T a, T c,
+                                                                SrcArgs src, T *__restrict__ zout, RecArgs<T> rec, Comp cmp)
+{
+    constexpr StepTab tab = make_step_tab();
+    const int nb = (int)blockIdx.x - rec.nsb;
+    if (nb < 0) {   // the leading blocks sample the receivers (no barrier below is reached)
+        sample_receivers<T>(rec, Uin, nnode, (int)(threadIdx.y * kSlotNodes + threadIdx.x), kSlotThreads);
+        return;
+    }
+    __shared__ T sx[7][kSlotNodes];
+    const int lane = threadIdx.x, d = threadIdx.y;
+    const size_t v = (size_t)nb * kSlotNodes + lane;
+    const bool valid = v < nnode;
+    if (rec.adv && v == 0 && d == 0) rec.ctl[1 - rec.par] = rec.ctl[rec.par] + 1;
+    const size_t f0 = (size_t)d * nnode + v, e0 = 7 * v;
+    T x = 0, u = 0;
+    unsigned char m = 0;
+    if (valid) {
+        const int2 r = __ldg(nrec + v);
+        const int have = (int)((unsigned)r.x >> 26), sy = r.x & 0x3ffffff, sz = r.y;
+        int off[13];
+#pragma unroll
+        for (int t = 0; t < 13; ++t)
+            off[t] = (tab.treq[t] & ~have) == 0 ? tab.tail[t][0] + tab.tail[t][1] * sy + tab.tail[t][2] * sz : 0;
+        T f = 0, fl = 0;
+        const T *u0 = Uin + v;
+        switch (d) {
+        case 0: slot_force<T, 0, COMP>(u0, nnode, off, have, f, fl); break;
+        case 1: slot_force<T, 1, COMP>(u0, nnode, off, have, f, fl); break;
+        case 2: slot_force<T, 2, COMP>(u0, nnode, off, have, f, fl); break;
+        case 3: slot_force<T, 3, COMP>(u0, nnode, off, have, f, fl); break;
+        case 4: slot_force<T, 4, COMP>(u0, nnode, off, have, f, fl); break;
+        case 5: slot_force<T, 5, COMP>(u0, nnode, off, have, f, fl); break;
+        default: slot_force<T, 6, COMP>(u0, nnode, off, have, f, fl); break;
+        }
+        u = Uin[f0];
+        m = pec[e0 + d];
+        x = P[f0];
+        // the kick of the node kernel (MODE 0, no losses)
+        if constexpr (COMP) {
+            T lp = comp_load(cmp.p, f0);
+            if (!(m & kPecBit)) {
+                const T p1 = mul_rn(-a, f);
+                T t = fma(-a, f, -p1) + lp;
+                t = fma(-a, fl, t);
+                if (m & kSrcBit) t = fma(a, (T)source_load(src, e0 + d), t);
+                T e;
+                const T s1 = two_sum(x, p1, e);
+                x = two_sum(s1, t + e, lp);
+            }
+            comp_store(cmp.p, f0, lp);
+        } else {
+            if (!(m & kPecBit)) {
+                x = fma(-a, f, x);
+                if (m & kSrcBit) x = fma(a, (T)source_load(src, e0 + d), x);
+            }
+        }
+        P[f0] = x;
+    }
+    sx[d][lane] = x;
+    __syncthreads();
+    if (!valid) return;
+    T y = 0;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) y = fma(minv[fpk(v, pk7(d, j), nnode)], sx[j][lane], y);
+    Uout[f0] = fma(c, y, u);
+    if (zout) zout[f0] = y;
+    if (REC && (m & kRecBit)) rec.rz_out[rec.kidx[e0 + d]] = y;
 }
 
 // Adjoint of the second loss factor of a lossy middle kick and the loss
@@ -1435,7 +1643,8 @@ struct TetFemSim : Sim {
     std::vector<double> sig_h, rho_h, lden_h;
     bool has_loss = false;
     DevBuf d_damp;
-    int step_block = 64;            // threads per block of tet_step_kernel (tune_step_block)
+    int step_block = 64;            // threads per block of tet_step_kernel (tune_launch_shape)
+    bool slot_split = true;         // symplectic lossless steps by tet_slot_kernel (tune_launch_shape)
     bool step_tuned = false;        // the block size depends on the mesh only: tuned once per handle
     DevBuf d_tet_edge, d_inc_ptr, d_inc, d_nrec, d_pec, d_eps, d_minv, d_U, d_P, d_Uold, d_status;
     // FP32 runs: bfloat16 compensation planes of U and then P, one
@@ -1687,48 +1896,37 @@ struct TetFemSim : Sim {
         }
         if (dtn >= dt_lim_n) throw Error{EMS_ERR_INVALID_ARGUMENT, "time step exceeds the stability limit of the integrator"};
         loss_setup();
-        tune_step_block();
+        force_launch_shape();
         ready = true;
     }
 
-    // Block size of the fused step, chosen once per handle (it depends on
-    // the mesh, not the material): the candidates are timed on this mesh in
-    // two sweeps (three warm-up and ten timed launches each, a = c = 0 so P
-    // keeps its values and U is copied into the spare buffer; both are
-    // rewritten before they are read again) and the one with the shortest
-    // sweep time is kept.  The environment variable EMS_TET_STEP_BLOCK
-    // forces one of the candidates.
-    void tune_step_block()
+    // Launch shape of the fused step: the node kernel at four block sizes
+    // (32, 64, 128, 256 threads) or the slot-split kernel.  It depends on
+    // the mesh, not the material, and changes no result, so it is chosen once
+    // per handle inside its first unrecorded run of at least 132 steps
+    // (symplectic or leapfrog): each candidate advances 12 real steps of that run from
+    // a CUDA graph, as the loop runs them, twice over, and the fastest is kept
+    // for the rest of the run and later ones.  (Timed on idle steps outside
+    // a run, the candidates ranked differently from the loop.)  Before that
+    // the slot-split kernel runs.  The environment variable
+    // EMS_TET_STEP_BLOCK (32, 64, 128, 256 or slot) forces one;
+    // EMS_TET_TUNE_LOG prints the candidates' times to stderr.
+    static constexpr int kShapes = 5, kTuneRounds = 2;
+    void set_shape(int ci)
     {
-        if (step_tuned) return;
+        slot_split = ci == kShapes - 1;
+        step_block = kStepBlocks[ci < 4 ? ci : 0];
+    }
+    void force_launch_shape()
+    {
+        const char *env = std::getenv("EMS_TET_STEP_BLOCK");
+        if (step_tuned || !env) return;
         step_tuned = true;
-        if (const char *env = std::getenv("EMS_TET_STEP_BLOCK")) {
-            const int b = std::atoi(env);
-            for (int c : kStepBlocks)
-                if (c == b) { step_block = b; return; }
-            throw Error{EMS_ERR_INVALID_ARGUMENT, "EMS_TET_STEP_BLOCK must be 32, 64, 128 or 256"};
-        }
-        float best[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        for (int sweep = 0; sweep < 2; ++sweep)
-            for (int ci = 0; ci < 4; ++ci) {
-                step_block = kStepBlocks[ci];
-                const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
-                for (int r = 0; r < 13; ++r) {
-                    if (r == 3) EMS_CUDA(cudaEventRecord(ev0, stream));
-                    idle_step(nbv, r % 2);
-                }
-                EMS_CUDA(cudaGetLastError());
-                EMS_CUDA(cudaEventRecord(ev1, stream));
-                EMS_CUDA(cudaEventSynchronize(ev1));
-                float ms = 0.0f;
-                EMS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
-                if (sweep == 0 || ms < best[ci]) best[ci] = ms;
-            }
-        int pick = kStepBlocks[0];
-        float bmin = best[0];
-        for (int ci = 1; ci < 4; ++ci)
-            if (best[ci] < bmin) { bmin = best[ci]; pick = kStepBlocks[ci]; }
-        step_block = pick;
+        if (std::strcmp(env, "slot") == 0) { set_shape(kShapes - 1); return; }
+        const int b = std::atoi(env);
+        for (int c = 0; c < 4; ++c)
+            if (kStepBlocks[c] == b) { set_shape(c); return; }
+        throw Error{EMS_ERR_INVALID_ARGUMENT, "EMS_TET_STEP_BLOCK must be 32, 64, 128, 256 or slot"};
     }
 
     // Conductivity as a per-node loss rate: rho_v = sum sigma_T w / sum
@@ -2005,6 +2203,21 @@ struct TetFemSim : Sim {
                 T *pmid = nullptr, const RecArgs<T> &rec = RecArgs<T>{}, Comp cm = Comp{})
     {
         if (Uin == Uout) throw Error{EMS_ERR_STATE, "fused step needs separate input and output fields"};
+        if constexpr (MODE == 0 && DAMP == 0) {
+            if (slot_split) {
+                // rec.nsb leading blocks sample the receivers when this launch does
+                const unsigned nbs = (unsigned)((nnode + kSlotNodes - 1) / kSlotNodes) + (unsigned)rec.nsb;
+                const dim3 blk(kSlotNodes, 7);
+                auto go = [&](auto kern) {
+                    kern<<<nbs, blk, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), d_minv.as<T>(), Pio,
+                                                  Uin, Uout, a, c, sa, zout, rec, cm);
+                    return 1;
+                };
+                const bool comp32 = std::is_same<T, float>::value && cm.p;
+                if (rec.rz_out) return comp32 ? go(tet_slot_kernel<T, 1, 1>) : go(tet_slot_kernel<T, 1, 0>);
+                return comp32 ? go(tet_slot_kernel<T, 0, 1>) : go(tet_slot_kernel<T, 0, 0>);
+            }
+        }
         // rec.nsb leading blocks sample the receivers when this launch does
         const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block) + (unsigned)rec.nsb;
         const T *dm = DAMP ? d_damp.as<T>() : nullptr;
@@ -2035,6 +2248,19 @@ struct TetFemSim : Sim {
             T *a = d_U.as<T>(), *b = d_Uold.as<T>();
             if (odd) std::swap(a, b);
             const Comp cm = comp();
+            if (slot_split) {
+                const unsigned nbs = (unsigned)((nnode + kSlotNodes - 1) / kSlotNodes);
+                const dim3 blk(kSlotNodes, 7);
+                if (cm.p)
+                    tet_slot_kernel<T, 0, std::is_same<T, float>::value><<<nbs, blk, 0, stream>>>(
+                        nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), d_minv.as<T>(), d_P.as<T>(), a, b, T(0), T(0),
+                        SrcArgs{}, nullptr, RecArgs<T>{}, cm);
+                else
+                    tet_slot_kernel<T, 0, 0><<<nbs, blk, 0, stream>>>(nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(),
+                                                                     d_minv.as<T>(), d_P.as<T>(), a, b, T(0), T(0), SrcArgs{},
+                                                                     nullptr, RecArgs<T>{}, Comp{});
+                return;
+            }
             if (cm.p)
                 tet_step_kernel<T, 0, 0, 0, std::is_same<T, float>::value><<<nbv, step_block, 0, stream>>>(
                     nnode, d_nrec.as<int2>(), d_pec.as<unsigned char>(), d_minv.as<T>(), d_P.as<T>(), a, b, nullptr, T(0), T(0),
@@ -2070,7 +2296,10 @@ struct TetFemSim : Sim {
         const int nrz = std::max(nk, 1);
         if (q == 0) {
             r.nrec = sample ? nobs : 0;
-            r.nsb = sample && nobs > 0 ? (nobs + step_block / 8 - 1) / (step_block / 8) : 0;   // eight lanes per receiver
+            // the first launch runs the slot-split kernel unless it is the lossy middle kick or leapfrog
+            const bool slot0 = slot_split && sc.symp && !(has_loss && sc.nsub / 2 == 0);
+            const int per = (slot0 ? kSlotThreads : step_block) / 8;   // eight lanes per receiver
+            r.nsb = sample && nobs > 0 ? (nobs + per - 1) / per : 0;
             r.adv = 1;
         }
         r.edges = d_rec_e.as<int>();
@@ -2274,7 +2503,15 @@ struct TetFemSim : Sim {
                 if (exec) cudaGraphExecDestroy(exec);
                 if (g) cudaGraphDestroy(g);
             }
-        } graph[2];
+        } graph[2], cand[kShapes];
+        struct Events {   // timing of the launch-shape candidates
+            cudaEvent_t e[kShapes * kTuneRounds + 1] = {};
+            ~Events()
+            {
+                for (cudaEvent_t x : e)
+                    if (x) cudaEventDestroy(x);
+            }
+        } tev;
         int per_graph = 0, par = 0;   // par: parity of the next step's counter copy
         auto capture = [&](StepGraph &G, T *u, T *p, T *o, int par0) {
             G.start = u;
@@ -2309,7 +2546,18 @@ struct TetFemSim : Sim {
             nseg = (nsteps + seg_len - 1) / seg_len;
             d_snap.alloc((size_t)nseg * snap_bytes());
         }
-        if ((record ? seg_len : nsteps) >= kGraphSteps) {
+        // launch-shape tuning in the first unrecorded run long enough: every
+        // candidate's graph of kGraphSteps steps starts from the assignment
+        // (Uc, parity 0) and returns to it, so they are captured up front
+        const int tune_steps = kShapes * kTuneRounds * kGraphSteps;
+        const bool tuning = !step_tuned && !record && nsteps >= tune_steps + kGraphSteps;
+        if (tuning) {
+            for (int ci = 0; ci < kShapes; ++ci) {
+                set_shape(ci);
+                capture(cand[ci], Uc, Pc, Uo, 0);
+            }
+            for (auto &x : tev.e) EMS_CUDA(cudaEventCreate(&x));
+        } else if ((record ? seg_len : nsteps) >= kGraphSteps) {
             capture(graph[0], Uc, Pc, Uo, 0);
             if (record && symp && sc.nsub % 2 == 1) capture(graph[1], Uo, Pc, Uc, 1);
         }
@@ -2319,6 +2567,38 @@ struct TetFemSim : Sim {
             rz_init<T>(Pc, 0);
             launches += nk > 0 ? 2 : 1;
         }
+        int done = 0;   // steps advanced by the tuning graphs
+        if (tuning) {
+            for (int r = 0; r < kTuneRounds; ++r)
+                for (int ci = 0; ci < kShapes; ++ci) {
+                    EMS_CUDA(cudaEventRecord(tev.e[r * kShapes + ci], stream));
+                    EMS_CUDA(cudaGraphLaunch(cand[ci].exec, stream));
+                    launches += per_graph;
+                }
+            EMS_CUDA(cudaEventRecord(tev.e[kShapes * kTuneRounds], stream));
+            EMS_CUDA(cudaEventSynchronize(tev.e[kShapes * kTuneRounds]));
+            float best[kShapes] = {};
+            for (int r = 0; r < kTuneRounds; ++r)
+                for (int ci = 0; ci < kShapes; ++ci) {
+                    float ms = 0.0f;
+                    EMS_CUDA(cudaEventElapsedTime(&ms, tev.e[r * kShapes + ci], tev.e[r * kShapes + ci + 1]));
+                    if (r == 0 || ms < best[ci]) best[ci] = ms;
+                }
+            int pick = 0;
+            for (int ci = 1; ci < kShapes; ++ci)
+                if (best[ci] < best[pick]) pick = ci;
+            if (std::getenv("EMS_TET_TUNE_LOG"))   // diagnostic: the candidates' times per step
+                std::fprintf(stderr, "tet step tuning (us per step): node32 %.3f node64 %.3f node128 %.3f node256 %.3f slot %.3f\n",
+                             1e3 * best[0] / kGraphSteps, 1e3 * best[1] / kGraphSteps, 1e3 * best[2] / kGraphSteps,
+                             1e3 * best[3] / kGraphSteps, 1e3 * best[4] / kGraphSteps);
+            set_shape(pick);
+            step_tuned = true;
+            std::swap(graph[0].g, cand[pick].g);
+            std::swap(graph[0].exec, cand[pick].exec);
+            graph[0].start = cand[pick].start;
+            graph[0].par = cand[pick].par;
+            done = tune_steps;
+        }
         if (record) {
             // snapshot of the merged state at the start of every segment
             for (int s = 0; s < nseg; ++s) {
@@ -2326,7 +2606,7 @@ struct TetFemSim : Sim {
                 advance(std::min(seg_len, nsteps - s * seg_len));
             }
         } else {
-            advance(nsteps);
+            advance(nsteps - done);
         }
         if (symp) {
             tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)(-sc.hfirst));
@@ -2725,35 +3005,48 @@ struct TetFemSim : Sim {
     void launch_shape(int b[3]) override
     {
         if (!ready) setup();
-        b[0] = step_block; b[1] = b[2] = 1;
+        if (slot_split) { b[0] = kSlotNodes; b[1] = 7; b[2] = 1; }
+        else { b[0] = step_block; b[1] = b[2] = 1; }
     }
 
     void time_dominant(int launches, double *ms, double *bytes, std::string *name) override
     {
         if (!ready) setup();
-        const size_t w = fp64 ? 8 : 4;
         const unsigned nbv = (unsigned)((nnode + step_block - 1) / step_block);
-        // the fused step of a substep as the time loop runs it: a = c = 0
-        // leaves P unchanged and copies U between the two buffers the loop
-        // alternates, so the fields keep their values and the caches see the
-        // loop's access pattern
-        for (int r = 0; r <= launches; ++r) {
-            if (r == 1) EMS_CUDA(cudaEventRecord(ev0, stream));
-            idle_step(nbv, r % 2);
-        }
-        EMS_CUDA(cudaGetLastError());
-        EMS_CUDA(cudaEventRecord(ev1, stream));
+        // the fused step of a substep in the handle's launch shape, as the time
+        // loop runs it: a CUDA graph of 12 launches (a = c = 0 leaves P
+        // unchanged and copies U between the two buffers the loop
+        // alternates), replayed; launched one by one, the kernels would wait
+        // on the host's launch rate
+        constexpr int kLaunches = 12;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t exec = nullptr;
         EMS_CUDA(cudaStreamSynchronize(stream));
+        EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        for (int r = 0; r < kLaunches; ++r) idle_step(nbv, r % 2);
+        cudaError_t ce = cudaStreamEndCapture(stream, &g);
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, g, 0);
+        const int reps = std::max(1, launches / kLaunches);
+        if (ce == cudaSuccess) ce = cudaGraphLaunch(exec, stream);
+        if (ce == cudaSuccess) ce = cudaEventRecord(ev0, stream);
+        for (int r = 0; r < reps && ce == cudaSuccess; ++r) ce = cudaGraphLaunch(exec, stream);
+        if (ce == cudaSuccess) ce = cudaEventRecord(ev1, stream);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
         float t = 0;
-        EMS_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
-        *ms = t / launches;
+        if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, ev0, ev1);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (g) cudaGraphDestroy(g);
+        if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("dominant-kernel timing: ") + cudaGetErrorString(ce)};
+        *ms = t / (reps * kLaunches);
+        const size_t w = fp64 ? 8 : 4;
         // unique bytes of one substep: node records (8 B per node) + U read
         // once (the neighbours' reads hit L1/L2) + P read and written + U
         // written + packed mass blocks + slot flags (+ FP32: P's bfloat16
         // compensation plane read and written)
         *bytes = (double)nnode * 8 + (double)nslot * 4 * w + (double)(28 * nnode) * w + (double)nslot +
                  (fp64 ? 0.0 : (double)nslot * 2 * 2);
-        *name = fp64 ? "tet_step_kernel<double>" : "tet_step_kernel<float>";
+        if (slot_split) *name = fp64 ? "tet_slot_kernel<double>" : "tet_slot_kernel<float>";
+        else *name = fp64 ? "tet_step_kernel<double>" : "tet_step_kernel<float>";
     }
 };
 

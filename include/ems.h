@@ -300,8 +300,10 @@ int ems_time_dominant_kernel(ems_sim *sim, int launches, double *ms_per_launch, 
                              char *name, size_t name_cap);
 /* Threads per block (x, y, z) of the main time-step kernels as the handle's
  * autotuner chose them by timing candidates on its own grid: tetrahedral
- * handles time 32, 64, 128, 256 threads when the material is set up
- * (EMS_TET_STEP_BLOCK forces one); FDTD handles time the shapes 32x8, 32x4,
+ * handles time the node kernel at 32, 64, 128, 256 threads and the
+ * slot-split kernel (block 32 x 7: one warp per edge direction of 32 nodes)
+ * when the material is set up (EMS_TET_STEP_BLOCK = 32, 64, 128, 256 or slot
+ * forces one); FDTD handles time the shapes 32x8, 32x4,
  * 64x4, 128x2, 256x1, 64x2 on the first steps of their first run of at
  * least 40 steps (EMS_FDTD_BLOCK="XxY" forces one; 32x8 before tuning).
  * Launch shapes change no result.  Zeros for solvers with fixed shapes.

@@ -216,39 +216,56 @@ def test_apply_stiffness_matches_oracle(precision, tol):
     assert np.all(s.get_field(0) == 0.0)
 
 
-def test_step_block_autotuner_picks_a_candidate_and_changes_no_result():
-    # forced block sizes (EMS_TET_STEP_BLOCK) in child processes: the block
-    # size is a launch shape only, so traces and fields are bit-identical
+_LAUNCH_SHAPE_CASE = (
+    "import sys, numpy as np, emsolvers_gb300 as ems\n"
+    "prec, lossy = {'fp32': ems.FP32, 'fp64': ems.FP64}[sys.argv[2]], sys.argv[3] == '1'\n"
+    "n = (9, 7, 8)\n"
+    "rng = np.random.default_rng(3)\n"
+    "eps = rng.uniform(1, 4, 6 * 9 * 7 * 8)\n"
+    "sig = rng.uniform(0.0, 0.3, eps.size) if lossy else None\n"
+    "s = ems.TetFemSimulation(n, 1e-3, 1, ems.SYMP4, prec, dt=0.0, cfl_fraction=0.8)\n"
+    "s.set_material(eps, sig)\n"
+    "s.add_dipole(np.array([4.1, 3.3, 4.2]) * 1e-3, (0.2, 0.3, 1.0), ems.WAVE_RICKER, 4e10, 1.0)\n"
+    "for p in ([6.2, 2.1, 3.3], [2.2, 5.1, 6.3], [4.4, 3.9, 1.1]):\n"
+    "    s.add_receiver(np.array(p) * 1e-3)\n"
+    "s.set_checkpoints(5)\n"
+    "s.reset()\n"
+    "s.run(80)\n"
+    "tg = s.traces().copy(); tg[..., 0] = 0.0\n"
+    "g = s.backward(tg)\n"
+    "print(*s.launch_shape())\n"
+    "np.save(sys.argv[1], np.concatenate([s.traces().ravel(), s.get_field(0), s.get_field(1), g]))\n")
+
+
+@pytest.mark.parametrize("prec,lossy", [("fp32", "0"), ("fp64", "0"), ("fp32", "1")], ids=["fp32", "fp64", "fp32-lossy"])
+def test_step_launch_shapes_change_no_result(prec, lossy):
+    # forced launch shapes (EMS_TET_STEP_BLOCK) in child processes: the node
+    # kernel at two block sizes and the slot-split kernel (seven warps per 32
+    # nodes) are launch shapes of the same arithmetic, so traces, fields and
+    # the adjoint gradient are bit-identical; the autotuner picks one of them
     import os
     import subprocess
     import sys
-    code = (
-        "import numpy as np, emsolvers_gb300 as ems\n"
-        "n = (9, 7, 8)\n"
-        "eps = np.random.default_rng(3).uniform(1, 4, 6 * 9 * 7 * 8)\n"
-        "s = ems.TetFemSimulation(n, 1e-3, 1, ems.SYMP4, ems.FP32, dt=0.0, cfl_fraction=0.8)\n"
-        "s.set_material(eps)\n"
-        "s.add_dipole(np.array([4.1, 3.3, 4.2]) * 1e-3, (0.2, 0.3, 1.0), ems.WAVE_RICKER, 4e10, 1.0)\n"
-        "s.add_receiver(np.array([6.2, 2.1, 3.3]) * 1e-3)\n"
-        "s.run(80)\n"
-        "print(s.launch_shape()[0])\n"
-        "np.save('%s', np.concatenate([s.traces().ravel(), s.get_field(0), s.get_field(1)]))\n")
     out = {}
-    for b in ("", "32", "256"):
+    for b in ("", "32", "256", "slot"):
         env = dict(os.environ)
         env.pop("EMS_TET_STEP_BLOCK", None)
         if b:
             env["EMS_TET_STEP_BLOCK"] = b
-        path = f"/tmp/ems_step_block_{b or 'auto'}_{os.getpid()}.npy"
-        r = subprocess.run([sys.executable, "-c", code % path], env=env, capture_output=True, text=True, timeout=300)
+        path = f"/tmp/ems_step_block_{b or 'auto'}_{prec}_{lossy}_{os.getpid()}.npy"
+        r = subprocess.run([sys.executable, "-c", _LAUNCH_SHAPE_CASE, path, prec, lossy], env=env, capture_output=True,
+                           text=True, timeout=300)
         assert r.returncode == 0, r.stderr
-        chosen = int(r.stdout.strip().splitlines()[-1])
-        assert chosen in (32, 64, 128, 256)
-        if b:
-            assert chosen == int(b)
+        shape = tuple(int(v) for v in r.stdout.strip().splitlines()[-1].split())
+        assert shape in ((32, 1, 1), (64, 1, 1), (128, 1, 1), (256, 1, 1), (32, 7, 1))
+        if b == "slot":
+            assert shape == (32, 7, 1)
+        elif b:
+            assert shape == (int(b), 1, 1)
         out[b] = np.load(path)
         os.remove(path)
-    assert np.array_equal(out[""], out["32"]) and np.array_equal(out["32"], out["256"])
+    for b in ("32", "256", "slot"):
+        assert np.array_equal(out[""], out[b]), b
 
 
 @pytest.mark.parametrize("integ", [oracle.SYMP4, oracle.LEAPFROG], ids=["symp4", "leapfrog"])
