@@ -971,11 +971,22 @@ __device__ __forceinline__ void slot_loads(T (&ue)[NU], const T *__restrict__ u0
     ((ue[K] = u0[(size_t)tab.edir[st.ue[D][K]] * nnode + off[tab.etail[st.ue[D][K]]]]), ...);
 }
 
-// Force of slot D of one node, f = K U restricted to the slot, as hi + lo
-// with COMP (see step_tet).
-template <class T, int D, int COMP>
-__device__ __forceinline__ void slot_force(const T *__restrict__ u0, size_t nnode, const int (&off)[13], int have, T &f, T &fl)
+// Row D of the node's packed mass block (plane layout), in column order.
+template <class T, int D, int... J>
+__device__ __forceinline__ void slot_mass_row(const T *__restrict__ minv, size_t v, size_t nnode, T (&row)[7],
+                                              std::integer_sequence<int, J...>)
 {
+    constexpr int idx[7] = {(D < J ? D * (13 - D) / 2 + J : J * (13 - J) / 2 + D)...};   // packed (D, j)
+    ((row[J] = minv[fpk(v, idx[J], nnode)]), ...);
+}
+
+// Force of slot D of one node, f = K U restricted to the slot, as hi + lo
+// with COMP (see step_tet), and row D of the node's mass block.
+template <class T, int D, int COMP>
+__device__ __forceinline__ void slot_force(const T *__restrict__ u0, size_t nnode, const int (&off)[13], int have, T &f, T &fl,
+                                           const T *__restrict__ minv, size_t v, T (&row)[7])
+{
+    slot_mass_row<T, D>(minv, v, nnode, row, std::make_integer_sequence<int, 7>{});
     constexpr SlotTab st = make_slot_tab();
     constexpr int nu = st.nu[D], nt = st.nt[D];
     T ue[nu];
@@ -1006,7 +1017,7 @@ __global__ void __launch_bounds__(kSlotThreads) tet_slot_kernel(size_t nnode, co
     const bool valid = v < nnode;
     if (rec.adv && v == 0 && d == 0) rec.ctl[1 - rec.par] = rec.ctl[rec.par] + 1;
     const size_t f0 = (size_t)d * nnode + v, e0 = 7 * v;
-    T x = 0, u = 0;
+    T x = 0, u = 0, row[7] = {0, 0, 0, 0, 0, 0, 0};   // row: the mass row of slot d, loaded before the barrier
     unsigned char m = 0;
     if (valid) {
         const int2 r = __ldg(nrec + v);
@@ -1017,14 +1028,14 @@ __global__ void __launch_bounds__(kSlotThreads) tet_slot_kernel(size_t nnode, co
             off[t] = (tab.treq[t] & ~have) == 0 ? tab.tail[t][0] + tab.tail[t][1] * sy + tab.tail[t][2] * sz : 0;
         T f = 0, fl = 0;
         const T *u0 = Uin + v;
-        switch (d) {
-        case 0: slot_force<T, 0, COMP>(u0, nnode, off, have, f, fl); break;
-        case 1: slot_force<T, 1, COMP>(u0, nnode, off, have, f, fl); break;
-        case 2: slot_force<T, 2, COMP>(u0, nnode, off, have, f, fl); break;
-        case 3: slot_force<T, 3, COMP>(u0, nnode, off, have, f, fl); break;
-        case 4: slot_force<T, 4, COMP>(u0, nnode, off, have, f, fl); break;
-        case 5: slot_force<T, 5, COMP>(u0, nnode, off, have, f, fl); break;
-        default: slot_force<T, 6, COMP>(u0, nnode, off, have, f, fl); break;
+        switch (d) {   // warp-uniform: warp d runs slot d
+        case 0: slot_force<T, 0, COMP>(u0, nnode, off, have, f, fl, minv, v, row); break;
+        case 1: slot_force<T, 1, COMP>(u0, nnode, off, have, f, fl, minv, v, row); break;
+        case 2: slot_force<T, 2, COMP>(u0, nnode, off, have, f, fl, minv, v, row); break;
+        case 3: slot_force<T, 3, COMP>(u0, nnode, off, have, f, fl, minv, v, row); break;
+        case 4: slot_force<T, 4, COMP>(u0, nnode, off, have, f, fl, minv, v, row); break;
+        case 5: slot_force<T, 5, COMP>(u0, nnode, off, have, f, fl, minv, v, row); break;
+        default: slot_force<T, 6, COMP>(u0, nnode, off, have, f, fl, minv, v, row); break;
         }
         u = Uin[f0];
         m = pec[e0 + d];
@@ -1055,7 +1066,7 @@ __global__ void __launch_bounds__(kSlotThreads) tet_slot_kernel(size_t nnode, co
     if (!valid) return;
     T y = 0;
 #pragma unroll
-    for (int j = 0; j < 7; ++j) y = fma(minv[fpk(v, pk7(d, j), nnode)], sx[j][lane], y);
+    for (int j = 0; j < 7; ++j) y = fma(row[j], sx[j][lane], y);
     Uout[f0] = fma(c, y, u);
     if (zout) zout[f0] = y;
     if (REC && (m & kRecBit)) rec.rz_out[rec.kidx[e0 + d]] = y;

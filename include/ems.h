@@ -36,7 +36,8 @@ enum ems_status {
     EMS_ERR_OUT_OF_MEMORY = -3,     /* device or host allocation failed */
     EMS_ERR_IO = -4,                /* file missing / unreadable / malformed */
     EMS_ERR_STATE = -5,             /* call not valid in the handle's state */
-    EMS_ERR_DEVICE_TIMEOUT = -6,    /* a bounded device-side wait gave up */
+    EMS_ERR_DEVICE_TIMEOUT = -6,    /* reserved for a bounded device-side wait that gives up; no kernel of
+                                       this version waits on another, so no call returns it */
     EMS_ERR_NOT_FINITE = -7,        /* NaN/Inf in the fields after ems_run (the run's traces stay readable),
                                        or a tetrahedral mass block that is not positive definite */
     EMS_ERR_UNSUPPORTED = -8        /* combination not implemented */

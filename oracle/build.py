@@ -25,13 +25,19 @@ def build(force=False):
     return LIB
 
 
+# where the development container keeps the EMSolvers checkout; the
+# environment variable EMS_REFERENCE_DIR overrides it
+DEFAULT_REFERENCE_DIR = "/root/reference/src"
+
+
 def build_reference():
     """Compiles the unmodified reference solvers into oracle/_ref when the
-    reference tree is present (only in the development container)."""
-    ref = os.environ.get("EMS_REFERENCE_DIR", "/root/reference/src")
+    reference tree is present (EMS_REFERENCE_DIR, else the development
+    container's checkout); returns False where it is absent."""
+    ref = os.environ.get("EMS_REFERENCE_DIR", DEFAULT_REFERENCE_DIR)
     if not os.path.isdir(ref):
         return False
-    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True)
+    subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, env=dict(os.environ, EMS_REFERENCE_DIR=ref))
     return True
 
 

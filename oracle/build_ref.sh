@@ -6,7 +6,7 @@
 # -ffp-contract=off keeps the reference's FP64 arithmetic free of fused
 # multiply-adds on every host, so its results are reproducible across hosts.
 set -euo pipefail
-REF=${EMS_REFERENCE_DIR:-/root/reference/src}
+REF=${EMS_REFERENCE_DIR:?set EMS_REFERENCE_DIR to the EMSolvers src/ directory}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 [ -d "$REF" ] || { echo "reference sources not found at $REF" >&2; exit 3; }

@@ -1,10 +1,10 @@
 """Generates the golden fixtures in this folder from the reference solvers.
 
-Run in a checkout that has the EMSolvers sources (default /root/reference/src,
-or $EMS_REFERENCE_DIR):
+Run in a checkout that has the EMSolvers sources, with EMS_REFERENCE_DIR
+naming their src/ directory:
 
-    python oracle/build.py            # builds oracle/_ref from the sources
-    python tests/golden/make_golden.py
+    EMS_REFERENCE_DIR=<EMSolvers>/src python oracle/build.py          # builds oracle/_ref
+    EMS_REFERENCE_DIR=<EMSolvers>/src python tests/golden/make_golden.py
 
 Outputs (committed, small):
   kmat/{1,2,3,lamped1}.csv   the reference's element-matrix data files
@@ -84,12 +84,15 @@ for variant in ("fem_v2", "symplectic_2", "symplectic_4"):
 
 
 def main():
+    src = os.environ.get("EMS_REFERENCE_DIR")
+    if not src or not os.path.isdir(src):
+        raise SystemExit("set EMS_REFERENCE_DIR to the EMSolvers src/ directory")
     if not refrun.available():
         raise SystemExit("reference binaries missing: run python oracle/build.py first")
     kdir = os.path.join(HERE, "kmat")
     os.makedirs(kdir, exist_ok=True)
     for f in ("1.csv", "2.csv", "3.csv", "lamped1.csv"):
-        shutil.copyfile(os.path.join(refrun.REF_SRC, "fem_v2", "kmat", f), os.path.join(kdir, f))
+        shutil.copyfile(os.path.join(src, "fem_v2", "kmat", f), os.path.join(kdir, f))
 
     out = {}
     meta = []

@@ -1,8 +1,9 @@
 """Runs the reference solvers built from the unmodified EMSolvers sources
 (oracle/_ref, produced by oracle/build_ref.sh) and reads back their traces
-and fields.  Only available where the reference tree exists; tests that need
-it skip elsewhere, and the committed fixtures in tests/golden/ carry their
-outputs to machines without it."""
+and fields.  Only available where those binaries were built (a checkout
+with the reference sources); tests that need them skip elsewhere, and the
+committed fixtures in tests/golden/ carry their outputs to machines without
+them."""
 import os
 import subprocess
 import tempfile
@@ -11,11 +12,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BIN = os.path.join(os.path.dirname(HERE), "oracle", "_ref")
-REF_SRC = os.environ.get("EMS_REFERENCE_DIR", "/root/reference/src")
+GOLDEN = os.path.join(HERE, "golden")   # holds kmat/, the reference's element-matrix files
 
 
 def available():
-    return os.path.isdir(REF_SRC) and os.path.exists(os.path.join(REF_BIN, "fdtd_ref"))
+    return all(os.access(os.path.join(REF_BIN, b), os.X_OK) for b in ("fdtd_ref", "fem_v2_ref", "fem_abm_ref", "fem_ref"))
 
 
 def fdtd(nx, ny, nz, h, dt, eps, mu, tf, nsteps, sources, observations):
@@ -54,7 +55,7 @@ def femv2(variant, order, use_ofem, grid, h, dt, eps, mu, tf, nsteps, src, obs):
     """variant: fem_v2 | symplectic_2 | symplectic_4; src: (comp, (i,j,k))."""
     with tempfile.TemporaryDirectory() as td:
         out = os.path.join(td, "o.bin")
-        args = [os.path.join(REF_BIN, f"{variant}_ref"), out, os.path.join(REF_SRC, variant), str(order), str(use_ofem),
+        args = [os.path.join(REF_BIN, f"{variant}_ref"), out, GOLDEN, str(order), str(use_ofem),
                 *map(str, grid), repr(float(h)), repr(float(dt)), repr(float(eps)), repr(float(mu)), str(tf), str(nsteps),
                 str(src[0]), *map(str, src[1]), *map(str, obs)]
         subprocess.run(args, check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
