@@ -43,9 +43,9 @@ N = 32
 STEPS_PER_SOLVE = 2000
 H = 1e-3
 SEED = 2024
-# DRAM bytes (read + write) of one fused-step launch on the headline mesh,
-# from the ncu capture summarised in profiles/tet_step_tet32_symp4.md
-TRAFFIC_PER_LAUNCH = 7125504
+# DRAM bytes (read + write) of one step launch on the headline mesh, from
+# the ncu capture summarised in profiles/tet_slot_tet32_symp4.md
+TRAFFIC_PER_LAUNCH = 7115776
 
 
 def peaks():
@@ -655,7 +655,7 @@ def run_gpu(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      # DRAM bytes of one step launch from the ncu capture in
-                     # profiles/tet_step_tet32_symp4.md (cold fill: the 8.6 MB
+                     # profiles/tet_slot_tet32_symp4.md (cold fill: the 7.1 MB
                      # working set is L2-resident in the timed loop)
                      "traffic": TRAFFIC_PER_LAUNCH, "kernel": kname, "kernel_us": inloop_ms * 1e3,
                      "kernel_us_alone": kms * 1e3, "launches_per_solve": step_launches, "bytes_per_launch": kbytes,

@@ -7,8 +7,8 @@ front end that mirrors the reference's solver classes.
 from ._lib import (ABM, FP32, FP64, LEAPFROG, SYMP2, SYMP4, WAVE_REFERENCE, WAVE_RICKER, EmsError,  # noqa: F401
                    declared_functions, lib)
 from .solvers import (MISFIT_L2, MISFIT_TF_ENVELOPE, MISFIT_TF_PHASE, FdtdSimulation, FemStabSimulation,  # noqa: F401
-                      HexFemSimulation, TetFemBatch, TetFemSimulation, trace_misfit)
+                      HexFemSimulation, TetFemBatch, TetFemSimulation, tet_element_matrices, trace_misfit)
 
 __all__ = ["FdtdSimulation", "HexFemSimulation", "FemStabSimulation", "TetFemSimulation", "TetFemBatch", "EmsError", "lib", "declared_functions",
            "FP32", "FP64", "LEAPFROG", "SYMP2", "SYMP4", "ABM", "WAVE_REFERENCE", "WAVE_RICKER", "trace_misfit",
-           "MISFIT_L2", "MISFIT_TF_ENVELOPE", "MISFIT_TF_PHASE"]
+           "MISFIT_L2", "MISFIT_TF_ENVELOPE", "MISFIT_TF_PHASE", "tet_element_matrices"]

@@ -87,6 +87,7 @@ def lib():
         "ems_femstab_create": (C.c_int, [C.POINTER(FemStabParams), C.POINTER(vp)]),
         "ems_femstab_element_matrix": (C.c_int, [vp, dp, C.c_size_t]),
         "ems_tetfem_create": (C.c_int, [C.POINTER(TetFemParams), C.POINTER(vp)]),
+        "ems_tetfem_element_matrices": (C.c_int, [C.c_int, C.c_int, dp, dp, C.c_size_t]),
         "ems_tetbatch_create": (C.c_int, [C.POINTER(TetFemParams), C.c_int, ip, C.POINTER(vp)]),
         "ems_tetbatch_add_dipole": (C.c_int, [vp, C.c_int, dp, dp, C.c_int, C.c_double, C.c_double]),
         "ems_tetbatch_add_receiver": (C.c_int, [vp, C.c_int, dp]),

@@ -169,6 +169,15 @@ int ems_femstab_element_matrix(const ems_sim *s, double *K, size_t n)
     });
 }
 
+int ems_tetfem_element_matrices(int order, int type, double *M, double *K, size_t n)
+{
+    return guard(nullptr, [&] {
+        if (order != 2) throw Error{EMS_ERR_UNSUPPORTED, "element matrices are defined for order-2 tetrahedra"};
+        EMS_CHECK_ARG(M != nullptr && K != nullptr && n == 400, "M and K must hold 400 values each");
+        ems::tet2_element_matrices(type, M, K);
+    });
+}
+
 int ems_tetfem_create(const ems_tetfem_params *p, ems_sim **out)
 {
     if (!p) return EMS_ERR_INVALID_ARGUMENT;

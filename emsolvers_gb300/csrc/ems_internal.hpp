@@ -100,6 +100,16 @@ Sim *make_tetbatch(const ems_tetfem_params *p, int nshots, const int *cells);
 void tetbatch_add_dipole(Sim *s, int shot, const double pos[3], const double dir[3], int waveform, double f0, double amp);
 void tetbatch_add_receiver(Sim *s, int shot, const double pos[3]);
 bool is_abm(const Sim *s);
+// second-order tetrahedra (tet2.cu)
+Sim *make_tet2(const ems_tetfem_params *p, const std::vector<std::array<int, 3>> &cells);
+bool is_tet2(const Sim *s);
+void tet2_set_material(Sim *s, const double *eps_r, const double *sigma);
+void tet2_add_dipole(Sim *s, int shot, const double pos[3], const double dir[3], int waveform, double f0, double amp);
+void tet2_add_receiver(Sim *s, int shot, const double pos[3]);
+void tet2_time_step(const Sim *s, double *dt, double *lim);
+void tet2_apply_stiffness(Sim *s, const double *u, double *f, size_t n);
+void tet2_energy(Sim *s, double *out, int n);
+void tet2_element_matrices(int type, double *M, double *K);
 Sim *make_femstab(const ems_femstab_params *p);
 bool is_femstab(const Sim *s);
 void femstab_set_source(Sim *s, int comp, const int ijk[3]);

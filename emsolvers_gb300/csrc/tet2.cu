@@ -1,0 +1,1438 @@
+// Second-order (20-DOF) Nedelec tetrahedra on Kuhn-split cubes, one GPU.
+//
+// The reference's higher-order edge elements are the hexahedral fem_v2
+// family (fem_v2/fem_kernels.hpp:6-8,13-86: per element, gather the DOFs,
+// contract them with the reference matrix of the order, scatter back); its
+// time loops are symplectic_2/fem_simulation.cpp:557-672 (drift, force,
+// kick, drift), symplectic_4/fem_simulation.cpp:1347-1350 (triple jump) and
+// fem_v2/fem_simulation.cpp:627-654 (three-level leapfrog).  This solver
+// runs those loops on the complete second-order Nedelec space of a cube mesh
+// split into six Kuhn tetrahedra:
+//
+//   space        per tetrahedron, with barycentrics l and Whitney functions
+//                w_ij: edge (i,j) tail (l_i - 5/8 (l_k + l_l)) w_ij and head
+//                (l_j - 5/8 (l_k + l_l)) w_ij, face (i,j,k) l_k w_ij and
+//                l_i w_jk (vertices in the global node order).
+//   layout       38 planes per node, DOF = plane * nnode + node (node = the
+//                entity's lowest vertex): 0..6 edge tails, 7..13 edge heads
+//                of the 7 edge directions, 14 + 2 f and 15 + 2 f the two
+//                functions of face type f.  Tetrahedra in type-major order
+//                (p * ncube + cube) so that a warp reads one type's tables.
+//   stiffness    element by element through the curl: the curl of the 20
+//                functions is linear, so the element computes its values at
+//                the four vertices (dyadic coefficients), the P1 mass of
+//                those values and the transposed curl; FP64 arithmetic in
+//                both precisions (the kick of an FP32 run is the one place
+//                where rounding accumulates without bound, in the null space
+//                of K).
+//   mass inverse the drift applies q(M) P, the degree-m Chebyshev polynomial
+//                of the mass preconditioned by its 2 x 2 edge and face
+//                blocks, on the element bounds of the preconditioned
+//                spectrum; one element pass (20 x 20 reference matrix times
+//                eps) and one entity pass (per-DOF gather in a fixed order,
+//                no atomics, the block inverse and the Chebyshev update) per
+//                iteration.
+//   time loop    one CUDA graph per step, replayed; a device step counter
+//                indexes the source table and the receiver samples.
+// Units are normalised (cube edge 1, c0 = 1); the API converts.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <vector>
+
+#include "ems_internal.hpp"
+
+namespace ems {
+
+double tet_wave_value(int kind, double f0, double t);
+double tet_stability_constant(int integrator);
+
+namespace {
+
+constexpr int kEnt = 19;       // entity types per node: 7 edge directions, 12 face types
+constexpr int kPlanes = 38;    // DOF planes per node
+constexpr int kMaxInc = 6;     // tetrahedra around one entity
+constexpr int kPerm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+constexpr int kEdge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+constexpr int kFace[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
+constexpr int kDir[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
+constexpr double kAdmix = -0.625;
+constexpr int kMassIters = 24;
+
+// ------------------------------------------------------- element geometry
+struct Kuhn {
+    double g[4][3];   // gradients of the barycentrics
+    int vert[4][3];   // vertex offsets in the cube
+};
+
+Kuhn kuhn(int p)
+{
+    Kuhn k{};
+    const int a = kPerm[p][0], b = kPerm[p][1], c = kPerm[p][2];
+    k.g[0][a] = -1; k.g[1][a] = 1; k.g[1][b] = -1; k.g[2][b] = 1; k.g[2][c] = -1; k.g[3][c] = 1;
+    k.vert[1][a] = 1; k.vert[2][a] = 1; k.vert[2][b] = 1;
+    k.vert[3][0] = k.vert[3][1] = k.vert[3][2] = 1;
+    return k;
+}
+
+int dir_of(const int d[3])
+{
+    for (int k = 0; k < 7; ++k)
+        if (kDir[k][0] == d[0] && kDir[k][1] == d[1] && kDir[k][2] == d[2]) return k;
+    return -1;
+}
+// face types: ordered pairs (S1, S2) of disjoint non-empty axis sets (bit q =
+// axis q) in the order s1 = 1..7, s2 = 1..7
+int face_type(int s1, int s2)
+{
+    int t = 0;
+    for (int a = 1; a < 8; ++a)
+        for (int b = 1; b < 8; ++b) {
+            if (a & b) continue;
+            if (a == s1 && b == s2) return t;
+            ++t;
+        }
+    return -1;
+}
+int face_axes(int f)   // S1 | S2 of face type f
+{
+    int t = 0;
+    for (int a = 1; a < 8; ++a)
+        for (int b = 1; b < 8; ++b) {
+            if (a & b) continue;
+            if (t++ == f) return a | b;
+        }
+    return 0;
+}
+int bits(const int d[3]) { return (d[0] ? 1 : 0) | (d[1] ? 2 : 0) | (d[2] ? 4 : 0); }
+
+// Function a of type p as (sum_n co[n] l_n) w_ij.
+struct Fun {
+    double co[4];
+    int i, j;
+};
+Fun fun(int a)
+{
+    Fun f{};
+    if (a < 12) {
+        const int l = a % 6;
+        f.i = kEdge[l][0]; f.j = kEdge[l][1];
+        for (int k = 0; k < 4; ++k) f.co[k] = (k == f.i || k == f.j) ? 0.0 : kAdmix;
+        f.co[a < 6 ? f.i : f.j] = 1.0;
+    } else {
+        const int *v = kFace[(a - 12) / 2];
+        if ((a - 12) % 2 == 0) { f.co[v[2]] = 1.0; f.i = v[0]; f.j = v[1]; }
+        else { f.co[v[0]] = 1.0; f.i = v[1]; f.j = v[2]; }
+    }
+    return f;
+}
+
+// plane and lowest local vertex of local DOF a of type p
+void local_dof(int p, int a, int &plane, int &low)
+{
+    const Kuhn k = kuhn(p);
+    if (a < 12) {
+        const int l = a % 6, i = kEdge[l][0], j = kEdge[l][1];
+        const int d[3] = {k.vert[j][0] - k.vert[i][0], k.vert[j][1] - k.vert[i][1], k.vert[j][2] - k.vert[i][2]};
+        plane = dir_of(d) + (a < 6 ? 0 : 7);
+        low = i;
+    } else {
+        const int *v = kFace[(a - 12) / 2];
+        int d1[3], d2[3];
+        for (int q = 0; q < 3; ++q) { d1[q] = k.vert[v[1]][q] - k.vert[v[0]][q]; d2[q] = k.vert[v[2]][q] - k.vert[v[1]][q]; }
+        plane = 14 + 2 * face_type(bits(d1), bits(d2)) + (a - 12) % 2;
+        low = v[0];
+    }
+}
+
+void cross(const double *x, const double *y, double *r)
+{
+    r[0] = x[1] * y[2] - x[2] * y[1];
+    r[1] = x[2] * y[0] - x[0] * y[2];
+    r[2] = x[0] * y[1] - x[1] * y[0];
+}
+
+// The 20 function values at barycentric point lam.
+void values(int p, const double lam[4], double val[20][3])
+{
+    const Kuhn k = kuhn(p);
+    for (int a = 0; a < 20; ++a) {
+        const Fun f = fun(a);
+        double pre = 0.0;
+        for (int n = 0; n < 4; ++n) pre += f.co[n] * lam[n];
+        for (int q = 0; q < 3; ++q) val[a][q] = pre * (lam[f.i] * k.g[f.j][q] - lam[f.j] * k.g[f.i][q]);
+    }
+}
+
+// Curl of function a at the four vertices (the curl is linear):
+// curl((sum co_n l_n) w_ij) = sum_v l_v C_v with
+// C_v = 2 co_v grad l_i x grad l_j + [v = i] G_j - [v = j] G_i,
+// G_m = sum_n co_n grad l_n x grad l_m.
+void curls(int p, double C[20][12])
+{
+    const Kuhn k = kuhn(p);
+    for (int a = 0; a < 20; ++a) {
+        const Fun f = fun(a);
+        double gij[3], Gi[3] = {0, 0, 0}, Gj[3] = {0, 0, 0}, t[3];
+        cross(k.g[f.i], k.g[f.j], gij);
+        for (int n = 0; n < 4; ++n) {
+            cross(k.g[n], k.g[f.j], t);
+            for (int q = 0; q < 3; ++q) Gj[q] += f.co[n] * t[q];
+            cross(k.g[n], k.g[f.i], t);
+            for (int q = 0; q < 3; ++q) Gi[q] += f.co[n] * t[q];
+        }
+        for (int v = 0; v < 4; ++v)
+            for (int q = 0; q < 3; ++q)
+                C[a][3 * v + q] = 2.0 * f.co[v] * gij[q] + (v == f.i ? Gj[q] : 0.0) - (v == f.j ? Gi[q] : 0.0);
+    }
+}
+
+// Element mass (eps = 1) by a collapsed-coordinate Gauss-Legendre rule, 4
+// points per direction (exact for the degree-4 integrands with the
+// collapse Jacobian (1-u)^2 (1-v)); the barycentric integrals of an affine
+// image of the unit tetrahedron are those of the unit tetrahedron (|T| = 1/6).
+void element_mass(int p, double M[400])
+{
+    const double s = std::sqrt(6.0 / 5.0);
+    const double xi[4] = {-std::sqrt(3.0 / 7.0 + 2.0 / 7.0 * s), -std::sqrt(3.0 / 7.0 - 2.0 / 7.0 * s),
+                          std::sqrt(3.0 / 7.0 - 2.0 / 7.0 * s), std::sqrt(3.0 / 7.0 + 2.0 / 7.0 * s)};
+    const double wo = (18.0 - std::sqrt(30.0)) / 36.0, wi = (18.0 + std::sqrt(30.0)) / 36.0;
+    const double wq[4] = {wo, wi, wi, wo};
+    std::fill(M, M + 400, 0.0);
+    for (int iu = 0; iu < 4; ++iu)
+        for (int iv = 0; iv < 4; ++iv)
+            for (int iw = 0; iw < 4; ++iw) {
+                const double u = 0.5 * (1 + xi[iu]), v = 0.5 * (1 + xi[iv]), w = 0.5 * (1 + xi[iw]);
+                const double x = u, y = v * (1 - u), z = w * (1 - u) * (1 - v);
+                const double W = 0.125 * wq[iu] * wq[iv] * wq[iw] * (1 - u) * (1 - u) * (1 - v);
+                const double lam[4] = {1 - x - y - z, x, y, z};
+                double val[20][3];
+                values(p, lam, val);
+                for (int a = 0; a < 20; ++a)
+                    for (int b = 0; b < 20; ++b)
+                        M[20 * a + b] += W * (val[a][0] * val[b][0] + val[a][1] * val[b][1] + val[a][2] * val[b][2]);
+            }
+}
+
+// Element stiffness (mu = 1) from the vertex curls: int l_v l_w = |T| (1 + d_vw) / 20.
+void element_stiffness(int p, double K[400])
+{
+    double C[20][12];
+    curls(p, C);
+    for (int a = 0; a < 20; ++a)
+        for (int b = 0; b < 20; ++b) {
+            double s = 0.0;
+            for (int v = 0; v < 4; ++v)
+                for (int w = 0; w < 4; ++w) {
+                    const double d = C[a][3 * v] * C[b][3 * w] + C[a][3 * v + 1] * C[b][3 * w + 1] + C[a][3 * v + 2] * C[b][3 * w + 2];
+                    s += d * (v == w ? 2.0 : 1.0) / 120.0;
+                }
+            K[20 * a + b] = s;
+        }
+}
+
+// eigenvalues of a symmetric n x n matrix by cyclic Jacobi rotations
+void sym_eigs(int n, std::vector<double> A, std::vector<double> &w)
+{
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0;
+        for (int i = 0; i < n; ++i)
+            for (int j = i + 1; j < n; ++j) off += A[i * n + j] * A[i * n + j];
+        if (off < 1e-30) break;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A[p * n + q];
+                if (std::fabs(apq) < 1e-300) continue;
+                const double th = (A[q * n + q] - A[p * n + p]) / (2.0 * apq);
+                const double t = (th >= 0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; ++k) {
+                    const double akp = A[k * n + p], akq = A[k * n + q];
+                    A[k * n + p] = c * akp - s * akq;
+                    A[k * n + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double apk = A[p * n + k], aqk = A[q * n + k];
+                    A[p * n + k] = c * apk - s * aqk;
+                    A[q * n + k] = s * apk + c * aqk;
+                }
+            }
+    }
+    w.resize(n);
+    for (int i = 0; i < n; ++i) w[i] = A[i * n + i];
+    std::sort(w.begin(), w.end());
+}
+
+// Bounds of the generalised eigenvalues of (M_T, its 2 x 2 entity blocks)
+// over the six types: the spectrum of the block-preconditioned global mass
+// lies inside (assembly of element inequalities), whatever eps.
+void cheb_bounds(const double Mref[6][400], double &lo, double &hi)
+{
+    lo = 1e300; hi = 0.0;
+    for (int p = 0; p < 6; ++p) {
+        const double *M = Mref[p];
+        std::vector<double> Li(400, 0.0), T(400), A(400), w;
+        for (int e = 0; e < 10; ++e) {
+            const int i0 = e < 6 ? e : 12 + 2 * (e - 6), i1 = e < 6 ? e + 6 : 13 + 2 * (e - 6);
+            const double l00 = std::sqrt(M[20 * i0 + i0]), l10 = M[20 * i0 + i1] / l00;
+            const double l11 = std::sqrt(M[20 * i1 + i1] - l10 * l10);
+            Li[20 * i0 + i0] = 1.0 / l00;
+            Li[20 * i1 + i1] = 1.0 / l11;
+            Li[20 * i1 + i0] = -l10 / (l00 * l11);
+        }
+        for (int i = 0; i < 20; ++i)
+            for (int j = 0; j < 20; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 20; ++k) s += Li[20 * i + k] * M[20 * k + j];
+                T[20 * i + j] = s;
+            }
+        for (int i = 0; i < 20; ++i)
+            for (int j = 0; j < 20; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 20; ++k) s += T[20 * i + k] * Li[20 * j + k];
+                A[20 * i + j] = s;
+            }
+        sym_eigs(20, A, w);
+        lo = std::min(lo, w.front());
+        hi = std::max(hi, w.back());
+    }
+}
+
+// Reference data of the element, computed once per process.
+struct Ref {
+    double M[6][400], K[6][400], C[6][20][12];
+    int plane[6][20], low[6][20];
+    double lo, hi;
+    // per entity type: incidences packed p | cube-offset bits << 3 | la << 6 | lb << 11
+    int ninc[kEnt], inc[kEnt][kMaxInc];
+    int axes[kEnt];   // axes the entity spans (bit q)
+    Ref()
+    {
+        for (int p = 0; p < 6; ++p) {
+            element_mass(p, M[p]);
+            element_stiffness(p, K[p]);
+            curls(p, C[p]);
+            for (int a = 0; a < 20; ++a) local_dof(p, a, plane[p][a], low[p][a]);
+        }
+        cheb_bounds(M, lo, hi);
+        for (int e = 0; e < kEnt; ++e) {
+            ninc[e] = 0;
+            axes[e] = e < 7 ? bits(kDir[e]) : face_axes(e - 7);
+        }
+        // ascending type, then ascending cube (descending offset bits)
+        for (int p = 0; p < 6; ++p) {
+            const Kuhn k = kuhn(p);
+            for (int ent = 0; ent < 10; ++ent) {
+                const int la = ent < 6 ? ent : 12 + 2 * (ent - 6), lb = ent < 6 ? ent + 6 : 13 + 2 * (ent - 6);
+                const int pl = plane[p][la], et = pl < 14 ? pl % 7 : 7 + (pl - 14) / 2;
+                const int ob = bits(k.vert[low[p][la]]);
+                inc[et][ninc[et]++] = p | (ob << 3) | (la << 6) | (lb << 11);
+            }
+        }
+        for (int e = 0; e < kEnt; ++e)
+            std::stable_sort(inc[e], inc[e] + ninc[e], [](int x, int y) {
+                const int px = x & 7, py = y & 7, ox = (x >> 3) & 7, oy = (y >> 3) & 7;
+                return px != py ? px < py : ox > oy;
+            });
+    }
+};
+const Ref &ref()
+{
+    static const Ref r;
+    return r;
+}
+
+// ------------------------------------------------------------ device side
+__constant__ int c2_dof[6][20];          // plane | vertex offset bits << 8
+__constant__ double c2_M64[6][400];
+__constant__ float c2_M32[6][400];
+__constant__ double c2_C[6][20][12];
+__constant__ int c2_ninc[kEnt], c2_inc[kEnt][kMaxInc], c2_axes[kEnt];
+
+struct T2Shot {
+    int n[3];
+    int pad;
+    unsigned long long nnode, ncube, dof0, tet0, ent0;
+};
+
+// shot holding flat index i of the per-tetrahedron (which = 0) or
+// per-entity (which = 1) ranges
+__device__ __forceinline__ int shot_of(const T2Shot *__restrict__ sh, int ns, unsigned long long i, int which)
+{
+    int lo = 0, hi = ns - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        const unsigned long long st = which ? sh[mid].ent0 : sh[mid].tet0;
+        if (st <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <class T> __device__ __forceinline__ T mref(int p, int a, int b);
+template <> __device__ __forceinline__ double mref<double>(int p, int a, int b) { return c2_M64[p][20 * a + b]; }
+template <> __device__ __forceinline__ float mref<float>(int p, int a, int b) { return c2_M32[p][20 * a + b]; }
+
+// DOF addressing of flat tetrahedron tl of a shot: DOF a is
+// dof0 + plane * nnode + v0 + the vertex offset of its lowest vertex
+struct TetAddr {
+    int p;
+    unsigned long long v0, nx1, nxy, nnode, dof0;
+    __device__ __forceinline__ unsigned long long dof(int a) const
+    {
+        const int d = c2_dof[p][a], ob = d >> 8;
+        return dof0 + (unsigned long long)(d & 255) * nnode + v0 + (ob & 1) + ((ob >> 1) & 1) * nx1 + ((ob >> 2) & 1) * nxy;
+    }
+};
+__device__ __forceinline__ TetAddr tet_addr(const T2Shot &S, unsigned long long tl)
+{
+    TetAddr ta;
+    ta.p = (int)(tl / S.ncube);
+    const unsigned long long cube = tl - (unsigned long long)ta.p * S.ncube;
+    const unsigned long long i = cube % S.n[0], r = cube / S.n[0];
+    const unsigned long long j = r % S.n[1], k = r / S.n[1];
+    ta.nx1 = S.n[0] + 1;
+    ta.nxy = ta.nx1 * (S.n[1] + 1);
+    ta.v0 = i + ta.nx1 * j + ta.nxy * k;
+    ta.nnode = S.nnode;
+    ta.dof0 = S.dof0;
+    return ta;
+}
+
+// Mass element pass: Yt[a][t] = eps_t (Mref_p x_t)_a.
+template <class T>
+__global__ void __launch_bounds__(128) t2_mass_elem_kernel(unsigned long long NT, const T2Shot *__restrict__ sh, int ns,
+                                                          const T *__restrict__ eps, const T *__restrict__ x, T *__restrict__ Yt)
+{
+    const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (t >= NT) return;
+    const T2Shot S = sh[shot_of(sh, ns, t, 0)];
+    const TetAddr ta = tet_addr(S, t - S.tet0);
+    T xv[20];
+#pragma unroll
+    for (int b = 0; b < 20; ++b) xv[b] = x[ta.dof(b)];
+    const T e = eps[t];
+    const int p = ta.p;
+#pragma unroll
+    for (int a = 0; a < 20; ++a) {
+        T y = T(0);
+#pragma unroll
+        for (int b = 0; b < 20; ++b) y = fma(mref<T>(p, a, b), xv[b], y);
+        Yt[(unsigned long long)a * NT + t] = e * y;
+    }
+}
+
+// Stiffness element pass in FP64: vertex curls c_v = sum_a U_a C_av, the P1
+// mass h_v = (c_v + sum_w c_w) / 120, Yt[a][t] = sum_v C_av . h_v.
+template <class TI>
+__global__ void __launch_bounds__(128) t2_stiff_elem_kernel(unsigned long long NT, const T2Shot *__restrict__ sh, int ns,
+                                                           const TI *__restrict__ U, double *__restrict__ Yt)
+{
+    const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (t >= NT) return;
+    const T2Shot S = sh[shot_of(sh, ns, t, 0)];
+    const TetAddr ta = tet_addr(S, t - S.tet0);
+    const int p = ta.p;
+    double c[12];
+#pragma unroll
+    for (int q = 0; q < 12; ++q) c[q] = 0.0;
+#pragma unroll 2
+    for (int a = 0; a < 20; ++a) {
+        const double u = (double)U[ta.dof(a)];
+#pragma unroll
+        for (int q = 0; q < 12; ++q) c[q] = fma(c2_C[p][a][q], u, c[q]);
+    }
+    double h[12];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const double s = c[q] + c[3 + q] + c[6 + q] + c[9 + q];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) h[3 * v + q] = (c[3 * v + q] + s) * (1.0 / 120.0);
+    }
+#pragma unroll 2
+    for (int a = 0; a < 20; ++a) {
+        double f = 0.0;
+#pragma unroll
+        for (int q = 0; q < 12; ++q) f = fma(c2_C[p][a][q], h[q], f);
+        Yt[(unsigned long long)a * NT + t] = f;
+    }
+}
+
+enum { G_FORCE = 0, G_KICK = 1, G_CHEB0 = 2, G_CHEB = 3 };
+enum { FIN_NONE = 0, FIN_DRIFT = 1, FIN_LEAP = 2 };
+
+template <class T> struct GArgs {
+    const void *Yt;
+    unsigned long long NT;
+    double *P;       // momentum (FP64 in both precisions)
+    T *Pc;           // P in the run precision (FP32 runs), the right-hand side of the solve
+    T *out;          // G_FORCE output
+    const T *b;      // right-hand side of the solve
+    T *x, *d;        // Chebyshev iterate and step
+    const T *pinv;   // 2 x 2 block inverses, three planes over the entities
+    T *U, *Uold;
+    double a;        // kick: P -= a F
+    double h;        // final iteration: U += h x (drift) or U = 2U - Uold - h x (leapfrog)
+    double c0, c1, c2;   // Chebyshev: d = c1 d + c2 z (c0 = 1 / theta for the first step)
+};
+
+// Entity pass: one thread per edge or face of a node (both its DOFs).  Sums
+// the element values of its tetrahedra in the fixed order of c2_inc, then
+// applies the mode's update.  Unused and boundary-tangential entities are
+// held at zero.
+template <class T, class TY, int MODE, int FIN>
+__global__ void __launch_bounds__(128) t2_gather_kernel(unsigned long long NE, const T2Shot *__restrict__ sh, int ns, GArgs<T> g)
+{
+    const unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (e >= NE) return;
+    const T2Shot S = sh[shot_of(sh, ns, e, 1)];
+    const unsigned long long el = e - S.ent0;
+    const int et = (int)(el / S.nnode);
+    const unsigned long long v = el - (unsigned long long)et * S.nnode;
+    const int nx1 = S.n[0] + 1, ny1 = S.n[1] + 1;
+    const int i = (int)(v % nx1), j = (int)((v / nx1) % ny1), k = (int)(v / ((unsigned long long)nx1 * ny1));
+    const int x3[3] = {i, j, k};
+    const int ax = c2_axes[et];
+    bool dead = false;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int in = (ax >> q) & 1;
+        if (x3[q] + in > S.n[q]) dead = true;
+        if (!in && (x3[q] == 0 || x3[q] == S.n[q])) dead = true;
+    }
+    const int pl0 = et < 7 ? et : 14 + 2 * (et - 7), pl1 = et < 7 ? et + 7 : pl0 + 1;
+    const unsigned long long d0 = S.dof0 + (unsigned long long)pl0 * S.nnode + v;
+    const unsigned long long d1 = S.dof0 + (unsigned long long)pl1 * S.nnode + v;
+    TY y0 = TY(0), y1 = TY(0);
+    if (MODE != G_CHEB0 && !dead) {
+        const TY *Y = static_cast<const TY *>(g.Yt);
+        const unsigned long long ncx = S.n[0], ncxy = ncx * S.n[1];
+        for (int q = 0; q < c2_ninc[et]; ++q) {
+            const int w = c2_inc[et][q];
+            const int p = w & 7, ob = (w >> 3) & 7, la = (w >> 6) & 31, lb = (w >> 11) & 31;
+            const int ci = i - (ob & 1), cj = j - ((ob >> 1) & 1), ck = k - ((ob >> 2) & 1);
+            if (ci < 0 || cj < 0 || ck < 0 || ci >= S.n[0] || cj >= S.n[1] || ck >= S.n[2]) continue;
+            const unsigned long long t = S.tet0 + (unsigned long long)p * S.ncube + (unsigned long long)ci + ncx * cj + ncxy * ck;
+            y0 += Y[(unsigned long long)la * g.NT + t];
+            y1 += Y[(unsigned long long)lb * g.NT + t];
+        }
+    }
+    if (MODE == G_FORCE) {
+        g.out[d0] = dead ? T(0) : (T)y0;
+        g.out[d1] = dead ? T(0) : (T)y1;
+        return;
+    }
+    if (MODE == G_KICK) {
+        if (dead) return;
+        const double p0 = g.P[d0] - g.a * (double)y0, p1 = g.P[d1] - g.a * (double)y1;
+        g.P[d0] = p0; g.P[d1] = p1;
+        if (g.Pc) { g.Pc[d0] = (T)p0; g.Pc[d1] = (T)p1; }
+        return;
+    }
+    // Chebyshev: r = b - M x, z = Pinv r, d = c1 d + c2 z (first: d = z / theta), x += d
+    if (dead) {
+        g.x[d0] = T(0); g.x[d1] = T(0); g.d[d0] = T(0); g.d[d1] = T(0);
+        return;
+    }
+    const T r0 = g.b[d0] - (T)y0, r1 = g.b[d1] - (T)y1;
+    const T q00 = g.pinv[e], q01 = g.pinv[NE + e], q11 = g.pinv[2 * NE + e];
+    const T z0 = fma(q00, r0, q01 * r1), z1 = fma(q01, r0, q11 * r1);
+    T n0, n1, x0, x1;
+    if (MODE == G_CHEB0) {
+        n0 = (T)g.c0 * z0; n1 = (T)g.c0 * z1;
+        x0 = n0; x1 = n1;
+    } else {
+        n0 = fma((T)g.c1, g.d[d0], (T)g.c2 * z0);
+        n1 = fma((T)g.c1, g.d[d1], (T)g.c2 * z1);
+        x0 = g.x[d0] + n0; x1 = g.x[d1] + n1;
+    }
+    g.d[d0] = n0; g.d[d1] = n1;
+    g.x[d0] = x0; g.x[d1] = x1;
+    if (FIN == FIN_DRIFT) {
+        g.U[d0] = fma((T)g.h, x0, g.U[d0]);
+        g.U[d1] = fma((T)g.h, x1, g.U[d1]);
+    } else if (FIN == FIN_LEAP) {
+        const T u0 = g.U[d0], u1 = g.U[d1];
+        g.U[d0] = fma(-(T)g.h, x0, T(2) * u0 - g.Uold[d0]);
+        g.U[d1] = fma(-(T)g.h, x1, T(2) * u1 - g.Uold[d1]);
+        g.Uold[d0] = u0; g.Uold[d1] = u1;
+    }
+}
+
+// 2 x 2 block inverse per entity from the assembled eps-weighted mass (FP64).
+__global__ void __launch_bounds__(128) t2_pinv_kernel(unsigned long long NE, const T2Shot *__restrict__ sh, int ns,
+                                                      const double *__restrict__ eps, double *__restrict__ out)
+{
+    const unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (e >= NE) return;
+    const T2Shot S = sh[shot_of(sh, ns, e, 1)];
+    const unsigned long long el = e - S.ent0;
+    const int et = (int)(el / S.nnode);
+    const unsigned long long v = el - (unsigned long long)et * S.nnode;
+    const int nx1 = S.n[0] + 1, ny1 = S.n[1] + 1;
+    const int i = (int)(v % nx1), j = (int)((v / nx1) % ny1), k = (int)(v / ((unsigned long long)nx1 * ny1));
+    double a = 0.0, b = 0.0, c = 0.0;
+    const unsigned long long ncx = S.n[0], ncxy = ncx * S.n[1];
+    for (int q = 0; q < c2_ninc[et]; ++q) {
+        const int w = c2_inc[et][q];
+        const int p = w & 7, ob = (w >> 3) & 7, la = (w >> 6) & 31, lb = (w >> 11) & 31;
+        const int ci = i - (ob & 1), cj = j - ((ob >> 1) & 1), ck = k - ((ob >> 2) & 1);
+        if (ci < 0 || cj < 0 || ck < 0 || ci >= S.n[0] || cj >= S.n[1] || ck >= S.n[2]) continue;
+        const double ep = eps[S.tet0 + (unsigned long long)p * S.ncube + (unsigned long long)ci + ncx * cj + ncxy * ck];
+        a += ep * c2_M64[p][21 * la];
+        b += ep * c2_M64[p][20 * la + lb];
+        c += ep * c2_M64[p][21 * lb];
+    }
+    const double det = a * c - b * b;
+    const bool ok = a > 0.0 && det > 0.0;
+    out[e] = ok ? c / det : 0.0;
+    out[NE + e] = ok ? -b / det : 0.0;
+    out[2 * NE + e] = ok ? a / det : 0.0;
+}
+
+template <class T> __global__ void t2_narrow_kernel(unsigned long long n, const double *__restrict__ x, T *__restrict__ y)
+{
+    const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i < n) y[i] = (T)x[i];
+}
+
+template <class T> __global__ void t2_axpy_kernel(unsigned long long n, T *__restrict__ U, const T *__restrict__ x, double h)
+{
+    const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i < n) U[i] = fma((T)h, x[i], U[i]);
+}
+
+// Dipole loads, one thread per loaded DOF (its entries in dipole order):
+// symplectic P += s sum_k coef_k g_k (and the run-precision copy), leapfrog
+// b -= sum_k coef_k g_k.
+template <class T, int LEAP>
+__global__ void t2_source_kernel(int n, const unsigned long long *__restrict__ dof, const int *__restrict__ ptr,
+                                 const int *__restrict__ dip, const double *__restrict__ coef, const double *__restrict__ gt,
+                                 const int *__restrict__ ctl, int nsub, int q, int nd, double s, double *__restrict__ P,
+                                 T *__restrict__ vec)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double *g = gt + ((size_t)ctl[0] * nsub + q) * nd;
+    double f = 0.0;
+    for (int j = ptr[k]; j < ptr[k + 1]; ++j) f += coef[j] * g[dip[j]];
+    const unsigned long long e = dof[k];
+    if (LEAP) {
+        vec[e] = (T)((double)vec[e] - f);
+    } else {
+        const double p = P[e] + s * f;
+        P[e] = p;
+        if (vec) vec[e] = (T)p;
+    }
+}
+
+// Receivers: one warp each; lane a < 20 forms its function's terms, a fixed
+// shuffle tree sums them.
+template <class T>
+__global__ void t2_sample_kernel(int nrec, const unsigned long long *__restrict__ rdof, const double *__restrict__ rw,
+                                 const T *__restrict__ U, const int *__restrict__ ctl, int tf, int nsamp, double *__restrict__ tr)
+{
+    const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), l = threadIdx.x & 31;
+    const int step = ctl[0];
+    if (r >= nrec || step % tf != 0 || step / tf >= nsamp) return;
+    double c[3] = {0.0, 0.0, 0.0};
+    if (l < 20) {
+        const double u = (double)U[rdof[20 * r + l]];
+        for (int q = 0; q < 3; ++q) c[q] = u * rw[60 * r + 3 * l + q];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        for (int q = 0; q < 3; ++q) c[q] += __shfl_down_sync(0xffffffffu, c[q], o);
+    if (l == 0) {
+        double *o = tr + ((size_t)r * nsamp + step / tf) * 4;
+        o[1] = c[0]; o[2] = c[1]; o[3] = c[2];
+    }
+}
+
+__global__ void t2_advance_kernel(int *ctl) { ctl[0] += 1; }
+
+// Block partial sums of x . y (fixed grid, fixed order); the host adds them.
+template <class T>
+__global__ void __launch_bounds__(256) t2_dot_kernel(unsigned long long n, const T *__restrict__ x, const T *__restrict__ y,
+                                                    double *__restrict__ part)
+{
+    __shared__ double sm[256];
+    double s = 0.0;
+    for (unsigned long long i = blockIdx.x * 256ull + threadIdx.x; i < n; i += 256ull * gridDim.x) s += (double)x[i] * (double)y[i];
+    sm[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sm[0];
+}
+
+template <class T> __global__ void t2_scale_kernel(unsigned long long n, T *__restrict__ x, double s)
+{
+    const unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (i < n) x[i] = (T)((double)x[i] * s);
+}
+
+constexpr int kDotBlocks = 512;
+
+unsigned blocks(unsigned long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+}  // namespace
+
+// ---------------------------------------------------------------- host side
+struct Tet2Sim : Sim {
+    struct ShotH {
+        int n[3];
+        size_t nnode, ncube, dof0, tet0, ent0;
+    };
+    struct Dip {
+        size_t dof[20];
+        double coef[20];
+        int kind;
+        double f0n;
+    };
+    ems_tetfem_params P;
+    std::vector<ShotH> shots;
+    size_t ndof = 0, ntet = 0, nent = 0;
+    bool fp64 = false, ready = false, y_valid = false;
+    double c0 = 299792458.0, tscale = 1.0, dtn = 0.0, dt_lim_n = 0.0, lambda_max = 0.0, cur_time = 0.0;
+    int mass_iters = kMassIters;
+    std::vector<double> eps_h;   // API order per shot: 6 * cell + p
+    std::vector<Dip> dips;
+    std::vector<std::array<size_t, 20>> rec_dof;
+    std::vector<std::array<double, 60>> rec_w;
+    DevBuf d_shots, d_eps, d_pinv, d_U, d_Uold, d_P, d_Pc, d_x, d_d, d_b, d_YtM, d_YtK, d_ctl, d_part;
+    DevBuf d_src_dof, d_src_ptr, d_src_dip, d_src_coef, d_src_g, d_rec_dof, d_rec_w, d_tr;
+    std::vector<double> cheb_c1, cheb_c2;
+    double cheb_c0 = 0.0;
+
+    Tet2Sim(const ems_tetfem_params *p, const std::vector<std::array<int, 3>> &cells) : Sim(Kind::TETFEM), P(*p)
+    {
+        EMS_CHECK_ARG(!cells.empty(), "at least one shot");
+        size_t n0 = 0, t0 = 0, e0 = 0;
+        for (auto &c : cells) {
+            EMS_CHECK_ARG(c[0] > 0 && c[1] > 0 && c[2] > 0, "cell counts must be positive");
+            ShotH s{};
+            s.n[0] = c[0]; s.n[1] = c[1]; s.n[2] = c[2];
+            s.nnode = (size_t)(c[0] + 1) * (c[1] + 1) * (c[2] + 1);
+            s.ncube = (size_t)c[0] * c[1] * c[2];
+            s.dof0 = n0; s.tet0 = t0; s.ent0 = e0;
+            n0 += kPlanes * s.nnode;
+            t0 += 6 * s.ncube;
+            e0 += kEnt * s.nnode;
+            shots.push_back(s);
+        }
+        EMS_CHECK_ARG(P.h > 0, "h must be positive");
+        EMS_CHECK_ARG(P.integrator == EMS_LEAPFROG || P.integrator == EMS_SYMP2 || P.integrator == EMS_SYMP4,
+                      "tetrahedral integrator must be EMS_LEAPFROG, EMS_SYMP2 or EMS_SYMP4");
+        EMS_CHECK_ARG(P.precision == EMS_FP64 || P.precision == EMS_FP32, "precision must be EMS_FP64 or EMS_FP32");
+        EMS_CHECK_ARG(P.dt >= 0 && P.time_frequency > 0, "dt must be >= 0 and time_frequency > 0");
+        if (P.cfl_fraction <= 0) P.cfl_fraction = 0.9;
+        EMS_CHECK_ARG(P.cfl_fraction < 1.0, "cfl_fraction must be below 1");
+        fp64 = P.precision == EMS_FP64;
+        tscale = P.h / c0;
+        ndof = n0; ntet = t0; nent = e0;
+        EMS_CHECK_ARG(ndof < (size_t)1 << 40, "mesh too large");
+        eps_h.assign(ntet, 1.0);
+        init_stream();
+        upload_tables();
+        std::vector<T2Shot> sh(shots.size());
+        for (size_t s = 0; s < shots.size(); ++s) {
+            for (int q = 0; q < 3; ++q) sh[s].n[q] = shots[s].n[q];
+            sh[s].nnode = shots[s].nnode; sh[s].ncube = shots[s].ncube;
+            sh[s].dof0 = shots[s].dof0; sh[s].tet0 = shots[s].tet0; sh[s].ent0 = shots[s].ent0;
+        }
+        d_shots.alloc(sh.size() * sizeof(T2Shot));
+        EMS_CUDA(cudaMemcpy(d_shots.p, sh.data(), sh.size() * sizeof(T2Shot), cudaMemcpyHostToDevice));
+        const size_t w = fp64 ? 8 : 4;
+        d_U.alloc(ndof * w); d_Uold.alloc(ndof * w); d_P.alloc(ndof * 8);
+        d_x.alloc(ndof * w); d_d.alloc(ndof * w); d_b.alloc(ndof * w);
+        if (!fp64) d_Pc.alloc(ndof * 4);
+        d_YtM.alloc(20 * ntet * w);
+        d_YtK.alloc(20 * ntet * 8);
+        d_ctl.alloc(16);
+        d_part.alloc(kDotBlocks * 8);
+        reset();
+    }
+
+    static void upload_tables()
+    {
+        const Ref &R = ref();
+        int dof[6][20];
+        float m32[6][400];
+        for (int p = 0; p < 6; ++p) {
+            const Kuhn k = kuhn(p);
+            for (int a = 0; a < 20; ++a) dof[p][a] = R.plane[p][a] | (bits(k.vert[R.low[p][a]]) << 8);
+            for (int q = 0; q < 400; ++q) m32[p][q] = (float)R.M[p][q];
+        }
+        EMS_CUDA(cudaMemcpyToSymbol(c2_dof, dof, sizeof(dof)));
+        EMS_CUDA(cudaMemcpyToSymbol(c2_M64, R.M, sizeof(R.M)));
+        EMS_CUDA(cudaMemcpyToSymbol(c2_M32, m32, sizeof(m32)));
+        EMS_CUDA(cudaMemcpyToSymbol(c2_C, R.C, sizeof(R.C)));
+        EMS_CUDA(cudaMemcpyToSymbol(c2_ninc, R.ninc, sizeof(R.ninc)));
+        EMS_CUDA(cudaMemcpyToSymbol(c2_inc, R.inc, sizeof(R.inc)));
+        EMS_CUDA(cudaMemcpyToSymbol(c2_axes, R.axes, sizeof(R.axes)));
+    }
+
+    // API position (6 * cell + p within a shot) -> type-major device order
+    size_t tet_index(size_t api) const
+    {
+        size_t s = shots.size() - 1;
+        while (shots[s].tet0 > api) --s;
+        const size_t l = api - shots[s].tet0, cell = l / 6, p = l % 6;
+        return shots[s].tet0 + p * shots[s].ncube + cell;
+    }
+    // API DOF (38 * node + plane within a shot) -> device plane layout
+    size_t dof_index(size_t api) const
+    {
+        size_t s = shots.size() - 1;
+        while (shots[s].dof0 > api) --s;
+        const size_t l = api - shots[s].dof0, node = l / kPlanes, pl = l % kPlanes;
+        return shots[s].dof0 + pl * shots[s].nnode + node;
+    }
+
+    void set_material(const double *eps_r, const double *sigma)
+    {
+        EMS_CHECK_ARG(eps_r != nullptr, "eps_r required");
+        for (size_t t = 0; t < ntet; ++t) EMS_CHECK_ARG(eps_r[t] > 0 && std::isfinite(eps_r[t]), "eps_r must be positive");
+        if (sigma)
+            for (size_t t = 0; t < ntet; ++t)
+                if (sigma[t] != 0.0) throw Error{EMS_ERR_UNSUPPORTED, "conductivity is implemented for order-1 tetrahedra only"};
+        eps_h.assign(eps_r, eps_r + ntet);
+        ready = false;
+        y_valid = false;
+    }
+
+    template <class T> void launch_pinv_and_eps()
+    {
+        std::vector<double> e(ntet);
+        for (size_t t = 0; t < ntet; ++t) e[tet_index(t)] = eps_h[t];
+        DevBuf e64, p64;
+        e64.alloc(ntet * 8);
+        p64.alloc(3 * nent * 8);
+        EMS_CUDA(cudaMemcpy(e64.p, e.data(), ntet * 8, cudaMemcpyHostToDevice));
+        t2_pinv_kernel<<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), (int)shots.size(), e64.as<double>(),
+                                                              p64.as<double>());
+        d_eps.ensure(ntet * sizeof(T));
+        d_pinv.ensure(3 * nent * sizeof(T));
+        t2_narrow_kernel<T><<<blocks(ntet, 256), 256, 0, stream>>>(ntet, e64.as<double>(), d_eps.as<T>());
+        t2_narrow_kernel<T><<<blocks(3 * nent, 256), 256, 0, stream>>>(3 * nent, p64.as<double>(), d_pinv.as<T>());
+        EMS_CUDA(cudaGetLastError());
+        EMS_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    void cheb_coefficients()
+    {
+        const Ref &R = ref();
+        const double th = 0.5 * (R.hi + R.lo), de = 0.5 * (R.hi - R.lo), sg = th / de;
+        double rho = 1.0 / sg;
+        cheb_c0 = 1.0 / th;
+        cheb_c1.assign(mass_iters, 0.0);
+        cheb_c2.assign(mass_iters, 0.0);
+        for (int k = 1; k < mass_iters; ++k) {
+            const double rn = 1.0 / (2.0 * sg - rho);
+            cheb_c1[k] = rn * rho;
+            cheb_c2[k] = 2.0 * rn / de;
+            rho = rn;
+        }
+    }
+
+    template <class T> GArgs<T> gargs() const
+    {
+        GArgs<T> g{};
+        g.NT = ntet;
+        g.P = d_P.as<double>();
+        g.Pc = fp64 ? nullptr : reinterpret_cast<T *>(d_Pc.p);
+        g.pinv = d_pinv.as<T>();
+        g.x = d_x.as<T>(); g.d = d_d.as<T>();
+        g.U = d_U.as<T>(); g.Uold = d_Uold.as<T>();
+        return g;
+    }
+    template <class T> const T *rhs_P() const { return fp64 ? reinterpret_cast<const T *>(d_P.p) : reinterpret_cast<const T *>(d_Pc.p); }
+
+    // f = K u (element pass + entity pass), u and out device vectors
+    template <class T> int enqueue_force(const T *u, T *out)
+    {
+        t2_stiff_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), (int)shots.size(), u,
+                                                                       d_YtK.as<double>());
+        GArgs<T> g = gargs<T>();
+        g.Yt = d_YtK.p;
+        g.out = out;
+        t2_gather_kernel<T, double, G_FORCE, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(),
+                                                                                             (int)shots.size(), g);
+        return 2;
+    }
+
+    // x = q(M) b; the last iteration applies FIN with factor h
+    template <class T, int FIN> int enqueue_solve(const T *b, double h)
+    {
+        const int ns = (int)shots.size();
+        GArgs<T> g = gargs<T>();
+        g.b = b;
+        g.c0 = cheb_c0;
+        g.h = h;
+        g.Yt = d_YtM.p;
+        int nl = 0;
+        if (mass_iters == 1) {
+            t2_gather_kernel<T, T, G_CHEB0, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+            return 1;
+        }
+        t2_gather_kernel<T, T, G_CHEB0, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+        ++nl;
+        for (int k = 1; k < mass_iters; ++k) {
+            t2_mass_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_eps.as<T>(),
+                                                                          d_x.as<T>(), d_YtM.as<T>());
+            g.c1 = cheb_c1[k];
+            g.c2 = cheb_c2[k];
+            if (k + 1 == mass_iters)
+                t2_gather_kernel<T, T, G_CHEB, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+            else
+                t2_gather_kernel<T, T, G_CHEB, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+            nl += 2;
+        }
+        return nl;
+    }
+
+    double dot_host(const void *x, const void *y)
+    {
+        if (fp64) t2_dot_kernel<double><<<kDotBlocks, 256, 0, stream>>>(ndof, (const double *)x, (const double *)y, d_part.as<double>());
+        else t2_dot_kernel<float><<<kDotBlocks, 256, 0, stream>>>(ndof, (const float *)x, (const float *)y, d_part.as<double>());
+        std::vector<double> part(kDotBlocks);
+        EMS_CUDA(cudaMemcpyAsync(part.data(), d_part.p, kDotBlocks * 8, cudaMemcpyDeviceToHost, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        double s = 0.0;
+        for (double v : part) s += v;
+        return s;
+    }
+
+    // largest eigenvalue of q(M) K by power iteration with the Rayleigh
+    // quotient x.Kx / x.q(M)^-1 x (x = q(M) p)
+    template <class T> double lambda_max_t(int iters)
+    {
+        std::vector<T> x0(ndof, T(0));
+        std::vector<unsigned char> live(ndof, 0);
+        unsigned long long st = 0x9E3779B97F4A7C15ull;
+        for (size_t e = 0; e < ndof; ++e) {
+            st ^= st << 13; st ^= st >> 7; st ^= st << 17;
+            x0[e] = (T)((double)(st >> 11) / 9007199254740992.0 - 0.5);
+        }
+        // zero the dead DOFs by one force pass on the start vector's shape: the
+        // entity pass writes zeros there; the solve keeps them at zero
+        EMS_CUDA(cudaMemcpy(d_x.p, x0.data(), ndof * sizeof(T), cudaMemcpyHostToDevice));
+        T *x = d_x.as<T>(), *pb = d_b.as<T>(), *z = d_Uold.as<T>();
+        enqueue_force<T>(x, pb);                    // p = K x0
+        enqueue_solve<T, FIN_NONE>(pb, 0.0);        // x = q(M) p
+        double lam = 0.0;
+        for (int it = 0; it < iters; ++it) {
+            enqueue_force<T>(x, z);
+            const double num = dot_host(x, z), den = dot_host(x, pb);
+            lam = num / den;
+            EMS_CUDA(cudaMemcpyAsync(pb, z, ndof * sizeof(T), cudaMemcpyDeviceToDevice, stream));
+            enqueue_solve<T, FIN_NONE>(pb, 0.0);
+            const double nrm = 1.0 / std::sqrt(dot_host(x, x));
+            t2_scale_kernel<T><<<blocks(ndof, 256), 256, 0, stream>>>(ndof, x, nrm);
+            t2_scale_kernel<T><<<blocks(ndof, 256), 256, 0, stream>>>(ndof, pb, nrm);
+        }
+        EMS_CUDA(cudaGetLastError());
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        return lam;
+    }
+
+    void setup()
+    {
+        cheb_coefficients();
+        if (fp64) launch_pinv_and_eps<double>(); else launch_pinv_and_eps<float>();
+        // the power iteration uses the solver's scratch; the state (U, Uold, P) is kept
+        DevBuf keep;
+        keep.alloc(ndof * (fp64 ? 8 : 4));
+        EMS_CUDA(cudaMemcpy(keep.p, d_Uold.p, keep.bytes, cudaMemcpyDeviceToDevice));
+        lambda_max = fp64 ? lambda_max_t<double>(100) : lambda_max_t<float>(100);
+        EMS_CUDA(cudaMemcpy(d_Uold.p, keep.p, keep.bytes, cudaMemcpyDeviceToDevice));
+        dt_lim_n = tet_stability_constant(P.integrator) / std::sqrt(lambda_max);
+        dtn = P.dt > 0 ? P.dt / tscale : P.cfl_fraction * dt_lim_n;
+        ready = true;
+        y_valid = false;
+    }
+
+    void locate(const ShotH &S, const double x[3], double val[20][3], size_t dofs[20]) const
+    {
+        int cell[3];
+        double s[3];
+        for (int q = 0; q < 3; ++q) {
+            int c = (int)std::floor(x[q]);
+            c = std::max(0, std::min(c, S.n[q] - 1));
+            cell[q] = c;
+            s[q] = x[q] - c;
+        }
+        int ax[3] = {0, 1, 2};   // axes by decreasing fractional coordinate (stable)
+        for (int a = 1; a < 3; ++a)
+            for (int b = a; b > 0 && s[ax[b - 1]] < s[ax[b]]; --b) std::swap(ax[b], ax[b - 1]);
+        int p = 0;
+        while (!(kPerm[p][0] == ax[0] && kPerm[p][1] == ax[1] && kPerm[p][2] == ax[2])) ++p;
+        const double lam[4] = {1.0 - s[ax[0]], s[ax[0]] - s[ax[1]], s[ax[1]] - s[ax[2]], s[ax[2]]};
+        values(p, lam, val);
+        const Kuhn k = kuhn(p);
+        const Ref &R = ref();
+        for (int a = 0; a < 20; ++a) {
+            const int *vo = k.vert[R.low[p][a]];
+            const size_t node = (size_t)(cell[0] + vo[0]) +
+                                (size_t)(S.n[0] + 1) * ((size_t)(cell[1] + vo[1]) + (size_t)(S.n[1] + 1) * (cell[2] + vo[2]));
+            dofs[a] = S.dof0 + (size_t)R.plane[p][a] * S.nnode + node;
+        }
+    }
+
+    bool dead_dof(size_t dof) const
+    {
+        size_t s = shots.size() - 1;
+        while (shots[s].dof0 > dof) --s;
+        const ShotH &S = shots[s];
+        const size_t l = dof - S.dof0, pl = l / S.nnode, v = l % S.nnode;
+        const int et = pl < 14 ? (int)(pl % 7) : 7 + (int)(pl - 14) / 2;
+        const int x3[3] = {(int)(v % (S.n[0] + 1)), (int)((v / (S.n[0] + 1)) % (S.n[1] + 1)),
+                           (int)(v / ((size_t)(S.n[0] + 1) * (S.n[1] + 1)))};
+        const int ax = ref().axes[et];
+        for (int q = 0; q < 3; ++q) {
+            const int in = (ax >> q) & 1;
+            if (x3[q] + in > S.n[q]) return true;
+            if (!in && (x3[q] == 0 || x3[q] == S.n[q])) return true;
+        }
+        return false;
+    }
+
+    void add_dipole(int shot, const double pos[3], const double dir[3], int waveform, double f0, double amp)
+    {
+        EMS_CHECK_ARG(shot >= 0 && shot < (int)shots.size(), "shot index out of range");
+        EMS_CHECK_ARG(pos && dir, "position and direction required");
+        EMS_CHECK_ARG(waveform == EMS_WAVE_REFERENCE || waveform == EMS_WAVE_RICKER, "unknown waveform");
+        EMS_CHECK_ARG(f0 > 0 && std::isfinite(amp), "f0 must be positive");
+        const ShotH &S = shots[shot];
+        const double xn[3] = {pos[0] / P.h, pos[1] / P.h, pos[2] / P.h};
+        for (int q = 0; q < 3; ++q) EMS_CHECK_ARG(xn[q] >= 0 && xn[q] <= S.n[q], "dipole outside the domain");
+        EMS_CHECK_ARG(dips.size() < 4096, "at most 4096 dipoles");
+        double val[20][3];
+        Dip d{};
+        locate(S, xn, val, d.dof);
+        for (int a = 0; a < 20; ++a)
+            d.coef[a] = dead_dof(d.dof[a]) ? 0.0 : (val[a][0] * dir[0] + val[a][1] * dir[1] + val[a][2] * dir[2]) * amp;
+        d.kind = waveform;
+        d.f0n = f0 * tscale;
+        dips.push_back(d);
+    }
+
+    void add_receiver(int shot, const double pos[3])
+    {
+        EMS_CHECK_ARG(pos != nullptr, "position required");
+        EMS_CHECK_ARG(shot >= 0 && shot < (int)shots.size(), "shot index out of range");
+        const ShotH &S = shots[shot];
+        const double xn[3] = {pos[0] / P.h, pos[1] / P.h, pos[2] / P.h};
+        for (int q = 0; q < 3; ++q) EMS_CHECK_ARG(xn[q] >= 0 && xn[q] <= S.n[q], "receiver outside the domain");
+        double val[20][3];
+        std::array<size_t, 20> d;
+        locate(S, xn, val, d.data());
+        std::array<double, 60> w;
+        for (int a = 0; a < 20; ++a)
+            for (int q = 0; q < 3; ++q) w[3 * a + q] = val[a][q];
+        rec_dof.push_back(d);
+        rec_w.push_back(w);
+    }
+
+    template <class V> void up(DevBuf &b, const std::vector<V> &v)
+    {
+        b.ensure(std::max<size_t>(v.size(), 1) * sizeof(V));
+        if (!v.empty()) EMS_CUDA(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, stream));
+    }
+
+    bool symp() const { return P.integrator != EMS_LEAPFROG; }
+    int nsub() const { return P.integrator == EMS_SYMP4 ? 3 : 1; }
+    void substeps(double sub[3], double off[3]) const
+    {
+        const double x1 = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0)), x2 = 1.0 - 2.0 * x1;
+        sub[0] = dtn; sub[1] = sub[2] = 0.0;
+        off[0] = off[1] = off[2] = 0.0;
+        if (P.integrator == EMS_SYMP4) {
+            sub[0] = x1 * dtn; sub[1] = x2 * dtn; sub[2] = x1 * dtn;
+            off[1] = x1 * dtn; off[2] = (x1 + x2) * dtn;
+        }
+    }
+
+    int nsrc = 0;
+    // source table (entries sorted by DOF, in dipole order per DOF), the wave
+    // values of every step and substep, receivers and the step counter
+    void prepare_run(int nsteps, std::vector<double> &times)
+    {
+        const int tf = P.time_frequency;
+        nobs = (int)rec_dof.size();
+        nsamp = nsteps > 0 ? (nsteps - 1) / tf + 1 : 0;
+        ncols = 4;
+        std::vector<unsigned long long> rd;
+        std::vector<double> rw;
+        for (int r = 0; r < nobs; ++r) {
+            for (int a = 0; a < 20; ++a) rd.push_back(rec_dof[r][a]);
+            rw.insert(rw.end(), rec_w[r].begin(), rec_w[r].end());
+        }
+        up(d_rec_dof, rd);
+        up(d_rec_w, rw);
+        const size_t ntr = (size_t)std::max(nobs, 1) * std::max(nsamp, 1) * 4;
+        d_tr.ensure(ntr * 8);
+        d_tr.zero(stream);
+        std::vector<std::array<size_t, 2>> ent;   // (dof, dipole * 20 + a)
+        for (size_t k = 0; k < dips.size(); ++k)
+            for (int a = 0; a < 20; ++a)
+                if (dips[k].coef[a] != 0.0) ent.push_back({dips[k].dof[a], 20 * k + a});
+        std::stable_sort(ent.begin(), ent.end(), [](const std::array<size_t, 2> &x, const std::array<size_t, 2> &y) { return x[0] < y[0]; });
+        std::vector<unsigned long long> sd;
+        std::vector<int> sp, sdip;
+        std::vector<double> sc;
+        for (size_t q = 0; q < ent.size(); ++q) {
+            if (q == 0 || ent[q][0] != ent[q - 1][0]) { sd.push_back(ent[q][0]); sp.push_back((int)q); }
+            sdip.push_back((int)(ent[q][1] / 20));
+            sc.push_back(dips[ent[q][1] / 20].coef[ent[q][1] % 20]);
+        }
+        sp.push_back((int)ent.size());
+        nsrc = (int)sd.size();
+        up(d_src_dof, sd);
+        up(d_src_ptr, sp);
+        up(d_src_dip, sdip);
+        up(d_src_coef, sc);
+        const size_t nd = std::max<size_t>(dips.size(), 1);
+        const int ns = nsub();
+        double sub[3], off[3];
+        substeps(sub, off);
+        std::vector<double> gv((size_t)std::max(nsteps, 1) * ns * nd, 0.0);
+        times.assign(std::max(nsamp, 1), 0.0);
+        double t = cur_time;
+        for (int st = 0; st < nsteps; ++st) {
+            for (int q = 0; q < ns; ++q)
+                for (size_t k = 0; k < dips.size(); ++k)
+                    gv[((size_t)st * ns + q) * nd + k] = tet_wave_value(dips[k].kind, dips[k].f0n, symp() ? t + off[q] + 0.5 * sub[q] : t);
+            if (st % tf == 0) times[st / tf] = t;
+            t += dtn;
+        }
+        up(d_src_g, gv);
+        EMS_CUDA(cudaMemsetAsync(d_ctl.p, 0, 16, stream));
+    }
+
+    template <class T> int enqueue_step()
+    {
+        const int ns = (int)shots.size();
+        int nl = 0;
+        const int nd = (int)std::max<size_t>(dips.size(), 1);
+        if (nobs > 0) {
+            t2_sample_kernel<T><<<blocks((unsigned long long)nobs * 32, 128), 128, 0, stream>>>(
+                nobs, d_rec_dof.as<unsigned long long>(), d_rec_w.as<double>(), d_U.as<T>(), d_ctl.as<int>(), P.time_frequency,
+                nsamp, d_tr.as<double>());
+            ++nl;
+        }
+        if (symp()) {
+            double sub[3], off[3];
+            substeps(sub, off);
+            const int nq = nsub();
+            t2_axpy_kernel<T><<<blocks(ndof, 256), 256, 0, stream>>>(ndof, d_U.as<T>(), d_x.as<T>(), 0.5 * sub[0]);
+            ++nl;
+            for (int q = 0; q < nq; ++q) {
+                t2_stiff_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_U.as<T>(),
+                                                                               d_YtK.as<double>());
+                GArgs<T> g = gargs<T>();
+                g.Yt = d_YtK.p;
+                g.a = sub[q];
+                t2_gather_kernel<T, double, G_KICK, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+                nl += 2;
+                if (nsrc > 0) {
+                    t2_source_kernel<T, 0><<<blocks(nsrc, 128), 128, 0, stream>>>(
+                        nsrc, d_src_dof.as<unsigned long long>(), d_src_ptr.as<int>(), d_src_dip.as<int>(), d_src_coef.as<double>(),
+                        d_src_g.as<double>(), d_ctl.as<int>(), nq, q, nd, sub[q], d_P.as<double>(), fp64 ? nullptr : d_Pc.as<T>());
+                    ++nl;
+                }
+                const double h = 0.5 * sub[q] + (q + 1 < nq ? 0.5 * sub[q + 1] : 0.0);
+                nl += enqueue_solve<T, FIN_DRIFT>(rhs_P<T>(), h);
+            }
+        } else {
+            nl += enqueue_force<T>(d_U.as<T>(), d_b.as<T>());
+            if (nsrc > 0) {
+                t2_source_kernel<T, 1><<<blocks(nsrc, 128), 128, 0, stream>>>(
+                    nsrc, d_src_dof.as<unsigned long long>(), d_src_ptr.as<int>(), d_src_dip.as<int>(), d_src_coef.as<double>(),
+                    d_src_g.as<double>(), d_ctl.as<int>(), 1, 0, nd, 1.0, nullptr, d_b.as<T>());
+                ++nl;
+            }
+            nl += enqueue_solve<T, FIN_LEAP>(d_b.as<T>(), dtn * dtn);
+        }
+        t2_advance_kernel<<<1, 1, 0, stream>>>(d_ctl.as<int>());
+        return nl + 1;
+    }
+
+    template <class T> void run_t(int nsteps)
+    {
+        if (!ready) setup();
+        std::vector<double> times;
+        prepare_run(nsteps, times);
+        long long launches = 0;
+        if (symp() && !y_valid && nsteps > 0) {   // Y = q(M) P of the current state
+            launches += enqueue_solve<T, FIN_NONE>(rhs_P<T>(), 0.0);
+            y_valid = true;
+        }
+        EMS_CUDA(cudaGetLastError());
+        EMS_CUDA(cudaEventRecord(ev0, stream));
+        if (nsteps > 0) {
+            struct Graph {
+                cudaGraph_t g = nullptr;
+                cudaGraphExec_t exec = nullptr;
+                ~Graph()
+                {
+                    if (exec) cudaGraphExecDestroy(exec);
+                    if (g) cudaGraphDestroy(g);
+                }
+            } G;
+            EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            const int per = enqueue_step<T>();
+            cudaError_t ce = cudaStreamEndCapture(stream, &G.g);
+            if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
+            EMS_CUDA(cudaGraphInstantiate(&G.exec, G.g, 0));
+            for (int st = 0; st < nsteps; ++st) EMS_CUDA(cudaGraphLaunch(G.exec, stream));
+            launches += (long long)per * nsteps;
+        }
+        EMS_CUDA(cudaGetLastError());
+        EMS_CUDA(cudaEventRecord(ev1, stream));
+        EMS_CUDA(cudaStreamSynchronize(stream));
+        float ms = 0;
+        EMS_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+        last_ms = ms;
+        last_launches = launches;
+        cur_time += nsteps * dtn;
+        const size_t ntr = (size_t)std::max(nobs, 1) * std::max(nsamp, 1) * 4;
+        traces.assign(ntr, 0.0);
+        EMS_CUDA(cudaMemcpy(traces.data(), d_tr.p, ntr * 8, cudaMemcpyDeviceToHost));
+        traces.resize((size_t)nobs * nsamp * 4);
+        for (int r = 0; r < nobs; ++r)
+            for (int s = 0; s < nsamp; ++s) traces[((size_t)r * nsamp + s) * 4] = times[s] * tscale;
+    }
+
+    void run(int nsteps) override
+    {
+        EMS_CHECK_ARG(nsteps >= 0, "num_steps must be >= 0");
+        if (fp64) run_t<double>(nsteps); else run_t<float>(nsteps);
+        check_finite({{d_U.p, ndof}}, fp64);
+        check_finite({{d_P.p, ndof}}, true);
+    }
+
+    size_t field_size(int which) const override
+    {
+        if (which < 0 || which > 1) throw Error{EMS_ERR_INVALID_ARGUMENT, "field index must be 0 (U) or 1 (P)"};
+        return ndof;
+    }
+    // Fields cross the API node-major (38 * node + plane per shot) and live on
+    // the device in planes.  which = 1 is P (symplectic, FP64 on the device)
+    // or E^{n-1} (leapfrog).
+    void get_field(int which, double *out) const override
+    {
+        field_size(which);
+        std::vector<double> tmp(ndof);
+        const bool pfield = which == 1 && symp();
+        const DevBuf &b = which == 0 ? d_U : (pfield ? d_P : d_Uold);
+        if (pfield || fp64) {
+            EMS_CUDA(cudaMemcpy(tmp.data(), b.p, ndof * 8, cudaMemcpyDeviceToHost));
+        } else {
+            std::vector<float> f(ndof);
+            EMS_CUDA(cudaMemcpy(f.data(), b.p, ndof * 4, cudaMemcpyDeviceToHost));
+            for (size_t e = 0; e < ndof; ++e) tmp[e] = f[e];
+        }
+        for (size_t e = 0; e < ndof; ++e) out[e] = tmp[dof_index(e)];
+    }
+    void set_field(int which, const double *in) override
+    {
+        field_size(which);
+        std::vector<double> tmp(ndof);
+        for (size_t e = 0; e < ndof; ++e) tmp[dof_index(e)] = dead_dof(dof_index(e)) ? 0.0 : in[e];
+        const bool pfield = which == 1 && symp();
+        DevBuf &b = which == 0 ? d_U : (pfield ? d_P : d_Uold);
+        if (pfield || fp64) {
+            EMS_CUDA(cudaMemcpy(b.p, tmp.data(), ndof * 8, cudaMemcpyHostToDevice));
+        } else {
+            std::vector<float> f(tmp.begin(), tmp.end());
+            EMS_CUDA(cudaMemcpy(b.p, f.data(), ndof * 4, cudaMemcpyHostToDevice));
+        }
+        if (pfield && !fp64) {
+            std::vector<float> f(tmp.begin(), tmp.end());
+            EMS_CUDA(cudaMemcpy(d_Pc.p, f.data(), ndof * 4, cudaMemcpyHostToDevice));
+        }
+        y_valid = false;
+    }
+
+    void save(const char *path) const override
+    {
+        EMS_CHECK_ARG(path && *path, "file name required");
+        for (int o = 0; o < nobs; ++o) {
+            std::string fn = path;
+            if (o > 0) {
+                size_t dot = fn.rfind('.');
+                std::string suf = "_" + std::to_string(o);
+                if (dot == std::string::npos) fn += suf; else fn.insert(dot, suf);
+            }
+            std::ofstream f(fn);
+            if (!f.is_open()) throw Error{EMS_ERR_IO, "cannot open " + fn};
+            f << std::setprecision(15) << std::scientific << "time,Ex,Ey,Ez" << std::endl;
+            for (int s = 0; s < nsamp; ++s) {
+                const double *r = &traces[((size_t)o * nsamp + s) * 4];
+                f << r[0] << "," << r[1] << "," << r[2] << "," << r[3] << std::endl;
+            }
+        }
+    }
+
+    void reset() override
+    {
+        d_U.zero(stream); d_Uold.zero(stream); d_P.zero(stream); d_x.zero(stream); d_d.zero(stream); d_b.zero(stream);
+        if (d_Pc.p) d_Pc.zero(stream);
+        cur_time = 0.0;
+        y_valid = false;
+        EMS_CUDA(cudaStreamSynchronize(stream));
+    }
+
+    void launch_shape(int b[3]) override { b[0] = 128; b[1] = b[2] = 1; }
+
+    // One Chebyshev iteration (mass element pass + entity pass) replayed in a
+    // graph of `launches` iterations; bytes: x, eps, b, d (read and write), x
+    // (write) and the block inverses once per iteration (a fused iteration's
+    // minimum; the per-tetrahedron values between the two passes are extra).
+    void time_dominant(int launches, double *ms, double *bytes, std::string *name) override
+    {
+        if (!ready) setup();
+        const int n = std::max(launches, 1);
+        const int ns = (int)shots.size();
+        auto body = [&](auto tag) {
+            using T = decltype(tag);
+            GArgs<T> g = gargs<T>();
+            g.b = d_b.as<T>();
+            g.Yt = d_YtM.p;
+            g.c1 = 0.5; g.c2 = 0.1;
+            cudaGraph_t gr = nullptr;
+            cudaGraphExec_t ex = nullptr;
+            EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            for (int k = 0; k < n; ++k) {
+                t2_mass_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_eps.as<T>(),
+                                                                              d_x.as<T>(), d_YtM.as<T>());
+                t2_gather_kernel<T, T, G_CHEB, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+            }
+            cudaError_t ce = cudaStreamEndCapture(stream, &gr);
+            if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
+            EMS_CUDA(cudaGraphInstantiate(&ex, gr, 0));
+            EMS_CUDA(cudaGraphLaunch(ex, stream));   // warm-up
+            EMS_CUDA(cudaEventRecord(ev0, stream));
+            EMS_CUDA(cudaGraphLaunch(ex, stream));
+            EMS_CUDA(cudaEventRecord(ev1, stream));
+            EMS_CUDA(cudaStreamSynchronize(stream));
+            cudaGraphExecDestroy(ex);
+            cudaGraphDestroy(gr);
+            float t = 0;
+            EMS_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
+            *ms = t / n;
+            *bytes = (double)sizeof(T) * (6.0 * ndof + ntet + 3.0 * nent);
+        };
+        // the iteration runs on zeroed scratch: x, d and b are the solver's own buffers
+        d_x.zero(stream); d_d.zero(stream); d_b.zero(stream);
+        if (fp64) body(double()); else body(float());
+        y_valid = false;
+        *name = fp64 ? "t2_mass_elem_kernel<double> + t2_gather_kernel<double, G_CHEB>"
+                     : "t2_mass_elem_kernel<float> + t2_gather_kernel<float, G_CHEB>";
+    }
+
+    // f = K u in the handle's precision (API DOF order)
+    void apply_stiffness(const double *u, double *f)
+    {
+        std::vector<double> tmp(ndof);
+        for (size_t e = 0; e < ndof; ++e) tmp[dof_index(e)] = u[e];
+        auto body = [&](auto tag) {
+            using T = decltype(tag);
+            std::vector<T> in(tmp.begin(), tmp.end()), out(ndof);
+            DevBuf a, b;
+            a.alloc(ndof * sizeof(T));
+            b.alloc(ndof * sizeof(T));
+            EMS_CUDA(cudaMemcpy(a.p, in.data(), ndof * sizeof(T), cudaMemcpyHostToDevice));
+            enqueue_force<T>(a.as<T>(), b.as<T>());
+            EMS_CUDA(cudaGetLastError());
+            EMS_CUDA(cudaStreamSynchronize(stream));
+            EMS_CUDA(cudaMemcpy(out.data(), b.p, ndof * sizeof(T), cudaMemcpyDeviceToHost));
+            for (size_t e = 0; e < ndof; ++e) f[e] = (double)out[dof_index(e)];
+        };
+        if (fp64) body(double()); else body(float());
+    }
+
+    // H = 1/2 P.q(M)P + 1/2 U.KU in FP64 (symplectic state)
+    void energy(double *out, int n)
+    {
+        EMS_CHECK_ARG(symp(), "energy is defined for the symplectic integrators");
+        EMS_CHECK_ARG(out && n == (int)shots.size(), "one value per shot");
+        if (!ready) setup();
+        std::vector<double> U(ndof), Pv(ndof);
+        get_field(0, U.data());
+        get_field(1, Pv.data());
+        // an FP64 twin of this handle computes the products
+        ems_tetfem_params p2 = P;
+        p2.precision = EMS_FP64;
+        p2.dt = dtn * tscale;
+        std::vector<std::array<int, 3>> cells;
+        for (auto &s : shots) cells.push_back({s.n[0], s.n[1], s.n[2]});
+        Tet2Sim tw(&p2, cells);
+        tw.eps_h = eps_h;
+        tw.cheb_coefficients();
+        tw.launch_pinv_and_eps<double>();
+        tw.set_field(0, U.data());
+        tw.set_field(1, Pv.data());
+        tw.enqueue_force<double>(tw.d_U.as<double>(), tw.d_b.as<double>());        // b = K U
+        tw.enqueue_solve<double, FIN_NONE>(tw.d_P.as<double>(), 0.0);              // x = q(M) P
+        EMS_CUDA(cudaGetLastError());
+        EMS_CUDA(cudaStreamSynchronize(tw.stream));
+        std::vector<double> KU(ndof), Y(ndof), Ud(ndof), Pd(ndof);
+        EMS_CUDA(cudaMemcpy(KU.data(), tw.d_b.p, ndof * 8, cudaMemcpyDeviceToHost));
+        EMS_CUDA(cudaMemcpy(Y.data(), tw.d_x.p, ndof * 8, cudaMemcpyDeviceToHost));
+        EMS_CUDA(cudaMemcpy(Ud.data(), tw.d_U.p, ndof * 8, cudaMemcpyDeviceToHost));
+        EMS_CUDA(cudaMemcpy(Pd.data(), tw.d_P.p, ndof * 8, cudaMemcpyDeviceToHost));
+        for (size_t s = 0; s < shots.size(); ++s) {
+            double e = 0.0;
+            const size_t a = shots[s].dof0, b = a + kPlanes * shots[s].nnode;
+            for (size_t q = a; q < b; ++q) e += 0.5 * (Pd[q] * Y[q] + Ud[q] * KU[q]);
+            out[s] = e;
+        }
+    }
+};
+
+bool is_tet2(const Sim *s) { return dynamic_cast<const Tet2Sim *>(s) != nullptr; }
+
+Sim *make_tet2(const ems_tetfem_params *p, const std::vector<std::array<int, 3>> &cells) { return new Tet2Sim(p, cells); }
+
+void tet2_set_material(Sim *s, const double *eps_r, const double *sigma) { static_cast<Tet2Sim *>(s)->set_material(eps_r, sigma); }
+void tet2_add_dipole(Sim *s, int shot, const double pos[3], const double dir[3], int waveform, double f0, double amp)
+{
+    static_cast<Tet2Sim *>(s)->add_dipole(shot, pos, dir, waveform, f0, amp);
+}
+void tet2_add_receiver(Sim *s, int shot, const double pos[3]) { static_cast<Tet2Sim *>(s)->add_receiver(shot, pos); }
+void tet2_time_step(const Sim *s, double *dt, double *lim)
+{
+    auto *f = const_cast<Tet2Sim *>(static_cast<const Tet2Sim *>(s));
+    if (!f->ready) f->setup();
+    if (dt) *dt = f->dtn * f->tscale;
+    if (lim) *lim = f->dt_lim_n * f->tscale;
+}
+void tet2_apply_stiffness(Sim *s, const double *u, double *f, size_t n)
+{
+    auto *t = static_cast<Tet2Sim *>(s);
+    EMS_CHECK_ARG(u && f, "input and output required");
+    EMS_CHECK_ARG(n == t->ndof, "vector length must be 38*(nx+1)*(ny+1)*(nz+1) per shot");
+    t->apply_stiffness(u, f);
+}
+void tet2_energy(Sim *s, double *out, int n) { static_cast<Tet2Sim *>(s)->energy(out, n); }
+
+// Reference matrices of the second-order element as the solver computes them.
+void tet2_element_matrices(int type, double *M, double *K)
+{
+    EMS_CHECK_ARG(type >= 0 && type < 6, "tetrahedron type must be 0..5");
+    const Ref &R = ref();
+    std::copy(R.M[type], R.M[type] + 400, M);
+    std::copy(R.K[type], R.K[type] + 400, K);
+}
+
+}  // namespace ems

@@ -3061,20 +3061,34 @@ struct TetFemSim : Sim {
     }
 };
 
+double tet_wave_value(int kind, double f0, double t) { return tet_wave(kind, f0, t); }
+double tet_stability_constant(int integrator) { return stability_constant(integrator); }
+
 Sim *make_tetfem(const ems_tetfem_params *p)
 {
-    return new TetFemSim(p, {std::array<int, 3>{p->cells[0], p->cells[1], p->cells[2]}});
+    EMS_CHECK_ARG(p != nullptr, "parameters required");
+    EMS_CHECK_ARG(p->order == 1 || p->order == 2, "Nedelec order must be 1 or 2");
+    std::vector<std::array<int, 3>> c{{p->cells[0], p->cells[1], p->cells[2]}};
+    if (p->order == 2) return make_tet2(p, c);
+    return new TetFemSim(p, c);
 }
 
 Sim *make_tetbatch(const ems_tetfem_params *p, int nshots, const int *cells)
 {
+    EMS_CHECK_ARG(p != nullptr, "parameters required");
     EMS_CHECK_ARG(nshots >= 1 && cells != nullptr, "need at least one shot");
+    EMS_CHECK_ARG(p->order == 1 || p->order == 2, "Nedelec order must be 1 or 2");
     std::vector<std::array<int, 3>> c(nshots);
     for (int s = 0; s < nshots; ++s) c[s] = {cells[3 * s], cells[3 * s + 1], cells[3 * s + 2]};
+    if (p->order == 2) return make_tet2(p, c);
     return new TetFemSim(p, c);
 }
 
-void tetfem_set_material(Sim *s, const double *eps_r, const double *sigma) { static_cast<TetFemSim *>(s)->set_material(eps_r, sigma); }
+void tetfem_set_material(Sim *s, const double *eps_r, const double *sigma)
+{
+    if (is_tet2(s)) return tet2_set_material(s, eps_r, sigma);
+    static_cast<TetFemSim *>(s)->set_material(eps_r, sigma);
+}
 
 void tetfem_add_dipole(Sim *s, const double pos[3], const double dir[3], int waveform, double f0, double amp)
 {
@@ -3083,6 +3097,7 @@ void tetfem_add_dipole(Sim *s, const double pos[3], const double dir[3], int wav
 
 void tetbatch_add_dipole(Sim *s, int shot, const double pos[3], const double dir[3], int waveform, double f0, double amp)
 {
+    if (is_tet2(s)) return tet2_add_dipole(s, shot, pos, dir, waveform, f0, amp);
     auto *f = static_cast<TetFemSim *>(s);
     EMS_CHECK_ARG(shot >= 0 && shot < (int)f->shots.size(), "shot index out of range");
     const Shot &S = f->shots[shot];
@@ -3112,6 +3127,7 @@ void tetfem_add_receiver(Sim *s, const double pos[3]) { tetbatch_add_receiver(s,
 
 void tetbatch_add_receiver(Sim *s, int shot, const double pos[3])
 {
+    if (is_tet2(s)) return tet2_add_receiver(s, shot, pos);
     auto *f = static_cast<TetFemSim *>(s);
     EMS_CHECK_ARG(pos != nullptr, "position required");
     EMS_CHECK_ARG(shot >= 0 && shot < (int)f->shots.size(), "shot index out of range");
@@ -3132,23 +3148,39 @@ void tetbatch_add_receiver(Sim *s, int shot, const double pos[3])
 
 void tetfem_apply_stiffness(Sim *s, const double *u, double *f, size_t n)
 {
+    if (is_tet2(s)) return tet2_apply_stiffness(s, u, f, n);
     auto *t = static_cast<TetFemSim *>(s);
     EMS_CHECK_ARG(u && f, "input and output required");
     EMS_CHECK_ARG(n == t->nslot, "vector length must be 7*(nx+1)*(ny+1)*(nz+1)");
     t->apply_stiffness(u, f);
 }
 
-void tetfem_set_checkpoints(Sim *s, int nsnap) { static_cast<TetFemSim *>(s)->set_checkpoints(nsnap); }
-void tetfem_energy(Sim *s, double *out, int n) { static_cast<TetFemSim *>(s)->energy(out, n); }
+static void need_order1(const Sim *s, const char *what)
+{
+    if (is_tet2(s)) throw Error{EMS_ERR_UNSUPPORTED, std::string(what) + " is implemented for order-1 tetrahedra only"};
+}
+
+void tetfem_set_checkpoints(Sim *s, int nsnap)
+{
+    need_order1(s, "the adjoint");
+    static_cast<TetFemSim *>(s)->set_checkpoints(nsnap);
+}
+void tetfem_energy(Sim *s, double *out, int n)
+{
+    if (is_tet2(s)) return tet2_energy(s, out, n);
+    static_cast<TetFemSim *>(s)->energy(out, n);
+}
 
 void tetfem_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, double *grad_sigma, size_t ngrad)
 {
+    need_order1(s, "the adjoint");
     static_cast<TetFemSim *>(s)->backward(trace_grad, ntg, grad_eps, ngrad, grad_sigma);
 }
 
 void tetfem_gradient(Sim *s, int nsteps, int nsnap, int kind, const double *obs, const double *band, double *misfit,
                      double *grad, double *grad_sigma, size_t ngrad)
 {
+    need_order1(s, "the adjoint");
     auto *f = static_cast<TetFemSim *>(s);
     EMS_CHECK_ARG(nsteps > 0 && nsnap > 0, "nsteps and nsnap must be positive");
     EMS_CHECK_ARG(obs && misfit && grad, "observed traces, misfit and gradient required");
@@ -3163,6 +3195,7 @@ void tetfem_gradient(Sim *s, int nsteps, int nsnap, int kind, const double *obs,
 
 void tetfem_time_step(const Sim *s, double *dt, double *lim)
 {
+    if (is_tet2(s)) return tet2_time_step(s, dt, lim);
     auto *f = const_cast<TetFemSim *>(static_cast<const TetFemSim *>(s));
     if (!f->ready) f->setup();
     if (dt) *dt = f->dtn * f->tscale;

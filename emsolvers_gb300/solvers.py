@@ -380,6 +380,14 @@ class TetFemBatch(TetFemSimulation):
 MISFIT_L2, MISFIT_TF_ENVELOPE, MISFIT_TF_PHASE = 0, 1, 2
 
 
+def tet_element_matrices(order, ptype):
+    """(M, K) of the second-order tetrahedron of Kuhn type ptype (20 x 20,
+    eps = mu = 1) as the solver computes them."""
+    M, K = np.zeros(400), np.zeros(400)
+    check(lib().ems_tetfem_element_matrices(int(order), int(ptype), _dptr(M), _dptr(K), 400))
+    return M.reshape(20, 20), K.reshape(20, 20)
+
+
 def trace_misfit(traces, observed, kind=MISFIT_L2, tf_band=None):
     """Misfit J of traces against observed traces (both [nobs, nsamp, 4] as
     returned by ``traces()``) and dJ/dtraces (same shape, column 0 zero).

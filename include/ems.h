@@ -155,7 +155,7 @@ int ems_femstab_element_matrix(const ems_sim *sim, double *K, size_t n);
 typedef struct {
     int cells[3];               /* structured cube of cells, each split into 6 tetrahedra */
     double h;                   /* cube edge [m] */
-    int order;                  /* Nedelec order (1) */
+    int order;                  /* Nedelec order: 1 (Whitney, 6 DOFs per tetrahedron) or 2 (20 DOFs) */
     int integrator;             /* EMS_LEAPFROG, EMS_SYMP2, EMS_SYMP4 */
     int precision;              /* EMS_FP64 or EMS_FP32 */
     double dt;                  /* time step [s]; 0 = cfl_fraction x stability limit */
@@ -163,7 +163,19 @@ typedef struct {
     int time_frequency;
 } ems_tetfem_params;
 
+/* Order 2: the complete second-order Nedelec space (2 DOFs per edge, 2 per
+ * face), 38 DOFs per node: fields and DOF vectors are 38*(nx+1)(ny+1)(nz+1)
+ * values per shot, DOF 38*node + plane (planes 0..6 the edge tails and 7..13
+ * the edge heads of the 7 edge directions, 14+2f and 15+2f the two
+ * functions of face type f), the consistent mass inverted by a fixed-degree
+ * Chebyshev polynomial in every drift.  Order-2 handles have no
+ * conductivity (sigma NULL or zero) and no adjoint (EMS_ERR_UNSUPPORTED). */
 int ems_tetfem_create(const ems_tetfem_params *params, ems_sim **out);
+/* The order-2 element's mass (eps = 1) and stiffness (mu = 1) matrices of
+ * Kuhn tetrahedron type 0..5 as the solver computes them, 20 x 20
+ * row-major each (n = 400); no handle needed.  New: the reference's element
+ * matrices are the fem_v2 kmat CSV files (fem_v2/fem_simulation.cpp:1477-1524). */
+int ems_tetfem_element_matrices(int order, int type, double *M, double *K, size_t n);
 /* Relative permittivity and conductivity [S/m] per tetrahedron (6 per cell,
  * cells x fastest, tetrahedron index = 6*cell + permutation). sigma may be NULL. */
 int ems_tetfem_set_material(ems_sim *sim, const double *eps_r, const double *sigma);

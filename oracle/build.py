@@ -8,7 +8,7 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["orc_fdtd.c", "orc_hexfem.c", "orc_tetfem.c", "orc_abm.c", "orc_femstab.c"]
+SOURCES = ["orc_fdtd.c", "orc_hexfem.c", "orc_tetfem.c", "orc_abm.c", "orc_femstab.c", "orc_tet2.c"]
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 
 

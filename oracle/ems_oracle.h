@@ -104,6 +104,25 @@ int orc_tet_mass_block(int nx, int ny, int nz, const double *eps_r, long v, long
 int orc_tet_gradient(const orc_tet_case *c, int nsteps, const double *trace_grad, double *grad_eps, double *grad_sigma);
 int orc_tet_loss_rate(int nx, int ny, int nz, const double *eps_r, const double *sigma, double *rho);
 
+/* ------------------------------- second-order tetrahedral FEM (orc_tet2.c) --- */
+/* Element mass and stiffness of Kuhn type p (20 x 20, eps = mu = 1). */
+void orc_tet2_element(int p, double *M, double *K);
+/* Plane (0..37) and lowest local vertex of local DOF a of type p. */
+void orc_tet2_dof(int p, int a, int *plane, int *lowvert);
+int orc_tet2_face_type(int s1, int s2);
+/* Unused / tangential-boundary DOFs (38 * nnode, plane layout). */
+void orc_tet2_pec_mask(int nx, int ny, int nz, unsigned char *mask);
+/* Element bounds of the pair-block preconditioned mass. */
+void orc_tet2_cheb_bounds(double *lo, double *hi);
+/* y = sum_T coef_T A_T x with A = Kref (stiff) or Mref; coef NULL = 1. */
+int orc_tet2_apply(int nx, int ny, int nz, int stiff, const double *coef, const double *x, double *y);
+/* x = q(M) b, the degree-iters Chebyshev mass inverse. */
+int orc_tet2_mass_solve(int nx, int ny, int nz, const double *eps_r, int iters, const double *b, double *x);
+long orc_tet2_locate(int nx, int ny, int nz, const double x[3], double val[20][3], long dofs[20]);
+double orc_tet2_lambda_max(int nx, int ny, int nz, const double *eps_r, const double *mu_r, int mass_iters, int iters);
+double orc_tet2_energy(int nx, int ny, int nz, const double *eps_r, int mass_iters, const double *U, const double *P);
+int orc_tet2_run(const orc_tet_case *c, int mass_iters, int nsteps, double *U, double *P, double *traces);
+
 /* ----------------------------------------- Adams-Bashforth-Moulton (hex) --- */
 typedef struct {
     int gx, gy, gz;

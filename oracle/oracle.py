@@ -341,6 +341,109 @@ def tet_apply_K(n, x):
     return f
 
 
+# ------------------------------------------------- second-order tetrahedra
+TET2_MASS_ITERS = 24
+
+
+def tet2_sizes(n):
+    nx, ny, nz = n
+    nnode = (nx + 1) * (ny + 1) * (nz + 1)
+    return nnode, 38 * nnode, 6 * nx * ny * nz
+
+
+def _t2lib():
+    L = _tlib()
+    L.orc_tet2_lambda_max.restype = C.c_double
+    L.orc_tet2_energy.restype = C.c_double
+    L.orc_tet2_locate.restype = C.c_long
+    return L
+
+
+def tet2_element(p):
+    """(M, K) 20 x 20 of Kuhn type p (eps = mu = 1), exact integration."""
+    M, K = np.zeros((20, 20)), np.zeros((20, 20))
+    _t2lib().orc_tet2_element(C.c_int(p), _ptr(M), _ptr(K))
+    return M, K
+
+
+def tet2_dof(p, a):
+    pl, lv = C.c_int(), C.c_int()
+    _t2lib().orc_tet2_dof(C.c_int(p), C.c_int(a), C.byref(pl), C.byref(lv))
+    return pl.value, lv.value
+
+
+def tet2_pec_mask(n):
+    _, ndof, _ = tet2_sizes(n)
+    m = np.zeros(ndof, np.uint8)
+    _t2lib().orc_tet2_pec_mask(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), m.ctypes.data_as(C.POINTER(C.c_uint8)))
+    return m.astype(bool)
+
+
+def tet2_cheb_bounds():
+    lo, hi = C.c_double(), C.c_double()
+    _t2lib().orc_tet2_cheb_bounds(C.byref(lo), C.byref(hi))
+    return lo.value, hi.value
+
+
+def tet2_apply(n, x, stiff, coef=None):
+    """y = sum_T coef_T A_T x (A = element stiffness if stiff else mass)."""
+    _, ndof, _ = tet2_sizes(n)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    cf = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64).reshape(-1)
+    y = np.zeros(ndof)
+    _t2lib().orc_tet2_apply(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), C.c_int(1 if stiff else 0),
+                            _ptr(cf) if cf is not None else None, _ptr(x), _ptr(y))
+    return y
+
+
+def tet2_mass_solve(n, eps_r, b, iters=TET2_MASS_ITERS):
+    _, ndof, _ = tet2_sizes(n)
+    eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
+    x = np.zeros(ndof)
+    _t2lib().orc_tet2_mass_solve(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(eps), C.c_int(iters),
+                                 _ptr(np.ascontiguousarray(b, np.float64)), _ptr(x))
+    return x
+
+
+def tet2_locate(n, x):
+    """(tet, values[20, 3], dofs[20]) of the point x (normalised)."""
+    val = np.zeros((20, 3))
+    dofs = np.zeros(20, np.int64)
+    t = _t2lib().orc_tet2_locate(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(np.asarray(x, np.float64)),
+                                 _ptr(val), dofs.ctypes.data_as(C.POINTER(C.c_long)))
+    return t, val, dofs
+
+
+def tet2_lambda_max(n, eps_r, iters=300, mu_r=None, mass_iters=TET2_MASS_ITERS):
+    eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
+    mu = None if mu_r is None else np.ascontiguousarray(mu_r, np.float64).reshape(-1)
+    return _t2lib().orc_tet2_lambda_max(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(eps),
+                                        _ptr(mu) if mu is not None else None, C.c_int(mass_iters), C.c_int(iters))
+
+
+def tet2_energy(n, eps_r, U, P, mass_iters=TET2_MASS_ITERS):
+    eps = np.ascontiguousarray(eps_r, dtype=np.float64).reshape(-1)
+    return _t2lib().orc_tet2_energy(C.c_int(n[0]), C.c_int(n[1]), C.c_int(n[2]), _ptr(eps), C.c_int(mass_iters),
+                                    _ptr(np.ascontiguousarray(U, np.float64)), _ptr(np.ascontiguousarray(P, np.float64)))
+
+
+def tet2_run(n, eps_r, integrator, dt, nsteps, tf=1, dipoles=(), receivers=(), mu_r=None, U=None, P=None,
+             mass_iters=TET2_MASS_ITERS):
+    """FP64 oracle of the second-order tetrahedral solver (normalised units).
+    U, P: 38 * nnode values in the plane layout (plane * nnode + node).
+    Returns (traces[nrec, nsamp, 4], U, P)."""
+    _, ndof, _ = tet2_sizes(n)
+    U = np.zeros(ndof) if U is None else np.ascontiguousarray(U, dtype=np.float64).copy()
+    P = np.zeros(ndof) if P is None else np.ascontiguousarray(P, dtype=np.float64).copy()
+    c, keep = _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r, None)
+    nsamp = (nsteps - 1) // tf + 1 if nsteps > 0 else 0
+    tr = np.zeros((max(len(receivers), 1), max(nsamp, 1), 4))
+    rc = _t2lib().orc_tet2_run(C.byref(c), C.c_int(mass_iters), C.c_int(nsteps), _ptr(U), _ptr(P), _ptr(tr))
+    if rc != 0:
+        raise RuntimeError(f"orc_tet2_run failed: {rc}")
+    return tr[:len(receivers), :nsamp], U, P
+
+
 # ------------------------------------------------- Adams-Bashforth-Moulton (hex)
 class _AbmCase(C.Structure):
     _fields_ = [("gx", C.c_int), ("gy", C.c_int), ("gz", C.c_int),
