@@ -72,6 +72,12 @@ def n_edges(n):
     return 3 * n * (n + 1) ** 2 + 3 * n ** 2 * (n + 1) + n ** 3
 
 
+def n_dofs2(n):
+    """DOFs of the second-order tetrahedra on an n^3 cube: 2 per edge, 2 per
+    face (6 face types span two axes, 6 span three)."""
+    return 2 * (n_edges(n) + 6 * n ** 2 * (n + 1) + 6 * n ** 3)
+
+
 class Clocks:
     """Samples SM clocks and throttle reasons with nvidia-smi while running."""
 
@@ -322,12 +328,17 @@ def head_solve(steps=STEPS_PER_SOLVE):
             "dof_updates_per_s": n_edges(N) * steps / (ms * 1e-3)}
 
 
-def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
+def batch64(nshots=64, steps=3000, sample=8, sample_steps=300, o2_steps=300, o2_sample=2, o2_sample_steps=50):
     """Batched forward shots: nshots cubes of side n ~ U[12,40] (6 n^3
-    tetrahedra each), eps_r ~ U[1,6] per tet, one Ricker dipole each, 4th-order
-    symplectic, `steps` steps, FP32, all shots advanced by the same kernels.
-    Compared with the plain per-shot FP64 GPU path on `sample` of the shots
-    (same time step, `sample_steps` steps, scaled to `steps`)."""
+    tetrahedra each), first- or second-order Nedelec by coin flip, eps_r ~
+    U[1,6] per tet, one Ricker dipole each, 4th-order symplectic, `steps`
+    steps, FP32, one common time step (the stiffest shot's).  The shots of
+    each order advance together in one batch handle (all shots of the order
+    in every launch, the time loop in CUDA graphs); the two handles run back
+    to back.  The order-1 batch runs all `steps`; the order-2 batch runs
+    `o2_steps` of them (its rate scaled to `steps`).  Compared with the
+    plain per-shot FP64 GPU path on `sample` order-1 and `o2_sample` order-2
+    shots (same time step, sample steps scaled to `steps`)."""
     import emsolvers_gb300 as ems
     rng = np.random.default_rng(SEED + 4)
     sides = rng.integers(12, 41, nshots)
@@ -335,38 +346,70 @@ def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
     eps = [rng.uniform(1.0, 6.0, 6 * n ** 3) for n in sides]
     pos = [np.array([n, n, n]) * rng.uniform(0.3, 0.7, 3) * H for n in sides]
     rec = [np.array([n, n, n]) * rng.uniform(0.2, 0.8, 3) * H for n in sides]
+    orders = rng.integers(1, 3, nshots)
     f0 = C0 / (10 * H * np.sqrt(3.5))
-    b = ems.TetFemBatch(cells, H, integrator=ems.SYMP4, precision=ems.FP32, dt=0.0, cfl_fraction=0.9)
-    b.set_material(np.concatenate(eps))
-    for s in range(nshots):
-        b.add_dipole(s, pos[s], (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
-        b.add_receiver(s, rec[s])
-    dt, _ = b.time_step()
-    b.run(20)
-    b.reset()
-    b.run(steps)
-    ms_batch, launches = b.run_stats()
-    kms, kbytes, kname = b.time_dominant_kernel(20)
-    block = list(b.launch_shape())
-    edges = sum(n_edges(int(n)) for n in sides)
-    b.close()
-    per = {ems.FP64: [], ems.FP32: []}
-    pick = rng.choice(nshots, size=min(sample, nshots), replace=False)
-    for prec in (ems.FP64, ems.FP32):
-        for s in pick:
-            one = ems.TetFemSimulation(cells[s], H, 1, ems.SYMP4, prec, dt=dt)
-            one.set_material(eps[s])
-            one.add_dipole(pos[s], (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
-            one.add_receiver(rec[s])
-            one.run(5)
-            one.reset()
-            one.run(sample_steps)
-            per[prec].append(one.run_stats()[0] * steps / sample_steps)
-            one.close()
+    groups = {o: [s for s in range(nshots) if orders[s] == o] for o in (1, 2)}
+
+    def handle(o, dt):
+        sh = groups[o]
+        b = ems.TetFemBatch([cells[s] for s in sh], H, order=o, integrator=ems.SYMP4, precision=ems.FP32, dt=dt,
+                            cfl_fraction=0.9)
+        b.set_material(np.concatenate([eps[s] for s in sh]))
+        for k, s in enumerate(sh):
+            b.add_dipole(k, pos[s], (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
+            b.add_receiver(k, rec[s])
+        return b
+
+    dts = []
+    for o in (1, 2):
+        if groups[o]:
+            b = handle(o, 0.0)
+            dts.append(b.time_step()[0])
+            b.close()
+    dt = min(dts)
+    res = {}
+    for o in (1, 2):
+        if not groups[o]:
+            continue
+        b = handle(o, dt)
+        nst = steps if o == 1 else min(o2_steps, steps)
+        b.run(20)
+        b.reset()
+        b.run(nst)
+        ms, launches = b.run_stats()
+        kms, kbytes, kname = b.time_dominant_kernel(20)
+        res[o] = {"shots": len(groups[o]), "ms": ms * steps / nst, "run_steps": nst, "launches_per_step": launches / nst,
+                  "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9,
+                  "launch_shape": list(b.launch_shape()),
+                  "dofs": int(sum(n_edges(int(sides[s])) if o == 1 else n_dofs2(int(sides[s])) for s in groups[o]))}
+        b.close()
+    ms_batch = sum(r["ms"] for r in res.values())
+    # plain per-shot paths on a sample of each order
+    per = {ems.FP64: 0.0, ems.FP32: 0.0}
+    picks = {}
+    for o, k, st in ((1, sample, sample_steps), (2, o2_sample, o2_sample_steps)):
+        if not groups[o]:
+            continue
+        pick = rng.choice(groups[o], size=min(k, len(groups[o])), replace=False)
+        picks[o] = (len(pick), st)
+        for prec in (ems.FP64, ems.FP32):
+            t = []
+            for s in pick:
+                one = ems.TetFemSimulation(cells[s], H, o, ems.SYMP4, prec, dt=dt)
+                one.set_material(eps[s])
+                one.add_dipole(pos[s], (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
+                one.add_receiver(rec[s])
+                one.run(3)
+                one.reset()
+                one.run(st)
+                t.append(one.run_stats()[0] * steps / st)
+                one.close()
+            per[prec] += np.mean(t) * len(groups[o])   # the order's shots at the sample's mean time
     shots_batch = nshots / (ms_batch * 1e-3)
-    shots_fp64 = 1.0 / (np.mean(per[ems.FP64]) * 1e-3)
-    shots_fp32 = 1.0 / (np.mean(per[ems.FP32]) * 1e-3)
-    # CPU: one shot of the batch's mean size, FP64 oracle, sample steps scaled
+    shots_fp64 = nshots / (per[ems.FP64] * 1e-3)
+    shots_fp32 = nshots / (per[ems.FP32] * 1e-3)
+    dofs = sum(r["dofs"] for r in res.values())
+    # CPU: one order-1 shot of the batch's mean size, FP64 oracle, sample steps scaled
     nm = int(round(np.cbrt(np.mean(sides.astype(float) ** 3))))
     cpu_steps = 100
     code = (f"n = {nm}; eps = np.random.default_rng(0).uniform(1.0, 6.0, 6 * n ** 3)\n"
@@ -376,17 +419,20 @@ def batch64(nshots=64, steps=3000, sample=8, sample_steps=300):
             f"oracle.tet_run((n, n, n), eps, oracle.SYMP4, dtn, {cpu_steps}, 1, [dip], [(0.3 * n, 0.6 * n, 0.4 * n)])\n"
             "print(time.perf_counter() - t0)\n")
     cpu = cpu_rates(code, cpu_steps / steps)
-    return {"workload": "tet_batch64_symp4_3000", "shots": nshots, "steps": steps, "tets": int(sum(6 * sides ** 3)),
-            "edges": int(edges), "order": 1, "dt_s": dt, "batch_ms": ms_batch, "launches": int(launches),
+    return {"workload": "tet_batch64_symp4_3000_mixed_order", "shots": nshots, "steps": steps,
+            "tets": int(sum(6 * sides ** 3)), "order_1_shots": len(groups[1]), "order_2_shots": len(groups[2]),
+            "dofs": int(dofs), "dt_s": dt, "batch_ms": ms_batch,
+            "per_order": {str(o): r for o, r in res.items()},
+            "order_2_timing": f"order-2 batch timed over {min(o2_steps, steps)} of the {steps} steps, scaled",
             "shots_per_s_fp32_batched": shots_batch, "shots_per_s_fp64_per_shot": shots_fp64,
             "shots_per_s_fp32_per_shot": shots_fp32, "speedup_vs_fp64_per_shot": shots_batch / shots_fp64,
-            "dof_updates_per_s": edges * steps / (ms_batch * 1e-3),
-            "per_shot_sample": f"{len(pick)} shots x {sample_steps} steps, scaled to {steps}",
-            "kernel": kname, "kernel_us": kms * 1e3, "kernel_gbs": kbytes / (kms * 1e-3) / 1e9, "launch_shape": block,
-            "cpu_baseline": {"value": cpu["single_core"], "unit": "shots/s", "cores": 1, "kind": "port",
+            "dof_updates_per_s": dofs * steps / (ms_batch * 1e-3),
+            "per_shot_sample": "; ".join(f"order {o}: {n} shots x {st} steps, scaled to {steps}" for o, (n, st) in picks.items()),
+            "cpu_baseline": {"value": cpu["single_core"], "unit": "shots/s (order 1)", "cores": 1, "kind": "port",
                              "nproc_processes_value": cpu["nproc_processes"], "processes": cpu["processes"],
-                             "sample": f"one {nm}^3 x 6 tet shot (the batch's mean size), {cpu_steps} steps of the FP64 "
-                                       f"oracle scaled to {steps}; single core, and nproc concurrent single-threaded processes"}}
+                             "sample": f"one order-1 {nm}^3 x 6 tet shot (the batch's mean size), {cpu_steps} steps of the "
+                                       f"FP64 oracle scaled to {steps}; single core, and nproc concurrent single-threaded "
+                                       "processes"}}
 
 
 def hex72(steps=200, order=2, sample_steps=10):
@@ -425,6 +471,42 @@ def hex72(steps=200, order=2, sample_steps=10):
     return out
 
 
+def tet2_forward(n=48, steps=200):
+    """Second-order (20-DOF) tetrahedra on an n^3 x 6 tet cube (the blob model
+    of the inversion configuration), one Ricker dipole, 8 receivers, symp4:
+    FP32 and FP64 device rates over `steps` steps, and one Chebyshev mass
+    iteration (element pass + entity pass) timed alone."""
+    import emsolvers_gb300 as ems
+    rng = np.random.default_rng(SEED + 7)
+    eps = blob_model(n, rng)
+    f0 = C0 / (10 * H * np.sqrt(2.0))
+    src = np.array([0.5, 0.47, 0.52]) * n * H
+    recs = [rng.uniform(0.1, 0.9, 3) * n * H for _ in range(8)]
+    out = {"workload": f"tet{n}_order2_symp4", "order": 2, "dofs": n_dofs2(n), "tets": 6 * n ** 3, "steps": steps}
+    dt = None
+    for prec, name in ((ems.FP32, "fp32"), (ems.FP64, "fp64")):
+        s = ems.TetFemSimulation((n, n, n), H, 2, ems.SYMP4, prec, dt=dt or 0.0, cfl_fraction=0.9)
+        s.set_material(eps)
+        s.add_dipole(src, (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0, 1.0)
+        for r in recs:
+            s.add_receiver(r)
+        dt = dt or s.time_step()[0]
+        s.run(3)
+        s.reset()
+        s.run(steps)
+        ms, launches = s.run_stats()
+        out[f"dof_updates_per_s_{name}"] = n_dofs2(n) * steps / (ms * 1e-3)
+        out[f"ms_per_step_{name}"] = ms / steps
+        out[f"launches_per_step_{name}"] = launches / steps
+        kms, kbytes, kname = s.time_dominant_kernel(20)
+        out[f"cheb_iteration_us_{name}"] = kms * 1e3
+        out[f"cheb_iteration_gbs_{name}"] = kbytes / (kms * 1e-3) / 1e9
+        s.close()
+    out["dt_s"] = dt
+    out["fp32_speedup_vs_fp64"] = out["dof_updates_per_s_fp32"] / out["dof_updates_per_s_fp64"]
+    return out
+
+
 def blob_model(n, rng, background=2.0, nblob=3):
     """Per-tet eps_r: background plus nblob Gaussian blobs (amplitude U[1,3],
     width U[4,8] cells) evaluated at the tetrahedron centroids."""
@@ -444,7 +526,8 @@ def blob_model(n, rng, background=2.0, nblob=3):
     return eps
 
 
-def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, fd_elements=32, fd_h=1e-4, cpu_steps=20):
+def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, fd_elements=32, fd_h=1e-4, cpu_steps=20, order=1,
+              full_steps=4000, fd_n=None, tf_backward=True):
     """Forward + adjoint misfit gradient: nshots Ricker dipole shots on an
     n^3 x 6 tet cube (true eps_r = 2 + 3 Gaussian blobs, start model 2), nrec
     receivers per shot, symp4, `steps` steps, nsnap snapshots; L2 and TF
@@ -452,7 +535,13 @@ def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, fd_elements=32, fd
     plain per-shot FP64 GPU path (shot 0, the whole run).  Checks: FP32 vs
     FP64 traces and gradient over the whole run of shot 0, and central
     differences (relative step fd_h, FP64, all perturbed models in one
-    batch) of the L2 misfit on fd_elements random tetrahedra."""
+    batch) of the L2 misfit on fd_elements random tetrahedra.  With steps <
+    full_steps the run is a sample of the full-length run: rates are scaled
+    by steps / full_steps and the accuracy figures cover the sample.
+    fd_n: run the central differences on an fd_n^3 model of the same recipe
+    instead (same sources and receivers in relative position), where FP64
+    runs are cheap; tf_backward=False reports the TF envelope misfit
+    without its backward sweep."""
     import emsolvers_gb300 as ems
     rng = np.random.default_rng(SEED + 5)
     true = blob_model(n, rng)
@@ -460,18 +549,19 @@ def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, fd_elements=32, fd
     f0 = C0 / (10 * H * np.sqrt(2.0))
     src = [rng.uniform(0.2, 0.8, 3) * n * H for _ in range(nshots)]
     rec = [rng.uniform(0.1, 0.9, 3) * n * H for _ in range(nrec)]
-    probe = ems.TetFemSimulation((n, n, n), H, 1, ems.SYMP4, ems.FP32, dt=0.0, cfl_fraction=0.9)
+    probe = ems.TetFemSimulation((n, n, n), H, order, ems.SYMP4, ems.FP32, dt=0.0, cfl_fraction=0.9)
     probe.set_material(start)
     dt, _ = probe.time_step()
     probe.close()
 
-    def handle(precision, shots, model):
-        b = ems.TetFemBatch([(n, n, n)] * len(shots), H, integrator=ems.SYMP4, precision=precision, dt=dt)
-        b.set_material(np.tile(model, len(shots)) if np.ndim(model) == 1 and len(model) == true.size else model)
+    def handle(precision, shots, model, nn=n):
+        sc = nn / n   # sources and receivers keep their relative positions
+        b = ems.TetFemBatch([(nn, nn, nn)] * len(shots), H, order=order, integrator=ems.SYMP4, precision=precision, dt=dt)
+        b.set_material(np.tile(model, len(shots)) if np.ndim(model) == 1 and len(model) == 6 * nn ** 3 else model)
         for k, sh in enumerate(shots):
-            b.add_dipole(k, src[sh], (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
+            b.add_dipole(k, src[sh] * sc, (0.0, 0.0, 1.0), ems.WAVE_RICKER, f0)
             for r in rec:
-                b.add_receiver(k, r)
+                b.add_receiver(k, r * sc)
         return b
 
     shots = list(range(nshots))
@@ -499,8 +589,10 @@ def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, fd_elements=32, fd
     stages = {"setup_s": ts[0] - t0, "forward_s": ts[1] - ts[0], "misfit_s": ts[2] - ts[1], "backward_s": ts[3] - ts[2]}
     # the TF envelope misfit on the same recorded run (a second backward sweep)
     t1 = time.perf_counter()
-    Jtf, tgtf = ems.trace_misfit(b.traces(), obs, ems.MISFIT_TF_ENVELOPE)
-    gtf = b.backward(tgtf).reshape(nshots, -1).sum(0)
+    Jtf, gtf = None, None
+    if tf_backward:
+        Jtf, tgtf = ems.trace_misfit(b.traces(), obs, ems.MISFIT_TF_ENVELOPE)
+        gtf = b.backward(tgtf).reshape(nshots, -1).sum(0)
     tf_s = time.perf_counter() - t1
     tr32_0 = b.traces()[:nrec]
     b.close()
@@ -523,20 +615,37 @@ def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, fd_elements=32, fd
     g_err = float(np.linalg.norm(g32[0] - g64_0) / np.linalg.norm(g64_0))
     # central differences of J0 on fd_elements tetrahedra, FP64, one batch of
     # 2 fd_elements perturbed copies of the start model (shot 0 each)
-    pick = rng.choice(true.size, size=fd_elements, replace=False)
-    models = np.tile(start, 2 * fd_elements).reshape(2 * fd_elements, -1)
-    for q, t in enumerate(pick):
-        models[2 * q, t] += fd_h * start[t]
-        models[2 * q + 1, t] -= fd_h * start[t]
     t1 = time.perf_counter()
-    fd = handle(ems.FP64, [0] * (2 * fd_elements), models.reshape(-1))
+    nf, start_f, obs_f, g_ref = n, start, obs0, g64_0
+    if fd_n:   # the same check on the small model: its own observed traces and FP64 adjoint
+        nf = fd_n
+        true_f = blob_model(nf, np.random.default_rng(SEED + 6))
+        start_f = np.full(true_f.size, 2.0)
+        h = handle(ems.FP64, [0], true_f, nf)
+        h.run(steps)
+        obs_f = h.traces()
+        h.close()
+        h = handle(ems.FP64, [0], start_f, nf)
+        h.set_checkpoints(nsnap)
+        h.reset()
+        h.run(steps)
+        g_ref = h.backward(ems.trace_misfit(h.traces(), obs_f, ems.MISFIT_L2)[1])
+        h.close()
+    pick = rng.choice(start_f.size, size=fd_elements, replace=False)
+    models = np.tile(start_f, 2 * fd_elements).reshape(2 * fd_elements, -1)
+    for q, t in enumerate(pick):
+        models[2 * q, t] += fd_h * start_f[t]
+        models[2 * q + 1, t] -= fd_h * start_f[t]
+    fd = handle(ems.FP64, [0] * (2 * fd_elements), models.reshape(-1), nf)
     fd.run(steps)
     trs = fd.traces().reshape(2 * fd_elements, nrec, -1, 4)
     fd.close()
     fd_s = time.perf_counter() - t1
-    Jp = np.array([ems.trace_misfit(trs[k], obs0, ems.MISFIT_L2)[0] for k in range(2 * fd_elements)])
-    g_fd = (Jp[0::2] - Jp[1::2]) / (2 * fd_h * start[pick])
-    fd_err = float(np.linalg.norm(g64_0[pick] - g_fd) / np.linalg.norm(g_fd))
+    Jp = np.array([ems.trace_misfit(trs[k], obs_f, ems.MISFIT_L2)[0] for k in range(2 * fd_elements)])
+    g_fd = (Jp[0::2] - Jp[1::2]) / (2 * fd_h * start_f[pick])
+    fd_err = float(np.linalg.norm(g_ref[pick] - g_fd) / np.linalg.norm(g_fd))
+    scale = steps / full_steps   # rates of the full-length run from a step sample
+    cpu = None
     # CPU: the FP64 oracle adjoint of one shot over cpu_steps steps, scaled
     code = (f"n = {n}; rng = np.random.default_rng(0); eps = np.full(6 * n ** 3, 2.0)\n"
             f"dip = ({tuple(src[0] / H)!r}, (0.0, 0.0, 1.0), 1, {f0 * H / C0!r}, 1.0)\n"
@@ -548,24 +657,33 @@ def adjoint16(n=48, nshots=16, nrec=32, steps=4000, nsnap=64, fd_elements=32, fd
             "g = tr.copy(); g[..., 0] = 0.0\n"
             f"oracle.tet_gradient((n, n, n), eps, oracle.SYMP4, dtn, {cpu_steps}, g, 1, [dip], recs)\n"
             "print(time.perf_counter() - t0)\n")
-    cpu = cpu_rates(code, cpu_steps / steps)   # shots per run of the sample
-    return {"workload": f"tet{n}_adjoint_{nshots}shots_symp4_{steps}", "tets_per_shot": int(true.size),
-            "shots": nshots, "receivers_per_shot": nrec, "steps": steps, "snapshots": nsnap, "misfits": ["L2", "TF_envelope"],
-            "order": 1, "dt_s": dt, "misfit_l2": J, "misfit_tf_envelope": Jtf,
-            "grad_norm_l2": float(np.linalg.norm(g32.sum(0))), "grad_norm_tf": float(np.linalg.norm(gtf)),
+    if order == 1 and cpu_steps > 0:
+        cpu = cpu_rates(code, cpu_steps / full_steps)   # shots per run of the sample
+    out = {"workload": f"tet{n}_adjoint_{nshots}shots_symp4_{full_steps}" + ("" if order == 1 else "_order2"),
+           "tets_per_shot": int(true.size),
+            "shots": nshots, "receivers_per_shot": nrec, "steps": steps, "snapshots": nsnap,
+            "misfits": ["L2", "TF_envelope"] if tf_backward else ["L2"],
+            "order": order, "dt_s": dt, "misfit_l2": J, "misfit_tf_envelope": Jtf,
+            "grad_norm_l2": float(np.linalg.norm(g32.sum(0))),
+            "grad_norm_tf": float(np.linalg.norm(gtf)) if gtf is not None else None,
             "fp32_batched_s": wall32, "fp32_forward_ms": fwd_ms, "fp32_stages": stages, "tf_envelope_backward_s": tf_s,
-            "shots_per_s_fp32_batched": nshots / wall32, "shots_per_s_fp64_per_shot": 1.0 / wall64,
+            "shots_per_s_fp32_batched": nshots / wall32 * scale, "shots_per_s_fp64_per_shot": 1.0 / wall64 * scale,
             "speedup_vs_fp64_per_shot": (nshots / wall32) * wall64,
             "fp64_per_shot": "shot 0, the whole run: material upload, FP64 mass setup, recorded forward, misfit, backward",
             "fp32_vs_fp64_trace_rel_l2": tr_err, "fp32_vs_fp64_grad_rel_l2": g_err,
             "fp32_vs_fp64_over": f"shot 0, all {steps} steps (forward traces and gradient)",
             "fd_check": {"elements": fd_elements, "h_rel": fd_h, "fp64_adjoint_vs_central_diff_rel_l2": fd_err,
-                         "seconds": fd_s},
-            "cpu_baseline": {"value": cpu["single_core"], "unit": "shots/s", "cores": 1, "kind": "port",
-                             "nproc_processes_value": cpu["nproc_processes"], "processes": cpu["processes"],
-                             "sample": f"one shot, {cpu_steps} steps forward + adjoint (FP64 oracle), scaled to {steps}; "
-                                       "single core, and nproc concurrent single-threaded processes"},
+                         "seconds": fd_s, "model": f"{nf}^3 x 6 tets, shot 0, {steps} steps"},
             "timing": "wall clock: material upload + FP64 mass setup + recorded forward + misfit + backward"}
+    if steps < full_steps:
+        out["step_sample"] = (f"{steps} of the {full_steps} steps ({nsnap} snapshots), all {nshots} shots; shots/s "
+                              f"scaled to the full run, accuracy figures over the sample")
+    if cpu is not None:
+        out["cpu_baseline"] = {"value": cpu["single_core"], "unit": "shots/s", "cores": 1, "kind": "port",
+                               "nproc_processes_value": cpu["nproc_processes"], "processes": cpu["processes"],
+                               "sample": f"one shot, {cpu_steps} steps forward + adjoint (FP64 oracle), scaled to "
+                                         f"{full_steps}; single core, and nproc concurrent single-threaded processes"}
+    return out
 
 
 def run_gpu(args):
@@ -706,6 +824,15 @@ def run_gpu(args):
                 out["hex72"] = {"error": str(e)}
         if not args.no_adjoint:
             try:
+                out["tet48_order2"] = tet2_forward(n=48, steps=100)
+            except Exception as e:  # secondary measurement only
+                out["tet48_order2"] = {"error": str(e)}
+            try:
+                out["adjoint16_order2"] = adjoint16(order=2, nshots=2, steps=200, nsnap=4, fd_elements=8, fd_n=12,
+                                                    tf_backward=False)
+            except Exception as e:  # secondary measurement only
+                out["adjoint16_order2"] = {"error": str(e)}
+            try:
                 out["adjoint16"] = adjoint16()
             except Exception as e:  # secondary measurement only
                 out["adjoint16"] = {"error": str(e)}
@@ -732,7 +859,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-hex", action="store_true")
-    ap.add_argument("--only", choices=["head", "batch", "fdtd", "adjoint", "hex", "sphere", "symp2"],
+    ap.add_argument("--only", choices=["head", "batch", "fdtd", "adjoint", "hex", "sphere", "symp2", "tet2"],
                     help="run one secondary workload alone and print its JSON (for profiling)")
     ap.add_argument("--fdtd-n", type=int, default=512, help="FDTD cube side for --only fdtd")
     ap.add_argument("--head-steps", type=int, default=STEPS_PER_SOLVE, help="time steps for --only head")
@@ -742,7 +869,11 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=4000, help="time steps for --only adjoint")
     ap.add_argument("--adj-shots", type=int, default=16, help="shots for --only adjoint")
     ap.add_argument("--adj-fd", type=int, default=32, help="central-difference elements for --only adjoint")
+    ap.add_argument("--adj-order", type=int, default=1, choices=[1, 2], help="Nedelec order for --only adjoint")
+    ap.add_argument("--adj-fd-n", type=int, default=0, help="cube side of the central-difference model (0: the same)")
+    ap.add_argument("--adj-no-tf", action="store_true", help="skip the TF envelope backward sweep")
     ap.add_argument("--fdtd-steps", type=int, default=4000, help="time steps for --only fdtd")
+    ap.add_argument("--tet2-steps", type=int, default=200, help="time steps for --only tet2")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -754,8 +885,11 @@ def main():
                                        sample_steps=min(300, args.batch_steps)),
               "fdtd": lambda: fdtd_512(n=args.fdtd_n, steps=args.fdtd_steps, compare_fp64=args.fdtd_steps >= 1000),
               "hex": hex72, "sphere": fdtd64_sphere, "symp2": tet32_symp2,
+              "tet2": lambda: tet2_forward(n=args.adj_n, steps=args.tet2_steps),
               "adjoint": lambda: adjoint16(n=args.adj_n, nshots=args.adj_shots, steps=args.adj_steps,
-                                           fd_elements=args.adj_fd)}[args.only]
+                                           fd_elements=args.adj_fd, order=args.adj_order,
+                                           nsnap=min(64, args.adj_steps), fd_n=args.adj_fd_n or None,
+                                           tf_backward=not args.adj_no_tf)}[args.only]
         print(json.dumps(fn()))
     elif args.impl == "reference":
         run_reference(args)

@@ -109,6 +109,9 @@ void tet2_add_receiver(Sim *s, int shot, const double pos[3]);
 void tet2_time_step(const Sim *s, double *dt, double *lim);
 void tet2_apply_stiffness(Sim *s, const double *u, double *f, size_t n);
 void tet2_energy(Sim *s, double *out, int n);
+void tet2_set_checkpoints(Sim *s, int nsnap);
+void tet2_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, double *grad_sigma, size_t ngrad);
+size_t tet2_ntet(const Sim *s);
 void tet2_element_matrices(int type, double *M, double *K);
 Sim *make_femstab(const ems_femstab_params *p);
 bool is_femstab(const Sim *s);

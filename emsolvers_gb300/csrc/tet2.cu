@@ -21,17 +21,19 @@
 //   stiffness    element by element through the curl: the curl of the 20
 //                functions is linear, so the element computes its values at
 //                the four vertices (dyadic coefficients), the P1 mass of
-//                those values and the transposed curl; FP64 arithmetic in
-//                both precisions (the kick of an FP32 run is the one place
-//                where rounding accumulates without bound, in the null space
-//                of K).
+//                those values and the transposed curl; FP64 for FP64 runs,
+//                double-float (compensated FP32) for FP32 runs, the kick
+//                summed and applied to P in FP64: the kick of an FP32 run is
+//                the one place where rounding accumulates without bound, in
+//                the null space of K.
 //   mass inverse the drift applies q(M) P, the degree-m Chebyshev polynomial
 //                of the mass preconditioned by its 2 x 2 edge and face
 //                blocks, on the element bounds of the preconditioned
-//                spectrum; one element pass (20 x 20 reference matrix times
-//                eps) and one entity pass (per-DOF gather in a fixed order,
-//                no atomics, the block inverse and the Chebyshev update) per
-//                iteration.
+//                spectrum; one entity pass per iteration: each edge or face
+//                forms its two mass rows from the iterate of its (up to six)
+//                tetrahedra in a fixed order (no atomics, no per-tetrahedron
+//                array), applies the block inverse and the Chebyshev update,
+//                and writes the next iterate to the other of two buffers.
 //   time loop    one CUDA graph per step, replayed; a device step counter
 //                indexes the source table and the receiver samples.
 // Units are normalised (cube edge 1, c0 = 1); the API converts.
@@ -41,9 +43,11 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iomanip>
+#include <type_traits>
 #include <vector>
 
 #include "ems_internal.hpp"
@@ -63,7 +67,7 @@ constexpr int kEdge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
 constexpr int kFace[4][3] = {{0, 1, 2}, {0, 1, 3}, {0, 2, 3}, {1, 2, 3}};
 constexpr int kDir[7][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1}, {1, 1, 1}};
 constexpr double kAdmix = -0.625;
-constexpr int kMassIters = 24;
+constexpr int kMassIters = 28;
 
 // ------------------------------------------------------- element geometry
 struct Kuhn {
@@ -353,6 +357,7 @@ __constant__ int c2_dof[6][20];          // plane | vertex offset bits << 8
 __constant__ double c2_M64[6][400];
 __constant__ float c2_M32[6][400];
 __constant__ double c2_C[6][20][12];
+__constant__ float c2_C32[6][20][12];   // the same, exact in FP32 (dyadic)
 __constant__ int c2_ninc[kEnt], c2_inc[kEnt][kMaxInc], c2_axes[kEnt];
 
 struct T2Shot {
@@ -404,7 +409,9 @@ __device__ __forceinline__ TetAddr tet_addr(const T2Shot &S, unsigned long long 
     return ta;
 }
 
-// Mass element pass: Yt[a][t] = eps_t (Mref_p x_t)_a.
+// Mass element pass: Yt[a][t] = eps_t (Mref_p x_t)_a (the two-pass
+// iteration: this pass, then the entity pass sums the values of an
+// entity's tetrahedra).
 template <class T>
 __global__ void __launch_bounds__(128) t2_mass_elem_kernel(unsigned long long NT, const T2Shot *__restrict__ sh, int ns,
                                                           const T *__restrict__ eps, const T *__restrict__ x, T *__restrict__ Yt)
@@ -463,6 +470,74 @@ __global__ void __launch_bounds__(128) t2_stiff_elem_kernel(unsigned long long N
     }
 }
 
+// Stiffness element pass of FP32 runs in double-float arithmetic: the same
+// vertex curls, P1 mass and transposed curl, each sum a compensated dot
+// product (Ogita, Rump and Oishi 2005, Dot2: products split exactly by FMA,
+// sums by two-sum, the errors accumulated alongside), so the element values
+// carry about twice the FP32 precision at FP32 throughput.  The curl
+// coefficients are dyadic (exact in FP32); zero coefficients are skipped
+// (the type p is uniform across a warp).
+__device__ __forceinline__ void dot2_add(float a, float b, float &s, float &c)
+{
+    const float p = __fmul_rn(a, b);
+    const float ep = fmaf(a, b, -p);
+    const float t = __fadd_rn(s, p);
+    const float bb = __fsub_rn(t, s);
+    const float es = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+    s = t;
+    c = __fadd_rn(c, __fadd_rn(ep, es));
+}
+
+__global__ void __launch_bounds__(128) t2_stiff_df_kernel(unsigned long long NT, const T2Shot *__restrict__ sh, int ns,
+                                                         const float *__restrict__ U, double *__restrict__ Yt)
+{
+    const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (t >= NT) return;
+    const T2Shot S = sh[shot_of(sh, ns, t, 0)];
+    const TetAddr ta = tet_addr(S, t - S.tet0);
+    const int p = ta.p;
+    float cs[12], cc[12];
+#pragma unroll
+    for (int q = 0; q < 12; ++q) { cs[q] = 0.0f; cc[q] = 0.0f; }
+#pragma unroll 2
+    for (int a = 0; a < 20; ++a) {
+        const float u = U[ta.dof(a)];
+#pragma unroll
+        for (int q = 0; q < 12; ++q) {
+            const float co = c2_C32[p][a][q];
+            if (co != 0.0f) dot2_add(co, u, cs[q], cc[q]);
+        }
+    }
+    // P1 mass in FP64 (12 values), split again into hi + lo
+    double c[12];
+#pragma unroll
+    for (int q = 0; q < 12; ++q) c[q] = (double)cs[q] + (double)cc[q];
+    float hh[12], hl[12];
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const double sm = c[q] + c[3 + q] + c[6 + q] + c[9 + q];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const double h = (c[3 * v + q] + sm) * (1.0 / 120.0);
+            hh[3 * v + q] = (float)h;
+            hl[3 * v + q] = (float)(h - (double)hh[3 * v + q]);
+        }
+    }
+#pragma unroll 2
+    for (int a = 0; a < 20; ++a) {
+        float fs = 0.0f, fc = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 12; ++q) {
+            const float co = c2_C32[p][a][q];
+            if (co != 0.0f) {
+                dot2_add(co, hh[q], fs, fc);
+                fc = fmaf(co, hl[q], fc);
+            }
+        }
+        Yt[(unsigned long long)a * NT + t] = (double)fs + (double)fc;
+    }
+}
+
 enum { G_FORCE = 0, G_KICK = 1, G_CHEB0 = 2, G_CHEB = 3 };
 enum { FIN_NONE = 0, FIN_DRIFT = 1, FIN_LEAP = 2 };
 
@@ -473,7 +548,9 @@ template <class T> struct GArgs {
     T *Pc;           // P in the run precision (FP32 runs), the right-hand side of the solve
     T *out;          // G_FORCE output
     const T *b;      // right-hand side of the solve
-    T *x, *d;        // Chebyshev iterate and step
+    T *x, *d;        // Chebyshev iterate (written) and step
+    const T *xin;    // Chebyshev iterate read by the fused mass rows (G_CHEB)
+    const T *eps;    // permittivity per tetrahedron (G_CHEB)
     const T *pinv;   // 2 x 2 block inverses, three planes over the entities
     T *U, *Uold;
     double a;        // kick: P -= a F
@@ -549,8 +626,90 @@ __global__ void __launch_bounds__(128) t2_gather_kernel(unsigned long long NE, c
     } else {
         n0 = fma((T)g.c1, g.d[d0], (T)g.c2 * z0);
         n1 = fma((T)g.c1, g.d[d1], (T)g.c2 * z1);
-        x0 = g.x[d0] + n0; x1 = g.x[d1] + n1;
+        x0 = g.xin[d0] + n0; x1 = g.xin[d1] + n1;   // the two-pass iteration reads and writes the same buffer
     }
+    g.d[d0] = n0; g.d[d1] = n1;
+    g.x[d0] = x0; g.x[d1] = x1;
+    if (FIN == FIN_DRIFT) {
+        g.U[d0] = fma((T)g.h, x0, g.U[d0]);
+        g.U[d1] = fma((T)g.h, x1, g.U[d1]);
+    } else if (FIN == FIN_LEAP) {
+        const T u0 = g.U[d0], u1 = g.U[d1];
+        g.U[d0] = fma(-(T)g.h, x0, T(2) * u0 - g.Uold[d0]);
+        g.U[d1] = fma(-(T)g.h, x1, T(2) * u1 - g.Uold[d1]);
+        g.Uold[d0] = u0; g.Uold[d1] = u1;
+    }
+}
+
+// Fused Chebyshev iteration: one thread per edge or face forms the entity's
+// two mass rows eps_t (Mref_p x_t) over its tetrahedra (fixed order) from
+// the previous iterate, then r = b - M x, z = Pinv r, d = c1 d + c2 z and
+// the next iterate x + d into the other buffer.  The block keeps the DOF
+// offsets of its shot (plane * nnode + vertex offset, 32-bit within a
+// shot) in shared memory; the reference rows are warp-uniform constant reads.
+template <class T, int FIN>
+__global__ void __launch_bounds__(128) t2_cheb_kernel(unsigned long long NE, const T2Shot *__restrict__ sh, int ns,
+                                                     const unsigned *__restrict__ ofs, GArgs<T> g)
+{
+    __shared__ unsigned sO[120];
+    const unsigned long long e0 = blockIdx.x * (unsigned long long)blockDim.x;
+    const int sb = shot_of(sh, ns, e0 < NE ? e0 : NE - 1, 1);
+    for (int q = threadIdx.x; q < 120; q += blockDim.x) sO[q] = ofs[(size_t)sb * 120 + q];
+    __syncthreads();
+    const unsigned long long e = e0 + threadIdx.x;
+    if (e >= NE) return;
+    const int si = shot_of(sh, ns, e, 1);
+    const T2Shot S = sh[si];
+    const unsigned *O = si == sb ? sO : ofs + (size_t)si * 120;
+    const unsigned nn = (unsigned)S.nnode;
+    const unsigned el = (unsigned)(e - S.ent0);
+    const int et = (int)(el / nn);
+    const unsigned v = el - (unsigned)et * nn;
+    const unsigned nx1 = S.n[0] + 1, ny1 = S.n[1] + 1;
+    const int i = (int)(v % nx1), j = (int)((v / nx1) % ny1), k = (int)(v / (nx1 * ny1));
+    const int x3[3] = {i, j, k};
+    const int ax = c2_axes[et];
+    bool dead = false;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        const int in = (ax >> q) & 1;
+        if (x3[q] + in > S.n[q]) dead = true;
+        if (!in && (x3[q] == 0 || x3[q] == S.n[q])) dead = true;
+    }
+    const int pl0 = et < 7 ? et : 14 + 2 * (et - 7), pl1 = et < 7 ? et + 7 : pl0 + 1;
+    const unsigned long long d0 = S.dof0 + (unsigned long long)pl0 * nn + v;
+    const unsigned long long d1 = S.dof0 + (unsigned long long)pl1 * nn + v;
+    if (dead) {
+        g.x[d0] = T(0); g.x[d1] = T(0); g.d[d0] = T(0); g.d[d1] = T(0);
+        return;
+    }
+    const T *xs = g.xin + S.dof0;
+    const unsigned ncx = S.n[0], ncxy = ncx * S.n[1], nxy = nx1 * ny1;
+    T y0 = T(0), y1 = T(0);
+    for (int q = 0; q < c2_ninc[et]; ++q) {
+        const int w = c2_inc[et][q];
+        const int p = w & 7, ob = (w >> 3) & 7, la = (w >> 6) & 31, lb = (w >> 11) & 31;
+        const int ci = i - (ob & 1), cj = j - ((ob >> 1) & 1), ck = k - ((ob >> 2) & 1);
+        if (ci < 0 || cj < 0 || ck < 0 || ci >= S.n[0] || cj >= S.n[1] || ck >= S.n[2]) continue;
+        const unsigned cube = (unsigned)ci + ncx * cj + ncxy * ck;
+        const unsigned v0 = (unsigned)ci + nx1 * cj + nxy * ck;
+        const unsigned *Op = O + p * 20;
+        T r0 = T(0), r1 = T(0);
+#pragma unroll
+        for (int b = 0; b < 20; ++b) {
+            const T xb = xs[v0 + Op[b]];
+            r0 = fma(mref<T>(p, la, b), xb, r0);
+            r1 = fma(mref<T>(p, lb, b), xb, r1);
+        }
+        const T ep = g.eps[S.tet0 + (unsigned long long)p * S.ncube + cube];
+        y0 = fma(ep, r0, y0);
+        y1 = fma(ep, r1, y1);
+    }
+    const T r0 = g.b[d0] - y0, r1 = g.b[d1] - y1;
+    const T q00 = g.pinv[e], q01 = g.pinv[NE + e], q11 = g.pinv[2 * NE + e];
+    const T z0 = fma(q00, r0, q01 * r1), z1 = fma(q01, r0, q11 * r1);
+    const T n0 = fma((T)g.c1, g.d[d0], (T)g.c2 * z0), n1 = fma((T)g.c1, g.d[d1], (T)g.c2 * z1);
+    const T x0 = g.xin[d0] + n0, x1 = g.xin[d1] + n1;
     g.d[d0] = n0; g.d[d1] = n1;
     g.x[d0] = x0; g.x[d1] = x1;
     if (FIN == FIN_DRIFT) {
@@ -679,6 +838,34 @@ template <class T> __global__ void t2_scale_kernel(unsigned long long n, T *__re
     if (i < n) x[i] = (T)((double)x[i] * s);
 }
 
+// Gradient contraction of the adjoint: grad_t += c * Z_t . (Mref_p Y_t), the
+// element product in the run precision, the sum over time in FP64.
+template <class T>
+__global__ void __launch_bounds__(128) t2_grad_kernel(unsigned long long NT, const T2Shot *__restrict__ sh, int ns,
+                                                     const T *__restrict__ Z, const T *__restrict__ Y, double c,
+                                                     double *__restrict__ grad)
+{
+    const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (t >= NT) return;
+    const T2Shot S = sh[shot_of(sh, ns, t, 0)];
+    const TetAddr ta = tet_addr(S, t - S.tet0);
+    T yv[20];
+#pragma unroll
+    for (int b = 0; b < 20; ++b) yv[b] = Y[ta.dof(b)];
+    const int p = ta.p;
+    T s = T(0);
+#pragma unroll 4
+    for (int a = 0; a < 20; ++a) {
+        T r = T(0);
+#pragma unroll
+        for (int b = 0; b < 20; ++b) r = fma(mref<T>(p, a, b), yv[b], r);
+        s = fma(Z[ta.dof(a)], r, s);
+    }
+    grad[t] += c * (double)s;
+}
+
+__global__ void t2_set_kernel(int *p, int v) { *p = v; }
+
 constexpr int kDotBlocks = 512;
 
 unsigned blocks(unsigned long long n, int b) { return (unsigned)((n + b - 1) / b); }
@@ -707,10 +894,13 @@ struct Tet2Sim : Sim {
     std::vector<Dip> dips;
     std::vector<std::array<size_t, 20>> rec_dof;
     std::vector<std::array<double, 60>> rec_w;
-    DevBuf d_shots, d_eps, d_pinv, d_U, d_Uold, d_P, d_Pc, d_x, d_d, d_b, d_YtM, d_YtK, d_ctl, d_part;
+    DevBuf d_shots, d_ofs, d_eps, d_pinv, d_U, d_Uold, d_P, d_Pc, d_x, d_xs, d_d, d_b, d_YtM, d_YtK, d_ctl, d_part;
     DevBuf d_src_dof, d_src_ptr, d_src_dip, d_src_coef, d_src_g, d_rec_dof, d_rec_w, d_tr;
     std::vector<double> cheb_c1, cheb_c2;
     double cheb_c0 = 0.0;
+    // adjoint: snapshots of (U, P) at segment starts of the recorded run
+    int ckpt_nsnap = 0, rec_nsteps = -1, rec_seg = 0;
+    DevBuf d_snap;
 
     Tet2Sim(const ems_tetfem_params *p, const std::vector<std::array<int, 3>> &cells) : Sim(Kind::TETFEM), P(*p)
     {
@@ -750,9 +940,26 @@ struct Tet2Sim : Sim {
         }
         d_shots.alloc(sh.size() * sizeof(T2Shot));
         EMS_CUDA(cudaMemcpy(d_shots.p, sh.data(), sh.size() * sizeof(T2Shot), cudaMemcpyHostToDevice));
+        // per shot: offset of local DOF b of type p from the cube's corner node
+        std::vector<unsigned> of(shots.size() * 120);
+        const Ref &R = ref();
+        for (size_t si = 0; si < shots.size(); ++si) {
+            const ShotH &S = shots[si];
+            EMS_CHECK_ARG(kPlanes * S.nnode < ((size_t)1 << 32), "shot too large for 32-bit DOF offsets");
+            const size_t nx1 = S.n[0] + 1, nxy = nx1 * (S.n[1] + 1);
+            for (int p = 0; p < 6; ++p) {
+                const Kuhn k = kuhn(p);
+                for (int b = 0; b < 20; ++b) {
+                    const int *vo = k.vert[R.low[p][b]];
+                    of[si * 120 + 20 * p + b] = (unsigned)(R.plane[p][b] * S.nnode + vo[0] + vo[1] * nx1 + vo[2] * nxy);
+                }
+            }
+        }
+        d_ofs.alloc(of.size() * 4);
+        EMS_CUDA(cudaMemcpy(d_ofs.p, of.data(), of.size() * 4, cudaMemcpyHostToDevice));
         const size_t w = fp64 ? 8 : 4;
         d_U.alloc(ndof * w); d_Uold.alloc(ndof * w); d_P.alloc(ndof * 8);
-        d_x.alloc(ndof * w); d_d.alloc(ndof * w); d_b.alloc(ndof * w);
+        d_x.alloc(ndof * w); d_xs.alloc(ndof * w); d_d.alloc(ndof * w); d_b.alloc(ndof * w);
         if (!fp64) d_Pc.alloc(ndof * 4);
         d_YtM.alloc(20 * ntet * w);
         d_YtK.alloc(20 * ntet * 8);
@@ -775,6 +982,14 @@ struct Tet2Sim : Sim {
         EMS_CUDA(cudaMemcpyToSymbol(c2_M64, R.M, sizeof(R.M)));
         EMS_CUDA(cudaMemcpyToSymbol(c2_M32, m32, sizeof(m32)));
         EMS_CUDA(cudaMemcpyToSymbol(c2_C, R.C, sizeof(R.C)));
+        float c32[6][20][12];
+        for (int p = 0; p < 6; ++p)
+            for (int a = 0; a < 20; ++a)
+                for (int q = 0; q < 12; ++q) {
+                    c32[p][a][q] = (float)R.C[p][a][q];
+                    if ((double)c32[p][a][q] != R.C[p][a][q]) throw Error{EMS_ERR_CUDA, "curl coefficient not exact in FP32"};
+                }
+        EMS_CUDA(cudaMemcpyToSymbol(c2_C32, c32, sizeof(c32)));
         EMS_CUDA(cudaMemcpyToSymbol(c2_ninc, R.ninc, sizeof(R.ninc)));
         EMS_CUDA(cudaMemcpyToSymbol(c2_inc, R.inc, sizeof(R.inc)));
         EMS_CUDA(cudaMemcpyToSymbol(c2_axes, R.axes, sizeof(R.axes)));
@@ -807,6 +1022,7 @@ struct Tet2Sim : Sim {
         eps_h.assign(eps_r, eps_r + ntet);
         ready = false;
         y_valid = false;
+        rec_nsteps = -1;
     }
 
     template <class T> void launch_pinv_and_eps()
@@ -856,11 +1072,21 @@ struct Tet2Sim : Sim {
     }
     template <class T> const T *rhs_P() const { return fp64 ? reinterpret_cast<const T *>(d_P.p) : reinterpret_cast<const T *>(d_Pc.p); }
 
+    // Stiffness element pass into d_YtK: FP64 for FP64 runs, double-float for FP32
+    template <class T> void enqueue_stiff(const T *u)
+    {
+        if (std::is_same<T, float>::value)
+            t2_stiff_df_kernel<<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), (int)shots.size(),
+                                                                      reinterpret_cast<const float *>(u), d_YtK.as<double>());
+        else
+            t2_stiff_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), (int)shots.size(), u,
+                                                                           d_YtK.as<double>());
+    }
+
     // f = K u (element pass + entity pass), u and out device vectors
     template <class T> int enqueue_force(const T *u, T *out)
     {
-        t2_stiff_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), (int)shots.size(), u,
-                                                                       d_YtK.as<double>());
+        enqueue_stiff<T>(u);
         GArgs<T> g = gargs<T>();
         g.Yt = d_YtK.p;
         g.out = out;
@@ -869,35 +1095,123 @@ struct Tet2Sim : Sim {
         return 2;
     }
 
-    // x = q(M) b; the last iteration applies FIN with factor h
-    template <class T, int FIN> int enqueue_solve(const T *b, double h)
+    // x = q(M) b; the last iteration applies FIN with factor h (to U, or to
+    // `target` when given); the iterate ends in `xo` (default: the solver's
+    // x).  Two forms of an iteration, chosen per handle by timing
+    // (choose_iteration): fused, one entity pass that forms the mass rows
+    // from the previous iterate and writes the next one to the other of two
+    // buffers (the iterates alternate, starting where the last lands in
+    // xo); or two-pass, the mass element pass into the per-tetrahedron
+    // array, then the entity pass updating x in place.
+    bool cheb_fused = false;
+    template <class T, int FIN> int enqueue_solve(const T *b, double h, T *xo = nullptr, T *target = nullptr)
     {
         const int ns = (int)shots.size();
         GArgs<T> g = gargs<T>();
         g.b = b;
         g.c0 = cheb_c0;
         g.h = h;
+        g.eps = d_eps.as<T>();
         g.Yt = d_YtM.p;
-        int nl = 0;
+        if (!xo) xo = d_x.as<T>();
+        if (target) g.U = target;
+        T *buf[2] = {xo, cheb_fused ? d_xs.as<T>() : xo};
+        int cur = cheb_fused ? (mass_iters - 1) % 2 : 0;   // buffer of the first iterate
+        g.x = buf[cur];
         if (mass_iters == 1) {
             t2_gather_kernel<T, T, G_CHEB0, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
             return 1;
         }
         t2_gather_kernel<T, T, G_CHEB0, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
-        ++nl;
+        int nl = 1;
         for (int k = 1; k < mass_iters; ++k) {
-            t2_mass_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_eps.as<T>(),
-                                                                          d_x.as<T>(), d_YtM.as<T>());
+            g.xin = buf[cur];
+            cur ^= cheb_fused ? 1 : 0;
+            g.x = buf[cur];
             g.c1 = cheb_c1[k];
             g.c2 = cheb_c2[k];
-            if (k + 1 == mass_iters)
-                t2_gather_kernel<T, T, G_CHEB, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
-            else
-                t2_gather_kernel<T, T, G_CHEB, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
-            nl += 2;
+            const bool last = k + 1 == mass_iters;
+            if (cheb_fused) {
+                if (last) t2_cheb_kernel<T, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, d_ofs.as<unsigned>(), g);
+                else t2_cheb_kernel<T, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, d_ofs.as<unsigned>(), g);
+                ++nl;
+            } else {
+                t2_mass_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_eps.as<T>(), g.xin,
+                                                                              d_YtM.as<T>());
+                if (last) t2_gather_kernel<T, T, G_CHEB, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+                else t2_gather_kernel<T, T, G_CHEB, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+                nl += 2;
+            }
         }
         return nl;
     }
+
+    // Times `n` iterations of the current form in a replayed graph (x, d and
+    // b are scratch here); ms per iteration.
+    template <class T> double time_iterations(int n)
+    {
+        const int ns = (int)shots.size();
+        GArgs<T> g = gargs<T>();
+        g.b = d_b.as<T>();
+        g.eps = d_eps.as<T>();
+        g.Yt = d_YtM.p;
+        g.c1 = 0.5; g.c2 = 0.1;
+        T *buf[2] = {d_x.as<T>(), cheb_fused ? d_xs.as<T>() : d_x.as<T>()};
+        cudaGraph_t gr = nullptr;
+        cudaGraphExec_t ex = nullptr;
+        EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < n; ++k) {
+            g.xin = buf[k & 1];
+            g.x = buf[(k + 1) & 1];
+            if (cheb_fused) {
+                t2_cheb_kernel<T, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, d_ofs.as<unsigned>(), g);
+            } else {
+                t2_mass_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_eps.as<T>(), g.xin,
+                                                                              d_YtM.as<T>());
+                t2_gather_kernel<T, T, G_CHEB, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+            }
+        }
+        cudaError_t ce = cudaStreamEndCapture(stream, &gr);
+        if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
+        ce = cudaGraphInstantiate(&ex, gr, 0);
+        if (ce != cudaSuccess) {
+            cudaGraphDestroy(gr);
+            throw Error{EMS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
+        }
+        float best = 1e30f;
+        for (int r = 0; r < 3; ++r) {   // the first replay warms the caches
+            EMS_CUDA(cudaEventRecord(ev0, stream));
+            EMS_CUDA(cudaGraphLaunch(ex, stream));
+            EMS_CUDA(cudaEventRecord(ev1, stream));
+            EMS_CUDA(cudaStreamSynchronize(stream));
+            float t = 0;
+            EMS_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
+            if (r > 0) best = std::min(best, t);
+        }
+        cudaGraphExecDestroy(ex);
+        cudaGraphDestroy(gr);
+        return best / n;
+    }
+
+    // The faster form of the Chebyshev iteration on this handle's meshes
+    // (EMS_TET2_ITERATION=fused|twopass forces one).
+    template <class T> void choose_iteration()
+    {
+        const char *force = std::getenv("EMS_TET2_ITERATION");
+        if (force && (!std::strcmp(force, "fused") || !std::strcmp(force, "twopass"))) {
+            cheb_fused = !std::strcmp(force, "fused");
+            return;
+        }
+        d_x.zero(stream); d_xs.zero(stream); d_d.zero(stream); d_b.zero(stream);
+        cheb_fused = false;
+        const double two = time_iterations<T>(8);
+        cheb_fused = true;
+        const double fused = time_iterations<T>(8);
+        cheb_fused = fused < two;
+        iter_ms[0] = two;
+        iter_ms[1] = fused;
+    }
+    double iter_ms[2] = {0.0, 0.0};
 
     double dot_host(const void *x, const void *y)
     {
@@ -948,6 +1262,7 @@ struct Tet2Sim : Sim {
     {
         cheb_coefficients();
         if (fp64) launch_pinv_and_eps<double>(); else launch_pinv_and_eps<float>();
+        if (fp64) choose_iteration<double>(); else choose_iteration<float>();
         // the power iteration uses the solver's scratch; the state (U, Uold, P) is kept
         DevBuf keep;
         keep.alloc(ndof * (fp64 ? 8 : 4));
@@ -1023,6 +1338,7 @@ struct Tet2Sim : Sim {
         d.kind = waveform;
         d.f0n = f0 * tscale;
         dips.push_back(d);
+        rec_nsteps = -1;
     }
 
     void add_receiver(int shot, const double pos[3])
@@ -1040,6 +1356,7 @@ struct Tet2Sim : Sim {
             for (int q = 0; q < 3; ++q) w[3 * a + q] = val[a][q];
         rec_dof.push_back(d);
         rec_w.push_back(w);
+        rec_nsteps = -1;
     }
 
     template <class V> void up(DevBuf &b, const std::vector<V> &v)
@@ -1118,12 +1435,18 @@ struct Tet2Sim : Sim {
         EMS_CUDA(cudaMemsetAsync(d_ctl.p, 0, 16, stream));
     }
 
-    template <class T> int enqueue_step()
+    size_t snap_bytes() const;
+    void save_snapshot(int s);
+    void set_checkpoints(int nsnap);
+    template <class T> void backward_t(const double *tg, double *grad);
+    void backward(const double *tg, size_t ntg, double *grad, size_t ngrad);
+
+    template <class T> int enqueue_step(bool sample = true)
     {
         const int ns = (int)shots.size();
         int nl = 0;
         const int nd = (int)std::max<size_t>(dips.size(), 1);
-        if (nobs > 0) {
+        if (sample && nobs > 0) {
             t2_sample_kernel<T><<<blocks((unsigned long long)nobs * 32, 128), 128, 0, stream>>>(
                 nobs, d_rec_dof.as<unsigned long long>(), d_rec_w.as<double>(), d_U.as<T>(), d_ctl.as<int>(), P.time_frequency,
                 nsamp, d_tr.as<double>());
@@ -1136,8 +1459,7 @@ struct Tet2Sim : Sim {
             t2_axpy_kernel<T><<<blocks(ndof, 256), 256, 0, stream>>>(ndof, d_U.as<T>(), d_x.as<T>(), 0.5 * sub[0]);
             ++nl;
             for (int q = 0; q < nq; ++q) {
-                t2_stiff_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_U.as<T>(),
-                                                                               d_YtK.as<double>());
+                enqueue_stiff<T>(d_U.as<T>());
                 GArgs<T> g = gargs<T>();
                 g.Yt = d_YtK.p;
                 g.a = sub[q];
@@ -1169,6 +1491,7 @@ struct Tet2Sim : Sim {
     template <class T> void run_t(int nsteps)
     {
         if (!ready) setup();
+        rec_nsteps = -1;   // the source table and counters below belong to this run
         std::vector<double> times;
         prepare_run(nsteps, times);
         long long launches = 0;
@@ -1193,8 +1516,16 @@ struct Tet2Sim : Sim {
             cudaError_t ce = cudaStreamEndCapture(stream, &G.g);
             if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
             EMS_CUDA(cudaGraphInstantiate(&G.exec, G.g, 0));
-            for (int st = 0; st < nsteps; ++st) EMS_CUDA(cudaGraphLaunch(G.exec, stream));
+            const bool record = ckpt_nsnap > 0 && symp() && cur_time == 0.0 && fresh;
+            const int seg = record ? (nsteps + ckpt_nsnap - 1) / ckpt_nsnap : nsteps;
+            if (record) d_snap.ensure((size_t)ckpt_nsnap * snap_bytes());
+            for (int st = 0; st < nsteps; ++st) {
+                if (record && st % seg == 0) save_snapshot(st / seg);
+                EMS_CUDA(cudaGraphLaunch(G.exec, stream));
+            }
             launches += (long long)per * nsteps;
+            if (record) { rec_nsteps = nsteps; rec_seg = seg; }
+            else rec_nsteps = -1;
         }
         EMS_CUDA(cudaGetLastError());
         EMS_CUDA(cudaEventRecord(ev1, stream));
@@ -1204,6 +1535,7 @@ struct Tet2Sim : Sim {
         last_ms = ms;
         last_launches = launches;
         cur_time += nsteps * dtn;
+        fresh = fresh && nsteps == 0;
         const size_t ntr = (size_t)std::max(nobs, 1) * std::max(nsamp, 1) * 4;
         traces.assign(ntr, 0.0);
         EMS_CUDA(cudaMemcpy(traces.data(), d_tr.p, ntr * 8, cudaMemcpyDeviceToHost));
@@ -1261,6 +1593,8 @@ struct Tet2Sim : Sim {
             EMS_CUDA(cudaMemcpy(d_Pc.p, f.data(), ndof * 4, cudaMemcpyHostToDevice));
         }
         y_valid = false;
+        fresh = false;
+        rec_nsteps = -1;
     }
 
     void save(const char *path) const override
@@ -1283,61 +1617,33 @@ struct Tet2Sim : Sim {
         }
     }
 
+    bool fresh = true;   // the state is the reset state (zero fields at t = 0)
     void reset() override
     {
-        d_U.zero(stream); d_Uold.zero(stream); d_P.zero(stream); d_x.zero(stream); d_d.zero(stream); d_b.zero(stream);
+        d_U.zero(stream); d_Uold.zero(stream); d_P.zero(stream); d_x.zero(stream); d_xs.zero(stream); d_d.zero(stream);
+        d_b.zero(stream);
         if (d_Pc.p) d_Pc.zero(stream);
         cur_time = 0.0;
+        fresh = true;
         y_valid = false;
         EMS_CUDA(cudaStreamSynchronize(stream));
     }
 
     void launch_shape(int b[3]) override { b[0] = 128; b[1] = b[2] = 1; }
 
-    // One Chebyshev iteration (mass element pass + entity pass) replayed in a
-    // graph of `launches` iterations; bytes: x, eps, b, d (read and write), x
-    // (write) and the block inverses once per iteration (a fused iteration's
-    // minimum; the per-tetrahedron values between the two passes are extra).
+    // One Chebyshev iteration in the handle's form replayed in a graph of
+    // `launches` iterations; bytes: x (read and written), b, d (read and
+    // written), the block inverses and eps once per iteration (a fused
+    // iteration's minimum: the neighbours' x re-read by the mass rows hit the
+    // caches; the two-pass form also moves the per-tetrahedron array).
     void time_dominant(int launches, double *ms, double *bytes, std::string *name) override
     {
         if (!ready) setup();
-        const int n = std::max(launches, 1);
-        const int ns = (int)shots.size();
-        auto body = [&](auto tag) {
-            using T = decltype(tag);
-            GArgs<T> g = gargs<T>();
-            g.b = d_b.as<T>();
-            g.Yt = d_YtM.p;
-            g.c1 = 0.5; g.c2 = 0.1;
-            cudaGraph_t gr = nullptr;
-            cudaGraphExec_t ex = nullptr;
-            EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-            for (int k = 0; k < n; ++k) {
-                t2_mass_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_eps.as<T>(),
-                                                                              d_x.as<T>(), d_YtM.as<T>());
-                t2_gather_kernel<T, T, G_CHEB, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
-            }
-            cudaError_t ce = cudaStreamEndCapture(stream, &gr);
-            if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
-            EMS_CUDA(cudaGraphInstantiate(&ex, gr, 0));
-            EMS_CUDA(cudaGraphLaunch(ex, stream));   // warm-up
-            EMS_CUDA(cudaEventRecord(ev0, stream));
-            EMS_CUDA(cudaGraphLaunch(ex, stream));
-            EMS_CUDA(cudaEventRecord(ev1, stream));
-            EMS_CUDA(cudaStreamSynchronize(stream));
-            cudaGraphExecDestroy(ex);
-            cudaGraphDestroy(gr);
-            float t = 0;
-            EMS_CUDA(cudaEventElapsedTime(&t, ev0, ev1));
-            *ms = t / n;
-            *bytes = (double)sizeof(T) * (6.0 * ndof + ntet + 3.0 * nent);
-        };
-        // the iteration runs on zeroed scratch: x, d and b are the solver's own buffers
-        d_x.zero(stream); d_d.zero(stream); d_b.zero(stream);
-        if (fp64) body(double()); else body(float());
+        d_x.zero(stream); d_xs.zero(stream); d_d.zero(stream); d_b.zero(stream);
+        *ms = fp64 ? time_iterations<double>(std::max(launches, 1)) : time_iterations<float>(std::max(launches, 1));
+        *bytes = (double)(fp64 ? 8 : 4) * (5.0 * ndof + ntet + 3.0 * nent);
         y_valid = false;
-        *name = fp64 ? "t2_mass_elem_kernel<double> + t2_gather_kernel<double, G_CHEB>"
-                     : "t2_mass_elem_kernel<float> + t2_gather_kernel<float, G_CHEB>";
+        *name = std::string(cheb_fused ? "t2_cheb_kernel<" : "t2_mass_elem_kernel + t2_gather_kernel<") + (fp64 ? "double>" : "float>");
     }
 
     // f = K u in the handle's precision (API DOF order)
@@ -1400,6 +1706,174 @@ struct Tet2Sim : Sim {
     }
 };
 
+// ---------------------------------------------------------------- adjoint
+// Reverse sweep of a recorded symplectic run (zero start state):
+//   forward step n (merged drifts): U += a_0/2 Y_0; for each substage q:
+//     P -= a_q (K U - f), Y_{q+1} = q(M) P, U += h_q Y_{q+1}
+//   reversed: for q = last..0: Z = q(M) Ubar, Pbar += h_q Z,
+//     grad -= h_q Z . dM/deps Y_{q+1}, Ubar -= a_q K Pbar; then the start
+//     drift (a_0/2, Y_0) and the receiver samples of step n (Ubar += w g).
+// dY/deps is taken as the derivative of M^-1 P (-q(M) M_t Y), within the
+// polynomial's error of the derivative of q(M) P.  Each segment between
+// snapshots is recomputed once, keeping (U, P) of its steps; each reversed
+// step recomputes its drift increments Y_0..Y_nsub from (U_n, P_n).  Ubar
+// accumulates the stiffness terms in FP64 (as P does forward) with a copy
+// in the run precision for the solves; Pbar is in the run precision.
+size_t Tet2Sim::snap_bytes() const { return ndof * ((fp64 ? 8 : 4) + 8); }
+
+void Tet2Sim::save_snapshot(int s)
+{
+    char *b = d_snap.as<char>() + (size_t)s * snap_bytes();
+    const size_t w = ndof * (fp64 ? 8 : 4);
+    EMS_CUDA(cudaMemcpyAsync(b, d_U.p, w, cudaMemcpyDeviceToDevice, stream));
+    EMS_CUDA(cudaMemcpyAsync(b + w, d_P.p, ndof * 8, cudaMemcpyDeviceToDevice, stream));
+}
+
+void Tet2Sim::set_checkpoints(int nsnap)
+{
+    EMS_CHECK_ARG(nsnap >= 0, "nsnap must be >= 0");
+    if (!symp()) throw Error{EMS_ERR_UNSUPPORTED, "the adjoint needs a symplectic integrator"};
+    ckpt_nsnap = nsnap;
+    rec_nsteps = -1;
+    if (nsnap == 0) d_snap.release();
+}
+
+template <class T> void Tet2Sim::backward_t(const double *tg, double *grad)
+{
+    const int ns = (int)shots.size(), nq = nsub();
+    const int nsteps = rec_nsteps, seg = rec_seg;
+    const size_t w = ndof * sizeof(T);
+    double sub[3], off[3];
+    substeps(sub, off);
+    double hq[3];
+    for (int k = 0; k < nq; ++k) hq[k] = 0.5 * sub[k] + (k + 1 < nq ? 0.5 * sub[k + 1] : 0.0);
+    // receiver adjoint loads: entries by DOF, table per step (zero off the sampling steps)
+    const int tf = P.time_frequency;
+    std::vector<std::array<size_t, 2>> ent;   // (dof, (r * 3 + c) * 20 + a)
+    for (int r = 0; r < nobs; ++r)
+        for (int a = 0; a < 20; ++a)
+            for (int c = 0; c < 3; ++c)
+                if (rec_w[r][3 * a + c] != 0.0 && !dead_dof(rec_dof[r][a])) ent.push_back({rec_dof[r][a], (size_t)(r * 3 + c) * 20 + a});
+    std::stable_sort(ent.begin(), ent.end(), [](const std::array<size_t, 2> &x, const std::array<size_t, 2> &y) { return x[0] < y[0]; });
+    std::vector<unsigned long long> rd;
+    std::vector<int> rp, ri;
+    std::vector<double> rc;
+    for (size_t q = 0; q < ent.size(); ++q) {
+        if (q == 0 || ent[q][0] != ent[q - 1][0]) { rd.push_back(ent[q][0]); rp.push_back((int)q); }
+        const size_t rcid = ent[q][1] / 20, a = ent[q][1] % 20;
+        ri.push_back((int)rcid);
+        rc.push_back(rec_w[rcid / 3][3 * a + rcid % 3]);
+    }
+    rp.push_back((int)ent.size());
+    const int nrd = (int)rd.size(), nd3 = std::max(3 * nobs, 1);
+    std::vector<double> gt((size_t)nsteps * nd3, 0.0);
+    for (int n = 0; n < nsteps; n += tf)
+        for (int r = 0; r < nobs; ++r)
+            for (int c = 0; c < 3; ++c) gt[(size_t)n * nd3 + 3 * r + c] = tg[((size_t)r * nsamp + n / tf) * 4 + 1 + c];
+    DevBuf a_dof, a_ptr, a_idx, a_coef, a_g;
+    up(a_dof, rd); up(a_ptr, rp); up(a_idx, ri); up(a_coef, rc); up(a_g, gt);
+    // buffers: the segment's states, drift increments, adjoint state, gradient, end state
+    DevBuf segb, Ys, Ub, Ubc, Pb, gd, keepU, keepP;
+    segb.alloc((size_t)seg * snap_bytes());
+    Ys.alloc((size_t)(nq + 1) * w);
+    Ub.alloc(ndof * 8);
+    Pb.alloc(w);
+    if (!fp64) Ubc.alloc(w);
+    gd.alloc(ntet * 8);
+    keepU.alloc(w);
+    keepP.alloc(ndof * 8);
+    EMS_CUDA(cudaMemcpyAsync(keepU.p, d_U.p, w, cudaMemcpyDeviceToDevice, stream));
+    EMS_CUDA(cudaMemcpyAsync(keepP.p, d_P.p, ndof * 8, cudaMemcpyDeviceToDevice, stream));
+    Ub.zero(stream); Pb.zero(stream); gd.zero(stream);
+    if (Ubc.p) Ubc.zero(stream);
+    T *Ubr = fp64 ? Ub.as<T>() : Ubc.as<T>();   // Ubar in the run precision (right-hand side of the solves)
+    auto Y = [&](int k) { return Ys.as<T>() + (size_t)k * ndof; };
+    const int nd = (int)std::max<size_t>(dips.size(), 1);
+    int *ctl = d_ctl.as<int>();
+    auto narrowP = [&]() {
+        if (!fp64) t2_narrow_kernel<T><<<blocks(ndof, 256), 256, 0, stream>>>(ndof, d_P.as<double>(), d_Pc.as<T>());
+    };
+    for (int s = (nsteps - 1) / seg; s >= 0; --s) {
+        const int n0 = s * seg, n1 = std::min(nsteps, n0 + seg);
+        // recompute the segment from its snapshot, keeping (U_n, P_n)
+        const char *sb = d_snap.as<char>() + (size_t)s * snap_bytes();
+        EMS_CUDA(cudaMemcpyAsync(d_U.p, sb, w, cudaMemcpyDeviceToDevice, stream));
+        EMS_CUDA(cudaMemcpyAsync(d_P.p, sb + w, ndof * 8, cudaMemcpyDeviceToDevice, stream));
+        narrowP();
+        enqueue_solve<T, FIN_NONE>(rhs_P<T>(), 0.0);
+        t2_set_kernel<<<1, 1, 0, stream>>>(ctl, n0);
+        for (int n = n0; n < n1; ++n) {
+            char *dst = segb.as<char>() + (size_t)(n - n0) * snap_bytes();
+            EMS_CUDA(cudaMemcpyAsync(dst, d_U.p, w, cudaMemcpyDeviceToDevice, stream));
+            EMS_CUDA(cudaMemcpyAsync(dst + w, d_P.p, ndof * 8, cudaMemcpyDeviceToDevice, stream));
+            if (n + 1 < n1) enqueue_step<T>(false);
+        }
+        // reversed steps
+        for (int n = n1 - 1; n >= n0; --n) {
+            const char *src = segb.as<char>() + (size_t)(n - n0) * snap_bytes();
+            EMS_CUDA(cudaMemcpyAsync(d_U.p, src, w, cudaMemcpyDeviceToDevice, stream));
+            EMS_CUDA(cudaMemcpyAsync(d_P.p, src + w, ndof * 8, cudaMemcpyDeviceToDevice, stream));
+            narrowP();
+            t2_set_kernel<<<1, 1, 0, stream>>>(ctl, n);
+            // drift increments of step n
+            enqueue_solve<T, FIN_DRIFT>(rhs_P<T>(), 0.5 * sub[0], Y(0));
+            for (int q = 0; q < nq; ++q) {
+                enqueue_stiff<T>(d_U.as<T>());
+                GArgs<T> g = gargs<T>();
+                g.Yt = d_YtK.p;
+                g.a = sub[q];
+                t2_gather_kernel<T, double, G_KICK, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+                if (nsrc > 0)
+                    t2_source_kernel<T, 0><<<blocks(nsrc, 128), 128, 0, stream>>>(
+                        nsrc, d_src_dof.as<unsigned long long>(), d_src_ptr.as<int>(), d_src_dip.as<int>(), d_src_coef.as<double>(),
+                        d_src_g.as<double>(), ctl, nq, q, nd, sub[q], d_P.as<double>(), fp64 ? nullptr : d_Pc.as<T>());
+                enqueue_solve<T, FIN_DRIFT>(rhs_P<T>(), hq[q], Y(q + 1));
+            }
+            // adjoint of the substages
+            for (int q = nq - 1; q >= 0; --q) {
+                enqueue_solve<T, FIN_DRIFT>(Ubr, hq[q], d_x.as<T>(), Pb.as<T>());
+                t2_grad_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_x.as<T>(), Y(q + 1),
+                                                                         -hq[q], gd.as<double>());
+                enqueue_stiff<T>(Pb.as<T>());
+                GArgs<T> g = gargs<T>();
+                g.Yt = d_YtK.p;
+                g.a = sub[q];
+                g.P = Ub.as<double>();
+                g.Pc = fp64 ? nullptr : Ubc.as<T>();
+                t2_gather_kernel<T, double, G_KICK, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+            }
+            enqueue_solve<T, FIN_DRIFT>(Ubr, 0.5 * sub[0], d_x.as<T>(), Pb.as<T>());
+            t2_grad_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_x.as<T>(), Y(0),
+                                                                     -0.5 * sub[0], gd.as<double>());
+            if (nrd > 0 && n % tf == 0)
+                t2_source_kernel<T, 0><<<blocks(nrd, 128), 128, 0, stream>>>(
+                    nrd, a_dof.as<unsigned long long>(), a_ptr.as<int>(), a_idx.as<int>(), a_coef.as<double>(), a_g.as<double>(),
+                    ctl, 1, 0, nd3, 1.0, Ub.as<double>(), fp64 ? nullptr : Ubc.as<T>());
+            EMS_CUDA(cudaGetLastError());
+        }
+    }
+    EMS_CUDA(cudaMemcpyAsync(d_U.p, keepU.p, w, cudaMemcpyDeviceToDevice, stream));
+    EMS_CUDA(cudaMemcpyAsync(d_P.p, keepP.p, ndof * 8, cudaMemcpyDeviceToDevice, stream));
+    narrowP();
+    y_valid = false;
+    std::vector<double> g(ntet);
+    EMS_CUDA(cudaStreamSynchronize(stream));
+    EMS_CUDA(cudaMemcpy(g.data(), gd.p, ntet * 8, cudaMemcpyDeviceToHost));
+    // dJ/deps_r: the mass scales with eps_r; back to the API order
+    for (size_t t = 0; t < ntet; ++t) grad[t] = g[tet_index(t)];
+}
+
+void Tet2Sim::backward(const double *tg, size_t ntg, double *grad, size_t ngrad)
+{
+    EMS_CHECK_ARG(tg && grad, "trace gradient and output required");
+    EMS_CHECK_ARG(ngrad == ntet, "gradient must have one value per tetrahedron");
+    if (rec_nsteps < 0 || d_snap.p == nullptr) throw Error{EMS_ERR_STATE, "no recorded run: set checkpoints, reset and run first"};
+    EMS_CHECK_ARG(ntg == (size_t)nobs * nsamp * 4, "trace gradient must have the shape of the traces");
+    if (fp64) backward_t<double>(tg, grad); else backward_t<float>(tg, grad);
+    for (size_t t = 0; t < ntet; ++t)
+        if (!std::isfinite(grad[t])) throw Error{EMS_ERR_NOT_FINITE, "the gradient holds a NaN or an Inf"};
+}
+
 bool is_tet2(const Sim *s) { return dynamic_cast<const Tet2Sim *>(s) != nullptr; }
 
 Sim *make_tet2(const ems_tetfem_params *p, const std::vector<std::array<int, 3>> &cells) { return new Tet2Sim(p, cells); }
@@ -1425,6 +1899,13 @@ void tet2_apply_stiffness(Sim *s, const double *u, double *f, size_t n)
     t->apply_stiffness(u, f);
 }
 void tet2_energy(Sim *s, double *out, int n) { static_cast<Tet2Sim *>(s)->energy(out, n); }
+void tet2_set_checkpoints(Sim *s, int nsnap) { static_cast<Tet2Sim *>(s)->set_checkpoints(nsnap); }
+void tet2_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, double *grad_sigma, size_t ngrad)
+{
+    if (grad_sigma) throw Error{EMS_ERR_UNSUPPORTED, "order-2 tetrahedra have no conductivity gradient"};
+    static_cast<Tet2Sim *>(s)->backward(trace_grad, ntg, grad_eps, ngrad);
+}
+size_t tet2_ntet(const Sim *s) { return static_cast<const Tet2Sim *>(s)->ntet; }
 
 // Reference matrices of the second-order element as the solver computes them.
 void tet2_element_matrices(int type, double *M, double *K)

@@ -3155,14 +3155,9 @@ void tetfem_apply_stiffness(Sim *s, const double *u, double *f, size_t n)
     t->apply_stiffness(u, f);
 }
 
-static void need_order1(const Sim *s, const char *what)
-{
-    if (is_tet2(s)) throw Error{EMS_ERR_UNSUPPORTED, std::string(what) + " is implemented for order-1 tetrahedra only"};
-}
-
 void tetfem_set_checkpoints(Sim *s, int nsnap)
 {
-    need_order1(s, "the adjoint");
+    if (is_tet2(s)) return tet2_set_checkpoints(s, nsnap);
     static_cast<TetFemSim *>(s)->set_checkpoints(nsnap);
 }
 void tetfem_energy(Sim *s, double *out, int n)
@@ -3173,24 +3168,23 @@ void tetfem_energy(Sim *s, double *out, int n)
 
 void tetfem_backward(Sim *s, const double *trace_grad, size_t ntg, double *grad_eps, double *grad_sigma, size_t ngrad)
 {
-    need_order1(s, "the adjoint");
+    if (is_tet2(s)) return tet2_backward(s, trace_grad, ntg, grad_eps, grad_sigma, ngrad);
     static_cast<TetFemSim *>(s)->backward(trace_grad, ntg, grad_eps, ngrad, grad_sigma);
 }
 
 void tetfem_gradient(Sim *s, int nsteps, int nsnap, int kind, const double *obs, const double *band, double *misfit,
                      double *grad, double *grad_sigma, size_t ngrad)
 {
-    need_order1(s, "the adjoint");
-    auto *f = static_cast<TetFemSim *>(s);
     EMS_CHECK_ARG(nsteps > 0 && nsnap > 0, "nsteps and nsnap must be positive");
     EMS_CHECK_ARG(obs && misfit && grad, "observed traces, misfit and gradient required");
-    EMS_CHECK_ARG(ngrad == f->ntet, "gradient must have one value per tetrahedron");
-    f->set_checkpoints(nsnap);
-    f->reset();
-    f->run(nsteps);
-    std::vector<double> tg(f->traces.size());
-    trace_misfit(kind, f->nobs, f->nsamp, f->traces.data(), obs, misfit, tg.data(), band);
-    f->backward(tg.data(), tg.size(), grad, ngrad, grad_sigma);
+    EMS_CHECK_ARG(ngrad == (is_tet2(s) ? tet2_ntet(s) : static_cast<TetFemSim *>(s)->ntet),
+                  "gradient must have one value per tetrahedron");
+    tetfem_set_checkpoints(s, nsnap);
+    s->reset();
+    s->run(nsteps);
+    std::vector<double> tg(s->traces.size());
+    trace_misfit(kind, s->nobs, s->nsamp, s->traces.data(), obs, misfit, tg.data(), band);
+    tetfem_backward(s, tg.data(), tg.size(), grad, grad_sigma, ngrad);
 }
 
 void tetfem_time_step(const Sim *s, double *dt, double *lim)

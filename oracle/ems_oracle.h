@@ -122,6 +122,9 @@ long orc_tet2_locate(int nx, int ny, int nz, const double x[3], double val[20][3
 double orc_tet2_lambda_max(int nx, int ny, int nz, const double *eps_r, const double *mu_r, int mass_iters, int iters);
 double orc_tet2_energy(int nx, int ny, int nz, const double *eps_r, int mass_iters, const double *U, const double *P);
 int orc_tet2_run(const orc_tet_case *c, int mass_iters, int nsteps, double *U, double *P, double *traces);
+/* dJ/deps_r per tetrahedron (API order 6 * cell + p) of the symplectic loop
+ * from zero fields, given dJ/dtraces (nrec x nsamp x 4, column 0 ignored). */
+int orc_tet2_gradient(const orc_tet_case *c, int mass_iters, int nsteps, const double *trace_grad, double *grad_eps);
 
 /* ----------------------------------------- Adams-Bashforth-Moulton (hex) --- */
 typedef struct {

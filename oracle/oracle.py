@@ -342,7 +342,7 @@ def tet_apply_K(n, x):
 
 
 # ------------------------------------------------- second-order tetrahedra
-TET2_MASS_ITERS = 24
+TET2_MASS_ITERS = 28
 
 
 def tet2_sizes(n):
@@ -442,6 +442,23 @@ def tet2_run(n, eps_r, integrator, dt, nsteps, tf=1, dipoles=(), receivers=(), m
     if rc != 0:
         raise RuntimeError(f"orc_tet2_run failed: {rc}")
     return tr[:len(receivers), :nsamp], U, P
+
+
+def tet2_gradient(n, eps_r, integrator, dt, nsteps, trace_grad, tf=1, dipoles=(), receivers=(), mu_r=None,
+                  mass_iters=TET2_MASS_ITERS):
+    """dJ/deps_r per tetrahedron by the FP64 discrete adjoint of tet2_run
+    (symplectic integrators, zero initial fields)."""
+    _, _, ntet = tet2_sizes(n)
+    nsamp = (nsteps - 1) // tf + 1 if nsteps > 0 else 0
+    g = np.zeros((max(len(receivers), 1), max(nsamp, 1), 4))
+    if len(receivers):
+        g[:len(receivers), :nsamp] = np.asarray(trace_grad, np.float64).reshape(len(receivers), nsamp, 4)
+    c, keep = _tet_case(n, eps_r, integrator, dt, tf, dipoles, receivers, mu_r, None)
+    out = np.zeros(ntet)
+    rc = _t2lib().orc_tet2_gradient(C.byref(c), C.c_int(mass_iters), C.c_int(nsteps), _ptr(g), _ptr(out))
+    if rc != 0:
+        raise RuntimeError(f"orc_tet2_gradient failed: {rc}")
+    return out
 
 
 # ------------------------------------------------- Adams-Bashforth-Moulton (hex)

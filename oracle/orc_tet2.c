@@ -754,3 +754,118 @@ int orc_tet2_run(const orc_tet_case *c, int mass_iters, int nsteps, double *U, d
     free_t2mesh(&m);
     return 0;
 }
+
+/* ------------------------------------------------------------ adjoint ---
+ * Gradient of a receiver-trace functional with respect to the per-tet
+ * permittivity by the discrete adjoint of the symplectic loop of
+ * orc_tet2_run (drifts merged as the GPU merges them: U += a_0/2 Y at the
+ * start of a step, U += (a_q + a_{q+1})/2 Y after kick q).  Only the mass
+ * depends on eps; the derivative of the drift increment Y = q(M) P is taken
+ * as that of M^-1 P, -q(M) M_T Y, which differs from the derivative of the
+ * polynomial by the polynomial's own error (within 2 r^m, see the mass
+ * inverse above).  All forward states are kept (small cases only). */
+static void elem_contract(const t2mesh *m, const double *Z, const double *Y, double c, double *grad)
+{
+#pragma omp parallel for schedule(static)
+    for (long t = 0; t < (long)m->ntet; ++t) {
+        const long *gd = m->tet_dof + 20 * t;
+        const double *A = m->Mref[t % 6];
+        double s = 0.0;
+        for (int a = 0; a < 20; ++a) {
+            double r = 0.0;
+            for (int b = 0; b < 20; ++b) r += A[20 * a + b] * Y[gd[b]];
+            s += Z[gd[a]] * r;
+        }
+        grad[t] += c * s;
+    }
+}
+
+int orc_tet2_gradient(const orc_tet_case *c, int mass_iters, int nsteps, const double *trace_grad, double *grad_eps)
+{
+    if (c->sigma || c->integrator == ORC_LEAPFROG) return -2;
+    t2mesh m;
+    t2mass q;
+    build_t2mesh(&m, c->nx, c->ny, c->nz);
+    mass_setup(&q, &m, c->eps_r, mass_iters);
+    double *mi = mu_inverse(&m, c->mu_r);
+    const size_t n = m.ndof;
+    int nd = c->ndip, nr = c->nrec;
+    double (*dw)[20] = malloc(sizeof(double) * 20 * (nd > 0 ? nd : 1));
+    long (*de)[20] = malloc(sizeof(long) * 20 * (nd > 0 ? nd : 1));
+    for (int s = 0; s < nd; ++s) {
+        double val[20][3];
+        orc_tet2_locate(c->nx, c->ny, c->nz, c->dip_pos + 3 * s, val, de[s]);
+        const double *dir = c->dip_dir + 3 * s;
+        for (int a = 0; a < 20; ++a) dw[s][a] = (val[a][0] * dir[0] + val[a][1] * dir[1] + val[a][2] * dir[2]) * c->dip_amp[s];
+    }
+    double (*rw)[20][3] = malloc(sizeof(double) * 60 * (nr > 0 ? nr : 1));
+    long (*re)[20] = malloc(sizeof(long) * 20 * (nr > 0 ? nr : 1));
+    for (int r = 0; r < nr; ++r) orc_tet2_locate(c->nx, c->ny, c->nz, c->rec_pos + 3 * r, rw[r], re[r]);
+    const int tf = c->time_frequency;
+    const int nsamp = nsteps > 0 ? (nsteps - 1) / tf + 1 : 0;
+    const double dt = c->dt;
+    const double x1 = 1.0 / (2.0 - pow(2.0, 1.0 / 3.0)), x2 = 1.0 - 2.0 * x1;
+    double sub[3] = {dt, 0, 0}, off[3] = {0, 0, 0};
+    int nsub = 1;
+    if (c->integrator == ORC_SYMP4) { nsub = 3; sub[0] = x1 * dt; sub[1] = x2 * dt; sub[2] = x1 * dt; off[1] = x1 * dt; off[2] = (x1 + x2) * dt; }
+    double hq[3];
+    for (int k = 0; k < nsub; ++k) hq[k] = 0.5 * sub[k] + (k + 1 < nsub ? 0.5 * sub[k + 1] : 0.0);
+
+    double *Us = calloc((size_t)(nsteps + 1) * n, sizeof(double)), *Ps = calloc((size_t)(nsteps + 1) * n, sizeof(double));
+    double *U = calloc(n, sizeof(double)), *P = calloc(n, sizeof(double)), *F = calloc(n, sizeof(double));
+    double *Y[4];
+    for (int k = 0; k < 4; ++k) Y[k] = calloc(n, sizeof(double));
+    double *Ub = calloc(n, sizeof(double)), *Pb = calloc(n, sizeof(double)), *Z = calloc(n, sizeof(double));
+    memset(grad_eps, 0, sizeof(double) * m.ntet);
+
+    /* one step from (U, P) at time t, keeping the drift increments Y[0..nsub] */
+#define T2_STEP(time)                                                                                   \
+    do {                                                                                                \
+        mass_solve(&q, P, Y[0]);                                                                        \
+        for (size_t e = 0; e < n; ++e) U[e] += 0.5 * sub[0] * Y[0][e];                                  \
+        for (int k = 0; k < nsub; ++k) {                                                                \
+            apply_elem(&m, 1, mi, U, F);                                                                \
+            for (int s = 0; s < nd; ++s) {                                                              \
+                double g = orc_tet_wave(c->dip_kind[s], c->dip_f0[s], (time) + off[k] + 0.5 * sub[k]);  \
+                for (int a = 0; a < 20; ++a) F[de[s][a]] -= dw[s][a] * g;                               \
+            }                                                                                           \
+            for (size_t e = 0; e < n; ++e) P[e] -= m.pec[e] ? 0.0 : sub[k] * F[e];                      \
+            mass_solve(&q, P, Y[k + 1]);                                                                \
+            for (size_t e = 0; e < n; ++e) U[e] += hq[k] * Y[k + 1][e];                                 \
+        }                                                                                               \
+    } while (0)
+
+    for (int st = 0; st < nsteps; ++st) {
+        memcpy(Us + (size_t)st * n, U, sizeof(double) * n);
+        memcpy(Ps + (size_t)st * n, P, sizeof(double) * n);
+        T2_STEP(st * dt);
+    }
+    for (int st = nsteps - 1; st >= 0; --st) {
+        memcpy(U, Us + (size_t)st * n, sizeof(double) * n);
+        memcpy(P, Ps + (size_t)st * n, sizeof(double) * n);
+        T2_STEP(st * dt);
+        for (int k = nsub - 1; k >= 0; --k) {
+            mass_solve(&q, Ub, Z);                      /* post-drift of substage k */
+            for (size_t e = 0; e < n; ++e) Pb[e] += hq[k] * Z[e];
+            elem_contract(&m, Z, Y[k + 1], -hq[k], grad_eps);
+            apply_elem(&m, 1, mi, Pb, F);                /* kick k */
+            for (size_t e = 0; e < n; ++e) Ub[e] -= m.pec[e] ? 0.0 : sub[k] * F[e];
+        }
+        mass_solve(&q, Ub, Z);                          /* start-of-step drift */
+        for (size_t e = 0; e < n; ++e) Pb[e] += 0.5 * sub[0] * Z[e];
+        elem_contract(&m, Z, Y[0], -0.5 * sub[0], grad_eps);
+        if (st % tf == 0 && st / tf < nsamp)           /* the sample taken at the start of the step */
+            for (int r = 0; r < nr; ++r) {
+                const double *gr = trace_grad + ((size_t)r * nsamp + st / tf) * 4;
+                for (int a = 0; a < 20; ++a)
+                    Ub[re[r][a]] += rw[r][a][0] * gr[1] + rw[r][a][1] * gr[2] + rw[r][a][2] * gr[3];
+            }
+    }
+#undef T2_STEP
+    free(Us); free(Ps); free(U); free(P); free(F); free(Ub); free(Pb); free(Z);
+    for (int k = 0; k < 4; ++k) free(Y[k]);
+    free(mi); free(dw); free(de); free(rw); free(re);
+    mass_free(&q);
+    free_t2mesh(&m);
+    return 0;
+}

@@ -143,8 +143,8 @@ def test_stiffness_and_energy_match_oracle():
     assert rel_l2(f, oracle.tet2_apply(n, U, True)) < 1e-13
     s.set_field(0, to_api(n, U))
     s.set_field(1, to_api(n, P))
-    e = s.energy()
-    assert abs(e[0] - oracle.tet2_energy(n, eps, U, P)) / abs(e[0]) < 1e-12
+    e = float(np.ravel(s.energy())[0])
+    assert abs(e - oracle.tet2_energy(n, eps, U, P)) / abs(e) < 1e-12
 
 
 def test_batch_shots_equal_single_runs_bitwise():
@@ -181,11 +181,70 @@ def test_fp32_runs_are_bitwise_deterministic():
     assert np.array_equal(a.get_field(0), b.get_field(0))
 
 
-def test_order2_rejects_conductivity_and_adjoint():
+def test_order2_rejects_conductivity_and_leapfrog_adjoint():
     n = (3, 3, 3)
     s = ems.TetFemSimulation(n, H, 2, ems.SYMP4, ems.FP32, dt=0.1 * TS)
     sigma = np.full(6 * 27, 0.01)
     with pytest.raises(ems.EmsError):
         s.set_material(np.ones(6 * 27), sigma)
+    lf = ems.TetFemSimulation(n, H, 2, ems.LEAPFROG, ems.FP32, dt=0.1 * TS)
     with pytest.raises(ems.EmsError):
-        s.set_checkpoints(4)
+        lf.set_checkpoints(4)
+
+
+def _adjoint(n, eps, dip, recs, integ, dtn, steps, precision, nsnap, g, batch=1):
+    if batch == 1:
+        s = ems.TetFemSimulation(n, H, 2, INTEG[integ], precision, dt=dtn * TS)
+        s.set_material(eps)
+        s.add_dipole(np.array(dip[0]) * H, dip[1], ems.WAVE_RICKER, dip[3] / TS, dip[4])
+        for r in recs:
+            s.add_receiver(np.array(r) * H)
+    else:
+        s = ems.TetFemBatch([n] * batch, H, order=2, integrator=INTEG[integ], precision=precision, dt=dtn * TS)
+        s.set_material(np.tile(eps, batch))
+        for k in range(batch):
+            s.add_dipole(k, np.array(dip[0]) * H, dip[1], ems.WAVE_RICKER, dip[3] / TS, dip[4])
+            for r in recs:
+                s.add_receiver(k, np.array(r) * H)
+    s.set_checkpoints(nsnap)
+    s.reset()
+    s.run(steps)
+    tr = s.traces()
+    gg = np.tile(g, (batch, 1, 1)) if batch > 1 else g
+    return tr, s.backward(gg)
+
+
+@pytest.mark.parametrize("integ,nsnap", [(oracle.SYMP4, 4), (oracle.SYMP2, 7)])
+def test_fp64_adjoint_matches_oracle(integ, nsnap):
+    n = (3, 4, 3)
+    _, _, ntet = oracle.tet2_sizes(n)
+    rng = np.random.default_rng(31)
+    eps = rng.uniform(1, 4, ntet)
+    dip = ((1.4, 1.6, 1.5), (0.2, 0.3, 1.0), 1, 0.25, 1.0)
+    recs = [(2.2, 1.3, 1.7), (0.8, 2.1, 1.2)]
+    steps, dtn = 30, 0.1
+    tr_o, _, _ = oracle.tet2_run(n, eps, integ, dtn, steps, 1, [dip], recs)
+    g = rng.standard_normal(tr_o.shape)
+    g[..., 0] = 0.0
+    grad_o = oracle.tet2_gradient(n, eps, integ, dtn, steps, g, 1, [dip], recs)
+    tr, grad = _adjoint(n, eps, dip, recs, integ, dtn, steps, ems.FP64, nsnap, g)
+    assert rel_l2(tr[..., 1:], tr_o[..., 1:]) < FP64_TOL
+    assert rel_l2(grad, grad_o) < 1e-9
+
+
+def test_fp32_adjoint_close_to_fp64_and_batch_equals_single():
+    n = (6, 6, 6)
+    _, _, ntet = oracle.tet2_sizes(n)
+    rng = np.random.default_rng(33)
+    eps = rng.uniform(1, 4, ntet)
+    dip = ((2.6, 3.1, 2.9), (0.0, 0.0, 1.0), 1, 0.12, 1.0)
+    recs = [(4.2, 1.3, 3.7), (1.8, 4.1, 2.2), (3.3, 3.3, 4.6)]
+    steps, dtn = 200, 0.12
+    tr64, _ = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP64, 8, np.zeros((3, steps, 4)))
+    g = np.zeros_like(tr64)
+    g[..., 1:] = tr64[..., 1:] * rng.uniform(0.5, 1.5, tr64[..., 1:].shape)
+    _, g64 = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP64, 8, g)
+    _, g32 = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g)
+    assert rel_l2(g32, g64) < 1e-3
+    _, gb = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g, batch=2)
+    assert np.array_equal(gb[:ntet], g32) and np.array_equal(gb[ntet:], g32)
