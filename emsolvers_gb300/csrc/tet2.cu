@@ -411,7 +411,24 @@ __device__ __forceinline__ TetAddr tet_addr(const T2Shot &S, unsigned long long 
 
 // Mass element pass: Yt[a][t] = eps_t (Mref_p x_t)_a (the two-pass
 // iteration: this pass, then the entity pass sums the values of an
-// entity's tetrahedra).
+// entity's tetrahedra).  The type p is dispatched to a compile-time
+// constant (tetrahedra are type-major, so a warp holds one type), so the
+// reference entries are constant operands of the multiply-adds.
+template <class T, int P> __device__ __forceinline__ void mass_elem_body(const TetAddr &ta, unsigned long long NT, unsigned long long t, T e,
+                                                                         const T *__restrict__ x, T *__restrict__ Yt)
+{
+    T xv[20];
+#pragma unroll
+    for (int b = 0; b < 20; ++b) xv[b] = x[ta.dof(b)];
+#pragma unroll
+    for (int a = 0; a < 20; ++a) {
+        T y = T(0);
+#pragma unroll
+        for (int b = 0; b < 20; ++b) y = fma(mref<T>(P, a, b), xv[b], y);
+        Yt[(unsigned long long)a * NT + t] = e * y;
+    }
+}
+
 template <class T>
 __global__ void __launch_bounds__(128) t2_mass_elem_kernel(unsigned long long NT, const T2Shot *__restrict__ sh, int ns,
                                                           const T *__restrict__ eps, const T *__restrict__ x, T *__restrict__ Yt)
@@ -420,17 +437,14 @@ __global__ void __launch_bounds__(128) t2_mass_elem_kernel(unsigned long long NT
     if (t >= NT) return;
     const T2Shot S = sh[shot_of(sh, ns, t, 0)];
     const TetAddr ta = tet_addr(S, t - S.tet0);
-    T xv[20];
-#pragma unroll
-    for (int b = 0; b < 20; ++b) xv[b] = x[ta.dof(b)];
     const T e = eps[t];
-    const int p = ta.p;
-#pragma unroll
-    for (int a = 0; a < 20; ++a) {
-        T y = T(0);
-#pragma unroll
-        for (int b = 0; b < 20; ++b) y = fma(mref<T>(p, a, b), xv[b], y);
-        Yt[(unsigned long long)a * NT + t] = e * y;
+    switch (ta.p) {
+    case 0: mass_elem_body<T, 0>(ta, NT, t, e, x, Yt); break;
+    case 1: mass_elem_body<T, 1>(ta, NT, t, e, x, Yt); break;
+    case 2: mass_elem_body<T, 2>(ta, NT, t, e, x, Yt); break;
+    case 3: mass_elem_body<T, 3>(ta, NT, t, e, x, Yt); break;
+    case 4: mass_elem_body<T, 4>(ta, NT, t, e, x, Yt); break;
+    default: mass_elem_body<T, 5>(ta, NT, t, e, x, Yt); break;
     }
 }
 
@@ -488,23 +502,18 @@ __device__ __forceinline__ void dot2_add(float a, float b, float &s, float &c)
     c = __fadd_rn(c, __fadd_rn(ep, es));
 }
 
-__global__ void __launch_bounds__(128) t2_stiff_df_kernel(unsigned long long NT, const T2Shot *__restrict__ sh, int ns,
-                                                         const float *__restrict__ U, double *__restrict__ Yt)
+template <int P> __device__ __forceinline__ void stiff_df_body(const TetAddr &ta, unsigned long long NT, unsigned long long t,
+                                                               const float *__restrict__ U, double *__restrict__ Yt)
 {
-    const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
-    if (t >= NT) return;
-    const T2Shot S = sh[shot_of(sh, ns, t, 0)];
-    const TetAddr ta = tet_addr(S, t - S.tet0);
-    const int p = ta.p;
     float cs[12], cc[12];
 #pragma unroll
     for (int q = 0; q < 12; ++q) { cs[q] = 0.0f; cc[q] = 0.0f; }
-#pragma unroll 2
+#pragma unroll
     for (int a = 0; a < 20; ++a) {
         const float u = U[ta.dof(a)];
 #pragma unroll
         for (int q = 0; q < 12; ++q) {
-            const float co = c2_C32[p][a][q];
+            const float co = c2_C32[P][a][q];
             if (co != 0.0f) dot2_add(co, u, cs[q], cc[q]);
         }
     }
@@ -523,18 +532,35 @@ __global__ void __launch_bounds__(128) t2_stiff_df_kernel(unsigned long long NT,
             hl[3 * v + q] = (float)(h - (double)hh[3 * v + q]);
         }
     }
-#pragma unroll 2
+#pragma unroll
     for (int a = 0; a < 20; ++a) {
         float fs = 0.0f, fc = 0.0f;
 #pragma unroll
         for (int q = 0; q < 12; ++q) {
-            const float co = c2_C32[p][a][q];
+            const float co = c2_C32[P][a][q];
             if (co != 0.0f) {
                 dot2_add(co, hh[q], fs, fc);
                 fc = fmaf(co, hl[q], fc);
             }
         }
         Yt[(unsigned long long)a * NT + t] = (double)fs + (double)fc;
+    }
+}
+
+__global__ void __launch_bounds__(128, 5) t2_stiff_df_kernel(unsigned long long NT, const T2Shot *__restrict__ sh, int ns,
+                                                         const float *__restrict__ U, double *__restrict__ Yt)
+{
+    const unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    if (t >= NT) return;
+    const T2Shot S = sh[shot_of(sh, ns, t, 0)];
+    const TetAddr ta = tet_addr(S, t - S.tet0);
+    switch (ta.p) {
+    case 0: stiff_df_body<0>(ta, NT, t, U, Yt); break;
+    case 1: stiff_df_body<1>(ta, NT, t, U, Yt); break;
+    case 2: stiff_df_body<2>(ta, NT, t, U, Yt); break;
+    case 3: stiff_df_body<3>(ta, NT, t, U, Yt); break;
+    case 4: stiff_df_body<4>(ta, NT, t, U, Yt); break;
+    default: stiff_df_body<5>(ta, NT, t, U, Yt); break;
     }
 }
 

@@ -163,23 +163,28 @@ def test_launch_shape_autotuner_picks_a_candidate_and_changes_no_result():
         "print('%%d %%d' %% s.launch_shape()[:2])\n"
         "f = s.fields()\n"
         "np.save('%s', np.concatenate([s.traces().ravel()] + [np.ravel(f[k]) for k in sorted(f)]))\n")
+    # the two-kernel step (default) in its autotuned and forced launch shapes
+    # and the opt-in fused H+E step give the same bits
     out = {}
-    for shape in ("", "32x8", "256x1", "64x2"):
+    for shape in ("fused", "", "32x8", "256x1", "64x2"):
         env = dict(os.environ)
         env.pop("EMS_FDTD_BLOCK", None)
-        if shape:
+        env.pop("EMS_FDTD_FUSED", None)
+        if shape == "fused":
+            env["EMS_FDTD_FUSED"] = "1"
+        if shape not in ("", "fused"):
             env["EMS_FDTD_BLOCK"] = shape
         path = f"/tmp/ems_fdtd_shape_{shape or 'auto'}_{os.getpid()}.npy"
         r = subprocess.run([sys.executable, "-c", code % path], env=env, capture_output=True, text=True, timeout=300)
         assert r.returncode == 0, r.stderr
         x, y = map(int, r.stdout.strip().splitlines()[-1].split())
         assert (x, y) in [(32, 8), (32, 4), (64, 4), (128, 2), (256, 1), (64, 2)]
-        if shape:
+        if shape not in ("", "fused"):
             assert f"{x}x{y}" == shape
         out[shape] = np.load(path)
         os.remove(path)
-    for shape in ("32x8", "256x1", "64x2"):
-        assert np.array_equal(out[""], out[shape])
+    for shape in ("", "32x8", "256x1", "64x2"):
+        assert np.array_equal(out["fused"], out[shape])
 
 
 def _cpml_traces(n, src, recs, steps, precision, pml_cells, kmax=1.0, amax=0.0, f0=None):
