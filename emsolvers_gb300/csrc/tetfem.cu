@@ -1656,6 +1656,11 @@ struct TetFemSim : Sim {
     DevBuf d_damp;
     int step_block = 64;            // threads per block of tet_step_kernel (tune_launch_shape)
     bool slot_split = true;         // symplectic lossless steps by tet_slot_kernel (tune_launch_shape)
+    // Until a run tunes the shape (recorded runs do not), the slot-split
+    // kernel serves meshes that fit in L2, the node kernel larger ones (on
+    // the 64-shot batch and the 16-shot 48^3 inversion the node kernel is
+    // the faster, bandwidth-bound one).
+    static constexpr size_t kSlotDefaultMaxNodes = 262144;
     bool step_tuned = false;        // the block size depends on the mesh only: tuned once per handle
     DevBuf d_tet_edge, d_inc_ptr, d_inc, d_nrec, d_pec, d_eps, d_minv, d_U, d_P, d_Uold, d_status;
     // FP32 runs: bfloat16 compensation planes of U and then P, one
@@ -1728,6 +1733,7 @@ struct TetFemSim : Sim {
         EMS_CHECK_ARG(ntet < (size_t)1 << 28, "mesh too large for 28-bit element indices");
         EMS_CHECK_ARG(nslot < (size_t)1 << 31, "mesh too large for 32-bit slot indices");
         build_mesh();
+        slot_split = nnode <= kSlotDefaultMaxNodes;
         eps_h.assign(ntet, 1.0);
         init_stream();
         upload_tables();
@@ -1919,7 +1925,8 @@ struct TetFemSim : Sim {
     // a CUDA graph, as the loop runs them, twice over, and the fastest is kept
     // for the rest of the run and later ones.  (Timed on idle steps outside
     // a run, the candidates ranked differently from the loop.)  Before that
-    // the slot-split kernel runs.  The environment variable
+    // the slot-split kernel runs on meshes of up to kSlotDefaultMaxNodes
+    // nodes and the 64-thread node kernel on larger ones.  The environment variable
     // EMS_TET_STEP_BLOCK (32, 64, 128, 256 or slot) forces one;
     // EMS_TET_TUNE_LOG prints the candidates' times to stderr.
     static constexpr int kShapes = 5, kTuneRounds = 2;
