@@ -48,6 +48,7 @@
 #include <fstream>
 #include <iomanip>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "ems_internal.hpp"
@@ -667,26 +668,154 @@ __global__ void __launch_bounds__(128) t2_gather_kernel(unsigned long long NE, c
     }
 }
 
+// ------------------------------------------- compile-time incidence tables
+// The incidences of the 19 entity types and the DOF placement of the six
+// tetrahedron types follow from the Kuhn split alone, so they are built at
+// compile time for the fused iteration (the same tables as Ref, whose
+// element matrices need floating-point setup and stay in constant memory).
+struct IncTab {
+    int n[kEnt];
+    int p[kEnt][kMaxInc], ob[kEnt][kMaxInc], la[kEnt][kMaxInc], lb[kEnt][kMaxInc];
+    int plane[6][20], vo[6][20];   // plane and lowest-vertex offset bits of local DOF b of type p
+};
+
+constexpr int cx_dir(int dx, int dy, int dz)
+{
+    for (int k = 0; k < 7; ++k)
+        if (kDir[k][0] == dx && kDir[k][1] == dy && kDir[k][2] == dz) return k;
+    return -1;
+}
+constexpr int cx_face(int s1, int s2)
+{
+    int t = 0;
+    for (int a = 1; a < 8; ++a)
+        for (int b = 1; b < 8; ++b) {
+            if (a & b) continue;
+            if (a == s1 && b == s2) return t;
+            ++t;
+        }
+    return -1;
+}
+
+constexpr IncTab make_inc_tab()
+{
+    IncTab T{};
+    int vert[6][4][3] = {};
+    for (int p = 0; p < 6; ++p) {
+        const int a = kPerm[p][0], b = kPerm[p][1];
+        vert[p][1][a] = 1;
+        vert[p][2][a] = 1; vert[p][2][b] = 1;
+        vert[p][3][0] = vert[p][3][1] = vert[p][3][2] = 1;
+        for (int d = 0; d < 20; ++d) {
+            int low = 0, plane = 0;
+            if (d < 12) {
+                const int l = d % 6, i = kEdge[l][0], j = kEdge[l][1];
+                plane = cx_dir(vert[p][j][0] - vert[p][i][0], vert[p][j][1] - vert[p][i][1], vert[p][j][2] - vert[p][i][2]) + (d < 6 ? 0 : 7);
+                low = i;
+            } else {
+                const int f = (d - 12) / 2, v0 = kFace[f][0], v1 = kFace[f][1], v2 = kFace[f][2];
+                int s1 = 0, s2 = 0;
+                for (int q = 0; q < 3; ++q) {
+                    s1 |= (vert[p][v1][q] - vert[p][v0][q]) << q;
+                    s2 |= (vert[p][v2][q] - vert[p][v1][q]) << q;
+                }
+                plane = 14 + 2 * cx_face(s1, s2) + (d - 12) % 2;
+                low = v0;
+            }
+            T.plane[p][d] = plane;
+            T.vo[p][d] = vert[p][low][0] | (vert[p][low][1] << 1) | (vert[p][low][2] << 2);
+        }
+    }
+    for (int p = 0; p < 6; ++p)
+        for (int ent = 0; ent < 10; ++ent) {
+            const int la = ent < 6 ? ent : 12 + 2 * (ent - 6), lb = ent < 6 ? ent + 6 : 13 + 2 * (ent - 6);
+            const int pl = T.plane[p][la], et = pl < 14 ? pl % 7 : 7 + (pl - 14) / 2;
+            const int q = T.n[et]++;
+            T.p[et][q] = p; T.ob[et][q] = T.vo[p][la]; T.la[et][q] = la; T.lb[et][q] = lb;
+        }
+    // ascending type, then ascending cube (descending offset bits), as Ref
+    for (int e = 0; e < kEnt; ++e)
+        for (int a = 1; a < T.n[e]; ++a)
+            for (int b = a; b > 0; --b) {
+                const bool swap = T.p[e][b - 1] > T.p[e][b] || (T.p[e][b - 1] == T.p[e][b] && T.ob[e][b - 1] < T.ob[e][b]);
+                if (!swap) break;
+                int t = 0;
+                t = T.p[e][b]; T.p[e][b] = T.p[e][b - 1]; T.p[e][b - 1] = t;
+                t = T.ob[e][b]; T.ob[e][b] = T.ob[e][b - 1]; T.ob[e][b - 1] = t;
+                t = T.la[e][b]; T.la[e][b] = T.la[e][b - 1]; T.la[e][b - 1] = t;
+                t = T.lb[e][b]; T.lb[e][b] = T.lb[e][b - 1]; T.lb[e][b - 1] = t;
+            }
+    return T;
+}
+constexpr IncTab kInc = make_inc_tab();
+static_assert(kInc.n[6] == 6 && kInc.n[7] == 2, "Kuhn split: the body diagonal lies in six tetrahedra, a face in two");
+
+// The two mass rows of entity type ET at node (i,j,k): sum over its
+// tetrahedra of eps_t (Mref_p x_t) at the entity's local DOFs, every table
+// entry a compile-time constant (the reference entries are constant-bank
+// operands, the DOF offsets plane * nnode + vertex offset).
+// r0 += Mref_p[LA][b] x_b, r1 += Mref_p[LB][b] x_b over b in order, the DOF
+// offset of b (plane * nnode + vertex offset) formed from compile-time parts
+template <class T, int P, int LA, int LB, int B>
+__device__ __forceinline__ void cheb_term(const T *__restrict__ xs, unsigned nn, unsigned nx1, unsigned nxy, T &r0, T &r1)
+{
+    constexpr int PL = kInc.plane[P][B], VO = kInc.vo[P][B];
+    const T xb = xs[(unsigned)PL * nn + (VO & 1) + ((VO >> 1) & 1) * nx1 + ((VO >> 2) & 1) * nxy];
+    r0 = fma(mref<T>(P, LA, B), xb, r0);
+    r1 = fma(mref<T>(P, LB, B), xb, r1);
+}
+template <class T, int P, int LA, int LB, int... B>
+__device__ __forceinline__ void cheb_terms(std::integer_sequence<int, B...>, const T *__restrict__ xs, unsigned nn, unsigned nx1,
+                                           unsigned nxy, T &r0, T &r1)
+{
+    (cheb_term<T, P, LA, LB, B>(xs, nn, nx1, nxy, r0, r1), ...);
+}
+
+template <class T, int ET, int Q>
+__device__ __forceinline__ void cheb_rows_inc(const T *__restrict__ xs, const T *__restrict__ eps, unsigned long long tet0,
+                                              unsigned ncube, unsigned nn, unsigned nx1, unsigned nxy, unsigned ncx, unsigned ncxy,
+                                              const int (&n)[3], int i, int j, int k, T &y0, T &y1)
+{
+    constexpr int P = kInc.p[ET][Q], OB = kInc.ob[ET][Q], LA = kInc.la[ET][Q], LB = kInc.lb[ET][Q];
+    const int ci = i - (OB & 1), cj = j - ((OB >> 1) & 1), ck = k - ((OB >> 2) & 1);
+    if (ci < 0 || cj < 0 || ck < 0 || ci >= n[0] || cj >= n[1] || ck >= n[2]) return;
+    const unsigned v0 = (unsigned)ci + nx1 * cj + nxy * ck;
+    T r0 = T(0), r1 = T(0);
+    cheb_terms<T, P, LA, LB>(std::make_integer_sequence<int, 20>{}, xs + v0, nn, nx1, nxy, r0, r1);
+    const T e = eps[tet0 + (unsigned long long)P * ncube + (unsigned)ci + ncx * cj + ncxy * ck];
+    y0 = fma(e, r0, y0);
+    y1 = fma(e, r1, y1);
+}
+
+template <class T, int ET, int... Q>
+__device__ __forceinline__ void cheb_rows_all(std::integer_sequence<int, Q...>, const T *__restrict__ xs, const T *__restrict__ eps,
+                                              unsigned long long tet0, unsigned ncube, unsigned nn, unsigned nx1, unsigned nxy,
+                                              unsigned ncx, unsigned ncxy, const int (&n)[3], int i, int j, int k, T &y0, T &y1)
+{
+    (cheb_rows_inc<T, ET, Q>(xs, eps, tet0, ncube, nn, nx1, nxy, ncx, ncxy, n, i, j, k, y0, y1), ...);
+}
+
+template <class T, int ET>
+__device__ __forceinline__ void cheb_rows(const T *__restrict__ xs, const T *__restrict__ eps, unsigned long long tet0, unsigned ncube,
+                                          unsigned nn, unsigned nx1, unsigned nxy, unsigned ncx, unsigned ncxy, const int (&n)[3], int i,
+                                          int j, int k, T &y0, T &y1)
+{
+    cheb_rows_all<T, ET>(std::make_integer_sequence<int, kInc.n[ET]>{}, xs, eps, tet0, ncube, nn, nx1, nxy, ncx, ncxy, n, i, j, k, y0,
+                         y1);
+}
+
 // Fused Chebyshev iteration: one thread per edge or face forms the entity's
 // two mass rows eps_t (Mref_p x_t) over its tetrahedra (fixed order) from
 // the previous iterate, then r = b - M x, z = Pinv r, d = c1 d + c2 z and
-// the next iterate x + d into the other buffer.  The block keeps the DOF
-// offsets of its shot (plane * nnode + vertex offset, 32-bit within a
-// shot) in shared memory; the reference rows are warp-uniform constant reads.
+// the next iterate x + d into the other buffer.  The entity type selects a
+// body compiled for its incidences (cheb_rows); the entity types are
+// plane-major, so a warp holds one type.
 template <class T, int FIN>
-__global__ void __launch_bounds__(128) t2_cheb_kernel(unsigned long long NE, const T2Shot *__restrict__ sh, int ns,
-                                                     const unsigned *__restrict__ ofs, GArgs<T> g)
+__global__ void __launch_bounds__(128) t2_cheb_kernel(unsigned long long NE, const T2Shot *__restrict__ sh, int ns, GArgs<T> g)
 {
-    __shared__ unsigned sO[120];
-    const unsigned long long e0 = blockIdx.x * (unsigned long long)blockDim.x;
-    const int sb = shot_of(sh, ns, e0 < NE ? e0 : NE - 1, 1);
-    for (int q = threadIdx.x; q < 120; q += blockDim.x) sO[q] = ofs[(size_t)sb * 120 + q];
-    __syncthreads();
-    const unsigned long long e = e0 + threadIdx.x;
+    const unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
     if (e >= NE) return;
-    const int si = shot_of(sh, ns, e, 1);
-    const T2Shot S = sh[si];
-    const unsigned *O = si == sb ? sO : ofs + (size_t)si * 120;
+    const T2Shot S = sh[shot_of(sh, ns, e, 1)];
     const unsigned nn = (unsigned)S.nnode;
     const unsigned el = (unsigned)(e - S.ent0);
     const int et = (int)(el / nn);
@@ -711,26 +840,17 @@ __global__ void __launch_bounds__(128) t2_cheb_kernel(unsigned long long NE, con
     }
     const T *xs = g.xin + S.dof0;
     const unsigned ncx = S.n[0], ncxy = ncx * S.n[1], nxy = nx1 * ny1;
+    const int n3[3] = {S.n[0], S.n[1], S.n[2]};
+    const unsigned nc = (unsigned)S.ncube;
     T y0 = T(0), y1 = T(0);
-    for (int q = 0; q < c2_ninc[et]; ++q) {
-        const int w = c2_inc[et][q];
-        const int p = w & 7, ob = (w >> 3) & 7, la = (w >> 6) & 31, lb = (w >> 11) & 31;
-        const int ci = i - (ob & 1), cj = j - ((ob >> 1) & 1), ck = k - ((ob >> 2) & 1);
-        if (ci < 0 || cj < 0 || ck < 0 || ci >= S.n[0] || cj >= S.n[1] || ck >= S.n[2]) continue;
-        const unsigned cube = (unsigned)ci + ncx * cj + ncxy * ck;
-        const unsigned v0 = (unsigned)ci + nx1 * cj + nxy * ck;
-        const unsigned *Op = O + p * 20;
-        T r0 = T(0), r1 = T(0);
-#pragma unroll
-        for (int b = 0; b < 20; ++b) {
-            const T xb = xs[v0 + Op[b]];
-            r0 = fma(mref<T>(p, la, b), xb, r0);
-            r1 = fma(mref<T>(p, lb, b), xb, r1);
-        }
-        const T ep = g.eps[S.tet0 + (unsigned long long)p * S.ncube + cube];
-        y0 = fma(ep, r0, y0);
-        y1 = fma(ep, r1, y1);
+#define EMS_T2_ROWS(E) \
+    case E: cheb_rows<T, E>(xs, g.eps, S.tet0, nc, nn, nx1, nxy, ncx, ncxy, n3, i, j, k, y0, y1); break;
+    switch (et) {
+        EMS_T2_ROWS(0) EMS_T2_ROWS(1) EMS_T2_ROWS(2) EMS_T2_ROWS(3) EMS_T2_ROWS(4) EMS_T2_ROWS(5) EMS_T2_ROWS(6)
+        EMS_T2_ROWS(7) EMS_T2_ROWS(8) EMS_T2_ROWS(9) EMS_T2_ROWS(10) EMS_T2_ROWS(11) EMS_T2_ROWS(12) EMS_T2_ROWS(13)
+        EMS_T2_ROWS(14) EMS_T2_ROWS(15) EMS_T2_ROWS(16) EMS_T2_ROWS(17) default: EMS_T2_ROWS(18)
     }
+#undef EMS_T2_ROWS
     const T r0 = g.b[d0] - y0, r1 = g.b[d1] - y1;
     const T q00 = g.pinv[e], q01 = g.pinv[NE + e], q11 = g.pinv[2 * NE + e];
     const T z0 = fma(q00, r0, q01 * r1), z1 = fma(q01, r0, q11 * r1);
@@ -920,7 +1040,7 @@ struct Tet2Sim : Sim {
     std::vector<Dip> dips;
     std::vector<std::array<size_t, 20>> rec_dof;
     std::vector<std::array<double, 60>> rec_w;
-    DevBuf d_shots, d_ofs, d_eps, d_pinv, d_U, d_Uold, d_P, d_Pc, d_x, d_xs, d_d, d_b, d_YtM, d_YtK, d_ctl, d_part;
+    DevBuf d_shots, d_eps, d_pinv, d_U, d_Uold, d_P, d_Pc, d_x, d_xs, d_d, d_b, d_YtM, d_YtK, d_ctl, d_part;
     DevBuf d_src_dof, d_src_ptr, d_src_dip, d_src_coef, d_src_g, d_rec_dof, d_rec_w, d_tr;
     std::vector<double> cheb_c1, cheb_c2;
     double cheb_c0 = 0.0;
@@ -966,23 +1086,8 @@ struct Tet2Sim : Sim {
         }
         d_shots.alloc(sh.size() * sizeof(T2Shot));
         EMS_CUDA(cudaMemcpy(d_shots.p, sh.data(), sh.size() * sizeof(T2Shot), cudaMemcpyHostToDevice));
-        // per shot: offset of local DOF b of type p from the cube's corner node
-        std::vector<unsigned> of(shots.size() * 120);
-        const Ref &R = ref();
-        for (size_t si = 0; si < shots.size(); ++si) {
-            const ShotH &S = shots[si];
+        for (const ShotH &S : shots)
             EMS_CHECK_ARG(kPlanes * S.nnode < ((size_t)1 << 32), "shot too large for 32-bit DOF offsets");
-            const size_t nx1 = S.n[0] + 1, nxy = nx1 * (S.n[1] + 1);
-            for (int p = 0; p < 6; ++p) {
-                const Kuhn k = kuhn(p);
-                for (int b = 0; b < 20; ++b) {
-                    const int *vo = k.vert[R.low[p][b]];
-                    of[si * 120 + 20 * p + b] = (unsigned)(R.plane[p][b] * S.nnode + vo[0] + vo[1] * nx1 + vo[2] * nxy);
-                }
-            }
-        }
-        d_ofs.alloc(of.size() * 4);
-        EMS_CUDA(cudaMemcpy(d_ofs.p, of.data(), of.size() * 4, cudaMemcpyHostToDevice));
         const size_t w = fp64 ? 8 : 4;
         d_U.alloc(ndof * w); d_Uold.alloc(ndof * w); d_P.alloc(ndof * 8);
         d_x.alloc(ndof * w); d_xs.alloc(ndof * w); d_d.alloc(ndof * w); d_b.alloc(ndof * w);
@@ -997,6 +1102,22 @@ struct Tet2Sim : Sim {
     static void upload_tables()
     {
         const Ref &R = ref();
+        // the fused iteration's compile-time tables must be the setup's
+        for (int e = 0; e < kEnt; ++e) {
+            bool same = kInc.n[e] == R.ninc[e];
+            for (int q = 0; same && q < R.ninc[e]; ++q) {
+                const int w = R.inc[e][q];
+                same = kInc.p[e][q] == (w & 7) && kInc.ob[e][q] == ((w >> 3) & 7) && kInc.la[e][q] == ((w >> 6) & 31) &&
+                       kInc.lb[e][q] == ((w >> 11) & 31);
+            }
+            if (!same) throw Error{EMS_ERR_CUDA, "compile-time incidence table differs from the setup's"};
+        }
+        for (int p = 0; p < 6; ++p) {
+            const Kuhn k = kuhn(p);
+            for (int a = 0; a < 20; ++a)
+                if (kInc.plane[p][a] != R.plane[p][a] || kInc.vo[p][a] != bits(k.vert[R.low[p][a]]))
+                    throw Error{EMS_ERR_CUDA, "compile-time DOF table differs from the setup's"};
+        }
         int dof[6][20];
         float m32[6][400];
         for (int p = 0; p < 6; ++p) {
@@ -1158,8 +1279,8 @@ struct Tet2Sim : Sim {
             g.c2 = cheb_c2[k];
             const bool last = k + 1 == mass_iters;
             if (cheb_fused) {
-                if (last) t2_cheb_kernel<T, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, d_ofs.as<unsigned>(), g);
-                else t2_cheb_kernel<T, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, d_ofs.as<unsigned>(), g);
+                if (last) t2_cheb_kernel<T, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+                else t2_cheb_kernel<T, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
                 ++nl;
             } else {
                 t2_mass_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_eps.as<T>(), g.xin,
@@ -1190,7 +1311,7 @@ struct Tet2Sim : Sim {
             g.xin = buf[k & 1];
             g.x = buf[(k + 1) & 1];
             if (cheb_fused) {
-                t2_cheb_kernel<T, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, d_ofs.as<unsigned>(), g);
+                t2_cheb_kernel<T, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
             } else {
                 t2_mass_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_eps.as<T>(), g.xin,
                                                                               d_YtM.as<T>());
