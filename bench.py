@@ -504,6 +504,21 @@ def tet2_forward(n=48, steps=200):
         s.close()
     out["dt_s"] = dt
     out["fp32_speedup_vs_fp64"] = out["dof_updates_per_s_fp32"] / out["dof_updates_per_s_fp64"]
+    # CPU: the FP64 oracle of the same scheme on the 16^3 model of the recipe,
+    # `cpu_steps` steps, DOF-updates/s
+    nc, cpu_steps = min(n, 16), 2
+    code = (f"import bench\n"
+            f"n = {nc}; eps = bench.blob_model(n, np.random.default_rng({SEED + 7}))\n"
+            f"dip = ((0.5 * n, 0.47 * n, 0.52 * n), (0.0, 0.0, 1.0), 1, {f0 * H / C0!r}, 1.0)\n"
+            f"dtn = {dt * C0 / H!r}\n"
+            "t0 = time.perf_counter()\n"
+            f"oracle.tet2_run((n, n, n), eps, oracle.SYMP4, dtn, {cpu_steps}, 1, [dip], [(0.3 * n, 0.6 * n, 0.4 * n)])\n"
+            "print(time.perf_counter() - t0)\n")
+    cpu = cpu_rates(code, n_dofs2(nc) * cpu_steps)
+    out["cpu_baseline"] = {"value": cpu["single_core"], "unit": "DOF-updates/s", "cores": 1, "kind": "port",
+                           "nproc_processes_value": cpu["nproc_processes"], "processes": cpu["processes"],
+                           "sample": f"{nc}^3 x 6 tets of the same recipe, {cpu_steps} steps of the FP64 oracle (setup "
+                                     "included); single core, and nproc concurrent single-threaded processes"}
     return out
 
 

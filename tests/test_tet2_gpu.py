@@ -248,3 +248,43 @@ def test_fp32_adjoint_close_to_fp64_and_batch_equals_single():
     assert rel_l2(g32, g64) < 1e-3
     _, gb = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g, batch=2)
     assert np.array_equal(gb[:ntet], g32) and np.array_equal(gb[ntet:], g32)
+
+
+def test_both_iteration_forms_match_the_oracle():
+    """The fused and the two-pass Chebyshev iteration (chosen per handle by
+    timing) both reproduce the oracle; each is forced here in a fresh
+    process through EMS_TET2_ITERATION."""
+    import os
+    import subprocess
+    import sys
+    n = (4, 5, 4)
+    eps, dip, recs = _case(n, 17)
+    dtn = 0.8 * oracle.stability_constant(oracle.SYMP4) / np.sqrt(oracle.tet2_lambda_max(n, eps, 200))
+    tr_o, _, _ = oracle.tet2_run(n, eps, oracle.SYMP4, dtn, 60, 1, [dip], recs)
+    code = (
+        "import sys, numpy as np, emsolvers_gb300 as ems\n"
+        f"n = {n!r}; H = {H!r}; TS = {TS!r}\n"
+        "eps = np.load(sys.argv[1])\n"
+        f"s = ems.TetFemSimulation(n, H, 2, ems.SYMP4, ems.{{p}}, dt={dtn!r} * TS)\n"
+        "s.set_material(eps)\n"
+        f"s.add_dipole(np.array({dip[0]!r}) * H, {dip[1]!r}, ems.WAVE_RICKER, {dip[3]!r} / TS, {dip[4]!r})\n"
+        f"for r in {recs!r}:\n"
+        "    s.add_receiver(np.array(r) * H)\n"
+        "s.run(60)\n"
+        "np.save(sys.argv[2], s.traces())\n")
+    path_e = f"/tmp/ems_t2_eps_{os.getpid()}.npy"
+    np.save(path_e, eps)
+    out = {}
+    for form in ("fused", "twopass"):
+        for prec in ("FP64", "FP32"):
+            env = dict(os.environ, EMS_TET2_ITERATION=form)
+            path = f"/tmp/ems_t2_{form}_{prec}_{os.getpid()}.npy"
+            r = subprocess.run([sys.executable, "-c", code.replace("{p}", prec), path_e, path], env=env,
+                               capture_output=True, text=True, timeout=300)
+            assert r.returncode == 0, r.stderr
+            out[form, prec] = np.load(path)
+            os.remove(path)
+    os.remove(path_e)
+    for form in ("fused", "twopass"):
+        assert rel_l2(out[form, "FP64"][..., 1:], tr_o[..., 1:]) < FP64_TOL
+        assert rel_l2(out[form, "FP32"][..., 1:], tr_o[..., 1:]) < FP32_TOL
