@@ -147,7 +147,10 @@ def test_stiffness_and_energy_match_oracle():
     assert abs(e - oracle.tet2_energy(n, eps, U, P)) / abs(e) < 1e-12
 
 
-def test_batch_shots_equal_single_runs_bitwise():
+def test_batch_shots_equal_single_runs_bitwise(monkeypatch):
+    # every handle times the two iteration forms and keeps the faster; the
+    # forms round differently, so bit equality needs the same form in all
+    monkeypatch.setenv("EMS_TET2_ITERATION", "twopass")
     cells = [(4, 4, 4), (6, 5, 4), (5, 6, 7)]
     rng = np.random.default_rng(21)
     dtn = 0.05
@@ -246,7 +249,13 @@ def test_fp32_adjoint_close_to_fp64_and_batch_equals_single():
     _, g64 = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP64, 8, g)
     _, g32 = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g)
     assert rel_l2(g32, g64) < 1e-3
-    _, gb = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g, batch=2)
+    import os
+    os.environ["EMS_TET2_ITERATION"] = "twopass"   # one form for the bitwise comparison
+    try:
+        _, g32 = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g)
+        _, gb = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g, batch=2)
+    finally:
+        del os.environ["EMS_TET2_ITERATION"]
     assert np.array_equal(gb[:ntet], g32) and np.array_equal(gb[ntet:], g32)
 
 
