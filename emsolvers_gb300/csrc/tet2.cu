@@ -384,6 +384,11 @@ template <class T> __device__ __forceinline__ T mref(int p, int a, int b);
 template <> __device__ __forceinline__ double mref<double>(int p, int a, int b) { return c2_M64[p][20 * a + b]; }
 template <> __device__ __forceinline__ float mref<float>(int p, int a, int b) { return c2_M32[p][20 * a + b]; }
 
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
 // DOF addressing of flat tetrahedron tl of a shot: DOF a is
 // dof0 + plane * nnode + v0 + the vertex offset of its lowest vertex
 struct TetAddr {
@@ -426,7 +431,7 @@ template <class T, int P> __device__ __forceinline__ void mass_elem_body(const T
         T y = T(0);
 #pragma unroll
         for (int b = 0; b < 20; ++b) y = fma(mref<T>(P, a, b), xv[b], y);
-        Yt[(unsigned long long)a * NT + t] = e * y;
+        Yt[(unsigned long long)a * NT + t] = mul_rn(e, y);
     }
 }
 
@@ -622,8 +627,8 @@ __global__ void __launch_bounds__(128) t2_gather_kernel(unsigned long long NE, c
             const int ci = i - (ob & 1), cj = j - ((ob >> 1) & 1), ck = k - ((ob >> 2) & 1);
             if (ci < 0 || cj < 0 || ck < 0 || ci >= S.n[0] || cj >= S.n[1] || ck >= S.n[2]) continue;
             const unsigned long long t = S.tet0 + (unsigned long long)p * S.ncube + (unsigned long long)ci + ncx * cj + ncxy * ck;
-            y0 += Y[(unsigned long long)la * g.NT + t];
-            y1 += Y[(unsigned long long)lb * g.NT + t];
+            y0 = add_rn(y0, Y[(unsigned long long)la * g.NT + t]);
+            y1 = add_rn(y1, Y[(unsigned long long)lb * g.NT + t]);
         }
     }
     if (MODE == G_FORCE) {
@@ -782,9 +787,12 @@ __device__ __forceinline__ void cheb_rows_inc(const T *__restrict__ xs, const T 
     const unsigned v0 = (unsigned)ci + nx1 * cj + nxy * ck;
     T r0 = T(0), r1 = T(0);
     cheb_terms<T, P, LA, LB>(std::make_integer_sequence<int, 20>{}, xs + v0, nn, nx1, nxy, r0, r1);
+    // the rounded product, then the rounded sum: the two-pass form stores
+    // e * r and sums the stored values in the same order, so both forms give
+    // the same bits
     const T e = eps[tet0 + (unsigned long long)P * ncube + (unsigned)ci + ncx * cj + ncxy * ck];
-    y0 = fma(e, r0, y0);
-    y1 = fma(e, r1, y1);
+    y0 = add_rn(y0, mul_rn(e, r0));
+    y1 = add_rn(y1, mul_rn(e, r1));
 }
 
 template <class T, int ET, int... Q>

@@ -147,10 +147,7 @@ def test_stiffness_and_energy_match_oracle():
     assert abs(e - oracle.tet2_energy(n, eps, U, P)) / abs(e) < 1e-12
 
 
-def test_batch_shots_equal_single_runs_bitwise(monkeypatch):
-    # every handle times the two iteration forms and keeps the faster; the
-    # forms round differently, so bit equality needs the same form in all
-    monkeypatch.setenv("EMS_TET2_ITERATION", "twopass")
+def test_batch_shots_equal_single_runs_bitwise():
     cells = [(4, 4, 4), (6, 5, 4), (5, 6, 7)]
     rng = np.random.default_rng(21)
     dtn = 0.05
@@ -249,20 +246,15 @@ def test_fp32_adjoint_close_to_fp64_and_batch_equals_single():
     _, g64 = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP64, 8, g)
     _, g32 = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g)
     assert rel_l2(g32, g64) < 1e-3
-    import os
-    os.environ["EMS_TET2_ITERATION"] = "twopass"   # one form for the bitwise comparison
-    try:
-        _, g32 = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g)
-        _, gb = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g, batch=2)
-    finally:
-        del os.environ["EMS_TET2_ITERATION"]
+    _, gb = _adjoint(n, eps, dip, recs, oracle.SYMP4, dtn, steps, ems.FP32, 8, g, batch=2)
     assert np.array_equal(gb[:ntet], g32) and np.array_equal(gb[ntet:], g32)
 
 
 def test_both_iteration_forms_match_the_oracle():
     """The fused and the two-pass Chebyshev iteration (chosen per handle by
-    timing) both reproduce the oracle; each is forced here in a fresh
-    process through EMS_TET2_ITERATION."""
+    timing) give the same bits, so the choice never changes a result, and
+    reproduce the oracle; each is forced here in a fresh process through
+    EMS_TET2_ITERATION."""
     import os
     import subprocess
     import sys
@@ -294,6 +286,8 @@ def test_both_iteration_forms_match_the_oracle():
             out[form, prec] = np.load(path)
             os.remove(path)
     os.remove(path_e)
+    for prec in ("FP64", "FP32"):
+        assert np.array_equal(out["fused", prec], out["twopass", prec])
     for form in ("fused", "twopass"):
         assert rel_l2(out[form, "FP64"][..., 1:], tr_o[..., 1:]) < FP64_TOL
         assert rel_l2(out[form, "FP32"][..., 1:], tr_o[..., 1:]) < FP32_TOL
