@@ -998,8 +998,11 @@ __device__ __forceinline__ void slot_force(const T *__restrict__ u0, size_t nnod
     fl *= T(4);
 }
 
+// FP32: at most 32 registers, so 8 blocks fit on an SM and the 1,125 blocks
+// of the 32^3 headline mesh run in one wave (40 registers left 61 blocks
+// for a second wave; 30.7 -> 29.8 ms per 2000-step solve).
 template <class T, int REC, int COMP>
-__global__ void __launch_bounds__(kSlotThreads) tet_slot_kernel(size_t nnode, const int2 *__restrict__ nrec,
+__global__ void __launch_bounds__(kSlotThreads, sizeof(T) == 4 ? 8 : 1) tet_slot_kernel(size_t nnode, const int2 *__restrict__ nrec,
                                                                 const unsigned char *__restrict__ pec,
                                                                 const T *__restrict__ minv, T *__restrict__ P,
                                                                 const T *__restrict__ Uin, T *__restrict__ Uout, T a, T c,
