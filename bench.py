@@ -143,6 +143,28 @@ def _cpu_timed(code, threads=1, procs=1):
     return out
 
 
+def cpu_model():
+    """The host CPU's model as /proc/cpuinfo or lscpu state it (Arm hosts
+    list implementer and part numbers rather than a name)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for key in ("Model name:", "Vendor ID:"):
+            for line in out.splitlines():
+                if line.strip().startswith(key):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part", "hardware")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
 def cpu_rates(code, work, procs=None):
     """`work` units per run of `code`: single-core units/s, and the
     aggregate units/s of nproc concurrent single-threaded processes."""
@@ -176,7 +198,8 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": "tet32_symp4_2000", "cells": N, "tets": 6 * N ** 3, "edges": n_edges(N),
                    "integrator": "symp4", "steps_per_solve": STEPS_PER_SOLVE, "parallelism": "replicas"},
-        "cpu_baseline": {"value": value, "unit": "DOF-updates/s", "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "DOF-updates/s", "cores": threads, "kind": "port", "sample": sample,
+                         "cpu_model": cpu_model()},
         "e2e": {"value": value, "unit": "DOF-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -811,6 +834,7 @@ def run_gpu(args):
                     "print(time.perf_counter() - t0)\n")
             per = cpu_rates(code, n_edges(N) * sample)
             out["cpu_baseline"] = {"value": r, "unit": "DOF-updates/s", "cores": os.cpu_count() or 1, "kind": "port",
+                                   "cpu_model": cpu_model(),
                                    "sample": f"three full solves ({STEPS_PER_SOLVE} time steps each), FP64 oracle, "
                                              f"{sum(secs):.1f} s",
                                    "single_core_value": per["single_core"], "nproc_processes_value": per["nproc_processes"],

@@ -263,7 +263,10 @@ class FemStabSimulation(_Sim):
 
 
 class TetFemSimulation(_Sim):
-    """Structured cube of cells x 6 tetrahedra, Nedelec elements."""
+    """Structured cube of cells x 6 tetrahedra, Nedelec elements of order 1
+    (Whitney, one DOF per edge, fields of 7*(n+1)^3 values in the order
+    7*node + direction) or 2 (two DOFs per edge and per face, 38*(n+1)^3
+    values in the order 38*node + plane; no conductivity)."""
 
     def __init__(self, cells, h, order=1, integrator=SYMP2, precision=FP32, dt=0.0, cfl_fraction=0.9,
                  time_frequency=1):
