@@ -1258,10 +1258,19 @@ struct Tet2Sim : Sim {
     // buffers (the iterates alternate, starting where the last lands in
     // xo); or two-pass, the mass element pass into the per-tetrahedron
     // array, then the entity pass updating x in place.
-    bool cheb_fused = false;
+    // 0: two-pass, 1: fused (one thread per edge or face).  A third form,
+    // one thread per node forming all 38 rows from its 18 tetrahedra (each
+    // tetrahedron's iterate loaded once, 118 registers), measured 77 us
+    // against 68 us (fused) at 48^3 and 30 against 9 us at 16^3; not kept.
+    int cheb_form = 0;
+    template <class T, int FIN> void launch_fused_iteration(const GArgs<T> &g)
+    {
+        t2_cheb_kernel<T, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), (int)shots.size(), g);
+    }
     template <class T, int FIN> int enqueue_solve(const T *b, double h, T *xo = nullptr, T *target = nullptr)
     {
         const int ns = (int)shots.size();
+        const bool fused = cheb_form != 0;
         GArgs<T> g = gargs<T>();
         g.b = b;
         g.c0 = cheb_c0;
@@ -1270,8 +1279,8 @@ struct Tet2Sim : Sim {
         g.Yt = d_YtM.p;
         if (!xo) xo = d_x.as<T>();
         if (target) g.U = target;
-        T *buf[2] = {xo, cheb_fused ? d_xs.as<T>() : xo};
-        int cur = cheb_fused ? (mass_iters - 1) % 2 : 0;   // buffer of the first iterate
+        T *buf[2] = {xo, fused ? d_xs.as<T>() : xo};
+        int cur = fused ? (mass_iters - 1) % 2 : 0;   // buffer of the first iterate
         g.x = buf[cur];
         if (mass_iters == 1) {
             t2_gather_kernel<T, T, G_CHEB0, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
@@ -1281,14 +1290,14 @@ struct Tet2Sim : Sim {
         int nl = 1;
         for (int k = 1; k < mass_iters; ++k) {
             g.xin = buf[cur];
-            cur ^= cheb_fused ? 1 : 0;
+            cur ^= fused ? 1 : 0;
             g.x = buf[cur];
             g.c1 = cheb_c1[k];
             g.c2 = cheb_c2[k];
             const bool last = k + 1 == mass_iters;
-            if (cheb_fused) {
-                if (last) t2_cheb_kernel<T, FIN><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
-                else t2_cheb_kernel<T, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+            if (fused) {
+                if (last) launch_fused_iteration<T, FIN>(g);
+                else launch_fused_iteration<T, FIN_NONE>(g);
                 ++nl;
             } else {
                 t2_mass_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_eps.as<T>(), g.xin,
@@ -1311,15 +1320,15 @@ struct Tet2Sim : Sim {
         g.eps = d_eps.as<T>();
         g.Yt = d_YtM.p;
         g.c1 = 0.5; g.c2 = 0.1;
-        T *buf[2] = {d_x.as<T>(), cheb_fused ? d_xs.as<T>() : d_x.as<T>()};
+        T *buf[2] = {d_x.as<T>(), cheb_form ? d_xs.as<T>() : d_x.as<T>()};
         cudaGraph_t gr = nullptr;
         cudaGraphExec_t ex = nullptr;
         EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
         for (int k = 0; k < n; ++k) {
             g.xin = buf[k & 1];
             g.x = buf[(k + 1) & 1];
-            if (cheb_fused) {
-                t2_cheb_kernel<T, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
+            if (cheb_form) {
+                launch_fused_iteration<T, FIN_NONE>(g);
             } else {
                 t2_mass_elem_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_eps.as<T>(), g.xin,
                                                                               d_YtM.as<T>());
@@ -1349,22 +1358,24 @@ struct Tet2Sim : Sim {
     }
 
     // The faster form of the Chebyshev iteration on this handle's meshes
-    // (EMS_TET2_ITERATION=fused|twopass forces one).
+    // (EMS_TET2_ITERATION=twopass|fused forces one; EMS_TET2_TUNE_LOG prints
+    // the times); the forms give the same bits, so the choice changes no result.
     template <class T> void choose_iteration()
     {
-        const char *force = std::getenv("EMS_TET2_ITERATION");
-        if (force && (!std::strcmp(force, "fused") || !std::strcmp(force, "twopass"))) {
-            cheb_fused = !std::strcmp(force, "fused");
-            return;
-        }
+        static const char *names[2] = {"twopass", "fused"};
+        if (const char *force = std::getenv("EMS_TET2_ITERATION"))
+            for (int f = 0; f < 2; ++f)
+                if (!std::strcmp(force, names[f])) { cheb_form = f; return; }
         d_x.zero(stream); d_xs.zero(stream); d_d.zero(stream); d_b.zero(stream);
-        cheb_fused = false;
-        const double two = time_iterations<T>(8);
-        cheb_fused = true;
-        const double fused = time_iterations<T>(8);
-        cheb_fused = fused < two;
-        iter_ms[0] = two;
-        iter_ms[1] = fused;
+        int best = 0;
+        for (int f = 0; f < 2; ++f) {
+            cheb_form = f;
+            iter_ms[f] = time_iterations<T>(8);
+            if (iter_ms[f] < iter_ms[best]) best = f;
+        }
+        cheb_form = best;
+        if (std::getenv("EMS_TET2_TUNE_LOG"))   // diagnostic: the forms' times per iteration
+            std::fprintf(stderr, "tet2 iteration (us): twopass %.2f fused %.2f\n", 1e3 * iter_ms[0], 1e3 * iter_ms[1]);
     }
     double iter_ms[2] = {0.0, 0.0};
 
@@ -1798,7 +1809,8 @@ struct Tet2Sim : Sim {
         *ms = fp64 ? time_iterations<double>(std::max(launches, 1)) : time_iterations<float>(std::max(launches, 1));
         *bytes = (double)(fp64 ? 8 : 4) * (5.0 * ndof + ntet + 3.0 * nent);
         y_valid = false;
-        *name = std::string(cheb_fused ? "t2_cheb_kernel<" : "t2_mass_elem_kernel + t2_gather_kernel<") + (fp64 ? "double>" : "float>");
+        static const char *kern[2] = {"t2_mass_elem_kernel + t2_gather_kernel<", "t2_cheb_kernel<"};
+        *name = std::string(kern[cheb_form]) + (fp64 ? "double>" : "float>");
     }
 
     // f = K u in the handle's precision (API DOF order)

@@ -276,7 +276,8 @@ def test_both_iteration_forms_match_the_oracle():
     path_e = f"/tmp/ems_t2_eps_{os.getpid()}.npy"
     np.save(path_e, eps)
     out = {}
-    for form in ("fused", "twopass"):
+    forms = ("fused", "twopass")
+    for form in forms:
         for prec in ("FP64", "FP32"):
             env = dict(os.environ, EMS_TET2_ITERATION=form)
             path = f"/tmp/ems_t2_{form}_{prec}_{os.getpid()}.npy"
@@ -288,6 +289,6 @@ def test_both_iteration_forms_match_the_oracle():
     os.remove(path_e)
     for prec in ("FP64", "FP32"):
         assert np.array_equal(out["fused", prec], out["twopass", prec])
-    for form in ("fused", "twopass"):
+    for form in forms:
         assert rel_l2(out[form, "FP64"][..., 1:], tr_o[..., 1:]) < FP64_TOL
         assert rel_l2(out[form, "FP32"][..., 1:], tr_o[..., 1:]) < FP32_TOL
