@@ -30,6 +30,24 @@ def test_tetrahedral_run_from_huge_fields_reports_not_finite():
     s.run(5)
 
 
+def test_order2_tetrahedral_run_from_huge_fields_reports_not_finite():
+    n = (4, 4, 3)
+    _, ndof, ntet = oracle.tet2_sizes(n)
+    pec = oracle.tet2_pec_mask(n)
+    s = ems.TetFemSimulation(n, 1e-3, 2, ems.SYMP4, ems.FP32, dt=0.0, cfl_fraction=0.9)
+    s.set_material(np.full(ntet, 2.0))
+    s.add_receiver(np.array([2.1, 1.4, 1.2]) * 1e-3)
+    nnode = ndof // 38
+    U = np.where(pec, 0.0, 3e38).reshape(38, nnode).T.reshape(-1)   # API order: 38 * node + plane
+    s.set_field(0, U)
+    with pytest.raises(ems.EmsError) as e:
+        s.run(5)
+    assert e.value.status == NOT_FINITE
+    assert s.traces().shape == (1, 5, 4)
+    s.reset()
+    s.run(5)
+
+
 def test_fdtd_run_with_a_nan_field_reports_not_finite():
     s = ems.FdtdSimulation((8, 8, 8), 1e-3, 1e-12, 8.854187817e-12, 1.25663706212e-6, 1)
     ez = s.get_field(2)

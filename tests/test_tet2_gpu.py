@@ -192,9 +192,9 @@ def test_order2_rejects_conductivity_and_leapfrog_adjoint():
         lf.set_checkpoints(4)
 
 
-def _adjoint(n, eps, dip, recs, integ, dtn, steps, precision, nsnap, g, batch=1):
+def _adjoint(n, eps, dip, recs, integ, dtn, steps, precision, nsnap, g, batch=1, tf=1):
     if batch == 1:
-        s = ems.TetFemSimulation(n, H, 2, INTEG[integ], precision, dt=dtn * TS)
+        s = ems.TetFemSimulation(n, H, 2, INTEG[integ], precision, dt=dtn * TS, time_frequency=tf)
         s.set_material(eps)
         s.add_dipole(np.array(dip[0]) * H, dip[1], ems.WAVE_RICKER, dip[3] / TS, dip[4])
         for r in recs:
@@ -214,8 +214,8 @@ def _adjoint(n, eps, dip, recs, integ, dtn, steps, precision, nsnap, g, batch=1)
     return tr, s.backward(gg)
 
 
-@pytest.mark.parametrize("integ,nsnap", [(oracle.SYMP4, 4), (oracle.SYMP2, 7)])
-def test_fp64_adjoint_matches_oracle(integ, nsnap):
+@pytest.mark.parametrize("integ,nsnap,tf", [(oracle.SYMP4, 4, 1), (oracle.SYMP2, 7, 1), (oracle.SYMP4, 5, 3)])
+def test_fp64_adjoint_matches_oracle(integ, nsnap, tf):
     n = (3, 4, 3)
     _, _, ntet = oracle.tet2_sizes(n)
     rng = np.random.default_rng(31)
@@ -223,11 +223,11 @@ def test_fp64_adjoint_matches_oracle(integ, nsnap):
     dip = ((1.4, 1.6, 1.5), (0.2, 0.3, 1.0), 1, 0.25, 1.0)
     recs = [(2.2, 1.3, 1.7), (0.8, 2.1, 1.2)]
     steps, dtn = 30, 0.1
-    tr_o, _, _ = oracle.tet2_run(n, eps, integ, dtn, steps, 1, [dip], recs)
+    tr_o, _, _ = oracle.tet2_run(n, eps, integ, dtn, steps, tf, [dip], recs)
     g = rng.standard_normal(tr_o.shape)
     g[..., 0] = 0.0
-    grad_o = oracle.tet2_gradient(n, eps, integ, dtn, steps, g, 1, [dip], recs)
-    tr, grad = _adjoint(n, eps, dip, recs, integ, dtn, steps, ems.FP64, nsnap, g)
+    grad_o = oracle.tet2_gradient(n, eps, integ, dtn, steps, g, tf, [dip], recs)
+    tr, grad = _adjoint(n, eps, dip, recs, integ, dtn, steps, ems.FP64, nsnap, g, tf=tf)
     assert rel_l2(tr[..., 1:], tr_o[..., 1:]) < FP64_TOL
     assert rel_l2(grad, grad_o) < 1e-9
 
