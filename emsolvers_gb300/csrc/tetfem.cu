@@ -420,6 +420,7 @@ __device__ __forceinline__ double source_load(const SrcArgs &s, size_t e)
     return f;
 }
 
+
 // Receivers sampled inside the step launches.  The first launch of step n
 // reads the step counter ctl[par] (n) and, from one block beyond the node
 // blocks, records E(x) = sum_l w_l(x) U_l of every receiver when n is a
@@ -452,7 +453,7 @@ template <class T> struct RecArgs {
 // receiver, lane l < 6 forms its slot's terms (explicitly rounded FP64
 // products), lane 0 sums them in slot order.
 template <class T>
-__device__ __noinline__ void sample_receivers(const RecArgs<T> rec, const T *__restrict__ U, size_t nnode, int tid, int nthr)
+__device__ __noinline__ void sample_receivers(const RecArgs<T> rec, const T *U, size_t nnode, int tid, int nthr)
 {
     const int step = rec.ctl[rec.par];
     if (step % rec.tf != 0 || step / rec.tf >= rec.nsamp) return;
@@ -962,13 +963,17 @@ __device__ __forceinline__ void slot_feeds(const T (&ue)[NU], int have, T &f, T 
     (slot_feed<T, D, K, COMP, NU>(ue, have, f, fl), ...);
 }
 
-template <class T, int D, int NU, int... K>
-__device__ __forceinline__ void slot_loads(T (&ue)[NU], const T *__restrict__ u0, size_t nnode, const int (&off)[13],
+// u0 carries no __restrict__: the persistent step reads U buffers that
+// other blocks of the same launch wrote before a grid barrier, so its loads
+// must not take the non-coherent read-only path.
+// I: the index type (size_t, or int where every slot index fits in 31 bits).
+template <class T, int D, int NU, class I, int... K>
+__device__ __forceinline__ void slot_loads(T (&ue)[NU], const T *u0, I nnode, const int (&off)[13],
                                            std::integer_sequence<int, K...>)
 {
     constexpr StepTab tab = make_step_tab();
     constexpr SlotTab st = make_slot_tab();
-    ((ue[K] = u0[(size_t)tab.edir[st.ue[D][K]] * nnode + off[tab.etail[st.ue[D][K]]]]), ...);
+    ((ue[K] = u0[(I)tab.edir[st.ue[D][K]] * nnode + off[tab.etail[st.ue[D][K]]]]), ...);
 }
 
 // Row D of the node's packed mass block (plane layout), in column order.
@@ -981,12 +986,10 @@ __device__ __forceinline__ void slot_mass_row(const T *__restrict__ minv, size_t
 }
 
 // Force of slot D of one node, f = K U restricted to the slot, as hi + lo
-// with COMP (see step_tet), and row D of the node's mass block.
-template <class T, int D, int COMP>
-__device__ __forceinline__ void slot_force(const T *__restrict__ u0, size_t nnode, const int (&off)[13], int have, T &f, T &fl,
-                                           const T *__restrict__ minv, size_t v, T (&row)[7])
+// with COMP (see step_tet).
+template <class T, int D, int COMP, class I>
+__device__ __forceinline__ void slot_curl(const T *u0, I nnode, const int (&off)[13], int have, T &f, T &fl)
 {
-    slot_mass_row<T, D>(minv, v, nnode, row, std::make_integer_sequence<int, 7>{});
     constexpr SlotTab st = make_slot_tab();
     constexpr int nu = st.nu[D], nt = st.nt[D];
     T ue[nu];
@@ -996,6 +999,15 @@ __device__ __forceinline__ void slot_force(const T *__restrict__ u0, size_t nnod
     slot_feeds<T, D, COMP, nu>(ue, have, f, fl, std::make_integer_sequence<int, nt>{});
     f *= T(4);
     fl *= T(4);
+}
+
+// The force of slot D and row D of the node's mass block.
+template <class T, int D, int COMP>
+__device__ __forceinline__ void slot_force(const T *u0, size_t nnode, const int (&off)[13], int have, T &f, T &fl,
+                                           const T *__restrict__ minv, size_t v, T (&row)[7])
+{
+    slot_mass_row<T, D>(minv, v, nnode, row, std::make_integer_sequence<int, 7>{});
+    slot_curl<T, D, COMP>(u0, nnode, off, have, f, fl);
 }
 
 // FP32: at most 32 registers, so 8 blocks fit on an SM and the 1,125 blocks
@@ -1073,6 +1085,219 @@ __global__ void __launch_bounds__(kSlotThreads, sizeof(T) == 4 ? 8 : 1) tet_slot
     Uout[f0] = fma(c, y, u);
     if (zout) zout[f0] = y;
     if (REC && (m & kRecBit)) rec.rz_out[rec.kidx[e0 + d]] = y;
+}
+
+// ------------------------------------------------------ persistent step
+// A grid barrier with a bounded wait, for kernels launched cooperatively
+// (every block resident).  Block 0 adds 2^31 - (expected - 1) to the
+// arrival counter, every other block 1: the counter's top bit flips when
+// the last block arrives and its low bits return to zero, so the barrier
+// resets itself.  One thread per block polls for the flip (relaxed loads;
+// the fence after the last one makes the wait an acquire) at most limit_ns
+// and at most kBarrierPolls times, then sets err and returns false; so
+// does every block that finds err set while it waits.  A launch whose
+// barrier cannot complete therefore ends within about limit_ns, and the
+// host reads err.
+struct GridBarrier {
+    unsigned *count;               // arrivals (zero before the first launch of a run)
+    int *err;                      // nonzero: a wait gave up
+    unsigned expected;             // blocks that arrive at every barrier
+    unsigned long long limit_ns;   // longest wait of one block
+};
+constexpr unsigned kBarrierPolls = 1u << 24;
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned load_relaxed(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ bool grid_barrier(const GridBarrier &b, int *ok_sh)
+{
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        const unsigned add = blockIdx.x == 0 ? 0x80000000u - (b.expected - 1u) : 1u;
+        __threadfence();   // the block's writes (ordered by the block barrier) before the arrival
+        const unsigned old = atomicAdd(b.count, add);
+        int ok = 1;
+        const unsigned long long t0 = global_ns();
+        for (unsigned it = 0; ((load_relaxed(b.count) ^ old) & 0x80000000u) == 0; ++it) {
+            if (*(volatile int *)b.err != 0 || it >= kBarrierPolls || ((it & 31) == 31 && global_ns() - t0 > b.limit_ns)) {
+                atomicExch(b.err, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+        *ok_sh = ok;
+    }
+    __syncthreads();
+    return *ok_sh != 0;
+}
+
+// Arguments of the persistent step.
+template <class T> struct PersistArgs {
+    T *U[2];                  // substep k of the launch reads U[k & 1] and writes U[(k + 1) & 1]
+    T *P;
+    __nv_bfloat16 *cp;        // P's compensation plane (COMP)
+    T a[3], c[3];             // kick and merged drift lengths of the substeps
+    int nsub, nsteps, par0;   // substeps per step, steps of the launch, counter parity of its first step
+    T *rz;                    // Minv P at the receiver slots: two copies of nrz, by counter parity
+    int nrz, keep_rz;         // keep_rz: the last substep of a step writes the next step's copy
+    GridBarrier bar;
+};
+
+// nsteps symplectic lossless steps in one cooperative launch: the
+// slot-split step of tet_slot_kernel, with a grid barrier between
+// substeps instead of a launch boundary.  Each block owns one 32-node unit
+// for the whole launch (the grid covers the mesh in one wave), so the
+// node's record, slot flags and mass row are read once per launch, and P,
+// its compensation and the slot's own U value stay in shared memory
+// between substeps (P in the exchange array the drift reads; the bfloat16
+// rounding of the compensation plane applied where tet_slot_kernel stores
+// it).  The first rec.nsb blocks sample the receivers at the start of every
+// step; block 0's first thread advances the step counter as the first
+// launch of a step does.  Every sum is the slot kernel's, so both give the
+// same bits.
+template <class T, int COMP>
+__global__ void __launch_bounds__(kSlotThreads, sizeof(T) == 4 ? 8 : 1) tet_persist_kernel(size_t nnode, const int2 *__restrict__ nrec,
+                                                                   const unsigned char *__restrict__ pec,
+                                                                   const T *__restrict__ minv, PersistArgs<T> pa,
+                                                                   SrcArgs src, RecArgs<T> rec)
+{
+    static_assert(!COMP || std::is_same<T, float>::value, "compensated updates: FP32");
+    constexpr StepTab tab = make_step_tab();
+    __shared__ T srow[7][7][kSlotNodes];   // the mass rows: [slot][column][node]
+    __shared__ T sx[7][kSlotNodes];        // P (the drift reads the node's seven values)
+    __shared__ T su[7][kSlotNodes];        // the slot's own U value
+    __shared__ T slo[COMP ? 7 : 1][kSlotNodes];   // P's compensation (bfloat16 values)
+    __shared__ int2 srec[kSlotNodes];      // the node records
+    __shared__ unsigned char sm[7][kSlotNodes];   // slot flags
+    __shared__ int sok;
+    const int lane = threadIdx.x, d = threadIdx.y;
+    const int nb = (int)blockIdx.x - rec.nsb;
+    if (nb < 0) {   // a sampling block: the receivers at the start of every step
+        int k = 0;
+        for (int s = 0; s < pa.nsteps; ++s)
+            for (int q = 0; q < pa.nsub; ++q, ++k) {
+                if (k > 0 && !grid_barrier(pa.bar, &sok)) return;
+                if (q == 0) {
+                    RecArgs<T> r = rec;
+                    r.par = (pa.par0 + s) & 1;
+                    r.rz_in = pa.rz + (size_t)r.par * pa.nrz;
+                    sample_receivers<T>(r, (k & 1) ? pa.U[1] : pa.U[0], nnode, d * kSlotNodes + lane, kSlotThreads);
+                }
+            }
+        return;
+    }
+    const int nn = (int)nnode;   // slot indices fit in 31 bits
+    const int v = nb * kSlotNodes + lane;
+    const bool valid = v < nn;
+    if (valid) {
+        const int f0 = d * nn + v;
+        if (d == 0) srec[lane] = __ldg(nrec + v);
+        T row[7];
+        switch (d) {
+        case 0: slot_mass_row<T, 0>(minv, v, nnode, row, std::make_integer_sequence<int, 7>{}); break;
+        case 1: slot_mass_row<T, 1>(minv, v, nnode, row, std::make_integer_sequence<int, 7>{}); break;
+        case 2: slot_mass_row<T, 2>(minv, v, nnode, row, std::make_integer_sequence<int, 7>{}); break;
+        case 3: slot_mass_row<T, 3>(minv, v, nnode, row, std::make_integer_sequence<int, 7>{}); break;
+        case 4: slot_mass_row<T, 4>(minv, v, nnode, row, std::make_integer_sequence<int, 7>{}); break;
+        case 5: slot_mass_row<T, 5>(minv, v, nnode, row, std::make_integer_sequence<int, 7>{}); break;
+        default: slot_mass_row<T, 6>(minv, v, nnode, row, std::make_integer_sequence<int, 7>{}); break;
+        }
+#pragma unroll
+        for (int j = 0; j < 7; ++j) srow[d][j][lane] = row[j];
+        sm[d][lane] = pec[7 * v + d];
+        sx[d][lane] = pa.P[f0];
+        su[d][lane] = pa.U[0][f0];
+        if constexpr (COMP) slo[d][lane] = comp_load(pa.cp, f0);
+    } else {
+        sx[d][lane] = T(0);
+    }
+    __syncthreads();
+    int k = 0;   // substep of the launch
+    for (int s = 0; s < pa.nsteps; ++s) {
+        const int par = (pa.par0 + s) & 1;
+        for (int q = 0; q < pa.nsub; ++q, ++k) {
+            if (k > 0 && !grid_barrier(pa.bar, &sok)) return;
+            // selects, not indexing: a runtime index into the parameter
+            // arrays would copy them to local memory
+            const T *Uin = (k & 1) ? pa.U[1] : pa.U[0];
+            if (q == 0 && rec.adv && v == 0 && d == 0) rec.ctl[1 - par] = rec.ctl[par] + 1;
+            if (valid) {
+                const int2 r = srec[lane];
+                const int have = (int)((unsigned)r.x >> 26), sy = r.x & 0x3ffffff, sz = r.y;
+                int off[13];
+#pragma unroll
+                for (int t = 0; t < 13; ++t)
+                    off[t] = (tab.treq[t] & ~have) == 0 ? tab.tail[t][0] + tab.tail[t][1] * sy + tab.tail[t][2] * sz : 0;
+                T f = 0, fl = 0;
+                const T *u0 = Uin + v;
+                switch (d) {
+                case 0: slot_curl<T, 0, COMP>(u0, nn, off, have, f, fl); break;
+                case 1: slot_curl<T, 1, COMP>(u0, nn, off, have, f, fl); break;
+                case 2: slot_curl<T, 2, COMP>(u0, nn, off, have, f, fl); break;
+                case 3: slot_curl<T, 3, COMP>(u0, nn, off, have, f, fl); break;
+                case 4: slot_curl<T, 4, COMP>(u0, nn, off, have, f, fl); break;
+                case 5: slot_curl<T, 5, COMP>(u0, nn, off, have, f, fl); break;
+                default: slot_curl<T, 6, COMP>(u0, nn, off, have, f, fl); break;
+                }
+                const unsigned char m = sm[d][lane];
+                if (!(m & kPecBit)) {
+                    const T a = q == 0 ? pa.a[0] : q == 1 ? pa.a[1] : pa.a[2];
+                    T sv = 0;
+                    if (m & kSrcBit) {
+                        SrcArgs sq = src;
+                        sq.q = q;
+                        sq.par = par;
+                        sv = (T)source_load(sq, 7 * v + d);
+                    }
+                    T x = sx[d][lane];
+                    if constexpr (COMP) {
+                        T lp = slo[d][lane];
+                        const T p1 = mul_rn(-a, f);
+                        T t = fma(-a, f, -p1) + lp;
+                        t = fma(-a, fl, t);
+                        if (m & kSrcBit) t = fma(a, sv, t);
+                        T e;
+                        const T s1 = two_sum(x, p1, e);
+                        x = two_sum(s1, t + e, lp);
+                        slo[d][lane] = __bfloat162float(__float2bfloat16_rn(lp));   // the plane holds bfloat16
+                    } else {
+                        x = fma(-a, f, x);
+                        if (m & kSrcBit) x = fma(a, sv, x);
+                    }
+                    sx[d][lane] = x;
+                }
+            }
+            __syncthreads();
+            if (valid) {
+                T y = 0;
+#pragma unroll
+                for (int j = 0; j < 7; ++j) y = fma(srow[d][j][lane], sx[j][lane], y);
+                const T u = fma(q == 0 ? pa.c[0] : q == 1 ? pa.c[1] : pa.c[2], y, su[d][lane]);
+                su[d][lane] = u;
+                ((k & 1) ? pa.U[0] : pa.U[1])[d * nn + v] = u;
+                if (pa.keep_rz && q == pa.nsub - 1 && (sm[d][lane] & kRecBit))
+                    pa.rz[(size_t)(1 - par) * pa.nrz + rec.kidx[7 * v + d]] = y;
+            }
+        }
+    }
+    if (valid) {
+        const int f0 = d * nn + v;
+        pa.P[f0] = sx[d][lane];
+        if constexpr (COMP) comp_store(pa.cp, f0, slo[d][lane]);
+    }
 }
 
 // Adjoint of the second loss factor of a lossy middle kick and the loss
@@ -1665,6 +1890,13 @@ struct TetFemSim : Sim {
     // the faster, bandwidth-bound one).
     static constexpr size_t kSlotDefaultMaxNodes = 262144;
     bool step_tuned = false;        // the block size depends on the mesh only: tuned once per handle
+    // the persistent step (tet_persist_kernel, a tuner candidate): its grid
+    // barrier's counter and error word, the resident-block capacity of its
+    // launch (-1: not queried yet), and whether the current run launched it
+    bool persist = false;
+    int persist_cap = -1;
+    bool bar_used = false;
+    DevBuf d_bar;
     DevBuf d_tet_edge, d_inc_ptr, d_inc, d_nrec, d_pec, d_eps, d_minv, d_U, d_P, d_Uold, d_status;
     // FP32 runs: bfloat16 compensation planes of U and then P, one
     // allocation (plane layout, updated in place; zero after a reset)
@@ -1891,6 +2123,10 @@ struct TetFemSim : Sim {
         else
             up(d_eps, eps_h);
         if (!d_status.p) d_status.alloc(sizeof(int));
+        if (!d_bar.p) {
+            d_bar.alloc(16);
+            d_bar.zero(stream);
+        }
         d_status.zero(stream);
         // FP64 packed blocks for the stability limit: the run's own array in
         // FP64 runs, a copy kept with the Lanczos workspace in FP32 runs
@@ -1921,21 +2157,26 @@ struct TetFemSim : Sim {
     }
 
     // Launch shape of the fused step: the node kernel at four block sizes
-    // (32, 64, 128, 256 threads) or the slot-split kernel.  It depends on
-    // the mesh, not the material, and changes no result, so it is chosen once
-    // per handle inside its first unrecorded run of at least 132 steps
-    // (symplectic or leapfrog): each candidate advances 12 real steps of that run from
-    // a CUDA graph, as the loop runs them, twice over, and the fastest is kept
-    // for the rest of the run and later ones.  (Timed on idle steps outside
-    // a run, the candidates ranked differently from the loop.)  Before that
-    // the slot-split kernel runs on meshes of up to kSlotDefaultMaxNodes
-    // nodes and the 64-thread node kernel on larger ones.  The environment variable
-    // EMS_TET_STEP_BLOCK (32, 64, 128, 256 or slot) forces one;
-    // EMS_TET_TUNE_LOG prints the candidates' times to stderr.
-    static constexpr int kShapes = 5, kTuneRounds = 2;
+    // (32, 64, 128, 256 threads), the slot-split kernel, or the persistent
+    // step (the slot-split step for a graph's 12 steps in one cooperative
+    // launch with grid barriers between substeps; symplectic lossless runs
+    // whose grid fits in one wave, else its runs take the slot-split
+    // kernel).  It depends on the mesh, not the material, and changes no
+    // result, so it is chosen once per handle inside its first unrecorded
+    // run of at least 156 steps (symplectic or leapfrog): each available
+    // candidate advances 12 real steps of that run from a CUDA graph, as the
+    // loop runs them, twice over, and the fastest is kept for the rest of
+    // the run and later ones.  (Timed on idle steps outside a run, the
+    // candidates ranked differently from the loop.)  Before that the
+    // slot-split kernel runs on meshes of up to kSlotDefaultMaxNodes nodes
+    // and the 64-thread node kernel on larger ones.  The environment
+    // variable EMS_TET_STEP_BLOCK (32, 64, 128, 256, slot or persist) forces
+    // one; EMS_TET_TUNE_LOG prints the candidates' times to stderr.
+    static constexpr int kShapes = 6, kTuneRounds = 2, kShapeSlot = 4, kShapePersist = 5;
     void set_shape(int ci)
     {
-        slot_split = ci == kShapes - 1;
+        slot_split = ci >= kShapeSlot;
+        persist = ci == kShapePersist;
         step_block = kStepBlocks[ci < 4 ? ci : 0];
     }
     void force_launch_shape()
@@ -1943,11 +2184,52 @@ struct TetFemSim : Sim {
         const char *env = std::getenv("EMS_TET_STEP_BLOCK");
         if (step_tuned || !env) return;
         step_tuned = true;
-        if (std::strcmp(env, "slot") == 0) { set_shape(kShapes - 1); return; }
+        if (std::strcmp(env, "slot") == 0) { set_shape(kShapeSlot); return; }
+        if (std::strcmp(env, "persist") == 0) { set_shape(kShapePersist); return; }
         const int b = std::atoi(env);
         for (int c = 0; c < 4; ++c)
             if (kStepBlocks[c] == b) { set_shape(c); return; }
-        throw Error{EMS_ERR_INVALID_ARGUMENT, "EMS_TET_STEP_BLOCK must be 32, 64, 128, 256 or slot"};
+        throw Error{EMS_ERR_INVALID_ARGUMENT, "EMS_TET_STEP_BLOCK must be 32, 64, 128, 256, slot or persist"};
+    }
+
+    // Blocks of the persistent step that are resident at once on this
+    // device (its cooperative launch needs the whole grid resident).
+    int persist_capacity()
+    {
+        if (persist_cap >= 0) return persist_cap;
+        int dev = 0, nsm = 0, nbps = 0;
+        EMS_CUDA(cudaGetDevice(&dev));
+        EMS_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        if (fp64) EMS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbps, tet_persist_kernel<double, 0>, kSlotThreads, 0));
+        else EMS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbps, tet_persist_kernel<float, 1>, kSlotThreads, 0));
+        persist_cap = nbps * nsm;
+        return persist_cap;
+    }
+    // Grid of the persistent step: the receiver-sampling blocks (eight
+    // lanes per receiver), then one block per 32 nodes.
+    unsigned persist_grid(bool sampling) const
+    {
+        const int nsb = sampling && nobs > 0 ? (nobs + kSlotThreads / 8 - 1) / (kSlotThreads / 8) : 0;
+        return (unsigned)nsb + (unsigned)((nnode + kSlotNodes - 1) / kSlotNodes);
+    }
+    bool can_persist(bool symp)
+    {
+        return symp && !has_loss && persist_grid(true) <= (unsigned)persist_capacity();
+    }
+    // The barrier of a persistent launch: the whole grid arrives, a wait
+    // gives up after one second.  EMS_TET_BARRIER_PROBE=1 makes the barrier
+    // expect one block more than the grid holds, a count that is never
+    // reached, so every wait runs out (after 20 ms) and the run returns
+    // EMS_ERR_DEVICE_TIMEOUT: the test of that status path.
+    GridBarrier barrier_args(unsigned grid) const
+    {
+        GridBarrier b{d_bar.as<unsigned>(), d_bar.as<int>() + 1, grid, 1000000000ull};
+        const char *probe = std::getenv("EMS_TET_BARRIER_PROBE");
+        if (probe && std::strcmp(probe, "1") == 0) {
+            b.expected = grid + 1;
+            b.limit_ns = 20000000ull;
+        }
+        return b;
     }
 
     // Conductivity as a per-node loss rate: rho_v = sum sigma_T w / sum
@@ -2374,6 +2656,70 @@ struct TetFemSim : Sim {
         return nl;
     }
 
+    // nst symplectic lossless steps from step parity par0 in one
+    // cooperative launch of tet_persist_kernel (U from Uc, the pair swapped
+    // when the launch runs an odd number of substeps).  idle: a = c = 0, no
+    // sources, receivers or counter (the dominant-kernel timing).  Returns 1.
+    template <class T>
+    int persist_launch(int nst, T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa, int par0, Comp cm,
+                       bool idle = false)
+    {
+        PersistArgs<T> pa{};
+        pa.U[0] = Uc;
+        pa.U[1] = Uo;
+        pa.P = Pc;
+        pa.cp = cm.p;
+        for (int q = 0; q < sc.nsub; ++q) {
+            pa.a[q] = idle ? T(0) : (T)sc.sub[q];
+            pa.c[q] = idle ? T(0) : (T)sc.c[q];
+        }
+        pa.nsub = sc.nsub;
+        pa.nsteps = nst;
+        pa.par0 = par0;
+        pa.rz = d_rz.as<T>();
+        pa.nrz = std::max(nk, 1);
+        pa.keep_rz = !idle && nk > 0;
+        const RecArgs<T> ra = idle ? RecArgs<T>{} : rec_args<T>(sc, 0, par0, true);
+        const unsigned grid = persist_grid(!idle);
+        pa.bar = barrier_args(grid);
+        const SrcArgs src = idle ? SrcArgs{} : sa;
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(kSlotNodes, 7);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        const int2 *nr = d_nrec.as<int2>();
+        const unsigned char *pc = d_pec.as<unsigned char>();
+        const T *mv = d_minv.as<T>();
+        if constexpr (std::is_same<T, float>::value) {
+            if (cm.p) EMS_CUDA(cudaLaunchKernelEx(&cfg, tet_persist_kernel<T, 1>, nnode, nr, pc, mv, pa, src, ra));
+            else EMS_CUDA(cudaLaunchKernelEx(&cfg, tet_persist_kernel<T, 0>, nnode, nr, pc, mv, pa, src, ra));
+        } else {
+            EMS_CUDA(cudaLaunchKernelEx(&cfg, tet_persist_kernel<T, 0>, nnode, nr, pc, mv, pa, src, ra));
+        }
+        bar_used = true;
+        if ((nst * sc.nsub) & 1) std::swap(Uc, Uo);
+        return 1;
+    }
+
+    // nst steps of the time loop from step parity par0: one persistent
+    // launch in that launch shape, else enqueue_step per step.  Returns the
+    // number of launches.
+    template <class T>
+    int enqueue_steps(int nst, T *&Uc, T *&Pc, T *&Uo, const Schedule &sc, const SrcArgs &sa, int par0, Comp cm)
+    {
+        if (nst <= 0) return 0;
+        if (persist && can_persist(sc.symp)) return persist_launch<T>(nst, Uc, Pc, Uo, sc, sa, par0, cm);
+        int nl = 0;
+        for (int st = 0; st < nst; ++st) nl += enqueue_step<T>(Uc, Pc, Uo, sc, sa, nullptr, (par0 + st) & 1, nullptr, true, cm);
+        return nl;
+    }
+
     // Minv P of the receiver slots into rz[par] (symplectic runs, before the
     // first step of a run or of a recomputed segment).
     template <class T> void rz_init(const T *Pc, int par)
@@ -2499,6 +2845,7 @@ struct TetFemSim : Sim {
         // record for ems_tetfem_backward: symplectic runs from the reset state
         const bool record = ckpt_nsnap > 0 && symp && fresh && nsteps > 0;
         rec_nsteps = -1;
+        bar_used = false;   // set when this run enqueues a persistent launch
         std::vector<double> times;
         double t_end = 0.0;
         const SrcArgs sa = prepare_run(nsteps, sc, times, t_end);
@@ -2519,6 +2866,7 @@ struct TetFemSim : Sim {
             cudaGraphExec_t exec = nullptr;
             const void *start = nullptr;
             int par = 0;
+            int launches = 0;   // kernel launches of one replay
             ~StepGraph()
             {
                 if (exec) cudaGraphExecDestroy(exec);
@@ -2533,33 +2881,39 @@ struct TetFemSim : Sim {
                     if (x) cudaEventDestroy(x);
             }
         } tev;
-        int per_graph = 0, par = 0;   // par: parity of the next step's counter copy
+        int par = 0;   // parity of the next step's counter copy
         auto capture = [&](StepGraph &G, T *u, T *p, T *o, int par0) {
             G.start = u;
             G.par = par0;
             int nl = 0;
             EMS_CUDA(cudaStreamSynchronize(stream));
             EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-            for (int st = 0; st < kGraphSteps; ++st)
-                nl += enqueue_step<T>(u, p, o, sc, sa, nullptr, (par0 + st) & 1, nullptr, true, cm);
+            try {
+                nl += enqueue_steps<T>(kGraphSteps, u, p, o, sc, sa, par0, cm);
+            } catch (...) {   // end the capture before the error leaves
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(stream, &g);
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                throw;
+            }
             cudaError_t ce = cudaStreamEndCapture(stream, &G.g);
             if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce)};
             ce = cudaGraphInstantiate(&G.exec, G.g, 0);
             if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)};
-            per_graph = nl;
+            G.launches = nl;
         };
         long long launches = 0;
         auto advance = [&](int k) {
-            cudaGraphExec_t exec = nullptr;
+            const StepGraph *sg = nullptr;
             for (auto &G : graph)
-                if (G.exec && G.start == Uc && G.par == par) exec = G.exec;
-            const int nrep = exec ? k / kGraphSteps : 0;
-            for (int r = 0; r < nrep; ++r) EMS_CUDA(cudaGraphLaunch(exec, stream));
-            launches += (long long)nrep * per_graph;
-            for (int st = nrep * kGraphSteps; st < k; ++st) {
-                launches += enqueue_step<T>(Uc, Pc, Uo, sc, sa, nullptr, par, nullptr, true, cm);
-                par ^= 1;
-            }
+                if (G.exec && G.start == Uc && G.par == par) sg = &G;
+            const int nrep = sg ? k / kGraphSteps : 0;
+            for (int r = 0; r < nrep; ++r) EMS_CUDA(cudaGraphLaunch(sg->exec, stream));
+            launches += (long long)nrep * (sg ? sg->launches : 0);
+            const int rest = k - nrep * kGraphSteps;
+            launches += enqueue_steps<T>(rest, Uc, Pc, Uo, sc, sa, par, cm);
+            par ^= rest & 1;
         };
         int seg_len = 0, nseg = 0;
         if (record) {
@@ -2570,18 +2924,31 @@ struct TetFemSim : Sim {
         // launch-shape tuning in the first unrecorded run long enough: every
         // candidate's graph of kGraphSteps steps starts from the assignment
         // (Uc, parity 0) and returns to it, so they are captured up front
-        const int tune_steps = kShapes * kTuneRounds * kGraphSteps;
+        int cl[kShapes], ncl = 0;   // the candidates this run can launch
+        for (int ci = 0; ci < kShapes; ++ci)
+            if (ci != kShapePersist || can_persist(symp)) cl[ncl++] = ci;
+        const int tune_steps = ncl * kTuneRounds * kGraphSteps;
         const bool tuning = !step_tuned && !record && nsteps >= tune_steps + kGraphSteps;
         if (tuning) {
-            for (int ci = 0; ci < kShapes; ++ci) {
-                set_shape(ci);
-                capture(cand[ci], Uc, Pc, Uo, 0);
+            int kept = 0;
+            for (int i = 0; i < ncl; ++i) {
+                set_shape(cl[i]);
+                try {
+                    capture(cand[cl[i]], Uc, Pc, Uo, 0);
+                } catch (const Error &) {   // a device without cooperative launches in graphs: no persistent step
+                    if (cl[i] != kShapePersist) throw;
+                    persist_cap = 0;
+                    continue;
+                }
+                cl[kept++] = cl[i];
             }
+            ncl = kept;
             for (auto &x : tev.e) EMS_CUDA(cudaEventCreate(&x));
         } else if ((record ? seg_len : nsteps) >= kGraphSteps) {
             capture(graph[0], Uc, Pc, Uo, 0);
             if (record && symp && sc.nsub % 2 == 1) capture(graph[1], Uo, Pc, Uc, 1);
         }
+        if (bar_used) EMS_CUDA(cudaMemsetAsync(d_bar.p, 0, 8, stream));   // the persistent step's barrier
         EMS_CUDA(cudaEventRecord(ev0, stream));
         if (symp) {
             tet_drift_kernel<T><<<nb128, 128, 0, stream>>>(nnode, d_minv.as<T>(), Pc, Uc, (T)sc.hfirst);
@@ -2591,34 +2958,38 @@ struct TetFemSim : Sim {
         int done = 0;   // steps advanced by the tuning graphs
         if (tuning) {
             for (int r = 0; r < kTuneRounds; ++r)
-                for (int ci = 0; ci < kShapes; ++ci) {
-                    EMS_CUDA(cudaEventRecord(tev.e[r * kShapes + ci], stream));
-                    EMS_CUDA(cudaGraphLaunch(cand[ci].exec, stream));
-                    launches += per_graph;
+                for (int i = 0; i < ncl; ++i) {
+                    EMS_CUDA(cudaEventRecord(tev.e[r * ncl + i], stream));
+                    EMS_CUDA(cudaGraphLaunch(cand[cl[i]].exec, stream));
+                    launches += cand[cl[i]].launches;
                 }
-            EMS_CUDA(cudaEventRecord(tev.e[kShapes * kTuneRounds], stream));
-            EMS_CUDA(cudaEventSynchronize(tev.e[kShapes * kTuneRounds]));
+            EMS_CUDA(cudaEventRecord(tev.e[ncl * kTuneRounds], stream));
+            EMS_CUDA(cudaEventSynchronize(tev.e[ncl * kTuneRounds]));
             float best[kShapes] = {};
             for (int r = 0; r < kTuneRounds; ++r)
-                for (int ci = 0; ci < kShapes; ++ci) {
+                for (int i = 0; i < ncl; ++i) {
                     float ms = 0.0f;
-                    EMS_CUDA(cudaEventElapsedTime(&ms, tev.e[r * kShapes + ci], tev.e[r * kShapes + ci + 1]));
-                    if (r == 0 || ms < best[ci]) best[ci] = ms;
+                    EMS_CUDA(cudaEventElapsedTime(&ms, tev.e[r * ncl + i], tev.e[r * ncl + i + 1]));
+                    if (r == 0 || ms < best[i]) best[i] = ms;
                 }
-            int pick = 0;
-            for (int ci = 1; ci < kShapes; ++ci)
-                if (best[ci] < best[pick]) pick = ci;
-            if (std::getenv("EMS_TET_TUNE_LOG"))   // diagnostic: the candidates' times per step
-                std::fprintf(stderr, "tet step tuning (us per step): node32 %.3f node64 %.3f node128 %.3f node256 %.3f slot %.3f\n",
-                             1e3 * best[0] / kGraphSteps, 1e3 * best[1] / kGraphSteps, 1e3 * best[2] / kGraphSteps,
-                             1e3 * best[3] / kGraphSteps, 1e3 * best[4] / kGraphSteps);
+            int pi = 0;
+            for (int i = 1; i < ncl; ++i)
+                if (best[i] < best[pi]) pi = i;
+            const int pick = cl[pi];
+            if (std::getenv("EMS_TET_TUNE_LOG")) {   // diagnostic: the candidates' times per step
+                static const char *names[kShapes] = {"node32", "node64", "node128", "node256", "slot", "persist"};
+                std::fprintf(stderr, "tet step tuning (us per step):");
+                for (int i = 0; i < ncl; ++i) std::fprintf(stderr, " %s %.3f", names[cl[i]], 1e3 * best[i] / kGraphSteps);
+                std::fprintf(stderr, "\n");
+            }
             set_shape(pick);
             step_tuned = true;
             std::swap(graph[0].g, cand[pick].g);
             std::swap(graph[0].exec, cand[pick].exec);
             graph[0].start = cand[pick].start;
             graph[0].par = cand[pick].par;
-            done = tune_steps;
+            graph[0].launches = cand[pick].launches;
+            done = ncl * kTuneRounds * kGraphSteps;
         }
         if (record) {
             // snapshot of the merged state at the start of every segment
@@ -2653,6 +3024,13 @@ struct TetFemSim : Sim {
         traces.resize((size_t)nobs * nsamp * 4);
         for (int r = 0; r < nobs; ++r)
             for (int s = 0; s < nsamp; ++s) traces[((size_t)r * nsamp + s) * 4] = times[s] * tscale;
+        if (bar_used) {   // a grid barrier of the persistent step that gave up
+            int err = 0;
+            EMS_CUDA(cudaMemcpy(&err, d_bar.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost));
+            if (err)
+                throw Error{EMS_ERR_DEVICE_TIMEOUT,
+                            "a grid barrier of the persistent step timed out; the fields are invalid (reset the handle)"};
+        }
     }
 
     // ---- discrete adjoint of the recorded run
@@ -3039,15 +3417,37 @@ struct TetFemSim : Sim {
         // unchanged and copies U between the two buffers the loop
         // alternates), replayed; launched one by one, the kernels would wait
         // on the host's launch rate
+        // (the persistent step: one idle launch of 12 steps, timed per substep)
         constexpr int kLaunches = 12;
+        const Schedule sc = schedule();
+        const bool pers = persist && can_persist(sc.symp);
+        const int per_graph = pers ? kLaunches * sc.nsub : kLaunches;   // substeps of one replay
         cudaGraph_t g = nullptr;
         cudaGraphExec_t exec = nullptr;
+        if (pers) EMS_CUDA(cudaMemsetAsync(d_bar.p, 0, 8, stream));
         EMS_CUDA(cudaStreamSynchronize(stream));
         EMS_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        for (int r = 0; r < kLaunches; ++r) idle_step(nbv, r % 2);
+        try {
+            if (pers) {
+                auto body = [&](auto tag) {
+                    using T = decltype(tag);
+                    T *u = d_U.as<T>(), *p = d_P.as<T>(), *o = d_Uold.as<T>();
+                    persist_launch<T>(kLaunches, u, p, o, sc, SrcArgs{}, 0, comp(), true);
+                };
+                if (fp64) body(double()); else body(float());
+            } else {
+                for (int r = 0; r < kLaunches; ++r) idle_step(nbv, r % 2);
+            }
+        } catch (...) {
+            cudaGraph_t gg = nullptr;
+            cudaStreamEndCapture(stream, &gg);
+            if (gg) cudaGraphDestroy(gg);
+            cudaGetLastError();
+            throw;
+        }
         cudaError_t ce = cudaStreamEndCapture(stream, &g);
         if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, g, 0);
-        const int reps = std::max(1, launches / kLaunches);
+        const int reps = std::max(1, launches / per_graph);
         if (ce == cudaSuccess) ce = cudaGraphLaunch(exec, stream);
         if (ce == cudaSuccess) ce = cudaEventRecord(ev0, stream);
         for (int r = 0; r < reps && ce == cudaSuccess; ++r) ce = cudaGraphLaunch(exec, stream);
@@ -3058,7 +3458,12 @@ struct TetFemSim : Sim {
         if (exec) cudaGraphExecDestroy(exec);
         if (g) cudaGraphDestroy(g);
         if (ce != cudaSuccess) throw Error{EMS_ERR_CUDA, std::string("dominant-kernel timing: ") + cudaGetErrorString(ce)};
-        *ms = t / (reps * kLaunches);
+        if (pers) {
+            int err = 0;
+            EMS_CUDA(cudaMemcpy(&err, d_bar.as<int>() + 1, sizeof(int), cudaMemcpyDeviceToHost));
+            if (err) throw Error{EMS_ERR_DEVICE_TIMEOUT, "a grid barrier of the persistent step timed out"};
+        }
+        *ms = t / (reps * per_graph);
         const size_t w = fp64 ? 8 : 4;
         // unique bytes of one substep: node records (8 B per node) + U read
         // once (the neighbours' reads hit L1/L2) + P read and written + U
@@ -3066,7 +3471,8 @@ struct TetFemSim : Sim {
         // compensation plane read and written)
         *bytes = (double)nnode * 8 + (double)nslot * 4 * w + (double)(28 * nnode) * w + (double)nslot +
                  (fp64 ? 0.0 : (double)nslot * 2 * 2);
-        if (slot_split) *name = fp64 ? "tet_slot_kernel<double>" : "tet_slot_kernel<float>";
+        if (pers) *name = fp64 ? "tet_persist_kernel<double> (per substep)" : "tet_persist_kernel<float> (per substep)";
+        else if (slot_split) *name = fp64 ? "tet_slot_kernel<double>" : "tet_slot_kernel<float>";
         else *name = fp64 ? "tet_step_kernel<double>" : "tet_step_kernel<float>";
     }
 };

@@ -36,8 +36,8 @@ enum ems_status {
     EMS_ERR_OUT_OF_MEMORY = -3,     /* device or host allocation failed */
     EMS_ERR_IO = -4,                /* file missing / unreadable / malformed */
     EMS_ERR_STATE = -5,             /* call not valid in the handle's state */
-    EMS_ERR_DEVICE_TIMEOUT = -6,    /* reserved for a bounded device-side wait that gives up; no kernel of
-                                       this version waits on another, so no call returns it */
+    EMS_ERR_DEVICE_TIMEOUT = -6,    /* a bounded device-side wait gave up: a grid barrier of the persistent
+                                       tetrahedral step (ems_run); the fields are invalid, reset the handle */
     EMS_ERR_NOT_FINITE = -7,        /* NaN/Inf in the fields after ems_run (the run's traces stay readable),
                                        or a tetrahedral mass block that is not positive definite */
     EMS_ERR_UNSUPPORTED = -8        /* combination not implemented */
@@ -313,10 +313,13 @@ int ems_time_dominant_kernel(ems_sim *sim, int launches, double *ms_per_launch, 
                              char *name, size_t name_cap);
 /* Threads per block (x, y, z) of the main time-step kernels as the handle's
  * autotuner chose them by timing candidates on its own grid: tetrahedral
- * handles time the node kernel at 32, 64, 128, 256 threads and the
- * slot-split kernel (block 32 x 7: one warp per edge direction of 32 nodes)
- * when the material is set up (EMS_TET_STEP_BLOCK = 32, 64, 128, 256 or slot
- * forces one); FDTD handles time the shapes 32x8, 32x4,
+ * handles time the node kernel at 32, 64, 128, 256 threads, the slot-split
+ * kernel (block 32 x 7: one warp per edge direction of 32 nodes) and the
+ * persistent step (the same block; 12 steps per cooperative launch with grid
+ * barriers between substeps, for symplectic lossless runs whose grid fits on
+ * the device at once; ems_time_dominant_kernel names it) inside their first
+ * unrecorded run of at least 156 steps (EMS_TET_STEP_BLOCK = 32, 64, 128,
+ * 256, slot or persist forces one); FDTD handles time the shapes 32x8, 32x4,
  * 64x4, 128x2, 256x1, 64x2 on the first steps of their first run of at
  * least 40 steps (EMS_FDTD_BLOCK="XxY" forces one; 32x8 before tuning).
  * Launch shapes change no result.  Zeros for solvers with fixed shapes.

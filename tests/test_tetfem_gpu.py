@@ -240,14 +240,16 @@ _LAUNCH_SHAPE_CASE = (
 @pytest.mark.parametrize("prec,lossy", [("fp32", "0"), ("fp64", "0"), ("fp32", "1")], ids=["fp32", "fp64", "fp32-lossy"])
 def test_step_launch_shapes_change_no_result(prec, lossy):
     # forced launch shapes (EMS_TET_STEP_BLOCK) in child processes: the node
-    # kernel at two block sizes and the slot-split kernel (seven warps per 32
-    # nodes) are launch shapes of the same arithmetic, so traces, fields and
-    # the adjoint gradient are bit-identical; the autotuner picks one of them
+    # kernel at two block sizes, the slot-split kernel (seven warps per 32
+    # nodes) and the persistent step (the slot-split step with grid barriers
+    # between substeps; lossy runs fall back to the slot-split kernel) are
+    # launch shapes of the same arithmetic, so traces, fields and the adjoint
+    # gradient are bit-identical; the autotuner picks one of them
     import os
     import subprocess
     import sys
     out = {}
-    for b in ("", "32", "256", "slot"):
+    for b in ("", "32", "256", "slot", "persist"):
         env = dict(os.environ)
         env.pop("EMS_TET_STEP_BLOCK", None)
         if b:
@@ -258,14 +260,49 @@ def test_step_launch_shapes_change_no_result(prec, lossy):
         assert r.returncode == 0, r.stderr
         shape = tuple(int(v) for v in r.stdout.strip().splitlines()[-1].split())
         assert shape in ((32, 1, 1), (64, 1, 1), (128, 1, 1), (256, 1, 1), (32, 7, 1))
-        if b == "slot":
+        if b in ("slot", "persist"):
             assert shape == (32, 7, 1)
         elif b:
             assert shape == (int(b), 1, 1)
         out[b] = np.load(path)
         os.remove(path)
-    for b in ("32", "256", "slot"):
+    for b in ("32", "256", "slot", "persist"):
         assert np.array_equal(out[""], out[b]), b
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("integ", [ems.SYMP2, ems.SYMP4], ids=["symp2", "symp4"])
+def test_persistent_step_matches_the_slot_kernel(monkeypatch, integ, prec):
+    # the persistent step (one cooperative launch per CUDA graph of 12 steps,
+    # grid barriers between substeps, P and its compensation kept in shared
+    # memory between them) gives the slot-split kernel's bits: 30 receivers
+    # (two sampling blocks), samples every third step, a run continued
+    # across calls (a graph of 12 steps and a shorter remainder launch)
+    n = (10, 9, 8)
+    rng = np.random.default_rng(11)
+    eps = rng.uniform(1, 4, 6 * n[0] * n[1] * n[2])
+    recs = rng.uniform(0.5, 1.0, (30, 3)) * (np.array(n) - 1.0)
+    P = {"fp32": ems.FP32, "fp64": ems.FP64}[prec]
+    out = {}
+    for shape in ("slot", "persist"):
+        monkeypatch.setenv("EMS_TET_STEP_BLOCK", shape)
+        s = ems.TetFemSimulation(n, H, 1, integ, P, dt=0.0, cfl_fraction=0.85, time_frequency=3)
+        s.set_material(eps)
+        s.add_dipole(np.array([4.1, 3.3, 4.2]) * H, (0.2, 0.3, 1.0), ems.WAVE_RICKER, 4e10, 1.0)
+        for r in recs:
+            s.add_receiver(r * H)
+        s.run(40)
+        t1 = s.traces().copy()
+        s.run(23)
+        t2 = s.traces().copy()
+        name = s.time_dominant_kernel(24)[2]
+        out[shape] = (t1, t2, s.get_field(0), s.get_field(1), name)
+        s.close()
+    for i in range(4):
+        assert np.array_equal(out["slot"][i], out["persist"][i]), i
+    assert np.abs(out["slot"][1][..., 1:]).max() > 0
+    assert out["slot"][4].startswith("tet_slot_kernel")
+    assert out["persist"][4].startswith("tet_persist_kernel")
 
 
 @pytest.mark.parametrize("integ", [oracle.SYMP4, oracle.LEAPFROG], ids=["symp4", "leapfrog"])
