@@ -1939,10 +1939,13 @@ template <class T> void Tet2Sim::backward_t(const double *tg, double *grad)
             for (int c = 0; c < 3; ++c) gt[(size_t)n * nd3 + 3 * r + c] = tg[((size_t)r * nsamp + n / tf) * 4 + 1 + c];
     DevBuf a_dof, a_ptr, a_idx, a_coef, a_g;
     up(a_dof, rd); up(a_ptr, rp); up(a_idx, ri); up(a_coef, rc); up(a_g, gt);
-    // buffers: the segment's states, drift increments, adjoint state, gradient, end state
-    DevBuf segb, Ys, Ub, Ubc, Pb, gd, keepU, keepP;
-    segb.alloc((size_t)seg * snap_bytes());
-    Ys.alloc((size_t)(nq + 1) * w);
+    // buffers: the drift increments of the segment's steps, adjoint state,
+    // gradient, end state.  Increment q of step n (q(M) P before the first
+    // drift, q = 0, and after kick q, q = 1..nq) sits in slot n * nq + q of
+    // the segment, so the last one of step n is the first of step n + 1 (the
+    // same P); the recompute keeps them and the reversed steps read them.
+    DevBuf Ys, Ub, Ubc, Pb, gd, keepU, keepP;
+    Ys.alloc(((size_t)seg * nq + 1) * w);
     Ub.alloc(ndof * 8);
     Pb.alloc(w);
     if (!fp64) Ubc.alloc(w);
@@ -1954,7 +1957,8 @@ template <class T> void Tet2Sim::backward_t(const double *tg, double *grad)
     Ub.zero(stream); Pb.zero(stream); gd.zero(stream);
     if (Ubc.p) Ubc.zero(stream);
     T *Ubr = fp64 ? Ub.as<T>() : Ubc.as<T>();   // Ubar in the run precision (right-hand side of the solves)
-    auto Y = [&](int k) { return Ys.as<T>() + (size_t)k * ndof; };
+    int nseg0 = 0;   // first step of the segment being reversed
+    auto Y = [&](int n, int q) { return Ys.as<T>() + ((size_t)(n - nseg0) * nq + q) * ndof; };
     const int nd = (int)std::max<size_t>(dips.size(), 1);
     int *ctl = d_ctl.as<int>();
     auto narrowP = [&]() {
@@ -1962,28 +1966,19 @@ template <class T> void Tet2Sim::backward_t(const double *tg, double *grad)
     };
     for (int s = (nsteps - 1) / seg; s >= 0; --s) {
         const int n0 = s * seg, n1 = std::min(nsteps, n0 + seg);
-        // recompute the segment from its snapshot, keeping (U_n, P_n)
+        nseg0 = n0;
+        // recompute the segment from its snapshot (the forward step's
+        // kernels and arithmetic: the half drift with the previous step's
+        // last increment, then per substep stiffness, kick, source and the
+        // solve whose drift ends the substep), keeping the increments
         const char *sb = d_snap.as<char>() + (size_t)s * snap_bytes();
         EMS_CUDA(cudaMemcpyAsync(d_U.p, sb, w, cudaMemcpyDeviceToDevice, stream));
         EMS_CUDA(cudaMemcpyAsync(d_P.p, sb + w, ndof * 8, cudaMemcpyDeviceToDevice, stream));
         narrowP();
-        enqueue_solve<T, FIN_NONE>(rhs_P<T>(), 0.0);
+        enqueue_solve<T, FIN_NONE>(rhs_P<T>(), 0.0, Y(n0, 0));
         t2_set_kernel<<<1, 1, 0, stream>>>(ctl, n0);
         for (int n = n0; n < n1; ++n) {
-            char *dst = segb.as<char>() + (size_t)(n - n0) * snap_bytes();
-            EMS_CUDA(cudaMemcpyAsync(dst, d_U.p, w, cudaMemcpyDeviceToDevice, stream));
-            EMS_CUDA(cudaMemcpyAsync(dst + w, d_P.p, ndof * 8, cudaMemcpyDeviceToDevice, stream));
-            if (n + 1 < n1) enqueue_step<T>(false);
-        }
-        // reversed steps
-        for (int n = n1 - 1; n >= n0; --n) {
-            const char *src = segb.as<char>() + (size_t)(n - n0) * snap_bytes();
-            EMS_CUDA(cudaMemcpyAsync(d_U.p, src, w, cudaMemcpyDeviceToDevice, stream));
-            EMS_CUDA(cudaMemcpyAsync(d_P.p, src + w, ndof * 8, cudaMemcpyDeviceToDevice, stream));
-            narrowP();
-            t2_set_kernel<<<1, 1, 0, stream>>>(ctl, n);
-            // drift increments of step n
-            enqueue_solve<T, FIN_DRIFT>(rhs_P<T>(), 0.5 * sub[0], Y(0));
+            t2_axpy_kernel<T><<<blocks(ndof, 256), 256, 0, stream>>>(ndof, d_U.as<T>(), Y(n, 0), 0.5 * sub[0]);
             for (int q = 0; q < nq; ++q) {
                 enqueue_stiff<T>(d_U.as<T>());
                 GArgs<T> g = gargs<T>();
@@ -1994,12 +1989,17 @@ template <class T> void Tet2Sim::backward_t(const double *tg, double *grad)
                     t2_source_kernel<T, 0><<<blocks(nsrc, 128), 128, 0, stream>>>(
                         nsrc, d_src_dof.as<unsigned long long>(), d_src_ptr.as<int>(), d_src_dip.as<int>(), d_src_coef.as<double>(),
                         d_src_g.as<double>(), ctl, nq, q, nd, sub[q], d_P.as<double>(), fp64 ? nullptr : d_Pc.as<T>());
-                enqueue_solve<T, FIN_DRIFT>(rhs_P<T>(), hq[q], Y(q + 1));
+                enqueue_solve<T, FIN_DRIFT>(rhs_P<T>(), hq[q], Y(n, q + 1));
             }
+            t2_advance_kernel<<<1, 1, 0, stream>>>(ctl);
+        }
+        // reversed steps
+        for (int n = n1 - 1; n >= n0; --n) {
+            t2_set_kernel<<<1, 1, 0, stream>>>(ctl, n);
             // adjoint of the substages
             for (int q = nq - 1; q >= 0; --q) {
                 enqueue_solve<T, FIN_DRIFT>(Ubr, hq[q], d_x.as<T>(), Pb.as<T>());
-                t2_grad_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_x.as<T>(), Y(q + 1),
+                t2_grad_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_x.as<T>(), Y(n, q + 1),
                                                                          -hq[q], gd.as<double>());
                 enqueue_stiff<T>(Pb.as<T>());
                 GArgs<T> g = gargs<T>();
@@ -2010,7 +2010,7 @@ template <class T> void Tet2Sim::backward_t(const double *tg, double *grad)
                 t2_gather_kernel<T, double, G_KICK, FIN_NONE><<<blocks(nent, 128), 128, 0, stream>>>(nent, d_shots.as<T2Shot>(), ns, g);
             }
             enqueue_solve<T, FIN_DRIFT>(Ubr, 0.5 * sub[0], d_x.as<T>(), Pb.as<T>());
-            t2_grad_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_x.as<T>(), Y(0),
+            t2_grad_kernel<T><<<blocks(ntet, 128), 128, 0, stream>>>(ntet, d_shots.as<T2Shot>(), ns, d_x.as<T>(), Y(n, 0),
                                                                      -0.5 * sub[0], gd.as<double>());
             if (nrd > 0 && n % tf == 0)
                 t2_source_kernel<T, 0><<<blocks(nrd, 128), 128, 0, stream>>>(
