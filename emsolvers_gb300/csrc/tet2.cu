@@ -619,17 +619,33 @@ __global__ void __launch_bounds__(128) t2_gather_kernel(unsigned long long NE, c
     const unsigned long long d1 = S.dof0 + (unsigned long long)pl1 * S.nnode + v;
     TY y0 = TY(0), y1 = TY(0);
     if (MODE != G_CHEB0 && !dead) {
+        // every value of the entity's tetrahedra loaded first (all loads in
+        // flight together), then summed in the fixed order of c2_inc
         const TY *Y = static_cast<const TY *>(g.Yt);
         const unsigned long long ncx = S.n[0], ncxy = ncx * S.n[1];
-        for (int q = 0; q < c2_ninc[et]; ++q) {
+        const int ninc = c2_ninc[et];
+        TY v0[kMaxInc], v1[kMaxInc];
+        bool in[kMaxInc];
+#pragma unroll
+        for (int q = 0; q < kMaxInc; ++q) {
+            in[q] = false;
+            v0[q] = v1[q] = TY(0);
+            if (q >= ninc) continue;
             const int w = c2_inc[et][q];
             const int p = w & 7, ob = (w >> 3) & 7, la = (w >> 6) & 31, lb = (w >> 11) & 31;
             const int ci = i - (ob & 1), cj = j - ((ob >> 1) & 1), ck = k - ((ob >> 2) & 1);
             if (ci < 0 || cj < 0 || ck < 0 || ci >= S.n[0] || cj >= S.n[1] || ck >= S.n[2]) continue;
             const unsigned long long t = S.tet0 + (unsigned long long)p * S.ncube + (unsigned long long)ci + ncx * cj + ncxy * ck;
-            y0 = add_rn(y0, Y[(unsigned long long)la * g.NT + t]);
-            y1 = add_rn(y1, Y[(unsigned long long)lb * g.NT + t]);
+            in[q] = true;
+            v0[q] = Y[(unsigned long long)la * g.NT + t];
+            v1[q] = Y[(unsigned long long)lb * g.NT + t];
         }
+#pragma unroll
+        for (int q = 0; q < kMaxInc; ++q)
+            if (in[q]) {
+                y0 = add_rn(y0, v0[q]);
+                y1 = add_rn(y1, v1[q]);
+            }
     }
     if (MODE == G_FORCE) {
         g.out[d0] = dead ? T(0) : (T)y0;
