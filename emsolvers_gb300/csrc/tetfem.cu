@@ -420,7 +420,6 @@ __device__ __forceinline__ double source_load(const SrcArgs &s, size_t e)
     return f;
 }
 
-
 // Receivers sampled inside the step launches.  The first launch of step n
 // reads the step counter ctl[par] (n) and, from one block beyond the node
 // blocks, records E(x) = sum_l w_l(x) U_l of every receiver when n is a
